@@ -1,0 +1,487 @@
+/*
+ * oracle.c -- CPU restatement of Starflood's force-and-step path.
+ *
+ * TEST INFRASTRUCTURE ONLY (the checker, never the product): see oracle.h.
+ *
+ * Each routine restates the reference algorithm in this code's own words;
+ * the comments cite the reference lines (src/<file>:<line>) whose arithmetic
+ * is reproduced.  Association order of every floating-point expression is
+ * the reference's, and the library is built with -ffp-contract=off, so the
+ * FP32 build is bit-identical to the reference on the same inputs (this is
+ * checked against the compiled reference by tests/test_oracle.py).
+ */
+#include "oracle.h"
+
+#include <math.h>
+#include <stddef.h>
+#include <string.h>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+typedef orc_real R;
+
+#if defined(ORC_IS_DOUBLE)
+#define R_SQRT(x) sqrt(x)
+#define R_EXP(x) exp(x)
+#define R_POW(x, y) pow((x), (y))
+#else
+#define R_SQRT(x) sqrtf(x)
+#define R_EXP(x) expf(x)
+#define R_POW(x, y) powf((x), (y))
+#endif
+
+/* 2^-32 rounded down to the float below it (rng.h:9). */
+static const double k_inv_u32 = 2.3283062977608182109179324470460414886474609375e-10;
+/* common.h:24, common.h:29 (the latter holds pi^(3/2) despite its name). */
+static const double k_inv_sqrt_pi = 0.56418958354775628694807945156077258584405062932900;
+static const double k_pi_pow_1_5 = 5.56832799683170784528481798211883570201362439028324;
+
+/* Compensated running sum (the Kahan idiom of gravity.c:521-533).  The
+ * volatile temporaries keep the compiler from reassociating, as in the
+ * reference. */
+typedef struct { R s, c; } ksum;
+static inline void ksum_add(ksum* k, R x) {
+    const R y = x - k->c;
+    volatile R t = k->s + y;
+    volatile R z = t - k->s;
+    k->c = z - y;
+    k->s = t;
+}
+typedef struct { double s, c; } ksum64;
+static inline void ksum64_add(ksum64* k, double x) {
+    const double y = x - k->c;
+    volatile double t = k->s + y;
+    volatile double z = t - k->s;
+    k->c = z - y;
+    k->s = t;
+}
+
+int orc_real_size(void) { return (int)sizeof(R); }
+
+int orc_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+/* ---- rng.h:13-40: one round of the pcg4d hash (Jarzynski & Olano 2020). */
+void orc_pcg4d(uint32_t s[4]) {
+    uint32_t a = s[0] * 1664525u + 1013904223u;
+    uint32_t b = s[1] * 1664525u + 1013904223u;
+    uint32_t c = s[2] * 1664525u + 1013904223u;
+    uint32_t d = s[3] * 1664525u + 1013904223u;
+    a += b * d; b += c * a; c += a * b; d += b * c;
+    a ^= a >> 16; b ^= b >> 16; c ^= c >> 16; d ^= d >> 16;
+    a += b * d; b += c * a; c += a * b; d += b * c;
+    s[0] = a; s[1] = b; s[2] = c; s[3] = d;
+}
+
+/* ---- simulation.c:245-277: mean distance from the origin, FP64 + Kahan. */
+double orc_mean_radius(uint32_t n, const R* pos) {
+    ksum64 acc = {0.0, 0.0};
+    for (uint32_t i = 0; i < n; i++) {
+        const double x = (double)pos[3u * i + 0u];
+        const double y = (double)pos[3u * i + 1u];
+        const double z = (double)pos[3u * i + 2u];
+        ksum64_add(&acc, sqrt((x * x) + (y * y) + (z * z)));
+    }
+    return acc.s * (1.0 / (double)n);
+}
+
+/* ---- simulation.c:279-301: root cube = [-2r, 2r] shifted by r*j/2 per axis,
+ * j in [-1, 1) from pcg4d seeded with the step number. */
+void orc_root_bounds(uint32_t n, const R* pos, uint32_t step_number, R bounds[6]) {
+    const double rbar = orc_mean_radius(n, pos);
+    uint32_t h[4] = {0x638FE17Bu + step_number, 0xB10BDCE7u, 0x7B8ADB9Bu, 0xD8C5850Eu};
+    orc_pcg4d(h);
+    for (int a = 0; a < 3; a++) {
+        const double j = 2.0 * (k_inv_u32 * (double)h[a]) - 1.0;
+        bounds[a] = (R)(-2.000 * rbar + 0.5 * j * rbar);
+        bounds[3 + a] = (R)(2.000 * rbar + 0.5 * j * rbar);
+    }
+}
+
+/* ---- tree.c:118-362: build by inserting particles one at a time. */
+static void node_clear(orc_node* nd, uint32_t parent) {
+    memset(nd, 0, sizeof(*nd));
+    nd->parent = parent;
+}
+
+int orc_tree_build(const orc_params* p, uint32_t n, const R* pos, const R* mas,
+                   const R bounds[6], orc_node* nodes, uint32_t* num_nodes) {
+    const uint32_t cap = p->leaf_cap;
+    const uint32_t max_nodes = p->nodes_max;
+    const int depth_max = (int)p->depth_max;
+    uint32_t count = 1u;
+
+    /* tree.c:129-151 purge, 156-159 root bounds */
+    for (uint32_t i = 0; i < max_nodes; i++) node_clear(&nodes[i], 0u);
+    for (int a = 0; a < 6; a++) nodes[0].bounds[a] = bounds[a];
+
+    int status = 0;
+    for (uint32_t idx = 0; idx < n && status == 0; idx++) {
+        const R x[3] = {pos[3u * idx], pos[3u * idx + 1u], pos[3u * idx + 2u]};
+        const R m = mas[idx];
+        R lo[3] = {bounds[0], bounds[1], bounds[2]};
+        R hi[3] = {bounds[3], bounds[4], bounds[5]};
+
+        /* tree.c:186-190: particles outside the closed root cube are skipped */
+        int outside = 0;
+        for (int a = 0; a < 3; a++) outside |= (lo[a] > x[a]) | (x[a] > hi[a]);
+        if (outside) continue;
+
+        uint32_t cur = 0u;
+        for (int depth = 0; depth <= depth_max; depth++) {
+            orc_node* nd = &nodes[cur];
+            const uint32_t before = nd->bodies;           /* tree.c:198-200 */
+            nd->bodies = before + 1u;
+            R mid[3];
+            for (int a = 0; a < 3; a++) mid[a] = (R)0.5 * (lo[a] + hi[a]);  /* 203-207 */
+            nd->params[0] += m * x[0];                    /* 210-213 */
+            nd->params[1] += m * x[1];
+            nd->params[2] += m * x[2];
+            nd->params[3] += m;
+
+            if (before < cap) {                           /* 216-219 */
+                nd->branch[before] = idx;
+                break;
+            }
+            if (before == cap) {                          /* 222-318: split */
+                if (max_nodes <= count + 8u) { status = -1; break; }
+                if (depth_max <= depth) { status = -1; break; }
+                orc_node kids[8];
+                for (int o = 0; o < 8; o++) {
+                    node_clear(&kids[o], cur);
+                    for (int a = 0; a < 3; a++) {
+                        const int up = (o >> a) & 1;
+                        kids[o].bounds[a] = up ? mid[a] : lo[a];
+                        kids[o].bounds[3 + a] = up ? hi[a] : mid[a];
+                    }
+                }
+                /* 273-304: the resident particles move down, in slot order,
+                 * choosing the upper half only when strictly above mid. */
+                for (uint32_t k = 0; k < cap; k++) {
+                    const uint32_t q = nd->branch[k];
+                    const R y[3] = {pos[3u * q], pos[3u * q + 1u], pos[3u * q + 2u]};
+                    const R mq = mas[q];
+                    const int o = (mid[0] < y[0] ? 1 : 0) + (mid[1] < y[1] ? 2 : 0) +
+                                  (mid[2] < y[2] ? 4 : 0);
+                    orc_node* kd = &kids[o];
+                    kd->branch[kd->bodies] = q;
+                    kd->bodies += 1u;
+                    kd->params[0] += mq * y[0];
+                    kd->params[1] += mq * y[1];
+                    kd->params[2] += mq * y[2];
+                    kd->params[3] += mq;
+                }
+                for (int o = 0; o < 8; o++) {             /* 307-317 */
+                    nodes[count + (uint32_t)o] = kids[o];
+                    nd->branch[o] = count + (uint32_t)o;
+                }
+                for (uint32_t k = 8; k < ORC_LEAF_MAX; k++) nd->branch[k] = 0u;
+                count += 8u;
+            }
+            /* 326-338: the arriving particle picks the upper half when at or
+             * above mid. */
+            const int o = (mid[0] <= x[0] ? 1 : 0) + (mid[1] <= x[1] ? 2 : 0) +
+                          (mid[2] <= x[2] ? 4 : 0);
+            for (int a = 0; a < 3; a++) {
+                if ((o >> a) & 1) lo[a] = mid[a]; else hi[a] = mid[a];
+            }
+            cur = nd->branch[o];
+        }
+    }
+    *num_nodes = count;
+    if (status != 0) return -1;   /* tree.c:224-233 leave COMs unnormalised */
+
+    for (uint32_t i = 0; i < count; i++) {                /* tree.c:346-354 */
+        const R w = nodes[i].params[3];
+        const R inv = (R)0.0 < w ? (R)1.0 / w : (R)1.0;
+        nodes[i].params[0] *= inv;
+        nodes[i].params[1] *= inv;
+        nodes[i].params[2] *= inv;
+    }
+    return 0;
+}
+
+/* ---- gravity.c:242-663: per-particle depth-first walk without a stack of
+ * node ids: parent links plus the octant being visited at every depth. */
+void orc_gravity_tree(const orc_params* p, uint32_t n, const R* pos, const R* mas,
+                      const orc_node* nodes, R* acc, R* pot, orc_walk_stats* stats) {
+    const uint32_t cap = p->leaf_cap;
+    const R eps2 = (R)(p->eps * p->eps);
+    const R theta = (R)p->theta;
+    const R third = (R)(1.0 / 3.0);
+    const R neg_g = (R)(-p->G);
+    const int depth_max = (int)p->depth_max;
+    const uint64_t iter_cap = 2ull * 8ull * (uint64_t)p->nodes_max;   /* 306 */
+
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 256)
+#endif
+    for (int64_t ii = 0; ii < (int64_t)n; ii++) {
+        const uint32_t i = (uint32_t)ii;
+        const R ri[3] = {pos[3u * i], pos[3u * i + 1u], pos[3u * i + 2u]};
+        const R mi = mas[i];
+        ksum ax = {0, 0}, ay = {0, 0}, az = {0, 0}, ph = {0, 0};
+        uint32_t n_int = 0u, n_open = 0u;
+
+        int path[64];
+        for (int d = 0; d < depth_max; d++) path[d] = -1;
+        uint32_t at = 0u;
+        int depth = 0;
+        for (uint64_t it = 0; it < iter_cap && depth >= 0; it++) {
+            const orc_node* nd = &nodes[at];
+            const R* lo = &nd->bounds[0];
+            const R* hi = &nd->bounds[3];
+            if (nd->bodies == 0u) {                       /* 324-328 */
+                at = nd->parent;
+                depth--;
+                continue;
+            }
+            if (nd->bodies > cap) {                       /* 331-461 */
+                const int oct = path[depth];
+                if (oct >= 7) {
+                    at = nd->parent;
+                    path[depth] = -1;
+                    depth--;
+                    continue;
+                }
+                if (oct >= 0) {
+                    at = nd->branch[oct + 1];
+                    path[depth] = oct + 1;
+                    depth++;
+                    continue;
+                }
+                /* 352-377: squared width over squared distance to the
+                 * geometric centre of the cell. */
+                n_open++;
+                const R cx = (R)0.5 * (lo[0] + hi[0]);
+                const R cy = (R)0.5 * (lo[1] + hi[1]);
+                const R cz = (R)0.5 * (lo[2] + hi[2]);
+                const R ox = cx - ri[0], oy = cy - ri[1], oz = cz - ri[2];
+                const R d2 = (ox * ox) + (oy * oy) + (oz * oz);
+                const R w = third * ((hi[0] - lo[0]) + (hi[1] - lo[1]) + (hi[2] - lo[2]));
+                const R ratio = (R)0.0 < d2 ? (w * w) / d2 : (R)0.0;
+                if (theta <= ratio) {                     /* 448-453 */
+                    at = nd->branch[0];
+                    path[depth] = 0;
+                    depth++;
+                    continue;
+                }
+            }
+            /* 463-490: monopole, with particle i taken out when it lies in
+             * the closed cell and the cell holds more than one body. */
+            R cm[3] = {nd->params[0], nd->params[1], nd->params[2]};
+            R mj = nd->params[3];
+            if (lo[0] <= ri[0] && ri[0] <= hi[0] && lo[1] <= ri[1] && ri[1] <= hi[1] &&
+                lo[2] <= ri[2] && ri[2] <= hi[2] && 1u < nd->bodies) {
+                for (int a = 0; a < 3; a++) cm[a] *= mj;
+                for (int a = 0; a < 3; a++) cm[a] -= mi * ri[a];
+                mj -= mi;
+                for (int a = 0; a < 3; a++) cm[a] *= (R)0.0 < mj ? (R)1.0 / mj : (R)1.0;
+            }
+            /* 493-548 */
+            const R dx = ri[0] - cm[0], dy = ri[1] - cm[1], dz = ri[2] - cm[2];
+            const R r2 = (dx * dx) + (dy * dy) + (dz * dz);
+            const R inv2 = (R)1.0 / (r2 + eps2);
+            const R inv1 = (R)1.0 / R_SQRT(r2 + eps2);
+            const R phi = mj * inv1;
+            if (p->kahan) {
+                ksum_add(&ax, phi * inv2 * dx);
+                ksum_add(&ay, phi * inv2 * dy);
+                ksum_add(&az, phi * inv2 * dz);
+                ksum_add(&ph, phi);
+            } else {
+                ax.s += phi * inv2 * dx;
+                ay.s += phi * inv2 * dy;
+                az.s += phi * inv2 * dz;
+                ph.s += phi;
+            }
+            n_int++;
+            at = nd->parent;                              /* 577-578 */
+            depth--;
+        }
+        acc[3u * i + 0u] = neg_g * mi * ax.s;             /* 656-659 */
+        acc[3u * i + 1u] = neg_g * mi * ay.s;
+        acc[3u * i + 2u] = neg_g * mi * az.s;
+        pot[i] = neg_g * ph.s;
+        if (stats) {
+            stats[i].interactions = n_int;
+            stats[i].opening_tests = n_open;
+        }
+    }
+}
+
+/* ---- gravity.c:666-819: every j, including j == i. */
+void orc_gravity_pp(const orc_params* p, uint32_t n, const R* pos, const R* mas,
+                    R* acc, R* pot) {
+    const R eps2 = (R)(p->eps * p->eps);
+    const R neg_g = (R)(-p->G);
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 256)
+#endif
+    for (int64_t ii = 0; ii < (int64_t)n; ii++) {
+        const uint32_t i = (uint32_t)ii;
+        const R mi = mas[i];
+        const R xi = pos[3u * i], yi = pos[3u * i + 1u], zi = pos[3u * i + 2u];
+        ksum ax = {0, 0}, ay = {0, 0}, az = {0, 0}, ph = {0, 0};
+        for (uint32_t j = 0; j < n; j++) {
+            const R dx = xi - pos[3u * j];
+            const R dy = yi - pos[3u * j + 1u];
+            const R dz = zi - pos[3u * j + 2u];
+            const R r2 = (dx * dx) + (dy * dy) + (dz * dz);
+            const R inv2 = (R)1.0 / (r2 + eps2);
+            const R inv1 = (R)1.0 / R_SQRT(r2 + eps2);
+            const R phi = mas[j] * inv1;
+            if (p->kahan) {
+                ksum_add(&ax, phi * inv2 * dx);
+                ksum_add(&ay, phi * inv2 * dy);
+                ksum_add(&az, phi * inv2 * dz);
+                ksum_add(&ph, phi);
+            } else {
+                ax.s += phi * inv2 * dx;
+                ay.s += phi * inv2 * dy;
+                az.s += phi * inv2 * dz;
+                ph.s += phi;
+            }
+        }
+        acc[3u * i + 0u] = neg_g * mi * ax.s;
+        acc[3u * i + 1u] = neg_g * mi * ay.s;
+        acc[3u * i + 2u] = neg_g * mi * az.s;
+        pot[i] = neg_g * ph.s;
+    }
+}
+
+/* ---- sph.c:14-282: Gaussian kernel W = (1/(sqrt(pi) h))^3 exp(-r^2/h^2),
+ * density over all pairs, polytrope P = (0.1 rho)^2, momentum over pairs with
+ * r^2 <= 1. */
+void orc_sph_reference(const orc_params* p, uint32_t n, const R* pos, const R* mas,
+                       const R* rad, R* rho, R* prs, R* acc, uint32_t* nbr) {
+    (void)p;
+    const R inv_sqrt_pi = (R)k_inv_sqrt_pi;
+    const R pi_1_5 = (R)k_pi_pow_1_5;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 256)
+#endif
+    for (int64_t ii = 0; ii < (int64_t)n; ii++) {          /* sph.c:35-145 */
+        const uint32_t i = (uint32_t)ii;
+        const R hi = rad[i];
+        const R xi = pos[3u * i], yi = pos[3u * i + 1u], zi = pos[3u * i + 2u];
+        ksum s = {0, 0};
+        for (uint32_t j = 0; j < n; j++) {
+            const R hj = rad[j];
+            const R dx = xi - pos[3u * j];
+            const R dy = yi - pos[3u * j + 1u];
+            const R dz = zi - pos[3u * j + 2u];
+            const R r2 = (dx * dx) + (dy * dy) + (dz * dz);
+            const R ai = inv_sqrt_pi / hi;
+            const R aj = inv_sqrt_pi / hj;
+            const R wi = (ai * ai * ai) * R_EXP(-r2 / (hi * hi));
+            const R wj = (aj * aj * aj) * R_EXP(-r2 / (hj * hj));
+            ksum_add(&s, (R)0.5 * (wi + wj) * mas[j]);
+        }
+        rho[i] = s.s;
+    }
+    const R eos_k = (R)0.100;                               /* sph.c:148-159 */
+    const R eos_e = (R)((1.0 / 1.0) + 1.0);
+    for (uint32_t i = 0; i < n; i++) prs[i] = R_POW(eos_k * rho[i], eos_e);
+
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 256)
+#endif
+    for (int64_t ii = 0; ii < (int64_t)n; ii++) {          /* sph.c:172-277 */
+        const uint32_t i = (uint32_t)ii;
+        const R mi = mas[i];
+        const R hi = rad[i];
+        const R xi = pos[3u * i], yi = pos[3u * i + 1u], zi = pos[3u * i + 2u];
+        const R rhoi2 = rho[i] * rho[i];
+        const R ci = (R)0.0 < rhoi2 ? prs[i] / rhoi2 : (R)0.0;
+        ksum sx = {0, 0}, sy = {0, 0}, sz = {0, 0};
+        uint32_t count = 0u;
+        for (uint32_t j = 0; j < n; j++) {
+            const R hj = rad[j];
+            const R dx = xi - pos[3u * j];
+            const R dy = yi - pos[3u * j + 1u];
+            const R dz = zi - pos[3u * j + 2u];
+            const R rhoj2 = rho[j] * rho[j];
+            const R cj = (R)0.0 < rhoj2 ? prs[j] / rhoj2 : (R)0.0;
+            const R r2 = (dx * dx) + (dy * dy) + (dz * dz);
+            if (r2 > (R)(1.000 * 1.000)) continue;          /* sph.c:231 */
+            count++;
+            const R ni = (R)-2.0 * R_EXP(-r2 / (hi * hi)) / (pi_1_5 * hi * hi * hi * hi * hi);
+            const R nj = (R)-2.0 * R_EXP(-r2 / (hj * hj)) / (pi_1_5 * hj * hj * hj * hj * hj);
+            const R g = (R)0.5 * (ni + nj);
+            ksum_add(&sx, (ci + cj) * (g * dx));
+            ksum_add(&sy, (ci + cj) * (g * dy));
+            ksum_add(&sz, (ci + cj) * (g * dz));
+        }
+        acc[3u * i + 0u] += -mi * sx.s;
+        acc[3u * i + 1u] += -mi * sy.s;
+        acc[3u * i + 2u] += -mi * sz.s;
+        if (nbr) nbr[i] = count;
+    }
+}
+
+/* ---- simulation.h:17-51: SIM_DOF = 13, or 16 with SPH. */
+uint32_t orc_sim_dof(const orc_params* p) { return p->use_sph ? 16u : 13u; }
+
+/* slab offsets (simulation.c:33-53) */
+#define SLAB(s, k) ((s)->mem + (size_t)(s)->N * (size_t)(k))
+
+int orc_sim_solv(const orc_params* p, orc_sim* s) {
+    const uint32_t n = s->N;
+    R* pos = SLAB(s, 0);
+    R* acc = SLAB(s, 6);
+    R* mas = SLAB(s, 9);
+    R* pot = SLAB(s, 10);
+    int status = 0;
+    if (p->use_tree) {                                      /* simulation.c:244-325 */
+        orc_root_bounds(n, pos, s->step_number, s->bounds);
+        s->tree_status = orc_tree_build(p, n, pos, mas, s->bounds, s->nodes, &s->num_nodes);
+        /* the reference ignores the build status (simulation.c:312) */
+        orc_gravity_tree(p, n, pos, mas, s->nodes, acc, pot, NULL);
+    } else {                                                /* simulation.c:329 */
+        orc_gravity_pp(p, n, pos, mas, acc, pot);
+    }
+    if (p->use_sph) {                                       /* simulation.c:338 */
+        orc_sph_reference(p, n, pos, mas, SLAB(s, 13), SLAB(s, 14), SLAB(s, 15), acc, NULL);
+    }
+    return status;
+}
+
+int orc_sim_step(const orc_params* p, orc_sim* s, double* T, double* V) {
+    const uint32_t n = s->N;
+    R* pos = SLAB(s, 0);
+    R* vel = SLAB(s, 3);
+    R* acc = SLAB(s, 6);
+    R* mas = SLAB(s, 9);
+    R* pot = SLAB(s, 10);
+    R* ken = SLAB(s, 11);
+    R* pen = SLAB(s, 12);
+    const R dt = (R)p->dt;
+    const R half_dt = (R)0.5 * dt;
+
+    for (uint32_t k = 0; k < 3u * n; k++) vel[k] += half_dt * acc[k];   /* 381-383 */
+    for (uint32_t k = 0; k < 3u * n; k++) pos[k] += dt * vel[k];        /* 393-395 */
+    const int status = orc_sim_solv(p, s);                               /* 406-413 */
+    for (uint32_t k = 0; k < 3u * n; k++) vel[k] += half_dt * acc[k];   /* 423-425 */
+
+    for (uint32_t i = 0; i < n; i++) {                                   /* 434-446 */
+        const R vx = vel[3u * i], vy = vel[3u * i + 1u], vz = vel[3u * i + 2u];
+        const R v2 = (vx * vx) + (vy * vy) + (vz * vz);
+        ken[i] = (R)0.5 * mas[i] * v2;
+    }
+    for (uint32_t i = 0; i < n; i++) pen[i] = mas[i] * pot[i];          /* 449-451 */
+
+    ksum64 tk = {0.0, 0.0}, vk = {0.0, 0.0};                             /* 455-497 */
+    for (uint32_t i = 0; i < n; i++) ksum64_add(&tk, (double)ken[i]);
+    for (uint32_t i = 0; i < n; i++) ksum64_add(&vk, (double)pen[i]);
+    if (T) *T = tk.s;
+    if (V) *V = vk.s;
+    return status;
+}

@@ -1,0 +1,125 @@
+/*
+ * oracle.h -- CPU restatement of Starflood's force-and-step path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker for the GPU
+ * implementation in starflood_gb300/: only tests/, __graft_entry__.smoke()
+ * and the cpu_baseline / reference arm of bench.py may load it.  Nothing in
+ * the product links or calls it.
+ *
+ * The file is compiled twice: with ORC_REAL=float (liboracle_f32.so, the
+ * reference's FP32 semantics, bit-for-bit) and with ORC_REAL=double
+ * (liboracle_f64.so, the FP64 oracle).  Every routine cites the reference
+ * file:line it restates (paths relative to the Starflood source tree).
+ *
+ * Floating-point contract: compiled with -ffp-contract=off and without
+ * -ffast-math, expressions are written in the same association order as the
+ * reference, so the FP32 build reproduces the reference's results exactly.
+ */
+#ifndef SF_ORACLE_H
+#define SF_ORACLE_H
+
+#include <stdint.h>
+
+#ifndef ORC_REAL
+#define ORC_REAL float
+#endif
+typedef ORC_REAL orc_real;
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Run-time counterpart of the reference's compile-time config.h macros. */
+typedef struct {
+    double   dt;          /* TIMESTEP_SIZE   (config.h)                   */
+    double   eps;         /* EPSILON         (config.h), > 0              */
+    double   G;           /* G               (config.h)                   */
+    double   theta;       /* TREE_THETA      (config.h)                   */
+    int32_t  use_tree;    /* ENABLE_TREE: 1 = BH walk, 0 = PP             */
+    int32_t  use_sph;     /* ENABLE_SPH:  0 off, 1 = reference Gaussian SPH */
+    int32_t  kahan;       /* ENABLE_KAHAN_SUMMATION_SOLVER/_ENERGY (1 = on) */
+    uint32_t leaf_cap;    /* bodies per leaf (reference: 8, tree.h:20)    */
+    uint32_t depth_max;   /* TREE_DEPTH_MAX (16)                          */
+    uint32_t nodes_max;   /* TREE_NODES_MAX (262144)                      */
+} orc_params;
+
+/* Tree node.  Same meaning as the reference node_t (tree.h:16-25), with
+ * room for leaf capacities above 8 (an extension used only by the leaf-16
+ * variant).  params[] = {COM x, COM y, COM z, mass} after orc_tree_build. */
+#define ORC_LEAF_MAX 16
+typedef struct {
+    uint32_t parent;
+    uint32_t bodies;
+    uint32_t branch[ORC_LEAF_MAX];
+    orc_real bounds[6];
+    orc_real params[4];
+} orc_node;
+
+/* Walk statistics per particle (no counterpart in the reference: it has no
+ * interaction counter). */
+typedef struct {
+    uint32_t interactions;   /* monopole interactions accumulated */
+    uint32_t opening_tests;  /* internal-node opening tests        */
+} orc_walk_stats;
+
+/* rng.h:13-40 */
+void orc_pcg4d(uint32_t s[4]);
+
+/* simulation.c:244-277: FP64 Kahan mean radius. */
+double orc_mean_radius(uint32_t n, const orc_real* pos);
+
+/* simulation.c:279-308: jittered root cube for a step number. */
+void orc_root_bounds(uint32_t n, const orc_real* pos, uint32_t step_number,
+                     orc_real bounds[6]);
+
+/* tree.c:118-362: serial insertion build.  Returns 0, or -1 on node or depth
+ * overflow (the tree is left partial, as in the reference).  *num_nodes gets
+ * the node count (the reference forgets to store it, tree.c:121,359). */
+int orc_tree_build(const orc_params* p, uint32_t n, const orc_real* pos,
+                   const orc_real* mas, const orc_real bounds[6],
+                   orc_node* nodes, uint32_t* num_nodes);
+
+/* gravity.c:242-663: stackless DFS walk.  stats may be NULL. */
+void orc_gravity_tree(const orc_params* p, uint32_t n, const orc_real* pos,
+                      const orc_real* mas, const orc_node* nodes,
+                      orc_real* acc, orc_real* pot, orc_walk_stats* stats);
+
+/* gravity.c:666-819: all-pairs softened gravity with Kahan sums. */
+void orc_gravity_pp(const orc_params* p, uint32_t n, const orc_real* pos,
+                    const orc_real* mas, orc_real* acc, orc_real* pot);
+
+/* sph.c:14-282: reference SPH (Gaussian, all pairs).  Adds the pressure
+ * force into acc, writes rho and prs.  nbr (may be NULL) receives, per
+ * particle, the size of the momentum-pass neighbour set {j: r2 <= 1}. */
+void orc_sph_reference(const orc_params* p, uint32_t n, const orc_real* pos,
+                       const orc_real* mas, const orc_real* rad, orc_real* rho,
+                       orc_real* prs, orc_real* acc, uint32_t* nbr);
+
+/* Simulation over one slab in the reference layout (simulation.h:17-51):
+ * pos[3N] vel[3N] acc[3N] mas[N] pot[N] ken[N] pen[N] (+ rad rho prs). */
+typedef struct {
+    uint32_t  step_number;
+    uint32_t  N;
+    orc_real* mem;          /* caller-owned slab of N * dof reals          */
+    orc_node* nodes;        /* caller-owned, p->nodes_max entries (tree)    */
+    uint32_t  num_nodes;    /* out: nodes of the last build                 */
+    int32_t   tree_status;  /* out: return of the last tree build           */
+    orc_real  bounds[6];    /* out: root cube of the last build             */
+} orc_sim;
+
+uint32_t orc_sim_dof(const orc_params* p);                 /* SIM_DOF */
+
+/* simulation.c:230-345 */
+int orc_sim_solv(const orc_params* p, orc_sim* s);
+/* simulation.c:347-519; energies written to *T and *V (may be NULL). */
+int orc_sim_step(const orc_params* p, orc_sim* s, double* T, double* V);
+
+/* Informational: sizeof(orc_real). */
+int orc_real_size(void);
+/* Informational: OpenMP threads the parallel loops use. */
+int orc_threads(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,250 @@
+"""ctypes bindings for the test oracle (TEST INFRASTRUCTURE ONLY).
+
+``Oracle`` wraps ``liboracle_f32.so`` / ``liboracle_f64.so`` (the C
+restatement, see ``oracle/oracle.c``); ``Reference`` wraps the compiled
+Starflood reference in ``oracle/_ref`` (present only where the reference
+sources were available at build time).  Arrays use the reference layout:
+positions, velocities and accelerations are (N, 3) row-major.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs import
+this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+u32p = C.POINTER(C.c_uint32)
+
+
+class Params(C.Structure):
+    _fields_ = [("dt", C.c_double), ("eps", C.c_double), ("G", C.c_double),
+                ("theta", C.c_double), ("use_tree", C.c_int32), ("use_sph", C.c_int32),
+                ("kahan", C.c_int32), ("leaf_cap", C.c_uint32), ("depth_max", C.c_uint32),
+                ("nodes_max", C.c_uint32)]
+
+
+def make_params(dt=1e-3, eps=0.01, G=1.0, theta=0.5, use_tree=0, use_sph=0, kahan=1,
+                leaf_cap=8, depth_max=16, nodes_max=262144) -> Params:
+    return Params(dt, eps, G, theta, use_tree, use_sph, kahan, leaf_cap, depth_max, nodes_max)
+
+
+def node_dtype(real):
+    return np.dtype([("parent", np.uint32), ("bodies", np.uint32), ("branch", np.uint32, (16,)),
+                     ("bounds", real, (6,)), ("params", real, (4,))], align=True)
+
+
+class Oracle:
+    """The C restatement at one precision ('f32' reference arithmetic, 'f64')."""
+
+    def __init__(self, precision: str = "f32"):
+        path = os.path.join(HERE, "liboracle_%s.so" % precision)
+        if not os.path.exists(path):
+            from oracle import build as _b
+            _b.build_oracle()
+        self.lib = C.CDLL(path)
+        self.real = np.float32 if precision == "f32" else np.float64
+        self.creal = C.c_float if precision == "f32" else C.c_double
+        self.node_dtype = node_dtype(self.real)
+        rp = C.POINTER(self.creal)
+        self._rp = rp
+        L = self.lib
+        L.orc_real_size.restype = C.c_int
+        assert L.orc_real_size() == np.dtype(self.real).itemsize
+        L.orc_mean_radius.restype = C.c_double
+        L.orc_mean_radius.argtypes = [C.c_uint32, rp]
+        L.orc_root_bounds.argtypes = [C.c_uint32, rp, C.c_uint32, rp]
+        L.orc_tree_build.restype = C.c_int
+        L.orc_tree_build.argtypes = [C.POINTER(Params), C.c_uint32, rp, rp, rp, C.c_void_p, u32p]
+        L.orc_gravity_tree.argtypes = [C.POINTER(Params), C.c_uint32, rp, rp, C.c_void_p, rp, rp, u32p]
+        L.orc_gravity_pp.argtypes = [C.POINTER(Params), C.c_uint32, rp, rp, rp, rp]
+        L.orc_sph_reference.argtypes = [C.POINTER(Params), C.c_uint32, rp, rp, rp, rp, rp, rp, u32p]
+        L.orc_pcg4d.argtypes = [u32p]
+        L.orc_sim_dof.restype = C.c_uint32
+        L.orc_sim_dof.argtypes = [C.POINTER(Params)]
+        L.orc_threads.restype = C.c_int
+
+        class Sim(C.Structure):
+            _fields_ = [("step_number", C.c_uint32), ("N", C.c_uint32), ("mem", C.c_void_p),
+                        ("nodes", C.c_void_p), ("num_nodes", C.c_uint32), ("tree_status", C.c_int32),
+                        ("bounds", self.creal * 6)]
+        self.Sim = Sim
+        L.orc_sim_solv.restype = C.c_int
+        L.orc_sim_solv.argtypes = [C.POINTER(Params), C.POINTER(Sim)]
+        L.orc_sim_step.restype = C.c_int
+        L.orc_sim_step.argtypes = [C.POINTER(Params), C.POINTER(Sim), C.POINTER(C.c_double),
+                                   C.POINTER(C.c_double)]
+
+    def threads(self) -> int:
+        return int(self.lib.orc_threads())
+
+    def _arr(self, a, n_cols=None):
+        a = np.ascontiguousarray(a, dtype=self.real)
+        return a, a.ctypes.data_as(self._rp)
+
+    def pcg4d(self, s):
+        a = (C.c_uint32 * 4)(*[int(x) & 0xFFFFFFFF for x in s])
+        self.lib.orc_pcg4d(a)
+        return [a[i] for i in range(4)]
+
+    def mean_radius(self, pos):
+        pos, pp = self._arr(pos)
+        return float(self.lib.orc_mean_radius(len(pos), pp))
+
+    def root_bounds(self, pos, step):
+        pos, pp = self._arr(pos)
+        out = np.zeros(6, self.real)
+        self.lib.orc_root_bounds(len(pos), pp, step, out.ctypes.data_as(self._rp))
+        return out
+
+    def tree_build(self, pos, mas, bounds, params: Params | None = None):
+        p = params or make_params(use_tree=1)
+        pos, pp = self._arr(pos)
+        mas, mp = self._arr(mas)
+        b, bp = self._arr(bounds)
+        nodes = np.zeros(p.nodes_max, self.node_dtype)
+        nn = C.c_uint32(0)
+        st = self.lib.orc_tree_build(C.byref(p), len(pos), pp, mp, bp,
+                                     nodes.ctypes.data_as(C.c_void_p), C.byref(nn))
+        return st, nodes[: nn.value].copy() if st == 0 else nodes[: nn.value].copy()
+
+    def walk(self, pos, mas, nodes, params: Params | None = None):
+        p = params or make_params(use_tree=1)
+        pos, pp = self._arr(pos)
+        mas, mp = self._arr(mas)
+        n = len(pos)
+        full = np.zeros(max(p.nodes_max, len(nodes)), self.node_dtype)
+        full[: len(nodes)] = nodes
+        acc = np.zeros((n, 3), self.real)
+        pot = np.zeros(n, self.real)
+        stats = np.zeros((n, 2), np.uint32)
+        self.lib.orc_gravity_tree(C.byref(p), n, pp, mp, full.ctypes.data_as(C.c_void_p),
+                                  acc.ctypes.data_as(self._rp), pot.ctypes.data_as(self._rp),
+                                  stats.ctypes.data_as(u32p))
+        return acc, pot, stats
+
+    def pp(self, pos, mas, params: Params | None = None):
+        p = params or make_params()
+        pos, pp = self._arr(pos)
+        mas, mp = self._arr(mas)
+        n = len(pos)
+        acc = np.zeros((n, 3), self.real)
+        pot = np.zeros(n, self.real)
+        self.lib.orc_gravity_pp(C.byref(p), n, pp, mp, acc.ctypes.data_as(self._rp),
+                                pot.ctypes.data_as(self._rp))
+        return acc, pot
+
+    def sph_reference(self, pos, mas, rad, acc_in=None, params: Params | None = None):
+        p = params or make_params(use_sph=1)
+        pos, pp = self._arr(pos)
+        mas, mp = self._arr(mas)
+        rad, rp = self._arr(rad)
+        n = len(pos)
+        acc = np.zeros((n, 3), self.real) if acc_in is None else np.array(acc_in, self.real)
+        rho = np.zeros(n, self.real)
+        prs = np.zeros(n, self.real)
+        nbr = np.zeros(n, np.uint32)
+        self.lib.orc_sph_reference(C.byref(p), n, pp, mp, rp, rho.ctypes.data_as(self._rp),
+                                   prs.ctypes.data_as(self._rp), acc.ctypes.data_as(self._rp),
+                                   nbr.ctypes.data_as(u32p))
+        return rho, prs, acc, nbr
+
+    # --- slab-level simulation (simulation.c) -------------------------------
+    def new_sim(self, n, params: Params):
+        dof = int(self.lib.orc_sim_dof(C.byref(params)))
+        slab = np.zeros(n * dof, self.real)
+        nodes = np.zeros(params.nodes_max if params.use_tree else 1, self.node_dtype)
+        s = self.Sim()
+        s.N = n
+        s.mem = slab.ctypes.data
+        s.nodes = nodes.ctypes.data
+        return s, slab, nodes
+
+    def sim_solv(self, params, sim, step):
+        sim.step_number = step
+        return self.lib.orc_sim_solv(C.byref(params), C.byref(sim))
+
+    def sim_step(self, params, sim, step):
+        sim.step_number = step
+        T = C.c_double()
+        V = C.c_double()
+        rc = self.lib.orc_sim_step(C.byref(params), C.byref(sim), C.byref(T), C.byref(V))
+        return rc, T.value, V.value
+
+
+def slab_views(slab, n, dof):
+    """Views of the reference slab (simulation.h:17-51)."""
+    v = {"pos": slab[0: 3 * n].reshape(n, 3), "vel": slab[3 * n: 6 * n].reshape(n, 3),
+         "acc": slab[6 * n: 9 * n].reshape(n, 3), "mas": slab[9 * n: 10 * n],
+         "pot": slab[10 * n: 11 * n], "ken": slab[11 * n: 12 * n], "pen": slab[12 * n: 13 * n]}
+    if dof >= 16:
+        v["rad"] = slab[13 * n: 14 * n]
+        v["rho"] = slab[14 * n: 15 * n]
+        v["prs"] = slab[15 * n: 16 * n]
+    return v
+
+
+class Reference:
+    """The compiled Starflood reference (one configuration per library)."""
+
+    def __init__(self, variant: str):
+        path = os.path.join(HERE, "_ref", "libref_%s.so" % variant)
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        self.variant = variant
+        self.lib = C.CDLL(path)
+        L = self.lib
+        L.refh_real_size.restype = C.c_int
+        self.real = np.float32 if L.refh_real_size() == 4 else np.float64
+        L.refh_dof.restype = C.c_int
+        L.refh_has_tree.restype = C.c_int
+        self.dof = int(L.refh_dof())
+        self.has_tree = bool(L.refh_has_tree())
+        L.refh_init.argtypes = [C.c_uint]
+        L.refh_init.restype = C.c_int
+        L.refh_mem.restype = C.c_void_p
+        L.refh_solv.argtypes = [C.c_uint]
+        L.refh_step.argtypes = [C.c_uint]
+        if self.has_tree:
+            L.refh_tree_nodes.restype = C.c_uint
+            L.refh_tree_dump.restype = C.c_uint
+            L.refh_tree_dump.argtypes = [C.c_uint, u32p, u32p, u32p, C.c_void_p, C.c_void_p]
+            L.refh_tree_bounds.argtypes = [C.c_void_p]
+            L.refh_tree_build.argtypes = [C.c_uint, C.c_void_p]
+        self.n = 0
+
+    def init(self, n):
+        assert self.lib.refh_init(n) == 0
+        self.n = n
+        ptr = self.lib.refh_mem()
+        buf = (C.c_char * (n * self.dof * np.dtype(self.real).itemsize)).from_address(ptr)
+        self.slab = np.frombuffer(buf, dtype=self.real)
+        self.views = slab_views(self.slab, n, self.dof)
+        return self.views
+
+    def solv(self, step):
+        return self.lib.refh_solv(step)
+
+    def step(self, step):
+        return self.lib.refh_step(step)
+
+    def tree(self):
+        cnt = int(self.lib.refh_tree_nodes())
+        parent = np.zeros(cnt, np.uint32)
+        bodies = np.zeros(cnt, np.uint32)
+        branch = np.zeros((cnt, 8), np.uint32)
+        bounds = np.zeros((cnt, 6), self.real)
+        params = np.zeros((cnt, 4), self.real)
+        self.lib.refh_tree_dump(cnt, parent.ctypes.data_as(u32p), bodies.ctypes.data_as(u32p),
+                                branch.ctypes.data_as(u32p), bounds.ctypes.data, params.ctypes.data)
+        tb = np.zeros(6, self.real)
+        self.lib.refh_tree_bounds(tb.ctypes.data)
+        return dict(parent=parent, bodies=bodies, branch=branch, bounds=bounds, params=params,
+                    root_bounds=tb)
+
+    def free(self):
+        self.lib.refh_free()
