@@ -1,0 +1,428 @@
+"""Benchmark: Barnes-Hut KDK steps of the 65,536-body expanding uniform sphere
+(theta = 0.5 squared criterion, leaf 8, eps = 0.01, dt = 1e-3) on one GB300,
+plus PP gravity at N = 1,048,576 (Plummer, eps = 0.005), plain and
+compensated forms.  Prints one JSON line.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+value  particle-steps/s of K steps with the state resident in HBM, each step
+       one replay of the captured CUDA graph of sim_step; the L2 is flushed
+       (256 MiB memset) between timed steps and the flush is not timed.
+e2e    the same K steps through the drop-in sim_step() with host slabs:
+       every call uploads the slab from page-locked host memory, steps and
+       downloads the slab (host wall clock).
+roofline  the dominant kernel (the walk), from a CUDA-event-instrumented twin
+       run of the same K steps: algorithmic FP32 flops = 20 per monopole
+       interaction + 12 per opening test (both counted on the device).
+cpu_baseline  the CPU restatement of the reference path (oracle/, OpenMP,
+       all host threads) on a bounded sample of the same workload.
+--impl reference  times that CPU path as the reference arm.
+Multi-GPU (torchrun): every rank runs an independent replica of the workload
+on its own GPU (the walk and the tree are replicated, "replicas only").
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_BH = 65536
+N_PP = 1 << 20
+METRIC = "particle-steps/s & PP interactions/s, chosen vs plain, 1 GB300, rel err<=1e-6"
+WORKLOAD = "Barnes-Hut KDK step, N=65536 uniform unit sphere, v=0.5r, m=1/N, G=1, eps=0.01, theta=0.5, leaf=8, dt=1e-3"
+FLOP_INTERACTION = 20
+FLOP_OPEN = 12
+
+
+def env_rank():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=clocks.sm,clocks.max.sm,power.draw,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if s[3 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def fp32_peak_tflops():
+    """FP32 FMA peak: SMs x 128 lanes x 2 flop x the maximum SM clock recorded
+    in MEASURED_PEAKS.json (the file has no FP32 figure of its own)."""
+    mhz, src = 2070.0, "nominal 2070 MHz"
+    try:
+        mp = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        mhz, src = float(mp.get("sm_max_mhz", mhz)), "sm_max_mhz of MEASURED_PEAKS.json"
+    except Exception:
+        pass
+    sms = 152
+    try:
+        import torch
+        sms = torch.cuda.get_device_properties(0).multi_processor_count
+    except Exception:
+        pass
+    return sms * 128 * 2 * mhz * 1e6 / 1e12, "derived: %d SMs x 128 FP32 lanes x 2 flop x %.0f MHz (%s)" % (
+        sms, mhz, src)
+
+
+def bh_inputs(n=N_BH):
+    from starflood_gb300.ics import uniform_ball
+    return uniform_ball(n, seed=2024)
+
+
+# ---------------------------------------------------------------------------
+# CPU reference path (the oracle restatement, or the compiled reference here)
+# ---------------------------------------------------------------------------
+def cpu_bh_rate(max_seconds=12.0, max_steps=200, n=N_BH):
+    from oracle import build as ob
+    ob.build_oracle()
+    from oracle.pyoracle import Oracle, make_params, slab_views
+    pos, vel, mas = bh_inputs(n)
+    orc = Oracle("f32")
+    p = make_params(dt=1e-3, eps=0.01, theta=0.5, use_tree=1)
+    sim, slab, nodes = orc.new_sim(n, p)
+    v = slab_views(slab, n, 13)
+    v["pos"][:] = pos
+    v["vel"][:] = vel
+    v["mas"][:] = mas
+    orc.sim_solv(p, sim, 0)
+    t0 = time.perf_counter()
+    steps = 0
+    while steps < max_steps and (time.perf_counter() - t0) < max_seconds:
+        orc.sim_step(p, sim, steps)
+        steps += 1
+    dt = time.perf_counter() - t0
+    return {"value": n * steps / dt, "unit": "particle-steps/s", "cores": orc.threads(), "kind": "port",
+            "sample": "%d sim_step calls of the N=%d Barnes-Hut workload (%.1f s)" % (steps, n, dt)}
+
+
+def cpu_pp_rate(max_seconds=10.0):
+    from oracle.pyoracle import Oracle, make_params
+    from starflood_gb300.ics import plummer
+    orc = Oracle("f32")
+    n = 32768
+    pos, _, mas = plummer(n, seed=5)
+    p = make_params(eps=0.005)
+    t0 = time.perf_counter()
+    evals = 0
+    while evals < 1 or (time.perf_counter() - t0) < max_seconds and evals < 20:
+        orc.pp(pos, mas, p)
+        evals += 1
+    dt = time.perf_counter() - t0
+    return {"value": float(n) * n * evals / dt, "unit": "interactions/s", "cores": orc.threads(), "kind": "port",
+            "sample": "%d solve_gravity_part_part evals at N=%d (per-interaction rate is size independent)" % (
+                evals, n)}
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def gpu_bh(steps, warmup, sf):
+    import ctypes as C
+    pos, vel, mas = bh_inputs()
+    n = N_BH
+    L = sf.lib()
+
+    def new_sim(flags):
+        p = sf.default_params(solver=sf.SOLVER_TREE, eps=0.01, dt=1e-3, theta=0.5, flags=flags)
+        s = sf.Sim(n, p)
+        s.set_state(pos, vel, mas)
+        s.solve(0)
+        return s
+
+    # --- headline: graph replays, L2 flushed between timed steps -------------
+    import torch
+    s = new_sim(0)
+    stream = s.stream()
+    ext = torch.cuda.ExternalStream(stream)
+    s.run(0, warmup)
+    s.sync()
+    launches0 = sf.lib().sfgpu_kernel_launches()
+    s.run(warmup, 1)  # the graph exists now; count one eager capture's launches below
+    s.sync()
+    events = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    rank, world, local = env_rank()
+    with ClockSampler(local) as clk:
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+        for k in range(steps):
+            sf.check(L.sfgpu_flush_l2(C.c_void_p(stream)), "flush")
+            with torch.cuda.stream(ext):
+                events[k][0].record(ext)
+            s.run(warmup + 1 + k, 1)
+            with torch.cuda.stream(ext):
+                events[k][1].record(ext)
+        s.sync()
+        torch.cuda.synchronize()
+    step_ms = [a.elapsed_time(b) for a, b in events]
+    total_ms = float(sum(step_ms))
+    status = s.status()
+    s.close()
+
+    # kernels per step: one eager (uncaptured) step
+    p0 = sf.default_params(solver=sf.SOLVER_TREE, eps=0.01, dt=1e-3, theta=0.5, flags=sf.FLAG_NOGRAPH)
+    with sf.Sim(n, p0) as s2:
+        s2.set_state(pos, vel, mas)
+        s2.solve(0)
+        s2.sync()
+        c0 = L.sfgpu_kernel_launches()
+        s2.step(0)
+        s2.sync()
+        per_step = int(L.sfgpu_kernel_launches() - c0)
+    del launches0
+
+    # --- instrumented twin: per-stage CUDA events, walk counters ------------
+    st = new_sim(sf.FLAG_TIMING)
+    st.run(0, warmup)
+    st.sync()
+    st.stage_times()
+    st.walk_totals()
+    for k in range(steps):
+        sf.check(L.sfgpu_flush_l2(C.c_void_p(st.stream())), "flush")
+        st.step(warmup + k)
+    st.sync()
+    stages = st.stage_times()
+    n_int, n_open = st.walk_totals()
+    st.close()
+
+    # --- e2e through the drop-in sim_step() ---------------------------------
+    e2e = gpu_bh_e2e(steps, warmup, sf, pos, vel, mas)
+    return dict(total_ms=total_ms, step_ms=step_ms, status=status, stages=stages, n_int=n_int, n_open=n_open,
+                per_step=per_step, clocks=clk.summary(), e2e=e2e)
+
+
+def gpu_bh_e2e(steps, warmup, sf, pos, vel, mas):
+    import ctypes as C
+    n = N_BH
+    L = sf.compat_functions()
+    sf.compat_configure(sf.default_params(solver=sf.SOLVER_TREE, eps=0.01, dt=1e-3, theta=0.5))
+    sim = sf.SimT()
+    sf.check(L.sim_init(C.byref(sim), n), "sim_init")
+    dof = 13
+    buf = (C.c_float * (n * dof)).from_address(sim.mem)
+    slab = np.frombuffer(buf, np.float32)
+    v = sf.slab_views(slab, n, dof)
+    v["pos"][:] = pos
+    v["vel"][:] = vel
+    v["mas"][:] = mas
+    sf.check(L.sim_solv(C.byref(sim)), "sim_solv")
+    for k in range(warmup):
+        sim.step_number = k
+        sf.check(L.sim_step(C.byref(sim)), "sim_step")
+    t0 = time.perf_counter()
+    for k in range(steps):
+        sim.step_number = warmup + k
+        sf.check(L.sim_step(C.byref(sim)), "sim_step")
+    dt = time.perf_counter() - t0
+    bytes_ = 4 * n * dof
+    L.sim_free(C.byref(sim))
+    return {"value": n * steps / dt, "unit": "particle-steps/s", "h2d_bytes_per_step": bytes_,
+            "d2h_bytes_per_step": bytes_, "api": "sim_step() of include/starflood_compat.h, host slab"}
+
+
+def gpu_pp(sf, reps=2):
+    from starflood_gb300.ics import plummer
+    pos, vel, mas = plummer(N_PP, seed=5)
+    out = {}
+    for name, form in (("plain", sf.FORM_PLAIN), ("compensated", sf.FORM_COMPENSATED)):
+        p = sf.default_params(solver=sf.SOLVER_PP, eps=0.005, dt=1e-3, form=form, flags=sf.FLAG_TIMING)
+        with sf.Sim(N_PP, p) as s:
+            s.set_state(pos, vel, mas)
+            s.solve(0)
+            s.sync()
+            s.stage_times()
+            for _ in range(reps):
+                s.solve(0)
+            s.sync()
+            ms = s.stage_times()["pp"][0] / reps
+        out[name] = {"interactions_per_s": float(N_PP) * N_PP / (ms * 1e-3), "ms_per_eval": ms}
+    return out
+
+
+def pp_accuracy(sf):
+    """Force error of plain vs compensated against the FP64 oracle on a seeded
+    8192-body subsample of the N=1,048,576 Plummer sphere (i in the sample,
+    all j)."""
+    from oracle.pyoracle import Oracle, make_params
+    from starflood_gb300.ics import plummer
+    import ctypes as C
+    n = N_PP
+    pos, vel, mas = plummer(n, seed=5)
+    rng = np.random.default_rng(8192)
+    sub = np.sort(rng.choice(n, 8192, replace=False))
+    o64 = Oracle("f64")
+    # FP64 reference forces on the subsample: sum over all j, done in chunks
+    a64 = np.zeros((len(sub), 3))
+    p64 = make_params(eps=0.005)
+    # the oracle computes all-pairs; restrict i by evaluating a reduced system
+    # per chunk of j (superposition of partial sums)
+    pos64 = pos.astype(np.float64)
+    for j0 in range(0, n, 65536):
+        j1 = min(n, j0 + 65536)
+        xi = pos64[sub][:, None, :]
+        xj = pos64[j0:j1][None, :, :]
+        d = xi - xj
+        r2 = (d * d).sum(-1) + 0.005 ** 2
+        w = mas[j0:j1].astype(np.float64)[None, :] / (r2 * np.sqrt(r2))
+        a64 -= (d * w[..., None]).sum(1)
+    a64 *= mas[sub].astype(np.float64)[:, None]
+    del o64, p64
+    errs = {}
+    for name, form in (("plain", sf.FORM_PLAIN), ("compensated", sf.FORM_COMPENSATED)):
+        p = sf.default_params(solver=sf.SOLVER_PP, eps=0.005, form=form)
+        with sf.Sim(n, p) as s:
+            s.set_state(pos, vel, mas)
+            s.solve(0)
+            v = sf.slab_views(s.download(), n, 13)
+        a = v["acc"][sub].astype(np.float64)
+        errs[name] = float(np.linalg.norm(a - a64) / np.linalg.norm(a64))
+    return errs
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-pp", action="store_true", help="skip the N=1M PP sub-benchmark")
+    args = ap.parse_args()
+    rank, world, local = env_rank()
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        cb = cpu_bh_rate(max_seconds=min(60.0, 3.0 + 1.0 * args.steps), max_steps=args.steps + args.warmup)
+        line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "particle-steps/s",
+                "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": N_BH / cb["value"] * 1e3, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded uniform sphere)",
+                "config": {"workload": WORKLOAD, "N": N_BH, "parallelism": "host OpenMP"},
+                "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": "particle-steps/s",
+                                            "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    if world > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    import __graft_entry__
+    if rank == 0 or not os.path.exists(os.path.join(ROOT, "starflood_gb300", "libsfgpu.so")):
+        __graft_entry__.build()
+    if world > 1:
+        dist.barrier()
+    import starflood_gb300 as sf
+
+    r = gpu_bh(args.steps, args.warmup, sf)
+    t_ms = r["total_ms"]
+    if world > 1:
+        t = torch.tensor([t_ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_ms = float(t.item())
+    value = world * N_BH * args.steps / (t_ms * 1e-3)
+
+    peak, peak_src = fp32_peak_tflops()
+    walk_ms, walk_launches = r["stages"].get("walk", (0.0, 0))
+    walk_avg_ms = walk_ms / max(1, walk_launches)
+    flops_per_launch = (FLOP_INTERACTION * r["n_int"] + FLOP_OPEN * r["n_open"]) / max(1, walk_launches)
+    achieved = flops_per_launch / (walk_avg_ms * 1e-3) / 1e12 if walk_avg_ms > 0 else 0.0
+    stage_ms = {k: round(v[0] / max(1, v[1]), 4) for k, v in r["stages"].items()}
+
+    line = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded uniform unit sphere, pcg4d)",
+            "config": {"workload": WORKLOAD, "N": N_BH, "leaf": 8,
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "l2": "flushed between timed steps (256 MiB memset, untimed)",
+                       "step": "one CUDA-graph replay of sim_step (kick, drift, bounds, tree build, walk, kick, energies)"},
+            "clocks": r["clocks"], "e2e": r["e2e"], "gpu_launches": r["per_step"] * args.steps,
+            "roofline": {"kernel": "k_walk (Barnes-Hut walk)", "bound": "fp32", "achieved": achieved,
+                         "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
+                         "traffic": None, "peak_source": peak_src,
+                         "flops_per_launch": flops_per_launch, "avg_launch_ms": walk_avg_ms,
+                         "interactions_per_step": r["n_int"] / max(1, walk_launches),
+                         "opening_tests_per_step": r["n_open"] / max(1, walk_launches)},
+            "stage_ms_per_step": stage_ms, "device_status": r["status"]}
+    if rank == 0:
+        try:
+            line["cpu_baseline"] = cpu_bh_rate(max_seconds=10.0)
+        except Exception as e:  # the baseline must not hide the GPU line
+            line["cpu_baseline"] = {"error": str(e)}
+        if not args.no_pp:
+            pp = gpu_pp(sf)
+            try:
+                pp["force_error_vs_fp64"] = pp_accuracy(sf)
+            except Exception as e:
+                pp["force_error_vs_fp64"] = {"error": str(e)}
+            for k in ("plain", "compensated"):
+                ips = pp[k]["interactions_per_s"]
+                pp[k]["roofline_frac"] = ips * FLOP_INTERACTION / (peak * 1e12)
+            try:
+                pp["cpu_baseline"] = cpu_pp_rate()
+            except Exception as e:
+                pp["cpu_baseline"] = {"error": str(e)}
+            pp["workload"] = "PP gravity N=1048576 Plummer a=1 M=1 eps=0.005, 20 flop/interaction"
+            line["pp"] = pp
+        print(json.dumps(line))
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,247 @@
+/*
+ * sfgpu.h -- C ABI of starflood_gb300: Starflood's force-and-step path
+ * (particle-particle gravity, Barnes-Hut octree build and walk, SPH, and the
+ * kick-drift-kick leapfrog) as hand-written CUDA kernels for one GB300
+ * (sm_103a), with particle state resident in HBM across steps.
+ *
+ * Two layers sit on this ABI:
+ *   - this file: resident-mode handles (sfgpu_sim) plus the new precision,
+ *     batched and adjoint forms;
+ *   - starflood_compat.h: the reference's own function surface (sim_init,
+ *     sim_solv, sim_step, tree_build, solve_gravity_part_*, solve_sph over
+ *     sim_t) implemented on top of this one, for drop-in replacement.
+ *
+ * Conventions: every int-returning call returns SFGPU_OK (0) on success and
+ * SFGPU_FAILURE (-1) on failure, like the reference's STARFLOOD_SUCCESS /
+ * STARFLOOD_FAILURE (src/common.h:31-32); the reason is then available from
+ * sfgpu_last_error().  Arrays follow the reference slab layout
+ * (src/simulation.h:17-51): one block of N*dof floats where array k starts
+ * at k*N, positions / velocities / accelerations are xyz-interleaved.
+ * Calls on one sfgpu_sim are not re-entrant (like the reference, whose
+ * sim_* functions share global logs, src/simulation.c:24-30).
+ */
+#ifndef SFGPU_H
+#define SFGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SFGPU_OK 0
+#define SFGPU_FAILURE (-1)
+
+/* Which gravity solver sim_solv runs (reference: ENABLE_TREE, config.h:38). */
+enum sfgpu_solver { SFGPU_SOLVER_PP = 0, SFGPU_SOLVER_TREE = 1 };
+
+/* SPH (reference: ENABLE_SPH, config.h:190).  REFERENCE is the reference's
+ * Gaussian-kernel SPH of src/sph.c; CUBIC is the cubic-spline SPH with an
+ * ideal-gas equation of state and Monaghan artificial viscosity (new form,
+ * no reference counterpart). */
+enum sfgpu_sph { SFGPU_SPH_OFF = 0, SFGPU_SPH_REFERENCE = 1, SFGPU_SPH_CUBIC = 2 };
+
+/* Arithmetic of the force kernels.
+ *   EXACT: the reference's FP32 expressions and order (IEEE divide and square
+ *          root, Kahan sums per interaction) -- bit-identical to the
+ *          reference for PP and KDK.
+ *   FAST:  hardware reciprocal square root and fused multiply-adds. */
+enum sfgpu_math { SFGPU_MATH_FAST = 0, SFGPU_MATH_EXACT = 1 };
+
+/* Precision form.  PLAIN keeps the reference's FP32 state.  COMPENSATED
+ * keeps FP32 pair arithmetic but accumulates forces with two-sum
+ * compensation per j-tile, holds positions and velocities in FP64 for the
+ * leapfrog and centre-of-mass sums in FP64. */
+enum sfgpu_form { SFGPU_FORM_PLAIN = 0, SFGPU_FORM_COMPENSATED = 1 };
+
+/* What "acc" holds.  REFERENCE: acc_i = -G m_i sum_j m_j r_ij/(r^2+eps^2)^1.5,
+ * the m_i-scaled force the reference integrates as an acceleration
+ * (src/gravity.c:808-811).  PHYSICAL: the acceleration itself (no m_i). */
+enum sfgpu_acc { SFGPU_ACC_REFERENCE = 0, SFGPU_ACC_PHYSICAL = 1 };
+
+typedef struct {
+    double   dt;          /* TIMESTEP_SIZE (config.h:159)                   */
+    double   eps;         /* EPSILON, Plummer softening (config.h:162), > 0 */
+    double   G;           /* G (config.h:167)                               */
+    double   theta;       /* TREE_THETA, compared with (w/d)^2 (gravity.c:448) */
+    int32_t  solver;      /* enum sfgpu_solver                              */
+    int32_t  sph;         /* enum sfgpu_sph                                 */
+    int32_t  math;        /* enum sfgpu_math                                */
+    int32_t  form;        /* enum sfgpu_form                                */
+    int32_t  acc_mode;    /* enum sfgpu_acc                                 */
+    uint32_t leaf_cap;    /* bodies per leaf; 8 in the reference (tree.h:20), <= 16 */
+    uint32_t depth_max;   /* TREE_DEPTH_MAX (config.h:41), <= 16            */
+    uint32_t nodes_max;   /* TREE_NODES_MAX (config.h:44)                   */
+    double   sph_gamma;   /* CUBIC: adiabatic index                         */
+    double   sph_alpha;   /* CUBIC: Monaghan viscosity alpha                */
+    double   sph_beta;    /* CUBIC: Monaghan viscosity beta                 */
+    uint32_t flags;       /* SFGPU_FLAG_*                                   */
+    uint32_t reserved[7];
+} sfgpu_params;
+
+/* flags */
+#define SFGPU_FLAG_STATS   0x1u  /* count walk interactions / opening tests per particle */
+#define SFGPU_FLAG_TIMING  0x2u  /* record CUDA-event times per stage            */
+#define SFGPU_FLAG_NOGRAPH 0x4u  /* sfgpu_run launches kernels one by one         */
+#define SFGPU_FLAG_EXPORT_TREE 0x8u /* compat sim_solv/sim_step also fill sim_t.tree.node */
+#define SFGPU_FLAG_VERBOSE 0x10u /* compat sim_step prints the energies like the reference */
+
+/* Device status word bits (sfgpu_status). */
+#define SFGPU_STATUS_TREE_NODES   0x01u /* node capacity exceeded (tree.c:224)   */
+#define SFGPU_STATUS_TREE_DEPTH   0x02u /* depth limit exceeded  (tree.c:230)    */
+#define SFGPU_STATUS_TIES         0x04u /* too many bodies exactly on cell midplanes */
+#define SFGPU_STATUS_SPIN         0x08u /* a bounded device wait gave up         */
+#define SFGPU_STATUS_WALK         0x10u /* walk stack or iteration bound hit     */
+#define SFGPU_STATUS_SPH_CELLS    0x20u /* SPH cell grid capacity exceeded       */
+
+/* The reference's compiled-in defaults (src/config.h): dt=1, eps=1e-3, G=1,
+ * theta=0.5, tree on, SPH off, leaf 8, depth 16, 262144 nodes; FAST math,
+ * PLAIN form, REFERENCE acc. */
+void sfgpu_params_default(sfgpu_params* p);
+
+/* Number of reals per particle in the slab: 13, or 16 with SPH
+ * (SIM_DOF, src/simulation.h:46). */
+uint32_t sfgpu_dof(const sfgpu_params* p);
+
+/* Message for the last failure on the calling thread ("" if none). */
+const char* sfgpu_last_error(void);
+
+/* ---- resident simulations -------------------------------------------- */
+typedef struct sfgpu_sim sfgpu_sim;
+
+/* Replaces sim_init (src/simulation.c:55-187): allocates the device slab
+ * (zeroed, like the reference's memset) and every work array. */
+int sfgpu_create(sfgpu_sim** out, uint32_t n, const sfgpu_params* p);
+/* Replaces sim_free (src/simulation.c:189-228). */
+int sfgpu_destroy(sfgpu_sim* s);
+
+/* Copy a whole host slab (N*dof floats, reference layout) to / from HBM.
+ * Synchronous with respect to the host. */
+int sfgpu_upload(sfgpu_sim* s, const float* slab);
+int sfgpu_download(sfgpu_sim* s, float* slab);
+/* Copy only arrays [first, first+count) of the slab (count*N floats). */
+int sfgpu_upload_arrays(sfgpu_sim* s, const float* slab, uint32_t first, uint32_t count);
+int sfgpu_download_arrays(sfgpu_sim* s, float* slab, uint32_t first, uint32_t count);
+
+/* Replaces sim_solv (src/simulation.c:230-345): forces and potentials for the
+ * current positions; the tree's root cube is jittered with step_number. */
+int sfgpu_solve(sfgpu_sim* s, uint32_t step_number);
+/* Replaces sim_step (src/simulation.c:347-519): kick, drift, solve, kick,
+ * per-particle energies and their FP64 totals.  Asynchronous: returns once
+ * the work is queued on the simulation's stream. */
+int sfgpu_step(sfgpu_sim* s, uint32_t step_number);
+/* nsteps consecutive sfgpu_step calls with step numbers first, first+1, ...
+ * replayed from a captured CUDA graph (unless SFGPU_FLAG_NOGRAPH). */
+int sfgpu_run(sfgpu_sim* s, uint32_t first_step, uint32_t nsteps);
+/* Wait for queued work. */
+int sfgpu_synchronize(sfgpu_sim* s);
+/* FP64 kinetic and potential energy totals of the last step, as the
+ * reference prints them (src/simulation.c:453-503): T = sum ken, V = sum pen.
+ * Synchronises. */
+int sfgpu_energies(sfgpu_sim* s, double* T, double* V);
+/* Energy with the double counting and self terms removed:
+ * E = T + V/2 - (1/2) sum_i G m_i^2 / eps  (REFERENCE acc) . Synchronises. */
+int sfgpu_energies_corrected(sfgpu_sim* s, double* T, double* V, double* E);
+/* Device status word (SFGPU_STATUS_* bits) accumulated since the last call;
+ * reading it clears it.  Synchronises. */
+int sfgpu_status(sfgpu_sim* s, uint32_t* status);
+
+/* The simulation's CUDA stream (a cudaStream_t) and its device slab. */
+void* sfgpu_stream(sfgpu_sim* s);
+float* sfgpu_device_slab(sfgpu_sim* s);
+
+/* Stage timings (ms, summed since the last call) recorded with CUDA events
+ * when SFGPU_FLAG_TIMING is set.  names/ms arrays of length cap; returns
+ * the number of stages written. */
+int sfgpu_stage_times(sfgpu_sim* s, const char** names, double* ms, uint32_t* launches, int cap);
+
+/* Per-particle walk counters of the last tree solve (SFGPU_FLAG_STATS):
+ * monopole interactions and opening tests, by particle index. */
+int sfgpu_walk_stats(sfgpu_sim* s, uint32_t* interactions, uint32_t* opening_tests);
+/* Totals of the same counters (no flag needed). */
+int sfgpu_walk_totals(sfgpu_sim* s, uint64_t* interactions, uint64_t* opening_tests);
+
+/* Replaces tree_build (src/tree.c:74-318) for the positions and masses
+ * already on the device: builds in the given root cube (min xyz, max xyz).
+ * The status word reports node or depth overflow (tree.c:224-233). */
+int sfgpu_tree_build(sfgpu_sim* s, const float bounds[6]);
+/* Replaces solve_gravity_part_tree (src/gravity.c:242-663): walks the last
+ * built tree for the current positions. */
+int sfgpu_gravity_tree(sfgpu_sim* s);
+/* Replaces solve_gravity_part_part (src/gravity.c:666-819) on the slab. */
+int sfgpu_gravity_part(sfgpu_sim* s);
+/* Replaces solve_sph (src/sph.c:14-282), or runs the cubic-spline SPH. */
+int sfgpu_solve_sph(sfgpu_sim* s);
+
+/* ---- tree inspection ---------------------------------------------------- */
+/* Sorted 48-bit octree keys (3 bits per level, level 0 most significant,
+ * octant bit 0 = x, 1 = y, 2 = z), the particle index of each sorted slot,
+ * the number of particles inside the root cube, and the root cube. */
+int sfgpu_tree_keys(sfgpu_sim* s, uint64_t* keys, uint32_t* index, uint32_t* n_inside,
+                    float bounds[6]);
+/* Number of nodes of the last build (1 + 8 * splits). */
+int sfgpu_tree_num_nodes(sfgpu_sim* s, uint32_t* num_nodes);
+/* The last build in the reference's node_t numbering and meaning
+ * (src/tree.h:16-25): parent, bodies, branch[8] (child node ids, or the
+ * particle ids of a leaf in insertion order), bounds[6], params[4] =
+ * {COM x, y, z, mass}.  Arrays hold num_nodes entries. */
+int sfgpu_tree_export(sfgpu_sim* s, uint32_t* parent, uint32_t* bodies, uint32_t* branch8,
+                      float* bounds6, float* params4);
+
+/* ---- process utilities ------------------------------------------------- */
+/* Kernel launches the host has issued through this library in this process.
+ * Replays of a captured CUDA graph issue no host launches and are not
+ * counted: a replayed step runs the kernels counted while capturing it. */
+unsigned long long sfgpu_kernel_launches(void);
+/* Page-lock a host range so that uploads / downloads run at full speed. */
+int sfgpu_host_register(void* ptr, size_t bytes);
+int sfgpu_host_unregister(void* ptr);
+/* Overwrite a 256 MiB device buffer (larger than the L2) on a stream, so
+ * that the next kernel starts with a cold L2. */
+int sfgpu_flush_l2(void* stream);
+
+/* ---- stateless solver calls on device arrays ---------------------------- */
+/* All pointers are device pointers in the reference layout; stream is a
+ * cudaStream_t (NULL = default stream).  Work space is allocated and cached
+ * per calling thread and device. */
+/* solve_gravity_part_part (src/gravity.c:666-819) */
+int sfgpu_gravity_pp(const sfgpu_params* p, uint32_t n, const float* pos, const float* mas,
+                     float* acc, float* pot, void* stream);
+
+/* ---- batched form ------------------------------------------------------- */
+/* Many independent systems of uneven size in one launch per step.  Systems
+ * are concatenated: system b owns particles [offset[b], offset[b+1]).
+ * pos/vel/acc are (total, 3), mas/pot (total). */
+typedef struct sfgpu_batch sfgpu_batch;
+int sfgpu_batch_create(sfgpu_batch** out, uint32_t nsys, const uint32_t* offsets,
+                       const sfgpu_params* p);
+int sfgpu_batch_destroy(sfgpu_batch* b);
+int sfgpu_batch_upload(sfgpu_batch* b, const float* pos, const float* vel, const float* mas);
+int sfgpu_batch_download(sfgpu_batch* b, float* pos, float* vel, float* acc, float* pot);
+/* Forces for all systems (one persistent launch). */
+int sfgpu_batch_solve(sfgpu_batch* b);
+/* nsteps KDK steps for all systems, replayed from one CUDA graph. */
+int sfgpu_batch_run(sfgpu_batch* b, uint32_t nsteps);
+/* Pick the tile shape by timing the candidates on this batch (autotuner);
+ * returns the chosen configuration index. */
+int sfgpu_batch_autotune(sfgpu_batch* b, int* chosen);
+int sfgpu_batch_synchronize(sfgpu_batch* b);
+void* sfgpu_batch_stream(sfgpu_batch* b);
+
+/* ---- adjoint (VJP) form ------------------------------------------------- */
+/* Reverse-mode gradient of loss = sum_b mean_i |x_i|^2 (final step) of the
+ * batch trajectory with respect to the initial positions and velocities,
+ * with checkpoints every `checkpoint` steps and recomputation in between.
+ * The batch state is left at the final step; grads are (total, 3).
+ * loss (may be NULL) receives the loss. */
+int sfgpu_batch_grad(sfgpu_batch* b, uint32_t nsteps, uint32_t checkpoint, float* grad_pos,
+                     float* grad_vel, double* loss);
+/* Single VJP of the softened PP force: given cotangents abar (total, 3) of
+ * the accelerations, accumulate xbar += (d acc / d pos)^T abar. Device ptrs. */
+int sfgpu_batch_force_vjp(sfgpu_batch* b, const float* d_abar, float* d_xbar);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

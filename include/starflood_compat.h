@@ -1,0 +1,106 @@
+/*
+ * starflood_compat.h -- the reference's own function surface, implemented by
+ * libsfgpu.so on the GPU.  A program written against Starflood's headers
+ * (src/simulation.h, src/tree.h, src/gravity.h, src/sph.h) links against
+ * libsfgpu.so instead of the reference objects and runs unchanged; this
+ * header restates the same declarations for programs built without them.
+ *
+ * ABI (FP32 build of the reference, ENABLE_TREE defined as shipped):
+ *   real = float, uint = uint32_t, node_t 80 bytes, tree_t, sim_t below.
+ * The slab mem holds N * SIM_DOF reals (13, or 16 with SPH) in the order of
+ * enum sim_conf; the library keeps an HBM copy per sim_t, keyed by mem.
+ *
+ * The reference fixes dt, eps, G, theta, the solver and SPH at compile time
+ * (src/config.h); here they are run-time parameters set with
+ * sfgpu_compat_configure() before sim_init (defaults: the shipped config.h).
+ * Every call uploads what it reads and downloads what it writes, so host
+ * arrays are current after each call, as with the reference.
+ */
+#ifndef STARFLOOD_COMPAT_H
+#define STARFLOOD_COMPAT_H
+
+#include <stdint.h>
+
+#include "sfgpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#ifndef STARFLOOD_COMPAT_NO_TYPES
+typedef float real;  /* src/types.h:19-23 (FP32 build) */
+
+/* src/simulation.h:17-51 */
+enum sim_conf {
+    _SIM_POS_0, _SIM_POS_1, _SIM_POS_2,
+    _SIM_VEL_0, _SIM_VEL_1, _SIM_VEL_2,
+    _SIM_ACC_0, _SIM_ACC_1, _SIM_ACC_2,
+    SIM_MAS, SIM_POT, SIM_KEN, SIM_PEN,
+    SIM_RAD, SIM_RHO, SIM_PRS,   /* present when SPH is enabled */
+    SIM_POS = _SIM_POS_0, SIM_VEL = _SIM_VEL_0, SIM_ACC = _SIM_ACC_0
+};
+
+/* src/tree.h:16-25 */
+typedef struct {
+    uint32_t parent;
+    uint32_t bodies;
+    uint32_t branch[8];
+    real bounds[6];
+    real params[4];
+} node_t;
+
+/* src/tree.h:28-35 */
+typedef struct {
+    uint32_t max_nodes;
+    uint32_t num_nodes;
+    real bounds[6];
+    node_t* node;
+} tree_t;
+
+/* src/simulation.h:53-67 (ENABLE_TREE defined, ENABLE_GRID not) */
+typedef struct {
+    unsigned int step_number;
+    unsigned int N;
+    void* mem;
+    tree_t tree;
+} sim_t;
+#endif
+
+/* Parameters used by every entry point below (process-wide). */
+int sfgpu_compat_configure(const sfgpu_params* p);
+void sfgpu_compat_params(sfgpu_params* out);
+/* The device simulation behind a sim_t (NULL if none). */
+sfgpu_sim* sfgpu_compat_handle(const sim_t* sim);
+
+/* src/simulation.c:33-53 */
+real* sim_find(const sim_t* sim, enum sim_conf parameter);
+/* src/simulation.c:55-187 */
+int sim_init(sim_t* sim, unsigned int N);
+/* src/simulation.c:189-228 */
+int sim_free(sim_t* sim);
+/* src/simulation.c:230-345 (without SOLVER_VIS) */
+int sim_solv(sim_t* sim);
+/* src/simulation.c:347-519 (without SOLVER_VIS) */
+int sim_step(sim_t* sim);
+/* src/simulation.h:90-95, the SOLVER_VIS signatures; the render buffer is
+ * ignored (tree-walk debug drawing is not part of this library). */
+int sim_solv_vis(sim_t* sim, float* render_buffer, unsigned int sizex, unsigned int sizey);
+int sim_step_vis(sim_t* sim, float* render_buffer, unsigned int sizex, unsigned int sizey);
+/* src/tree.c:14-55 */
+int tree_init(tree_t* tree, unsigned int max_nodes);
+/* src/tree.c:57-72 */
+int tree_free(tree_t* tree);
+/* src/tree.c:74-318: builds on the GPU and writes the node_t array in the
+ * reference's numbering; returns -1 on node or depth overflow. */
+int tree_build(tree_t* tree, unsigned int num_parts, const real* pos, const real* mas);
+/* src/gravity.c:242-663 */
+int solve_gravity_part_tree(const sim_t* sim);
+/* src/gravity.c:666-819 */
+int solve_gravity_part_part(const sim_t* sim);
+/* src/sph.c:14-282 */
+int solve_sph(const sim_t* sim);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,330 @@
+"""starflood_gb300 -- Starflood's force-and-step path on one GB300.
+
+Python host mirror of the C ABI in include/sfgpu.h (resident simulations)
+and include/starflood_compat.h (the reference's sim_t surface), through
+ctypes.  The compute path is libsfgpu.so (hand-written CUDA for sm_103a);
+there is no fallback: importing works without a GPU, but every call that
+reaches the device fails loudly when the library or a GPU is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libsfgpu.so")
+
+SOLVER_PP, SOLVER_TREE = 0, 1
+SPH_OFF, SPH_REFERENCE, SPH_CUBIC = 0, 1, 2
+MATH_FAST, MATH_EXACT = 0, 1
+FORM_PLAIN, FORM_COMPENSATED = 0, 1
+ACC_REFERENCE, ACC_PHYSICAL = 0, 1
+FLAG_STATS, FLAG_TIMING, FLAG_NOGRAPH, FLAG_EXPORT_TREE, FLAG_VERBOSE = 0x1, 0x2, 0x4, 0x8, 0x10
+STATUS_TREE_NODES, STATUS_TREE_DEPTH, STATUS_TIES, STATUS_SPIN, STATUS_WALK, STATUS_SPH_CELLS = (
+    0x01, 0x02, 0x04, 0x08, 0x10, 0x20)
+
+
+class SfgpuError(RuntimeError):
+    pass
+
+
+class Params(C.Structure):
+    """sfgpu_params (include/sfgpu.h)."""
+    _fields_ = [("dt", C.c_double), ("eps", C.c_double), ("G", C.c_double), ("theta", C.c_double),
+                ("solver", C.c_int32), ("sph", C.c_int32), ("math", C.c_int32), ("form", C.c_int32),
+                ("acc_mode", C.c_int32), ("leaf_cap", C.c_uint32), ("depth_max", C.c_uint32),
+                ("nodes_max", C.c_uint32), ("sph_gamma", C.c_double), ("sph_alpha", C.c_double),
+                ("sph_beta", C.c_double), ("flags", C.c_uint32), ("reserved", C.c_uint32 * 7)]
+
+
+_lib = None
+
+
+def lib():
+    """The loaded libsfgpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise SfgpuError("libsfgpu.so is missing: run `python -c 'import __graft_entry__ as g; g.build()'`")
+        L = C.CDLL(LIB_PATH)
+        vp, u32, i32, f32p, u32p = C.c_void_p, C.c_uint32, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_uint32)
+        P = C.POINTER(Params)
+        sig = {
+            "sfgpu_params_default": (None, [P]),
+            "sfgpu_dof": (u32, [P]),
+            "sfgpu_last_error": (C.c_char_p, []),
+            "sfgpu_create": (i32, [C.POINTER(vp), u32, P]),
+            "sfgpu_destroy": (i32, [vp]),
+            "sfgpu_upload": (i32, [vp, vp]),
+            "sfgpu_download": (i32, [vp, vp]),
+            "sfgpu_upload_arrays": (i32, [vp, vp, u32, u32]),
+            "sfgpu_download_arrays": (i32, [vp, vp, u32, u32]),
+            "sfgpu_solve": (i32, [vp, u32]),
+            "sfgpu_step": (i32, [vp, u32]),
+            "sfgpu_run": (i32, [vp, u32, u32]),
+            "sfgpu_synchronize": (i32, [vp]),
+            "sfgpu_energies": (i32, [vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+            "sfgpu_energies_corrected": (i32, [vp, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                               C.POINTER(C.c_double)]),
+            "sfgpu_status": (i32, [vp, u32p]),
+            "sfgpu_stream": (vp, [vp]),
+            "sfgpu_device_slab": (vp, [vp]),
+            "sfgpu_stage_times": (i32, [vp, C.POINTER(C.c_char_p), C.POINTER(C.c_double), u32p, i32]),
+            "sfgpu_walk_stats": (i32, [vp, u32p, u32p]),
+            "sfgpu_walk_totals": (i32, [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+            "sfgpu_tree_build": (i32, [vp, f32p]),
+            "sfgpu_gravity_tree": (i32, [vp]),
+            "sfgpu_gravity_part": (i32, [vp]),
+            "sfgpu_solve_sph": (i32, [vp]),
+            "sfgpu_tree_keys": (i32, [vp, C.POINTER(C.c_uint64), u32p, u32p, f32p]),
+            "sfgpu_tree_num_nodes": (i32, [vp, u32p]),
+            "sfgpu_tree_export": (i32, [vp, u32p, u32p, u32p, f32p, f32p]),
+            "sfgpu_gravity_pp": (i32, [P, u32, vp, vp, vp, vp, vp]),
+            "sfgpu_batch_create": (i32, [C.POINTER(vp), u32, u32p, P]),
+            "sfgpu_batch_destroy": (i32, [vp]),
+            "sfgpu_batch_upload": (i32, [vp, vp, vp, vp]),
+            "sfgpu_batch_download": (i32, [vp, vp, vp, vp, vp]),
+            "sfgpu_batch_solve": (i32, [vp]),
+            "sfgpu_batch_run": (i32, [vp, u32]),
+            "sfgpu_batch_autotune": (i32, [vp, C.POINTER(C.c_int)]),
+            "sfgpu_batch_synchronize": (i32, [vp]),
+            "sfgpu_batch_stream": (vp, [vp]),
+            "sfgpu_batch_grad": (i32, [vp, u32, u32, vp, vp, C.POINTER(C.c_double)]),
+            "sfgpu_batch_force_vjp": (i32, [vp, vp, vp]),
+            "sfgpu_kernel_launches": (C.c_ulonglong, []),
+            "sfgpu_host_register": (i32, [vp, C.c_size_t]),
+            "sfgpu_host_unregister": (i32, [vp]),
+            "sfgpu_flush_l2": (i32, [vp]),
+            "sfgpu_compat_configure": (i32, [P]),
+            "sfgpu_compat_params": (None, [P]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def last_error() -> str:
+    return (lib().sfgpu_last_error() or b"").decode()
+
+
+def check(rc, what=""):
+    if rc != 0:
+        raise SfgpuError("%s failed: %s" % (what, last_error()))
+
+
+def default_params(**kw) -> Params:
+    """The reference's config.h defaults, then keyword overrides."""
+    p = Params()
+    lib().sfgpu_params_default(C.byref(p))
+    for k, v in kw.items():
+        if not hasattr(p, k):
+            raise KeyError(k)
+        setattr(p, k, v)
+    return p
+
+
+def dof(p: Params) -> int:
+    return int(lib().sfgpu_dof(C.byref(p)))
+
+
+def _ptr(a: np.ndarray):
+    return C.c_void_p(a.ctypes.data)
+
+
+class Sim:
+    """A resident simulation (sfgpu_sim) of N bodies."""
+
+    def __init__(self, n: int, params: Params):
+        self.n = int(n)
+        self.params = params
+        self.dof = dof(params)
+        h = C.c_void_p()
+        check(lib().sfgpu_create(C.byref(h), self.n, C.byref(params)), "sfgpu_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().sfgpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # host transfers ------------------------------------------------------
+    def upload(self, slab: np.ndarray):
+        slab = np.ascontiguousarray(slab, np.float32)
+        assert slab.size == self.n * self.dof
+        check(lib().sfgpu_upload(self.h, _ptr(slab)), "sfgpu_upload")
+
+    def download(self) -> np.ndarray:
+        out = np.empty(self.n * self.dof, np.float32)
+        check(lib().sfgpu_download(self.h, _ptr(out)), "sfgpu_download")
+        return out
+
+    def set_state(self, pos, vel, mas, rad=None):
+        slab = np.zeros(self.n * self.dof, np.float32)
+        n = self.n
+        slab[0:3 * n] = np.asarray(pos, np.float32).ravel()
+        slab[3 * n:6 * n] = np.asarray(vel, np.float32).ravel()
+        slab[9 * n:10 * n] = np.asarray(mas, np.float32)
+        if rad is not None:
+            slab[13 * n:14 * n] = np.asarray(rad, np.float32)
+        self.upload(slab)
+        return slab
+
+    # steps -----------------------------------------------------------------
+    def solve(self, step=0):
+        check(lib().sfgpu_solve(self.h, step), "sfgpu_solve")
+
+    def step(self, step):
+        check(lib().sfgpu_step(self.h, step), "sfgpu_step")
+
+    def run(self, first, nsteps):
+        check(lib().sfgpu_run(self.h, first, nsteps), "sfgpu_run")
+
+    def sync(self):
+        check(lib().sfgpu_synchronize(self.h), "sfgpu_synchronize")
+
+    def energies(self):
+        T, V = C.c_double(), C.c_double()
+        check(lib().sfgpu_energies(self.h, C.byref(T), C.byref(V)), "sfgpu_energies")
+        return T.value, V.value
+
+    def energies_corrected(self):
+        T, V, E = C.c_double(), C.c_double(), C.c_double()
+        check(lib().sfgpu_energies_corrected(self.h, C.byref(T), C.byref(V), C.byref(E)), "energies")
+        return T.value, V.value, E.value
+
+    def status(self) -> int:
+        s = C.c_uint32()
+        check(lib().sfgpu_status(self.h, C.byref(s)), "sfgpu_status")
+        return s.value
+
+    def stream(self) -> int:
+        return int(lib().sfgpu_stream(self.h) or 0)
+
+    def stage_times(self):
+        cap = 64
+        names = (C.c_char_p * cap)()
+        ms = (C.c_double * cap)()
+        la = (C.c_uint32 * cap)()
+        m = lib().sfgpu_stage_times(self.h, names, ms, la, cap)
+        if m < 0:
+            raise SfgpuError(last_error())
+        return {names[i].decode(): (ms[i], la[i]) for i in range(m)}
+
+    def walk_stats(self):
+        a = np.zeros(self.n, np.uint32)
+        b = np.zeros(self.n, np.uint32)
+        check(lib().sfgpu_walk_stats(self.h, a.ctypes.data_as(C.POINTER(C.c_uint32)),
+                                     b.ctypes.data_as(C.POINTER(C.c_uint32))), "sfgpu_walk_stats")
+        return a, b
+
+    def walk_totals(self):
+        a, b = C.c_uint64(), C.c_uint64()
+        check(lib().sfgpu_walk_totals(self.h, C.byref(a), C.byref(b)), "sfgpu_walk_totals")
+        return a.value, b.value
+
+    def tree_build(self, bounds):
+        b = np.ascontiguousarray(bounds, np.float32)
+        check(lib().sfgpu_tree_build(self.h, b.ctypes.data_as(C.POINTER(C.c_float))), "sfgpu_tree_build")
+
+    def gravity_tree(self):
+        check(lib().sfgpu_gravity_tree(self.h), "sfgpu_gravity_tree")
+
+    def gravity_part(self):
+        check(lib().sfgpu_gravity_part(self.h), "sfgpu_gravity_part")
+
+    def solve_sph(self):
+        check(lib().sfgpu_solve_sph(self.h), "sfgpu_solve_sph")
+
+    def tree_keys(self):
+        keys = np.zeros(self.n, np.uint64)
+        idx = np.zeros(self.n, np.uint32)
+        nin = C.c_uint32()
+        b = np.zeros(6, np.float32)
+        check(lib().sfgpu_tree_keys(self.h, keys.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                    idx.ctypes.data_as(C.POINTER(C.c_uint32)), C.byref(nin),
+                                    b.ctypes.data_as(C.POINTER(C.c_float))), "sfgpu_tree_keys")
+        return keys, idx, nin.value, b
+
+    def num_nodes(self):
+        nn = C.c_uint32()
+        check(lib().sfgpu_tree_num_nodes(self.h, C.byref(nn)), "sfgpu_tree_num_nodes")
+        return nn.value
+
+    def tree_export(self):
+        nn = self.num_nodes()
+        u = C.POINTER(C.c_uint32)
+        f = C.POINTER(C.c_float)
+        parent = np.zeros(nn, np.uint32)
+        bodies = np.zeros(nn, np.uint32)
+        branch = np.zeros((nn, 8), np.uint32)
+        bounds = np.zeros((nn, 6), np.float32)
+        params = np.zeros((nn, 4), np.float32)
+        check(lib().sfgpu_tree_export(self.h, parent.ctypes.data_as(u), bodies.ctypes.data_as(u),
+                                      branch.ctypes.data_as(u), bounds.ctypes.data_as(f),
+                                      params.ctypes.data_as(f)), "sfgpu_tree_export")
+        return dict(parent=parent, bodies=bodies, branch=branch, bounds=bounds, params=params)
+
+
+def slab_views(slab: np.ndarray, n: int, dof_: int):
+    """Views of a slab in the reference layout (src/simulation.h:17-51)."""
+    v = {"pos": slab[0:3 * n].reshape(n, 3), "vel": slab[3 * n:6 * n].reshape(n, 3),
+         "acc": slab[6 * n:9 * n].reshape(n, 3), "mas": slab[9 * n:10 * n], "pot": slab[10 * n:11 * n],
+         "ken": slab[11 * n:12 * n], "pen": slab[12 * n:13 * n]}
+    if dof_ >= 16:
+        v["rad"] = slab[13 * n:14 * n]
+        v["rho"] = slab[14 * n:15 * n]
+        v["prs"] = slab[15 * n:16 * n]
+    return v
+
+
+# ---- the reference's sim_t surface (include/starflood_compat.h) -------------
+class NodeT(C.Structure):
+    _fields_ = [("parent", C.c_uint32), ("bodies", C.c_uint32), ("branch", C.c_uint32 * 8),
+                ("bounds", C.c_float * 6), ("params", C.c_float * 4)]
+
+
+class TreeT(C.Structure):
+    _fields_ = [("max_nodes", C.c_uint32), ("num_nodes", C.c_uint32), ("bounds", C.c_float * 6),
+                ("node", C.POINTER(NodeT))]
+
+
+class SimT(C.Structure):
+    _fields_ = [("step_number", C.c_uint), ("N", C.c_uint), ("mem", C.c_void_p), ("tree", TreeT)]
+
+
+def compat_configure(p: Params):
+    check(lib().sfgpu_compat_configure(C.byref(p)), "sfgpu_compat_configure")
+
+
+def compat_functions():
+    """The drop-in entry points with their C signatures."""
+    L = lib()
+    S = C.POINTER(SimT)
+    T = C.POINTER(TreeT)
+    for name, args in (("sim_init", [S, C.c_uint]), ("sim_free", [S]), ("sim_solv", [S]), ("sim_step", [S]),
+                       ("solve_gravity_part_part", [S]), ("solve_gravity_part_tree", [S]), ("solve_sph", [S]),
+                       ("tree_init", [T, C.c_uint]), ("tree_free", [T]),
+                       ("tree_build", [T, C.c_uint, C.c_void_p, C.c_void_p])):
+        fn = getattr(L, name)
+        fn.restype = C.c_int
+        fn.argtypes = args
+    L.sim_find.restype = C.c_void_p
+    L.sim_find.argtypes = [S, C.c_int]
+    return L

@@ -1,0 +1,245 @@
+// internal.cuh -- shared declarations of the starflood_gb300 CUDA sources.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "sfgpu.h"
+
+// ---------------------------------------------------------------------------
+// error handling
+// ---------------------------------------------------------------------------
+void sf_set_error(const char* fmt, ...);
+void sf_clear_error();
+
+#define SF_CUDA(call)                                                               \
+    do {                                                                            \
+        cudaError_t e_ = (call);                                                    \
+        if (e_ != cudaSuccess) {                                                    \
+            sf_set_error("%s:%d: %s: %s", __FILE__, __LINE__, #call,                \
+                         cudaGetErrorString(e_));                                   \
+            return SFGPU_FAILURE;                                                   \
+        }                                                                           \
+    } while (0)
+
+extern unsigned long long g_sf_launches;
+#define SF_CHECK_LAUNCH()                                                           \
+    do {                                                                            \
+        __atomic_add_fetch(&g_sf_launches, 1ull, __ATOMIC_RELAXED);                 \
+        cudaError_t e_ = cudaGetLastError();                                        \
+        if (e_ != cudaSuccess) {                                                    \
+            sf_set_error("%s:%d: kernel launch: %s", __FILE__, __LINE__,            \
+                         cudaGetErrorString(e_));                                   \
+            return SFGPU_FAILURE;                                                   \
+        }                                                                           \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// device helpers: reference-order FP32 arithmetic (no contraction into FMA)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ float fsqrt(float a) { return __fsqrt_rn(a); }
+
+// Kahan running sum (the idiom of src/gravity.c:521-533).
+struct KSum {
+    float s, c;
+    __device__ __forceinline__ void add(float x) {
+        const float y = fsub(x, c);
+        const float t = fadd(s, y);
+        const float z = fsub(t, s);
+        c = fsub(z, y);
+        s = t;
+    }
+};
+
+// 32-byte FP64 quadruple (x, y, z, w), one aligned 256-bit load.
+struct __align__(32) sfd4 {
+    double x, y, z, w;
+};
+__host__ __device__ __forceinline__ sfd4 mk_d4(double x, double y, double z, double w) {
+    sfd4 r;
+    r.x = x;
+    r.y = y;
+    r.z = z;
+    r.w = w;
+    return r;
+}
+
+// Error-free transformation a + b = s + e (Knuth's two-sum).
+__device__ __forceinline__ void two_sum(double a, double b, double& s, double& e) {
+    s = __dadd_rn(a, b);
+    const double bp = __dsub_rn(s, a);
+    e = __dadd_rn(__dsub_rn(a, __dsub_rn(s, bp)), __dsub_rn(b, bp));
+}
+__device__ __forceinline__ void two_sumf(float a, float b, float& s, float& e) {
+    s = fadd(a, b);
+    const float bp = fsub(s, a);
+    e = fadd(fsub(a, fsub(s, bp)), fsub(b, bp));
+}
+// double-double accumulate (hi, lo) += (b_hi, b_lo)
+__device__ __forceinline__ double2 dd_add(double2 a, double2 b) {
+    double s, e;
+    two_sum(a.x, b.x, s, e);
+    e = __dadd_rn(e, __dadd_rn(a.y, b.y));
+    double hi, lo;
+    two_sum(s, e, hi, lo);
+    return make_double2(hi, lo);
+}
+
+// rng.h:13-40 (pcg4d), used for the root-cube jitter.
+__host__ __device__ __forceinline__ void pcg4d(uint32_t& a, uint32_t& b, uint32_t& c, uint32_t& d) {
+    a = a * 1664525u + 1013904223u;
+    b = b * 1664525u + 1013904223u;
+    c = c * 1664525u + 1013904223u;
+    d = d * 1664525u + 1013904223u;
+    a += b * d; b += c * a; c += a * b; d += b * c;
+    a ^= a >> 16; b ^= b >> 16; c ^= c >> 16; d ^= d >> 16;
+    a += b * d; b += c * a; c += a * b; d += b * c;
+}
+
+// ---------------------------------------------------------------------------
+// constants derived from parameters exactly as the reference derives them
+// ---------------------------------------------------------------------------
+struct ForceConsts {
+    float eps2;    // (real)(EPSILON*EPSILON)           gravity.c:754
+    float neg_g;   // (real)(-G)                        gravity.c:808
+    float theta;   // (real)TREE_THETA                  gravity.c:448
+    float third;   // (real)(1.0/3.0)                   gravity.c:370
+    int physical;  // SFGPU_ACC_PHYSICAL
+};
+ForceConsts sf_force_consts(const sfgpu_params& p);
+
+// ---------------------------------------------------------------------------
+// stage timer (CUDA events on the simulation's stream)
+// ---------------------------------------------------------------------------
+struct StageTimer {
+    struct Rec {
+        int stage;
+        cudaEvent_t a, b;
+    };
+    std::vector<std::string> names;
+    std::vector<double> ms;
+    std::vector<uint32_t> launches;
+    std::vector<Rec> pending;
+    std::vector<cudaEvent_t> pool;
+    bool enabled = false;
+    int begin(cudaStream_t st, const char* name);
+    void end(cudaStream_t st, int token);
+    void collect();
+    ~StageTimer();
+};
+
+// ---------------------------------------------------------------------------
+// 3-phase exclusive scans (scan.cu)
+// ---------------------------------------------------------------------------
+struct ScanWork {
+    void* partials = nullptr;   // per-block sums
+    size_t cap_blocks = 0;
+};
+int sf_scan_reserve(ScanWork& w, uint32_t n, size_t elem);
+// exclusive scan of n uint32 values (out may alias in), total written to *d_total.
+int sf_scan_u32(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* d_total, ScanWork& w,
+                cudaStream_t st, const uint32_t* d_n = nullptr);
+// exclusive scan of n sfd4 values; out has n+1 entries (out[n] = total).
+int sf_scan_d4(const sfd4* in, sfd4* out, uint32_t n, ScanWork& w, cudaStream_t st,
+               const uint32_t* d_n = nullptr);
+
+// ---------------------------------------------------------------------------
+// radix sort of (u64 key, u32 value) pairs on the low `bits` key bits (sort.cu)
+// ---------------------------------------------------------------------------
+struct SortWork {
+    uint64_t* keys_b = nullptr;
+    uint32_t* vals_b = nullptr;
+    uint32_t* hist = nullptr;      // [passes][128]
+    uint32_t* status = nullptr;    // [tiles][128] lookback words
+    uint32_t* counters = nullptr;  // [passes] tile tickets
+    size_t cap = 0;
+    size_t tiles_cap = 0;
+};
+int sf_sort_alloc(SortWork& w, size_t n);
+void sf_sort_free(SortWork& w);
+// Sorts keys/vals in place (result back in keys/vals).  d_n (device, may be
+// NULL) overrides n as the element count when non-NULL (n is then the
+// capacity).  `enable` (device flag, may be NULL) skips the sort when zero.
+// The number of passes is ceil(bits/7); an odd count costs one extra copy.
+int sf_sort_pairs(uint64_t* keys, uint32_t* vals, uint32_t n, int bits, SortWork& w,
+                  cudaStream_t st, uint32_t* d_status, const uint32_t* d_n = nullptr,
+                  const uint32_t* enable = nullptr);
+
+// ---------------------------------------------------------------------------
+// simulation state
+// ---------------------------------------------------------------------------
+struct TreeWork;  // tree.cu
+int sf_tree_alloc(TreeWork** tw, uint32_t n, const sfgpu_params& p);
+void sf_tree_free(TreeWork* tw);
+
+struct sfgpu_sim {
+    uint32_t n = 0, dof = 13;
+    sfgpu_params p{};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    float* slab = nullptr;         // N*dof, reference layout
+    double* pos64 = nullptr;       // COMPENSATED: FP64 positions (3N)
+    double* vel64 = nullptr;       // COMPENSATED: FP64 velocities (3N)
+    float* u = nullptr;            // CUBIC SPH: specific internal energy
+    float* dudt = nullptr;         // CUBIC SPH: du/dt
+    // PP scratch
+    float4* pp_part = nullptr;
+    size_t pp_part_cap = 0;        // float4 entries
+    // reductions
+    double2* red = nullptr;        // block partials
+    uint32_t red_cap = 0;
+    double* sums = nullptr;        // [0]=T [1]=V [2]=Tcorr [3]=U [4]=mean radius ...
+    uint32_t* d_status = nullptr;
+    uint32_t* d_step = nullptr;
+    float* d_bounds = nullptr;     // root cube (6 floats)
+    TreeWork* tree = nullptr;
+    void* sph = nullptr;           // SphWork (sph.cu)
+    // pinned host mirrors
+    uint32_t* h_step = nullptr;
+    double* h_sums = nullptr;
+    uint32_t* h_status = nullptr;
+    // per-particle walk counters (optional)
+    uint32_t* stat_int = nullptr;
+    uint32_t* stat_open = nullptr;
+    unsigned long long* walk_tot = nullptr;  // [2]
+    StageTimer timer;
+    cudaGraphExec_t graph = nullptr;
+    bool graph_ok = true;
+};
+
+// stage entry points (each queues kernels on s->stream)
+int sf_stage_gravity_pp(sfgpu_sim* s);
+int sf_stage_tree_solve(sfgpu_sim* s, bool radius_ready);
+int sf_stage_sph(sfgpu_sim* s);
+int sf_stage_kick_drift(sfgpu_sim* s, bool want_radius);
+int sf_stage_radius(sfgpu_sim* s);
+int sf_stage_bounds(sfgpu_sim* s);
+int sf_stage_kick_energy(sfgpu_sim* s);
+int sf_sph_alloc(sfgpu_sim* s);
+void sf_sph_free(sfgpu_sim* s);
+
+// scratch (float4 entries) the PP launch needs for n bodies (pp.cu)
+size_t sf_pp_scratch_need(const sfgpu_params& p, uint32_t n);
+// the PP force on arbitrary device arrays (pp.cu)
+int sf_pp_launch(const sfgpu_params& p, uint32_t n, const float* pos, const float* mas,
+                 float* acc, float* pot, float4** part, size_t* part_cap, cudaStream_t st,
+                 const double* pos64);
+
+// tree inspection (tree.cu)
+int sf_tree_keys(sfgpu_sim* s, uint64_t* keys, uint32_t* index, uint32_t* n_inside);
+int sf_tree_num_nodes(sfgpu_sim* s, uint32_t* num_nodes);
+int sf_tree_export(sfgpu_sim* s, uint32_t* parent, uint32_t* bodies, uint32_t* branch8,
+                   float* bounds6, float* params4);
+
+static inline uint32_t sf_ceil_div(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
+int sf_num_sms();
+
+#define SF_RED_BLOCK 256

@@ -1,0 +1,229 @@
+// kdk.cu -- the leapfrog of sim_step (src/simulation.c:347-519) and the root
+// cube of sim_solv (src/simulation.c:244-308), fused into three passes over
+// the slab:
+//
+//   k_kick_drift   kick_0 and drift for one body per thread (each component
+//                  rounded exactly as the reference: v + ((dt/2) a), x + dt v)
+//                  and, for the tree, the body's FP64 distance from the origin
+//                  summed per block in double-double;
+//   k_bounds       mean radius from the block sums, pcg4d jitter of the step
+//                  number, the jittered root cube rounded to FP32;
+//   k_kick_energy  kick_1, ken = (m/2) v^2, pen = m pot, and per-block
+//                  double-double sums of ken, pen and the corrected energies;
+//   k_energy_final adds the block sums in a fixed order.
+//
+// Bytes per body: kick/drift reads pos, vel, acc (36 B) and writes pos, vel
+// (24 B); kick/energy reads vel, acc, mas, pot (32 B), writes vel, ken, pen
+// (20 B).  All HBM-bound.
+#include "internal.cuh"
+
+namespace {
+
+constexpr double K_INV_U32 = 2.3283062977608182109179324470460414886474609375e-10;  // rng.h:9
+
+template <int NV>
+__device__ void block_dd_reduce(double2 (&v)[NV], double2* out) {
+    __shared__ double2 sh[NV][SF_RED_BLOCK];
+    const int t = threadIdx.x;
+#pragma unroll
+    for (int k = 0; k < NV; k++) sh[k][t] = v[k];
+    __syncthreads();
+    for (int off = SF_RED_BLOCK / 2; off > 0; off >>= 1) {
+        if (t < off) {
+#pragma unroll
+            for (int k = 0; k < NV; k++) sh[k][t] = dd_add(sh[k][t], sh[k][t + off]);
+        }
+        __syncthreads();
+    }
+    if (t == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) out[(size_t)blockIdx.x * NV + k] = sh[k][0];
+    }
+}
+
+__device__ __forceinline__ double radius64(float x, float y, float z) {
+    // simulation.c:253-260: sqrt((x*x)+(y*y)+(z*z)) in FP64
+    const double dx = x, dy = y, dz = z;
+    return __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+}
+
+__global__ void __launch_bounds__(SF_RED_BLOCK) k_kick_drift(float* __restrict__ slab, uint32_t n, float half_dt,
+                                                             float dt, double* __restrict__ pos64,
+                                                             double* __restrict__ vel64, double dt64,
+                                                             int want_radius, double2* __restrict__ part) {
+    const uint32_t i = blockIdx.x * SF_RED_BLOCK + threadIdx.x;
+    float* pos = slab;
+    float* vel = slab + (size_t)3 * n;
+    const float* acc = slab + (size_t)6 * n;
+    double2 r[1] = {make_double2(0.0, 0.0)};
+    if (i < n) {
+        float x[3];
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            const size_t k = 3u * (size_t)i + c;
+            if (pos64) {
+                // precision form: FP64 state, FP32 copies for the force kernels
+                const double v = vel64[k] + 0.5 * dt64 * (double)acc[k];
+                const double xx = pos64[k] + dt64 * v;
+                vel64[k] = v;
+                pos64[k] = xx;
+                vel[k] = (float)v;
+                x[c] = (float)xx;
+                pos[k] = x[c];
+            } else {
+                const float v = fadd(vel[k], fmul(half_dt, acc[k]));  // simulation.c:382
+                x[c] = fadd(pos[k], fmul(dt, v));                      // simulation.c:394
+                vel[k] = v;
+                pos[k] = x[c];
+            }
+        }
+        if (want_radius) r[0] = make_double2(radius64(x[0], x[1], x[2]), 0.0);
+    }
+    if (want_radius) block_dd_reduce<1>(r, part);
+}
+
+__global__ void __launch_bounds__(SF_RED_BLOCK) k_radius(const float* __restrict__ pos, uint32_t n,
+                                                         double2* __restrict__ part) {
+    const uint32_t i = blockIdx.x * SF_RED_BLOCK + threadIdx.x;
+    double2 r[1] = {make_double2(0.0, 0.0)};
+    if (i < n) r[0] = make_double2(radius64(pos[3u * i], pos[3u * i + 1u], pos[3u * i + 2u]), 0.0);
+    block_dd_reduce<1>(r, part);
+}
+
+// simulation.c:276-301
+__global__ void __launch_bounds__(SF_RED_BLOCK) k_bounds(const double2* __restrict__ part, uint32_t nparts,
+                                                         uint32_t n, const uint32_t* __restrict__ d_step,
+                                                         float* __restrict__ bounds, double* __restrict__ sums) {
+    double2 v[1] = {make_double2(0.0, 0.0)};
+    for (uint32_t b = threadIdx.x; b < nparts; b += SF_RED_BLOCK) v[0] = dd_add(v[0], part[b]);
+    __shared__ double2 total[1];
+    // reuse the block reducer with a one-block grid (writes total[0])
+    block_dd_reduce<1>(v, total);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const double sum = __dadd_rn(total[0].x, total[0].y);
+        const double rbar = __dmul_rn(sum, 1.0 / (double)n);
+        uint32_t a = 0x638FE17Bu + *d_step, b = 0xB10BDCE7u, c = 0x7B8ADB9Bu, d = 0xD8C5850Eu;
+        pcg4d(a, b, c, d);
+        const uint32_t h[3] = {a, b, c};
+        for (int k = 0; k < 3; k++) {
+            const double j = __dsub_rn(__dmul_rn(2.0, __dmul_rn(K_INV_U32, (double)h[k])), 1.0);
+            const double shift = __dmul_rn(__dmul_rn(0.5, j), rbar);
+            bounds[k] = __double2float_rn(__dadd_rn(__dmul_rn(-2.000, rbar), shift));
+            bounds[3 + k] = __double2float_rn(__dadd_rn(__dmul_rn(2.000, rbar), shift));
+        }
+        sums[4] = rbar;
+    }
+}
+
+__global__ void __launch_bounds__(SF_RED_BLOCK) k_kick_energy(float* __restrict__ slab, uint32_t n, float half_dt,
+                                                              double* __restrict__ vel64, double dt64,
+                                                              float g_over_eps, int physical,
+                                                              double2* __restrict__ part) {
+    const uint32_t i = blockIdx.x * SF_RED_BLOCK + threadIdx.x;
+    float* vel = slab + (size_t)3 * n;
+    const float* acc = slab + (size_t)6 * n;
+    const float* mas = slab + (size_t)9 * n;
+    const float* pot = slab + (size_t)10 * n;
+    float* ken = slab + (size_t)11 * n;
+    float* pen = slab + (size_t)12 * n;
+    double2 e[4] = {make_double2(0, 0), make_double2(0, 0), make_double2(0, 0), make_double2(0, 0)};
+    if (i < n) {
+        float v[3];
+        double v64[3];
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            const size_t k = 3u * (size_t)i + c;
+            if (vel64) {
+                v64[c] = vel64[k] + 0.5 * dt64 * (double)acc[k];
+                vel64[k] = v64[c];
+                v[c] = (float)v64[c];
+            } else {
+                v[c] = fadd(vel[k], fmul(half_dt, acc[k]));  // simulation.c:424
+                v64[c] = v[c];
+            }
+            vel[k] = v[c];
+        }
+        const float m = mas[i];
+        // simulation.c:443-450
+        const float v2 = fadd(fadd(fmul(v[0], v[0]), fmul(v[1], v[1])), fmul(v[2], v[2]));
+        const float k_i = fmul(fmul(0.5f, m), v2);
+        const float p_i = fmul(m, pot[i]);
+        ken[i] = k_i;
+        pen[i] = p_i;
+        // corrected totals: kinetic term of the integrated dynamics and the
+        // pair potential without self terms, each pair once
+        const double v2d = v64[0] * v64[0] + v64[1] * v64[1] + v64[2] * v64[2];
+        const double kin = physical ? 0.5 * (double)m * v2d : 0.5 * v2d;
+        const double selfp = (double)g_over_eps * (double)m;  // G m_i / eps (the j = i term)
+        const double upair = 0.5 * (double)m * ((double)pot[i] + selfp);
+        e[0] = make_double2((double)k_i, 0.0);
+        e[1] = make_double2((double)p_i, 0.0);
+        e[2] = make_double2(kin, 0.0);
+        e[3] = make_double2(upair, 0.0);
+    }
+    block_dd_reduce<4>(e, part);
+}
+
+__global__ void __launch_bounds__(SF_RED_BLOCK) k_energy_final(const double2* __restrict__ part, uint32_t nparts,
+                                                               double* __restrict__ sums, uint32_t* d_step) {
+    double2 v[4] = {make_double2(0, 0), make_double2(0, 0), make_double2(0, 0), make_double2(0, 0)};
+    for (uint32_t b = threadIdx.x; b < nparts; b += SF_RED_BLOCK)
+        for (int k = 0; k < 4; k++) v[k] = dd_add(v[k], part[(size_t)b * 4 + k]);
+    __shared__ double2 total[4];
+    block_dd_reduce<4>(v, total);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < 4; k++) sums[k] = __dadd_rn(total[k].x, total[k].y);
+        *d_step += 1u;
+    }
+}
+
+}  // namespace
+
+static int ensure_red(sfgpu_sim* s, uint32_t entries) {
+    if (s->red_cap >= entries) return SFGPU_OK;
+    cudaFree(s->red);
+    s->red = nullptr;
+    SF_CUDA(cudaMalloc(&s->red, sizeof(double2) * entries));
+    s->red_cap = entries;
+    return SFGPU_OK;
+}
+
+int sf_stage_kick_drift(sfgpu_sim* s, bool want_radius) {
+    const uint32_t nb = sf_ceil_div(s->n, SF_RED_BLOCK);
+    if (ensure_red(s, nb * 4) != SFGPU_OK) return SFGPU_FAILURE;
+    const float dt = (float)s->p.dt;
+    k_kick_drift<<<nb, SF_RED_BLOCK, 0, s->stream>>>(s->slab, s->n, 0.5f * dt, dt, s->pos64, s->vel64,
+                                                     s->p.dt, want_radius ? 1 : 0, s->red);
+    SF_CHECK_LAUNCH();
+    return SFGPU_OK;
+}
+
+int sf_stage_radius(sfgpu_sim* s) {
+    const uint32_t nb = sf_ceil_div(s->n, SF_RED_BLOCK);
+    if (ensure_red(s, nb * 4) != SFGPU_OK) return SFGPU_FAILURE;
+    k_radius<<<nb, SF_RED_BLOCK, 0, s->stream>>>(s->slab, s->n, s->red);
+    SF_CHECK_LAUNCH();
+    return SFGPU_OK;
+}
+
+int sf_stage_bounds(sfgpu_sim* s) {
+    const uint32_t nb = sf_ceil_div(s->n, SF_RED_BLOCK);
+    k_bounds<<<1, SF_RED_BLOCK, 0, s->stream>>>(s->red, nb, s->n, s->d_step, s->d_bounds, s->sums);
+    SF_CHECK_LAUNCH();
+    return SFGPU_OK;
+}
+
+int sf_stage_kick_energy(sfgpu_sim* s) {
+    const uint32_t nb = sf_ceil_div(s->n, SF_RED_BLOCK);
+    if (ensure_red(s, nb * 4) != SFGPU_OK) return SFGPU_FAILURE;
+    const float dt = (float)s->p.dt;
+    const float g_over_eps = (float)(s->p.G / s->p.eps);
+    k_kick_energy<<<nb, SF_RED_BLOCK, 0, s->stream>>>(s->slab, s->n, 0.5f * dt, s->vel64, s->p.dt,
+                                                      g_over_eps, s->p.acc_mode == SFGPU_ACC_PHYSICAL, s->red);
+    SF_CHECK_LAUNCH();
+    k_energy_final<<<1, SF_RED_BLOCK, 0, s->stream>>>(s->red, nb, s->sums, s->d_step);
+    SF_CHECK_LAUNCH();
+    return SFGPU_OK;
+}

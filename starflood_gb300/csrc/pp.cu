@@ -1,0 +1,260 @@
+// pp.cu -- O(N^2) softened gravity, solve_gravity_part_part
+// (src/gravity.c:666-819), three ways:
+//
+//   k_pp_exact  one thread per body, every j in index order, the reference's
+//               FP32 expression tree with IEEE divide / square root and a
+//               Kahan sum per component (bit-identical to the reference);
+//   k_pp_fast   j-tiles staged in shared memory and broadcast to the warp,
+//               IPT bodies per thread in registers, hardware rsqrt and FMA;
+//               the j range is split over blockIdx.y so the grid covers the
+//               152 SMs several times, partial sums land in a scratch array
+//               and a second kernel adds them in a fixed order;
+//   compensated the same tiles, but each j-tile's partial sum is added to a
+//               (hi, lo) pair with two-sum (the precision form), and the
+//               split partials are added in FP64.
+#include <algorithm>
+
+#include "internal.cuh"
+
+namespace {
+
+// ---- exact ----------------------------------------------------------------
+constexpr int EXACT_BS = 128;
+
+__global__ void __launch_bounds__(EXACT_BS) k_pp_exact(const float* __restrict__ pos, const float* __restrict__ mas,
+                                                       uint32_t n, ForceConsts fc, float* __restrict__ acc,
+                                                       float* __restrict__ pot) {
+    __shared__ float4 sj[EXACT_BS];
+    const uint32_t i = blockIdx.x * EXACT_BS + threadIdx.x;
+    const bool live = i < n;
+    const float xi = live ? pos[3u * i] : 0.f;
+    const float yi = live ? pos[3u * i + 1u] : 0.f;
+    const float zi = live ? pos[3u * i + 2u] : 0.f;
+    const float mi = live ? mas[i] : 0.f;
+    KSum ax{0.f, 0.f}, ay{0.f, 0.f}, az{0.f, 0.f}, ph{0.f, 0.f};
+    for (uint32_t jt = 0; jt < n; jt += EXACT_BS) {
+        const uint32_t j = jt + threadIdx.x;
+        __syncthreads();
+        if (j < n) sj[threadIdx.x] = make_float4(pos[3u * j], pos[3u * j + 1u], pos[3u * j + 2u], mas[j]);
+        __syncthreads();
+        const uint32_t cnt = min((uint32_t)EXACT_BS, n - jt);
+        for (uint32_t jj = 0; jj < cnt; jj++) {
+            const float4 q = sj[jj];
+            // gravity.c:744-769: r_ij = r_i - r_j, r2 = (x^2 + y^2) + z^2
+            const float dx = fsub(xi, q.x), dy = fsub(yi, q.y), dz = fsub(zi, q.z);
+            const float r2 = fadd(fadd(fmul(dx, dx), fmul(dy, dy)), fmul(dz, dz));
+            const float s = fadd(r2, fc.eps2);
+            const float inv2 = fdiv(1.0f, s);
+            const float inv1 = fdiv(1.0f, fsqrt(s));
+            const float phi = fmul(q.w, inv1);
+            const float f = fmul(phi, inv2);
+            ax.add(fmul(f, dx));
+            ay.add(fmul(f, dy));
+            az.add(fmul(f, dz));
+            ph.add(phi);
+        }
+    }
+    if (!live) return;
+    // gravity.c:808-811: acc = (-G) * m_i * sum, pot = (-G) * sum
+    const float scale = fc.physical ? fc.neg_g : fmul(fc.neg_g, mi);
+    acc[3u * i + 0u] = fmul(scale, ax.s);
+    acc[3u * i + 1u] = fmul(scale, ay.s);
+    acc[3u * i + 2u] = fmul(scale, az.s);
+    pot[i] = fmul(fc.neg_g, ph.s);
+}
+
+// ---- fast / compensated ---------------------------------------------------
+// Each thread owns IPT bodies i = ibase + k*BS + tid.  The sum accumulated is
+// S_i = sum_j m_j (r_j - r_i) / (r^2 + eps^2)^1.5 = -sum_j F_ij, so the
+// reference's acc = (-G) m_i sum F = G m_i S.
+template <int BS, int IPT, bool COMP>
+__global__ void __launch_bounds__(BS) k_pp_tile(const float* __restrict__ pos, const float* __restrict__ mas,
+                                                const double* __restrict__ pos64, uint32_t n, float eps2,
+                                                uint32_t jchunk, float4* __restrict__ part) {
+    __shared__ float4 sj[BS];
+    const uint32_t ibase = blockIdx.x * (BS * IPT);
+    float xi[IPT], yi[IPT], zi[IPT];
+    float ax[IPT], ay[IPT], az[IPT], ph[IPT];
+    float hx[IPT], hy[IPT], hz[IPT], hp[IPT];  // compensated totals
+    float lx[IPT], ly[IPT], lz[IPT], lp[IPT];
+#pragma unroll
+    for (int k = 0; k < IPT; k++) {
+        const uint32_t i = ibase + k * BS + threadIdx.x;
+        const bool live = i < n;
+        xi[k] = live ? pos[3u * i] : 0.f;
+        yi[k] = live ? pos[3u * i + 1u] : 0.f;
+        zi[k] = live ? pos[3u * i + 2u] : 0.f;
+        ax[k] = ay[k] = az[k] = ph[k] = 0.f;
+        hx[k] = hy[k] = hz[k] = hp[k] = 0.f;
+        lx[k] = ly[k] = lz[k] = lp[k] = 0.f;
+    }
+    const uint32_t j0 = blockIdx.y * jchunk;
+    const uint32_t j1 = min(n, j0 + jchunk);
+    for (uint32_t jt = j0; jt < j1; jt += BS) {
+        const uint32_t j = jt + threadIdx.x;
+        float4 q = make_float4(0.f, 0.f, 0.f, 0.f);  // padding: zero mass
+        if (j < j1) q = make_float4(pos[3u * j], pos[3u * j + 1u], pos[3u * j + 2u], mas[j]);
+        __syncthreads();
+        sj[threadIdx.x] = q;
+        __syncthreads();
+#pragma unroll 8
+        for (int jj = 0; jj < BS; jj++) {
+            const float4 s = sj[jj];
+#pragma unroll
+            for (int k = 0; k < IPT; k++) {
+                const float dx = s.x - xi[k];
+                const float dy = s.y - yi[k];
+                const float dz = s.z - zi[k];
+                const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
+                const float inv = rsqrtf(r2);
+                const float mphi = s.w * inv;
+                const float f = mphi * (inv * inv);
+                ax[k] = fmaf(f, dx, ax[k]);
+                ay[k] = fmaf(f, dy, ay[k]);
+                az[k] = fmaf(f, dz, az[k]);
+                ph[k] += mphi;
+            }
+        }
+        if (COMP) {
+#pragma unroll
+            for (int k = 0; k < IPT; k++) {
+                float e;
+                two_sumf(hx[k], ax[k], hx[k], e); lx[k] += e;
+                two_sumf(hy[k], ay[k], hy[k], e); ly[k] += e;
+                two_sumf(hz[k], az[k], hz[k], e); lz[k] += e;
+                two_sumf(hp[k], ph[k], hp[k], e); lp[k] += e;
+                ax[k] = ay[k] = az[k] = ph[k] = 0.f;
+            }
+        }
+    }
+    float4* out = part + (size_t)blockIdx.y * n * (COMP ? 2 : 1);
+#pragma unroll
+    for (int k = 0; k < IPT; k++) {
+        const uint32_t i = ibase + k * BS + threadIdx.x;
+        if (i >= n) continue;
+        if (COMP) {
+            out[i] = make_float4(hx[k], hy[k], hz[k], hp[k]);
+            out[(size_t)n + i] = make_float4(lx[k], ly[k], lz[k], lp[k]);
+        } else {
+            out[i] = make_float4(ax[k], ay[k], az[k], ph[k]);
+        }
+    }
+    (void)pos64;
+}
+
+template <bool COMP>
+__global__ void k_pp_reduce(const float4* __restrict__ part, uint32_t n, uint32_t nsplit,
+                            const float* __restrict__ mas, ForceConsts fc, float* __restrict__ acc,
+                            float* __restrict__ pot) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float g = -fc.neg_g;
+    const float mi = mas[i];
+    if (!COMP) {
+        float4 s = part[i];
+        for (uint32_t b = 1; b < nsplit; b++) {
+            const float4 t = part[(size_t)b * n + i];
+            s.x += t.x; s.y += t.y; s.z += t.z; s.w += t.w;
+        }
+        const float scale = fc.physical ? g : g * mi;
+        acc[3u * i + 0u] = scale * s.x;
+        acc[3u * i + 1u] = scale * s.y;
+        acc[3u * i + 2u] = scale * s.z;
+        pot[i] = fc.neg_g * s.w;
+    } else {
+        double sx = 0, sy = 0, sz = 0, sw = 0;
+        for (uint32_t b = 0; b < nsplit; b++) {
+            const float4 h = part[(size_t)b * 2 * n + i];
+            const float4 l = part[(size_t)b * 2 * n + n + i];
+            sx += (double)h.x + (double)l.x;
+            sy += (double)h.y + (double)l.y;
+            sz += (double)h.z + (double)l.z;
+            sw += (double)h.w + (double)l.w;
+        }
+        const double scale = fc.physical ? (double)g : (double)g * (double)mi;
+        acc[3u * i + 0u] = (float)(scale * sx);
+        acc[3u * i + 1u] = (float)(scale * sy);
+        acc[3u * i + 2u] = (float)(scale * sz);
+        pot[i] = (float)((double)fc.neg_g * sw);
+    }
+}
+
+constexpr int FAST_BS = 128;
+constexpr int FAST_IPT = 4;
+
+}  // namespace
+
+ForceConsts sf_force_consts(const sfgpu_params& p) {
+    ForceConsts c;
+    c.eps2 = (float)(p.eps * p.eps);
+    c.neg_g = (float)(-p.G);
+    c.theta = (float)p.theta;
+    c.third = (float)(1.0 / 3.0);
+    c.physical = p.acc_mode == SFGPU_ACC_PHYSICAL;
+    return c;
+}
+
+namespace {
+struct PPShape {
+    uint32_t iblocks, nsplit, jchunk;
+};
+PPShape pp_shape(uint32_t n) {
+    PPShape sh;
+    sh.iblocks = sf_ceil_div(n, FAST_BS * FAST_IPT);
+    // enough blocks for ~8 waves at 4 resident blocks per SM
+    const uint32_t target = (uint32_t)sf_num_sms() * 4u * 8u;
+    uint32_t nsplit = std::max<uint32_t>(1u, sf_ceil_div(target, sh.iblocks));
+    uint32_t jchunk = sf_ceil_div(n, nsplit);
+    jchunk = sf_ceil_div(jchunk, FAST_BS) * FAST_BS;
+    sh.jchunk = jchunk;
+    sh.nsplit = sf_ceil_div(n, jchunk);
+    return sh;
+}
+}  // namespace
+
+size_t sf_pp_scratch_need(const sfgpu_params& p, uint32_t n) {
+    if (n == 0 || (p.math == SFGPU_MATH_EXACT && p.form == SFGPU_FORM_PLAIN)) return 0;
+    const PPShape sh = pp_shape(n);
+    return (size_t)sh.nsplit * n * (p.form == SFGPU_FORM_COMPENSATED ? 2 : 1);
+}
+
+int sf_pp_launch(const sfgpu_params& p, uint32_t n, const float* pos, const float* mas, float* acc, float* pot,
+                 float4** part, size_t* part_cap, cudaStream_t st, const double* pos64) {
+    if (n == 0) return SFGPU_OK;
+    const ForceConsts fc = sf_force_consts(p);
+    if (p.math == SFGPU_MATH_EXACT && p.form == SFGPU_FORM_PLAIN) {
+        k_pp_exact<<<sf_ceil_div(n, EXACT_BS), EXACT_BS, 0, st>>>(pos, mas, n, fc, acc, pot);
+        SF_CHECK_LAUNCH();
+        return SFGPU_OK;
+    }
+    const bool comp = p.form == SFGPU_FORM_COMPENSATED;
+    const PPShape sh = pp_shape(n);
+    const uint32_t iblocks = sh.iblocks, nsplit = sh.nsplit, jchunk = sh.jchunk;
+    const size_t need = sf_pp_scratch_need(p, n);
+    if (*part_cap < need) {
+        cudaFree(*part);
+        *part = nullptr;
+        *part_cap = 0;
+        SF_CUDA(cudaMalloc(part, need * sizeof(float4)));
+        *part_cap = need;
+    }
+    dim3 grid(iblocks, nsplit);
+    if (comp)
+        k_pp_tile<FAST_BS, FAST_IPT, true><<<grid, FAST_BS, 0, st>>>(pos, mas, pos64, n, fc.eps2, jchunk, *part);
+    else
+        k_pp_tile<FAST_BS, FAST_IPT, false><<<grid, FAST_BS, 0, st>>>(pos, mas, pos64, n, fc.eps2, jchunk, *part);
+    SF_CHECK_LAUNCH();
+    if (comp)
+        k_pp_reduce<true><<<sf_ceil_div(n, 256), 256, 0, st>>>(*part, n, nsplit, mas, fc, acc, pot);
+    else
+        k_pp_reduce<false><<<sf_ceil_div(n, 256), 256, 0, st>>>(*part, n, nsplit, mas, fc, acc, pot);
+    SF_CHECK_LAUNCH();
+    return SFGPU_OK;
+}
+
+int sf_stage_gravity_pp(sfgpu_sim* s) {
+    float* acc = s->slab + (size_t)6 * s->n;
+    float* pot = s->slab + (size_t)10 * s->n;
+    return sf_pp_launch(s->p, s->n, s->slab, s->slab + (size_t)9 * s->n, acc, pot, &s->pp_part, &s->pp_part_cap,
+                        s->stream, s->pos64);
+}

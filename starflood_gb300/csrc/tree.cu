@@ -1,0 +1,556 @@
+// tree.cu -- the octree of tree_build (src/tree.c:118-362), built in parallel
+// with the reference's exact topology.
+//
+// The reference inserts bodies one at a time; a node splits when its
+// (leaf_cap+1)-th body arrives, the resident bodies move down by "mid < x"
+// (tree.c:289-291) and every later arrival by "mid <= x" (tree.c:327-329),
+// with mid = 0.5f*(min+max) recomputed per level in FP32.  Hence:
+//
+//  * the node set is {root} plus the 8 children of every cell holding more
+//    than leaf_cap bodies at depth < depth_max;
+//  * a body's path is the sequence of octants of its FP32 midpoint
+//    comparisons, which differs between the two rules only when a coordinate
+//    equals a midpoint exactly, and then only for the first leaf_cap bodies
+//    (in index order) of a node that splits.
+//
+// So: (1) every body gets a provisional 48-bit key (3 bits per level, level 0
+// most significant) with the "<=" rule, plus a mask of the levels where it sat
+// exactly on a midplane; (2) keys are radix sorted (stable, so ties keep index
+// order); (3) one block re-derives the digits of the few midplane bodies with
+// the rank rule and the keys are re-sorted when any changed; (4) split nodes
+// are read off the sorted keys: position k starts a split node at level L iff
+// k begins a level-L run (key[k-1] differs in the first L digits) and
+// key[k+leaf_cap] shares those L digits; an exclusive scan of the per-position
+// counts numbers the split nodes in depth-first (pre)order, and a split node s
+// owns nodes 1+8s .. 8+8s for its octants; (5) monopoles come from an FP64
+// exclusive prefix sum of (m x, m y, m z, m) over the sorted bodies.
+//
+// Work per body: key pass reads 12 B and writes 12 B; 7 sort passes move
+// 12 B each way; the gather reads 16 B (random) and writes 16 B + 32 B FP64.
+#include <algorithm>
+
+#include "internal.cuh"
+#include "tree.cuh"
+
+namespace {
+
+constexpr uint64_t KEY_OUT = 1ull << 48;  // bodies outside the root cube sort last
+constexpr int KEY_BITS = 49;
+constexpr uint32_t TIE_CAP = 1024;
+
+__device__ __forceinline__ int cpl_levels(uint64_t a, uint64_t b) {
+    const uint64_t x = a ^ b;
+    if (x == 0) return 16;
+    return (__clzll((long long)x) - 16) / 3;
+}
+
+struct Cube {
+    float lo[3], hi[3];
+};
+
+__device__ __forceinline__ float midf(float lo, float hi) { return fmul(0.5f, fadd(lo, hi)); }
+
+// Descend `levels` levels of `key` (digits of levels 0..levels-1) from the
+// root cube, reproducing the bounds of the reference's nodes (tree.c:203-207,
+// 263-270, 331-335).
+__device__ Cube cube_of(const float* __restrict__ root, uint64_t key, int levels) {
+    Cube c;
+    for (int a = 0; a < 3; a++) {
+        c.lo[a] = root[a];
+        c.hi[a] = root[3 + a];
+    }
+    for (int L = 0; L < levels; L++) {
+        const uint32_t o = (uint32_t)(key >> (3 * (15 - L))) & 7u;
+        for (int a = 0; a < 3; a++) {
+            const float m = midf(c.lo[a], c.hi[a]);
+            if ((o >> a) & 1u) c.lo[a] = m; else c.hi[a] = m;
+        }
+    }
+    return c;
+}
+
+// Digits of levels [from, 16) with the "<=" rule, starting in cube c; tie bits.
+__device__ uint64_t descend(const float x[3], Cube c, uint64_t key, int from, uint32_t& ties) {
+    for (int L = from; L < 16; L++) {
+        uint32_t o = 0;
+        bool tie = false;
+        for (int a = 0; a < 3; a++) {
+            const float m = midf(c.lo[a], c.hi[a]);
+            const bool up = m <= x[a];
+            tie |= (m == x[a]);
+            o |= (up ? 1u : 0u) << a;
+            if (up) c.lo[a] = m; else c.hi[a] = m;
+        }
+        key |= (uint64_t)o << (3 * (15 - L));
+        if (tie) ties |= 1u << L;
+    }
+    return key;
+}
+
+__global__ void k_keys(const float* __restrict__ pos, uint32_t n, const float* __restrict__ bounds,
+                       uint64_t* __restrict__ keys, uint32_t* __restrict__ vals, uint32_t* __restrict__ nin,
+                       uint2* __restrict__ ties, uint32_t* __restrict__ tie_count, uint32_t* d_status) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool inside = false;
+    if (i < n) {
+        const float x[3] = {pos[3u * i], pos[3u * i + 1u], pos[3u * i + 2u]};
+        Cube c;
+        for (int a = 0; a < 3; a++) {
+            c.lo[a] = bounds[a];
+            c.hi[a] = bounds[3 + a];
+        }
+        // tree.c:186-190: closed root cube (NaN coordinates fall outside)
+        inside = (c.lo[0] <= x[0] && x[0] <= c.hi[0]) && (c.lo[1] <= x[1] && x[1] <= c.hi[1]) &&
+                 (c.lo[2] <= x[2] && x[2] <= c.hi[2]);
+        uint64_t key = KEY_OUT;
+        if (inside) {
+            uint32_t tb = 0;
+            key = descend(x, c, 0ull, 0, tb);
+            if (tb) {
+                const uint32_t slot = atomicAdd(tie_count, 1u);
+                if (slot < TIE_CAP) ties[slot] = make_uint2(i, tb);
+                else atomicOr(d_status, SFGPU_STATUS_TIES);
+            }
+        }
+        keys[i] = key;
+        vals[i] = i;
+    }
+    const uint32_t bal = __ballot_sync(0xffffffffu, inside);
+    if ((threadIdx.x & 31) == 0 && bal) atomicAdd(nin, (uint32_t)__popc(bal));
+}
+
+// first index in [lo, hi) whose key >> shift is >= target
+__device__ __forceinline__ uint32_t lower_bound_shift(const uint64_t* __restrict__ K, uint32_t lo, uint32_t hi,
+                                                      int shift, uint64_t target) {
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if ((K[mid] >> shift) < target) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ uint64_t prefix_of(uint64_t key, int L) { return L == 0 ? 0ull : key >> (3 * (16 - L)); }
+
+// Exact digits for bodies lying on a midplane (one block; see file comment).
+constexpr int FIX_THREADS = 1024;
+__global__ void __launch_bounds__(FIX_THREADS) k_tie_fix(const float* __restrict__ pos, const float* __restrict__ bounds,
+                                                         uint64_t* __restrict__ K, const uint32_t* __restrict__ V,
+                                                         const uint32_t* __restrict__ nin_p, const uint2* __restrict__ ties,
+                                                         const uint32_t* __restrict__ tie_count, uint32_t leaf_cap,
+                                                         uint32_t depth_max, uint32_t* __restrict__ resort) {
+    __shared__ uint64_t prov[TIE_CAP];
+    __shared__ uint64_t cur[TIE_CAP];
+    __shared__ uint32_t body[TIE_CAP];
+    __shared__ uint32_t mask[TIE_CAP];
+    __shared__ uint32_t red[FIX_THREADS / 32];
+    __shared__ uint32_t s_lo, s_hi, s_changed;
+    const uint32_t T = min(*tie_count, TIE_CAP);
+    if (threadIdx.x == 0) {
+        *resort = 0u;
+        s_changed = 0u;
+    }
+    if (T == 0) return;
+    const uint32_t nin = *nin_p;
+    for (uint32_t t = threadIdx.x; t < T; t += FIX_THREADS) {
+        const uint2 e = ties[t];
+        body[t] = e.x;
+        mask[t] = e.y;
+        const float x[3] = {pos[3u * e.x], pos[3u * e.x + 1u], pos[3u * e.x + 2u]};
+        Cube c = cube_of(bounds, 0ull, 0);
+        uint32_t tb = 0;
+        prov[t] = descend(x, c, 0ull, 0, tb);
+        cur[t] = prov[t];
+    }
+    __syncthreads();
+
+    auto block_sum = [&](uint32_t v) -> uint32_t {
+        v = __reduce_add_sync(0xffffffffu, v);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+        __syncthreads();
+        uint32_t tot = 0;
+        for (int w = 0; w < FIX_THREADS / 32; w++) tot += red[w];
+        __syncthreads();
+        return tot;
+    };
+
+    for (int L = 0; L < (int)depth_max && L < 16; L++) {
+        for (uint32_t t = 0; t < T; t++) {
+            if (!((mask[t] >> L) & 1u)) continue;  // uniform
+            const uint64_t pre = prefix_of(cur[t], L);
+            const int shift = 3 * (16 - L);
+            if (threadIdx.x == 0) {
+                if (L == 0) {
+                    s_lo = 0;
+                    s_hi = nin;
+                } else {
+                    s_lo = lower_bound_shift(K, 0, nin, shift, pre);
+                    s_hi = lower_bound_shift(K, s_lo, nin, shift, pre + 1);
+                }
+            }
+            __syncthreads();
+            const uint32_t lo = s_lo, hi = s_hi;
+            const uint32_t p = body[t];
+            // membership corrections from midplane bodies already moved
+            uint32_t c_in = 0, c_out = 0, r_in = 0, r_out = 0;
+            for (uint32_t u = threadIdx.x; u < T; u += FIX_THREADS) {
+                const bool pin = prefix_of(prov[u], L) == pre;
+                const bool cin = prefix_of(cur[u], L) == pre;
+                if (cin && !pin) { c_in++; if (body[u] < p) r_in++; }
+                if (pin && !cin) { c_out++; if (body[u] < p) r_out++; }
+            }
+            const uint32_t add = block_sum(c_in), sub = block_sum(c_out);
+            const uint32_t radd = block_sum(r_in), rsub = block_sum(r_out);
+            const uint32_t count = (hi - lo) + add - sub;
+            if (count <= leaf_cap) continue;  // node does not split: digit unused
+            // rank of p among the node's bodies in index order, decided only
+            // up to leaf_cap (early exit once enough smaller indices are seen)
+            const uint32_t need = leaf_cap + rsub;
+            uint32_t seen = 0;
+            for (uint32_t k0 = lo; k0 < hi; k0 += FIX_THREADS) {
+                const uint32_t k = k0 + threadIdx.x;
+                const uint32_t v = (k < hi && V[k] < p) ? 1u : 0u;
+                seen += block_sum(v);
+                if (seen >= need) break;
+            }
+            const uint32_t rank = seen + radd - rsub;
+            const bool strict = rank < leaf_cap;
+            if (threadIdx.x == 0) {
+                const uint32_t q = p;
+                const float x[3] = {pos[3u * q], pos[3u * q + 1u], pos[3u * q + 2u]};
+                Cube c = cube_of(bounds, cur[t], L);
+                uint32_t o = 0;
+                for (int a = 0; a < 3; a++) {
+                    const float m = midf(c.lo[a], c.hi[a]);
+                    const bool up = strict ? (m < x[a]) : (m <= x[a]);
+                    o |= (up ? 1u : 0u) << a;
+                }
+                const uint32_t old = (uint32_t)(cur[t] >> (3 * (15 - L))) & 7u;
+                if (o != old) {
+                    uint64_t key = (L == 0 ? 0ull : (pre << (3 * (16 - L))));
+                    key |= (uint64_t)o << (3 * (15 - L));
+                    Cube cc = cube_of(bounds, key, L + 1);
+                    uint32_t tb = 0;
+                    key = descend(x, cc, key, L + 1, tb);
+                    cur[t] = key;
+                    mask[t] = (mask[t] & ((2u << L) - 1u)) | (tb & ~((2u << L) - 1u));
+                    s_changed = 1u;
+                }
+            }
+            __syncthreads();
+        }
+    }
+    __syncthreads();
+    // write changed keys back at their sorted slots
+    for (uint32_t t = threadIdx.x; t < T; t += FIX_THREADS) {
+        if (cur[t] == prov[t]) continue;
+        uint32_t k = lower_bound_shift(K, 0, nin, 0, prov[t]);
+        while (k < nin && K[k] == prov[t] && V[k] != body[t]) k++;
+        if (k < nin && V[k] == body[t]) K[k] = cur[t];
+    }
+    if (threadIdx.x == 0) *resort = s_changed;
+}
+
+// s(k): number of split nodes whose range starts at sorted position k.
+__global__ void k_split_count(const uint64_t* __restrict__ K, uint32_t n, const uint32_t* __restrict__ nin_p,
+                              uint32_t leaf_cap, uint32_t depth_max, uint32_t* __restrict__ scount,
+                              uint32_t* d_status) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const uint32_t nin = *nin_p;
+    if (k >= nin) {
+        scount[k] = 0;
+        return;
+    }
+    const uint64_t key = K[k];
+    const int a = (k == 0) ? -1 : cpl_levels(K[k - 1], key);
+    int b = -1;
+    if (k + leaf_cap < nin) {
+        const int c = cpl_levels(key, K[k + leaf_cap]);
+        if (c >= (int)depth_max && a < (int)depth_max) atomicOr(d_status, SFGPU_STATUS_TREE_DEPTH);
+        b = min(c, (int)depth_max - 1);
+    }
+    scount[k] = (uint32_t)max(0, b - a);
+}
+
+__global__ void k_split_emit(const uint64_t* __restrict__ K, uint32_t n, const uint32_t* __restrict__ nin_p,
+                             const uint32_t* __restrict__ scount, const uint32_t* __restrict__ sbase,
+                             const uint32_t* __restrict__ nsplit_p, uint32_t split_cap,
+                             uint32_t* __restrict__ split_start, uint8_t* __restrict__ split_level,
+                             uint32_t nodes_max, uint32_t* d_status) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k == 0) {
+        const uint64_t total = 1ull + 8ull * (uint64_t)*nsplit_p;
+        if (total >= nodes_max || *nsplit_p > split_cap) atomicOr(d_status, SFGPU_STATUS_TREE_NODES);
+    }
+    if (k >= n || k >= *nin_p) return;
+    const uint32_t c = scount[k];
+    if (!c) return;
+    const int a = (k == 0) ? -1 : cpl_levels(K[k - 1], K[k]);
+    for (uint32_t j = 0; j < c; j++) {
+        const uint32_t id = sbase[k] + j;
+        if (id < split_cap) {
+            split_start[id] = k;
+            split_level[id] = (uint8_t)(a + 1 + (int)j);
+        }
+    }
+}
+
+__device__ __forceinline__ void write_node(NodeArrays nd, uint32_t v, const Cube& c, uint32_t bodies,
+                                           uint32_t first_child, uint32_t parent, uint32_t start, float third) {
+    const float mx = midf(c.lo[0], c.hi[0]), my = midf(c.lo[1], c.hi[1]), mz = midf(c.lo[2], c.hi[2]);
+    // gravity.c:370-374: w = (1/3) * ((dx + dy) + dz), compared as w*w
+    const float w = fmul(third, fadd(fadd(fsub(c.hi[0], c.lo[0]), fsub(c.hi[1], c.lo[1])), fsub(c.hi[2], c.lo[2])));
+    nd.geo[v] = make_float4(mx, my, mz, fmul(w, w));
+    nd.lo[v] = make_float4(c.lo[0], c.lo[1], c.lo[2], c.hi[0]);
+    nd.hi[v] = make_float4(c.hi[1], c.hi[2], __uint_as_float(bodies), __uint_as_float(first_child));
+    nd.parent[v] = parent;
+    nd.start[v] = start;
+}
+
+__global__ void k_root(const float* __restrict__ bounds, const uint32_t* __restrict__ nin_p, uint32_t leaf_cap,
+                       uint32_t depth_max, NodeArrays nd, float third) {
+    if (blockIdx.x || threadIdx.x) return;
+    Cube c;
+    for (int a = 0; a < 3; a++) {
+        c.lo[a] = bounds[a];
+        c.hi[a] = bounds[3 + a];
+    }
+    const uint32_t nin = *nin_p;
+    const bool split = nin > leaf_cap && depth_max > 0;
+    write_node(nd, 0, c, nin, split ? 1u : NODE_NONE, 0u, 0u, third);
+}
+
+__global__ void k_split_fill(const uint64_t* __restrict__ K, const uint32_t* __restrict__ nin_p,
+                             const uint32_t* __restrict__ sbase, const uint32_t* __restrict__ nsplit_p,
+                             uint32_t split_cap, const uint32_t* __restrict__ split_start,
+                             const uint8_t* __restrict__ split_level, const float* __restrict__ bounds,
+                             uint32_t leaf_cap, uint32_t depth_max, NodeArrays nd, float third) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t ns = min(*nsplit_p, split_cap);
+    if (s >= ns) return;
+    const uint32_t nin = *nin_p;
+    const uint32_t k = split_start[s];
+    const int L = split_level[s];
+    const uint64_t pre = prefix_of(K[k], L);
+    const uint32_t end = (L == 0) ? nin : lower_bound_shift(K, k, nin, 3 * (16 - L), pre + 1);
+    const Cube c = cube_of(bounds, K[k], L);
+    float mid[3];
+    for (int a = 0; a < 3; a++) mid[a] = midf(c.lo[a], c.hi[a]);
+    const uint32_t nid = (L == 0) ? 0u : 0u;  // own id is written by the parent
+    (void)nid;
+    // node id of this split node (to be the children's parent)
+    uint32_t self = 0;
+    if (L > 0) {
+        const uint64_t ppre = pre >> 3;
+        const uint32_t kp = (L == 1) ? 0u : lower_bound_shift(K, 0, k + 1, 3 * (17 - L), ppre);
+        const int ap = (kp == 0) ? -1 : cpl_levels(K[kp - 1], K[kp]);
+        const uint32_t sp = sbase[kp] + (uint32_t)(L - 1 - (ap + 1));
+        self = 1u + 8u * sp + (uint32_t)(pre & 7ull);
+    }
+    uint32_t cstart = k;
+    for (int o = 0; o < 8; o++) {
+        const uint32_t cend = (o == 7) ? end : lower_bound_shift(K, cstart, end, 3 * (15 - L), (pre << 3) + (uint64_t)o + 1);
+        const uint32_t cnt = cend - cstart;
+        Cube cc;
+        for (int a = 0; a < 3; a++) {
+            const bool up = (o >> a) & 1;
+            cc.lo[a] = up ? mid[a] : c.lo[a];
+            cc.hi[a] = up ? c.hi[a] : mid[a];
+        }
+        uint32_t fc = NODE_NONE;
+        if (cnt > leaf_cap && L + 1 < (int)depth_max) {
+            const int ac = (cstart == 0) ? -1 : cpl_levels(K[cstart - 1], K[cstart]);
+            const uint32_t sid = sbase[cstart] + (uint32_t)(L + 1 - (ac + 1));
+            fc = 1u + 8u * sid;
+        }
+        write_node(nd, 1u + 8u * s + (uint32_t)o, cc, cnt, fc, self, cstart, third);
+        cstart = cend;
+    }
+}
+
+__global__ void k_gather(const uint32_t* __restrict__ V, uint32_t n, const uint32_t* __restrict__ nin_p,
+                         const float* __restrict__ pos, const float* __restrict__ mas, float4* __restrict__ sp,
+                         sfd4* __restrict__ msum) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const uint32_t p = V[k];
+    const float x = pos[3u * p], y = pos[3u * p + 1u], z = pos[3u * p + 2u], m = mas[p];
+    sp[k] = make_float4(x, y, z, m);
+    if (k < *nin_p) {
+        const double md = m;
+        msum[k] = mk_d4(md * (double)x, md * (double)y, md * (double)z, md);
+    } else {
+        msum[k] = mk_d4(0, 0, 0, 0);
+    }
+}
+
+// tree.c:346-354 (centre of mass = sum(m x) / sum(m)), from FP64 prefix sums
+__global__ void k_monopoles(const uint32_t* __restrict__ nsplit_p, uint32_t split_cap, NodeArrays nd,
+                            const sfd4* __restrict__ pre) {
+    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nn = 1u + 8u * min(*nsplit_p, split_cap);
+    if (v >= nn) return;
+    const uint32_t cnt = __float_as_uint(nd.hi[v].z);
+    const uint32_t s = nd.start[v];
+    float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
+    sfd4 d = mk_d4(0, 0, 0, 0);
+    if (cnt) {
+        const sfd4 a = pre[s], b = pre[s + cnt];
+        d = mk_d4(b.x - a.x, b.y - a.y, b.z - a.z, b.w - a.w);
+        if (d.w > 0.0) {
+            const double inv = 1.0 / d.w;
+            out = make_float4((float)(d.x * inv), (float)(d.y * inv), (float)(d.z * inv), (float)d.w);
+        } else {
+            out = make_float4((float)d.x, (float)d.y, (float)d.z, (float)d.w);
+        }
+    }
+    nd.com[v] = out;
+}
+
+}  // namespace
+
+int sf_tree_alloc(TreeWork** out, uint32_t n, const sfgpu_params& p) {
+    TreeWork* t = new TreeWork();
+    *out = t;
+    t->n = n;
+    t->nodes_max = p.nodes_max;
+    t->split_cap = p.nodes_max >= 9 ? (p.nodes_max - 1) / 8 : 0;
+    const size_t nn = std::max<size_t>(n, 1);
+    const size_t nodes = std::max<uint32_t>(p.nodes_max, 16u);
+    SF_CUDA(cudaMalloc(&t->keys, sizeof(uint64_t) * nn));
+    SF_CUDA(cudaMalloc(&t->vals, sizeof(uint32_t) * nn));
+    if (sf_sort_alloc(t->sort, nn) != SFGPU_OK) return SFGPU_FAILURE;
+    SF_CUDA(cudaMalloc(&t->counters, sizeof(uint32_t) * 8));
+    SF_CUDA(cudaMalloc(&t->ties, sizeof(uint2) * TIE_CAP));
+    SF_CUDA(cudaMalloc(&t->scount, sizeof(uint32_t) * nn));
+    SF_CUDA(cudaMalloc(&t->sbase, sizeof(uint32_t) * nn));
+    SF_CUDA(cudaMalloc(&t->split_start, sizeof(uint32_t) * std::max<uint32_t>(t->split_cap, 1)));
+    SF_CUDA(cudaMalloc(&t->split_level, sizeof(uint8_t) * std::max<uint32_t>(t->split_cap, 1)));
+    SF_CUDA(cudaMalloc(&t->nd.geo, sizeof(float4) * nodes));
+    SF_CUDA(cudaMalloc(&t->nd.lo, sizeof(float4) * nodes));
+    SF_CUDA(cudaMalloc(&t->nd.hi, sizeof(float4) * nodes));
+    SF_CUDA(cudaMalloc(&t->nd.com, sizeof(float4) * nodes));
+    SF_CUDA(cudaMalloc(&t->nd.parent, sizeof(uint32_t) * nodes));
+    SF_CUDA(cudaMalloc(&t->nd.start, sizeof(uint32_t) * nodes));
+    SF_CUDA(cudaMalloc(&t->sp, sizeof(float4) * nn));
+    SF_CUDA(cudaMalloc(&t->msum, sizeof(sfd4) * nn));
+    SF_CUDA(cudaMalloc(&t->mpre, sizeof(sfd4) * (nn + 1)));
+    if (sf_scan_reserve(t->scan_u32, (uint32_t)nn, sizeof(uint32_t)) != SFGPU_OK) return SFGPU_FAILURE;
+    if (sf_scan_reserve(t->scan_d4, (uint32_t)nn, sizeof(sfd4)) != SFGPU_OK) return SFGPU_FAILURE;
+    return SFGPU_OK;
+}
+
+void sf_tree_free(TreeWork* t) {
+    if (!t) return;
+    cudaFree(t->keys);
+    cudaFree(t->vals);
+    sf_sort_free(t->sort);
+    cudaFree(t->counters);
+    cudaFree(t->ties);
+    cudaFree(t->scount);
+    cudaFree(t->sbase);
+    cudaFree(t->split_start);
+    cudaFree(t->split_level);
+    cudaFree(t->nd.geo);
+    cudaFree(t->nd.lo);
+    cudaFree(t->nd.hi);
+    cudaFree(t->nd.com);
+    cudaFree(t->nd.parent);
+    cudaFree(t->nd.start);
+    cudaFree(t->sp);
+    cudaFree(t->msum);
+    cudaFree(t->mpre);
+    cudaFree(t->scan_u32.partials);
+    cudaFree(t->scan_d4.partials);
+    delete t;
+}
+
+// Build the tree of the slab's current positions inside s->d_bounds.
+int sf_tree_build(sfgpu_sim* s) {
+    TreeWork* t = s->tree;
+    const uint32_t n = s->n;
+    cudaStream_t st = s->stream;
+    const float* pos = s->slab;
+    const float* mas = s->slab + (size_t)9 * n;
+    const float third = (float)(1.0 / 3.0);
+    uint32_t* nin = t->counters + 0;
+    uint32_t* tie_count = t->counters + 1;
+    uint32_t* resort = t->counters + 2;
+    uint32_t* nsplit = t->counters + 3;
+    SF_CUDA(cudaMemsetAsync(t->counters, 0, sizeof(uint32_t) * 4, st));
+    const uint32_t nb = sf_ceil_div(n, 256);
+    int tk = s->timer.begin(st, "tree_keys");
+    k_keys<<<nb, 256, 0, st>>>(pos, n, s->d_bounds, t->keys, t->vals, nin, t->ties, tie_count, s->d_status);
+    SF_CHECK_LAUNCH();
+    s->timer.end(st, tk);
+    tk = s->timer.begin(st, "tree_sort");
+    if (sf_sort_pairs(t->keys, t->vals, n, KEY_BITS, t->sort, st, s->d_status) != SFGPU_OK) return SFGPU_FAILURE;
+    s->timer.end(st, tk);
+    tk = s->timer.begin(st, "tree_ties");
+    k_tie_fix<<<1, FIX_THREADS, 0, st>>>(pos, s->d_bounds, t->keys, t->vals, nin, t->ties, tie_count,
+                                         s->p.leaf_cap, s->p.depth_max, resort);
+    SF_CHECK_LAUNCH();
+    if (sf_sort_pairs(t->keys, t->vals, n, KEY_BITS, t->sort, st, s->d_status, nullptr, resort) != SFGPU_OK)
+        return SFGPU_FAILURE;
+    s->timer.end(st, tk);
+    tk = s->timer.begin(st, "tree_nodes");
+    k_split_count<<<nb, 256, 0, st>>>(t->keys, n, nin, s->p.leaf_cap, s->p.depth_max, t->scount, s->d_status);
+    SF_CHECK_LAUNCH();
+    if (sf_scan_u32(t->scount, t->sbase, n, nsplit, t->scan_u32, st) != SFGPU_OK) return SFGPU_FAILURE;
+    k_split_emit<<<nb, 256, 0, st>>>(t->keys, n, nin, t->scount, t->sbase, nsplit, t->split_cap, t->split_start,
+                                     t->split_level, t->nodes_max, s->d_status);
+    SF_CHECK_LAUNCH();
+    k_root<<<1, 32, 0, st>>>(s->d_bounds, nin, s->p.leaf_cap, s->p.depth_max, t->nd, third);
+    SF_CHECK_LAUNCH();
+    const uint32_t sb = sf_ceil_div(std::max<uint32_t>(t->split_cap, 1), 128);
+    k_split_fill<<<sb, 128, 0, st>>>(t->keys, nin, t->sbase, nsplit, t->split_cap, t->split_start, t->split_level,
+                                     s->d_bounds, s->p.leaf_cap, s->p.depth_max, t->nd, third);
+    SF_CHECK_LAUNCH();
+    s->timer.end(st, tk);
+    tk = s->timer.begin(st, "tree_monopoles");
+    k_gather<<<nb, 256, 0, st>>>(t->vals, n, nin, pos, mas, t->sp, t->msum);
+    SF_CHECK_LAUNCH();
+    if (sf_scan_d4(t->msum, t->mpre, n, t->scan_d4, st) != SFGPU_OK) return SFGPU_FAILURE;
+    const uint32_t mb = sf_ceil_div(1u + 8u * t->split_cap, 256);
+    k_monopoles<<<mb, 256, 0, st>>>(nsplit, t->split_cap, t->nd, t->mpre);
+    SF_CHECK_LAUNCH();
+    s->timer.end(st, tk);
+    return SFGPU_OK;
+}
+
+int sf_stage_tree_solve(sfgpu_sim* s, bool radius_ready) {
+    int tk = s->timer.begin(s->stream, "bounds");
+    if (!radius_ready && sf_stage_radius(s) != SFGPU_OK) return SFGPU_FAILURE;
+    if (sf_stage_bounds(s) != SFGPU_OK) return SFGPU_FAILURE;
+    s->timer.end(s->stream, tk);
+    if (sf_tree_build(s) != SFGPU_OK) return SFGPU_FAILURE;
+    tk = s->timer.begin(s->stream, "walk");
+    if (sf_walk_launch(s) != SFGPU_OK) return SFGPU_FAILURE;
+    s->timer.end(s->stream, tk);
+    return SFGPU_OK;
+}
+
+// ---- inspection -------------------------------------------------------------
+int sf_tree_keys(sfgpu_sim* s, uint64_t* keys, uint32_t* index, uint32_t* n_inside) {
+    if (!s->tree) {
+        sf_set_error("the simulation has no tree");
+        return SFGPU_FAILURE;
+    }
+    SF_CUDA(cudaStreamSynchronize(s->stream));
+    if (keys) SF_CUDA(cudaMemcpy(keys, s->tree->keys, sizeof(uint64_t) * s->n, cudaMemcpyDeviceToHost));
+    if (index) SF_CUDA(cudaMemcpy(index, s->tree->vals, sizeof(uint32_t) * s->n, cudaMemcpyDeviceToHost));
+    if (n_inside) SF_CUDA(cudaMemcpy(n_inside, s->tree->counters, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    return SFGPU_OK;
+}
+
+int sf_tree_num_nodes(sfgpu_sim* s, uint32_t* num_nodes) {
+    if (!s->tree) {
+        sf_set_error("the simulation has no tree");
+        return SFGPU_FAILURE;
+    }
+    uint32_t ns = 0;
+    SF_CUDA(cudaStreamSynchronize(s->stream));
+    SF_CUDA(cudaMemcpy(&ns, s->tree->counters + 3, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    *num_nodes = 1u + 8u * std::min(ns, s->tree->split_cap);
+    return SFGPU_OK;
+}

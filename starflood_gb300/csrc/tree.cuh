@@ -1,0 +1,44 @@
+// tree.cuh -- device layout of the octree shared by the build, walk and export.
+#pragma once
+
+#include "internal.cuh"
+
+constexpr uint32_t NODE_NONE = 0xFFFFFFFFu;
+
+// Structure-of-arrays node records (16-byte vectors, one load per use):
+//   geo    (mid x, mid y, mid z, w*w)       opening test, gravity.c:352-377
+//   lo     (min x, min y, min z, max x)     self test, gravity.c:473-476
+//   hi     (max y, max z, bodies, first child) as raw bits in .z/.w
+//   com    (COM x, COM y, COM z, mass)      monopole, tree.c:346-354
+//   parent, start (first sorted body)       export and monopoles
+// Nodes are numbered: root 0; the children of the s-th split node in
+// depth-first preorder are 1+8s .. 8+8s, in octant order.
+struct NodeArrays {
+    float4* geo = nullptr;
+    float4* lo = nullptr;
+    float4* hi = nullptr;
+    float4* com = nullptr;
+    uint32_t* parent = nullptr;
+    uint32_t* start = nullptr;
+};
+
+struct TreeWork {
+    uint32_t n = 0, nodes_max = 0, split_cap = 0;
+    uint64_t* keys = nullptr;   // sorted keys
+    uint32_t* vals = nullptr;   // body index of each sorted slot
+    SortWork sort;
+    uint32_t* counters = nullptr;  // [0] bodies in cube [1] midplane bodies [2] resort [3] splits
+    uint2* ties = nullptr;
+    uint32_t* scount = nullptr;
+    uint32_t* sbase = nullptr;
+    uint32_t* split_start = nullptr;
+    uint8_t* split_level = nullptr;
+    NodeArrays nd;
+    float4* sp = nullptr;       // sorted bodies (x, y, z, m)
+    sfd4* msum = nullptr;    // (m x, m y, m z, m) per sorted slot, FP64
+    sfd4* mpre = nullptr;    // exclusive prefix of msum (n+1)
+    ScanWork scan_u32, scan_d4;
+};
+
+int sf_tree_build(sfgpu_sim* s);
+int sf_walk_launch(sfgpu_sim* s);

@@ -1,0 +1,208 @@
+// walk.cu -- Barnes-Hut monopole walk, solve_gravity_part_tree
+// (src/gravity.c:242-663).
+//
+// A warp takes 32 consecutive bodies of the key order (spatially close) and
+// walks the union of their trees with one shared stack of (node, lane mask)
+// entries.  At an internal node each lane in the mask runs the reference's
+// opening test with the reference's FP32 rounding (so the set of cells every
+// body interacts with is exactly the reference's); lanes that do not open
+// take the node as a monopole, the others continue into its children, which
+// are pushed in reverse octant order.  Each lane therefore meets its cells in
+// the same depth-first octant order as the reference's stackless walk
+// (gravity.c:306-579), which lets the EXACT variant reproduce its Kahan sums.
+// Leaves (bodies <= leaf_cap) are always monopoles; empty cells are skipped;
+// the reference's self-exclusion (gravity.c:473-490) is applied to every
+// cell whose closed bounds contain the body.
+#include "internal.cuh"
+#include "tree.cuh"
+
+namespace {
+
+constexpr int WALK_WARPS = 4;
+constexpr int WALK_THREADS = WALK_WARPS * 32;
+constexpr int STACK = 8 * 17 + 8;
+
+enum WalkKind { WALK_FAST = 0, WALK_EXACT = 1, WALK_COMP = 2 };
+
+template <int KIND, bool STATS>
+__global__ void __launch_bounds__(WALK_THREADS) k_walk(const float4* __restrict__ sp, const uint32_t* __restrict__ V,
+                                                       uint32_t n, NodeArrays nd, ForceConsts fc, uint32_t leaf_cap,
+                                                       float* __restrict__ acc, float* __restrict__ pot,
+                                                       uint32_t* __restrict__ st_int, uint32_t* __restrict__ st_open,
+                                                       unsigned long long* __restrict__ tot, uint32_t* d_status) {
+    __shared__ uint32_t s_node[WALK_WARPS][STACK];
+    __shared__ uint32_t s_mask[WALK_WARPS][STACK];
+    const int lane = threadIdx.x & 31;
+    const int w = threadIdx.x >> 5;
+    const uint32_t k = blockIdx.x * WALK_THREADS + threadIdx.x;
+    const bool live = k < n;
+    const float4 b = live ? sp[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float rx = b.x, ry = b.y, rz = b.z, mi = b.w;
+    const uint32_t live_mask = __ballot_sync(0xffffffffu, live);
+    if (!live_mask) return;
+
+    KSum ax{0.f, 0.f}, ay{0.f, 0.f}, az{0.f, 0.f}, ph{0.f, 0.f};
+    uint32_t n_int = 0, n_open = 0;
+    int top = 0;
+    if (lane == 0) {
+        s_node[w][0] = 0u;
+        s_mask[w][0] = live_mask;
+    }
+    top = 1;
+    __syncwarp();
+    uint32_t guard = 0;
+    while (top > 0) {
+        top--;
+        const uint32_t v = s_node[w][top];
+        const uint32_t M = s_mask[w][top];
+        __syncwarp();
+        if (++guard > (1u << 26)) {  // cannot happen for a well-formed tree
+            if (lane == 0) atomicOr(d_status, SFGPU_STATUS_WALK);
+            break;
+        }
+        const float4 H = nd.hi[v];
+        const uint32_t bodies = __float_as_uint(H.z);
+        if (bodies == 0u) continue;  // gravity.c:324-328
+        const bool me = (M >> lane) & 1u;
+        uint32_t take = M;
+        if (bodies > leaf_cap) {
+            const float4 G = nd.geo[v];
+            bool open = false;
+            if (me) {
+                // gravity.c:352-377, 448: open when theta <= (w*w)/d2
+                const float ox = fsub(G.x, rx), oy = fsub(G.y, ry), oz = fsub(G.z, rz);
+                const float d2 = fadd(fadd(fmul(ox, ox), fmul(oy, oy)), fmul(oz, oz));
+                const float ratio = (0.0f < d2) ? fdiv(G.w, d2) : 0.0f;
+                open = fc.theta <= ratio;
+                n_open++;
+            }
+            const uint32_t om = __ballot_sync(0xffffffffu, me && open);
+            take = M & ~om;
+            if (om) {
+                const uint32_t first = __float_as_uint(H.w);
+                if (top + 8 > STACK || first == NODE_NONE) {
+                    if (lane == 0) atomicOr(d_status, SFGPU_STATUS_WALK);
+                    take = M;  // fall back to the monopole rather than overflow
+                } else {
+                    if (lane < 8) {
+                        s_node[w][top + lane] = first + 7u - (uint32_t)lane;
+                        s_mask[w][top + lane] = om;
+                    }
+                    top += 8;
+                }
+            }
+            __syncwarp();
+        }
+        if ((take >> lane) & 1u) {
+            const float4 C = nd.com[v];
+            const float4 Lo = nd.lo[v];
+            float cx = C.x, cy = C.y, cz = C.z, mj = C.w;
+            // gravity.c:473-490: take body i out of a cell that contains it
+            if (Lo.x <= rx && rx <= Lo.w && Lo.y <= ry && ry <= H.x && Lo.z <= rz && rz <= H.y && 1u < bodies) {
+                cx = fmul(cx, mj);
+                cy = fmul(cy, mj);
+                cz = fmul(cz, mj);
+                cx = fsub(cx, fmul(mi, rx));
+                cy = fsub(cy, fmul(mi, ry));
+                cz = fsub(cz, fmul(mi, rz));
+                mj = fsub(mj, mi);
+                const float f = (0.0f < mj) ? fdiv(1.0f, mj) : 1.0f;
+                cx = fmul(cx, f);
+                cy = fmul(cy, f);
+                cz = fmul(cz, f);
+            }
+            if (KIND == WALK_EXACT) {
+                // gravity.c:493-548 with Kahan sums: accumulates sum F, F = phi/s r_ij
+                const float dx = fsub(rx, cx), dy = fsub(ry, cy), dz = fsub(rz, cz);
+                const float r2 = fadd(fadd(fmul(dx, dx), fmul(dy, dy)), fmul(dz, dz));
+                const float s = fadd(r2, fc.eps2);
+                const float inv2 = fdiv(1.0f, s);
+                const float inv1 = fdiv(1.0f, fsqrt(s));
+                const float phi = fmul(mj, inv1);
+                const float f = fmul(phi, inv2);
+                ax.add(fmul(f, dx));
+                ay.add(fmul(f, dy));
+                az.add(fmul(f, dz));
+                ph.add(phi);
+            } else {
+                // accumulates S = sum m_j (r_j - r_i) / s^1.5 = -sum F
+                const float dx = cx - rx, dy = cy - ry, dz = cz - rz;
+                const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, fc.eps2)));
+                const float inv = rsqrtf(r2);
+                const float mphi = mj * inv;
+                const float f = mphi * (inv * inv);
+                if (KIND == WALK_COMP) {
+                    ax.add(f * dx);
+                    ay.add(f * dy);
+                    az.add(f * dz);
+                    ph.add(mphi);
+                } else {
+                    ax.s = fmaf(f, dx, ax.s);
+                    ay.s = fmaf(f, dy, ay.s);
+                    az.s = fmaf(f, dz, az.s);
+                    ph.s += mphi;
+                }
+            }
+            n_int++;
+        }
+    }
+    if (live) {
+        const uint32_t p = V[k];
+        if (KIND == WALK_EXACT) {
+            // gravity.c:656-659
+            const float scale = fc.physical ? fc.neg_g : fmul(fc.neg_g, mi);
+            acc[3u * p + 0u] = fmul(scale, ax.s);
+            acc[3u * p + 1u] = fmul(scale, ay.s);
+            acc[3u * p + 2u] = fmul(scale, az.s);
+            pot[p] = fmul(fc.neg_g, ph.s);
+        } else {
+            const float g = -fc.neg_g;
+            const float scale = fc.physical ? g : g * mi;
+            acc[3u * p + 0u] = scale * (ax.s + (KIND == WALK_COMP ? -ax.c : 0.f));
+            acc[3u * p + 1u] = scale * (ay.s + (KIND == WALK_COMP ? -ay.c : 0.f));
+            acc[3u * p + 2u] = scale * (az.s + (KIND == WALK_COMP ? -az.c : 0.f));
+            pot[p] = fc.neg_g * (ph.s + (KIND == WALK_COMP ? -ph.c : 0.f));
+        }
+        if (STATS) {
+            st_int[p] = n_int;
+            st_open[p] = n_open;
+        }
+    }
+    // totals for the flop count
+    unsigned long long ci = n_int, co = n_open;
+    for (int o = 16; o > 0; o >>= 1) {
+        ci += __shfl_xor_sync(0xffffffffu, ci, o);
+        co += __shfl_xor_sync(0xffffffffu, co, o);
+    }
+    if (lane == 0) {
+        atomicAdd(&tot[0], ci);
+        atomicAdd(&tot[1], co);
+    }
+}
+
+template <int KIND>
+int launch_kind(sfgpu_sim* s, bool stats) {
+    TreeWork* t = s->tree;
+    const ForceConsts fc = sf_force_consts(s->p);
+    const uint32_t grid = sf_ceil_div(s->n, WALK_THREADS);
+    float* acc = s->slab + (size_t)6 * s->n;
+    float* pot = s->slab + (size_t)10 * s->n;
+    if (stats)
+        k_walk<KIND, true><<<grid, WALK_THREADS, 0, s->stream>>>(t->sp, t->vals, s->n, t->nd, fc, s->p.leaf_cap, acc,
+                                                                 pot, s->stat_int, s->stat_open, s->walk_tot,
+                                                                 s->d_status);
+    else
+        k_walk<KIND, false><<<grid, WALK_THREADS, 0, s->stream>>>(t->sp, t->vals, s->n, t->nd, fc, s->p.leaf_cap, acc,
+                                                                  pot, nullptr, nullptr, s->walk_tot, s->d_status);
+    SF_CHECK_LAUNCH();
+    return SFGPU_OK;
+}
+
+}  // namespace
+
+int sf_walk_launch(sfgpu_sim* s) {
+    const bool stats = (s->p.flags & SFGPU_FLAG_STATS) && s->stat_int;
+    if (s->p.math == SFGPU_MATH_EXACT && s->p.form == SFGPU_FORM_PLAIN) return launch_kind<WALK_EXACT>(s, stats);
+    if (s->p.form == SFGPU_FORM_COMPENSATED) return launch_kind<WALK_COMP>(s, stats);
+    return launch_kind<WALK_FAST>(s, stats);
+}

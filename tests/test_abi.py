@@ -1,0 +1,113 @@
+"""The C ABI: the library loads without a GPU, exports every function that
+include/*.h declares, and the ctypes mirrors have the C layouts (CPU only)."""
+import ctypes as C
+import os
+import re
+import subprocess
+import tempfile
+
+import pytest
+
+from conftest import ROOT
+
+INCLUDE = os.path.join(ROOT, "include")
+
+
+def _declared_functions():
+    names = set()
+    for h in ("sfgpu.h", "starflood_compat.h"):
+        text = open(os.path.join(INCLUDE, h)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"^[A-Za-z_][\w\s\*]*?\b(\w+)\s*\([^;{]*\)\s*;", text, flags=re.M):
+            name = m.group(1)
+            if name not in ("if", "while", "for", "return"):
+                names.add(name)
+    return sorted(names)
+
+
+@pytest.fixture(scope="module")
+def built_lib():
+    from starflood_gb300 import build
+    build.build()
+    import starflood_gb300 as sf
+    return sf.lib()
+
+
+def test_exports_every_declared_symbol(built_lib):
+    names = _declared_functions()
+    assert "sfgpu_create" in names and "sim_step" in names and "tree_build" in names
+    missing = [n for n in names if not hasattr(built_lib, n)]
+    assert not missing, missing
+
+
+def test_struct_layouts_match_c(built_lib):
+    import starflood_gb300 as sf
+    src = r"""
+    #include <stdio.h>
+    #include <stddef.h>
+    #include "starflood_compat.h"
+    int main(void) {
+        printf("%zu %zu %zu %zu %zu %zu\n", sizeof(sfgpu_params), offsetof(sfgpu_params, flags),
+               sizeof(node_t), sizeof(tree_t), sizeof(sim_t), offsetof(sim_t, tree));
+        return 0;
+    }
+    """
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "t.c")
+        exe = os.path.join(d, "t")
+        open(c, "w").write(src)
+        subprocess.check_call(["gcc", "-std=c11", "-I" + INCLUDE, c, "-o", exe])
+        out = [int(x) for x in subprocess.check_output([exe]).split()]
+    assert out[0] == C.sizeof(sf.Params)
+    assert out[1] == sf.Params.flags.offset
+    assert out[2] == C.sizeof(sf.NodeT) == 80  # node_t of the FP32 reference (tree.h:16-25)
+    assert out[3] == C.sizeof(sf.TreeT)
+    assert out[4] == C.sizeof(sf.SimT)
+    assert out[5] == sf.SimT.tree.offset
+
+
+def test_defaults_are_reference_config(built_lib):
+    import starflood_gb300 as sf
+    p = sf.default_params()
+    assert (p.dt, p.eps, p.G, p.theta) == (1.0, 1e-3, 1.0, 0.5)  # src/config.h
+    assert (p.leaf_cap, p.depth_max, p.nodes_max) == (8, 16, 262144)
+    assert p.solver == sf.SOLVER_TREE and p.sph == sf.SPH_OFF
+    assert sf.dof(p) == 13 and sf.dof(sf.default_params(sph=sf.SPH_REFERENCE)) == 16
+
+
+def test_reference_abi_sizes_when_available():
+    """node_t / tree_t / sim_t of the compiled reference have the same sizes."""
+    ref = "/root/reference/src"
+    if not os.path.isdir(ref):
+        pytest.skip("reference sources not present")
+    src = r"""
+    #include <stdio.h>
+    #include <stddef.h>
+    #include "simulation.h"
+    int main(void) { printf("%zu %zu %zu %zu\n", sizeof(node_t), sizeof(tree_t), sizeof(sim_t),
+                            offsetof(sim_t, tree)); return 0; }
+    """
+    from oracle.build import reference_config, REF_VARIANTS
+    with tempfile.TemporaryDirectory() as d:
+        open(os.path.join(d, "config.h"), "w").write(reference_config(REF_VARIANTS["tree_e0.01"]))
+        c = os.path.join(d, "t.c")
+        exe = os.path.join(d, "t")
+        open(c, "w").write(src)
+        subprocess.check_call(["gcc", "-std=c99", "-iquote", d, "-I-", "-I" + ref, c, "-o", exe],
+                              stderr=subprocess.DEVNULL)
+        out = [int(x) for x in subprocess.check_output([exe]).split()]
+    import starflood_gb300 as sf
+    assert out == [C.sizeof(sf.NodeT), C.sizeof(sf.TreeT), C.sizeof(sf.SimT), sf.SimT.tree.offset]
+
+
+def test_fails_loudly_without_gpu(built_lib):
+    import starflood_gb300 as sf
+    try:
+        import torch
+        has_gpu = torch.cuda.is_available()
+    except Exception:
+        has_gpu = False
+    if has_gpu:
+        pytest.skip("a GPU is present")
+    with pytest.raises(sf.SfgpuError):
+        sf.Sim(16, sf.default_params(solver=sf.SOLVER_PP))
