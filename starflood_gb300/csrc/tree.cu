@@ -361,7 +361,9 @@ __global__ void k_split_fill(const uint64_t* __restrict__ K, const uint32_t* __r
         if (cnt > leaf_cap && L + 1 < (int)depth_max) {
             const int ac = (cstart == 0) ? -1 : cpl_levels(K[cstart - 1], K[cstart]);
             const uint32_t sid = sbase[cstart] + (uint32_t)(L + 1 - (ac + 1));
-            fc = 1u + 8u * sid;
+            // beyond capacity (node overflow, flagged by k_split_emit) the
+            // child stays a leaf so nothing reads past the node arrays
+            fc = sid < split_cap ? 1u + 8u * sid : NODE_NONE;
         }
         write_node(nd, 1u + 8u * s + (uint32_t)o, cc, cnt, fc, self, cstart, third);
         cstart = cend;
