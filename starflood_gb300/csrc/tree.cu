@@ -324,7 +324,8 @@ __global__ void k_split_fill(const uint64_t* __restrict__ K, const uint32_t* __r
                              const uint32_t* __restrict__ sbase, const uint32_t* __restrict__ nsplit_p,
                              uint32_t split_cap, const uint32_t* __restrict__ split_start,
                              const uint8_t* __restrict__ split_level, const float* __restrict__ bounds,
-                             uint32_t leaf_cap, uint32_t depth_max, NodeArrays nd, float third) {
+                             uint32_t leaf_cap, uint32_t depth_max, NodeArrays nd, float third,
+                             uint32_t* __restrict__ split_node) {
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t ns = min(*nsplit_p, split_cap);
     if (s >= ns) return;
@@ -336,9 +337,8 @@ __global__ void k_split_fill(const uint64_t* __restrict__ K, const uint32_t* __r
     const Cube c = cube_of(bounds, K[k], L);
     float mid[3];
     for (int a = 0; a < 3; a++) mid[a] = midf(c.lo[a], c.hi[a]);
-    const uint32_t nid = (L == 0) ? 0u : 0u;  // own id is written by the parent
-    (void)nid;
-    // node id of this split node (to be the children's parent)
+    // node id of this split node (the children's parent); the node record
+    // itself is written by the parent's thread
     uint32_t self = 0;
     if (L > 0) {
         const uint64_t ppre = pre >> 3;
@@ -347,6 +347,7 @@ __global__ void k_split_fill(const uint64_t* __restrict__ K, const uint32_t* __r
         const uint32_t sp = sbase[kp] + (uint32_t)(L - 1 - (ap + 1));
         self = 1u + 8u * sp + (uint32_t)(pre & 7ull);
     }
+    split_node[s] = self;
     uint32_t cstart = k;
     for (int o = 0; o < 8; o++) {
         const uint32_t cend = (o == 7) ? end : lower_bound_shift(K, cstart, end, 3 * (15 - L), (pre << 3) + (uint64_t)o + 1);
@@ -409,6 +410,90 @@ __global__ void k_monopoles(const uint32_t* __restrict__ nsplit_p, uint32_t spli
     nd.com[v] = out;
 }
 
+// ---- reference-order monopoles (EXACT arithmetic) ----------------------------
+// The reference accumulates each node's sum(m x) and sum(m) in FP32 as bodies
+// arrive (tree.c:210-213, 300-303), i.e. in body-index order over the node's
+// members, then scales by 1/sum(m) (tree.c:346-354).  Reproduced here: every
+// leaf sorts its members by index; going up one level at a time, every split
+// node merges its eight children's index-ordered lists (children's ranges are
+// adjacent) and adds up its members in that order.
+__device__ __forceinline__ float4 ref_com(float sx, float sy, float sz, float sm) {
+    const float inv = (0.0f < sm) ? fdiv(1.0f, sm) : 1.0f;
+    return make_float4(fmul(sx, inv), fmul(sy, inv), fmul(sz, inv), sm);
+}
+
+__global__ void k_ref_leaf_sums(const uint32_t* __restrict__ nsplit_p, uint32_t split_cap, NodeArrays nd,
+                                const uint32_t* __restrict__ V, uint32_t* __restrict__ X,
+                                const float* __restrict__ pos, const float* __restrict__ mas) {
+    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nn = 1u + 8u * min(*nsplit_p, split_cap);
+    if (v >= nn) return;
+    const float4 H = nd.hi[v];
+    if (__float_as_uint(H.w) != NODE_NONE) return;  // split node: merged later
+    const uint32_t cnt = __float_as_uint(H.z);
+    const uint32_t s0 = nd.start[v];
+    for (uint32_t a = 0; a < cnt; a++) {  // insertion sort by body index
+        const uint32_t x = V[s0 + a];
+        uint32_t b = a;
+        while (b > 0 && X[s0 + b - 1] > x) {
+            X[s0 + b] = X[s0 + b - 1];
+            b--;
+        }
+        X[s0 + b] = x;
+    }
+    float sx = 0.f, sy = 0.f, sz = 0.f, sm = 0.f;
+    for (uint32_t a = 0; a < cnt; a++) {
+        const uint32_t p = X[s0 + a];
+        const float m = mas[p];
+        sx = fadd(sx, fmul(m, pos[3u * p]));
+        sy = fadd(sy, fmul(m, pos[3u * p + 1u]));
+        sz = fadd(sz, fmul(m, pos[3u * p + 2u]));
+        sm = fadd(sm, m);
+    }
+    nd.com[v] = cnt ? ref_com(sx, sy, sz, sm) : make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+__global__ void k_ref_merge(int level, const uint32_t* __restrict__ nsplit_p, uint32_t split_cap,
+                            const uint8_t* __restrict__ split_level, const uint32_t* __restrict__ split_node,
+                            NodeArrays nd, uint32_t* __restrict__ X, uint32_t* __restrict__ Y,
+                            const float* __restrict__ pos, const float* __restrict__ mas) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= min(*nsplit_p, split_cap) || split_level[s] != level) return;
+    const uint32_t v = split_node[s];
+    const uint32_t fc = 1u + 8u * s;
+    uint32_t cur[8], end[8];
+    for (int o = 0; o < 8; o++) {
+        cur[o] = nd.start[fc + o];
+        end[o] = cur[o] + __float_as_uint(nd.hi[fc + o].z);
+    }
+    const uint32_t s0 = nd.start[v];
+    const uint32_t cnt = __float_as_uint(nd.hi[v].z);
+    float sx = 0.f, sy = 0.f, sz = 0.f, sm = 0.f;
+    for (uint32_t a = 0; a < cnt; a++) {
+        int best = -1;
+        uint32_t bv = 0xFFFFFFFFu;
+        for (int o = 0; o < 8; o++) {
+            if (cur[o] < end[o]) {
+                const uint32_t x = X[cur[o]];
+                if (x < bv) {
+                    bv = x;
+                    best = o;
+                }
+            }
+        }
+        if (best < 0) break;
+        cur[best]++;
+        Y[s0 + a] = bv;
+        const float m = mas[bv];
+        sx = fadd(sx, fmul(m, pos[3u * bv]));
+        sy = fadd(sy, fmul(m, pos[3u * bv + 1u]));
+        sz = fadd(sz, fmul(m, pos[3u * bv + 2u]));
+        sm = fadd(sm, m);
+    }
+    for (uint32_t a = 0; a < cnt; a++) X[s0 + a] = Y[s0 + a];
+    nd.com[v] = ref_com(sx, sy, sz, sm);
+}
+
 }  // namespace
 
 int sf_tree_alloc(TreeWork** out, uint32_t n, const sfgpu_params& p) {
@@ -428,6 +513,11 @@ int sf_tree_alloc(TreeWork** out, uint32_t n, const sfgpu_params& p) {
     SF_CUDA(cudaMalloc(&t->sbase, sizeof(uint32_t) * nn));
     SF_CUDA(cudaMalloc(&t->split_start, sizeof(uint32_t) * std::max<uint32_t>(t->split_cap, 1)));
     SF_CUDA(cudaMalloc(&t->split_level, sizeof(uint8_t) * std::max<uint32_t>(t->split_cap, 1)));
+    SF_CUDA(cudaMalloc(&t->split_node, sizeof(uint32_t) * std::max<uint32_t>(t->split_cap, 1)));
+    if (p.math == SFGPU_MATH_EXACT) {
+        SF_CUDA(cudaMalloc(&t->ordA, sizeof(uint32_t) * nn));
+        SF_CUDA(cudaMalloc(&t->ordB, sizeof(uint32_t) * nn));
+    }
     SF_CUDA(cudaMalloc(&t->nd.geo, sizeof(float4) * nodes));
     SF_CUDA(cudaMalloc(&t->nd.lo, sizeof(float4) * nodes));
     SF_CUDA(cudaMalloc(&t->nd.hi, sizeof(float4) * nodes));
@@ -453,6 +543,9 @@ void sf_tree_free(TreeWork* t) {
     cudaFree(t->sbase);
     cudaFree(t->split_start);
     cudaFree(t->split_level);
+    cudaFree(t->split_node);
+    cudaFree(t->ordA);
+    cudaFree(t->ordB);
     cudaFree(t->nd.geo);
     cudaFree(t->nd.lo);
     cudaFree(t->nd.hi);
@@ -506,16 +599,27 @@ int sf_tree_build(sfgpu_sim* s) {
     SF_CHECK_LAUNCH();
     const uint32_t sb = sf_ceil_div(std::max<uint32_t>(t->split_cap, 1), 128);
     k_split_fill<<<sb, 128, 0, st>>>(t->keys, nin, t->sbase, nsplit, t->split_cap, t->split_start, t->split_level,
-                                     s->d_bounds, s->p.leaf_cap, s->p.depth_max, t->nd, third);
+                                     s->d_bounds, s->p.leaf_cap, s->p.depth_max, t->nd, third, t->split_node);
     SF_CHECK_LAUNCH();
     s->timer.end(st, tk);
     tk = s->timer.begin(st, "tree_monopoles");
     k_gather<<<nb, 256, 0, st>>>(t->vals, n, nin, pos, mas, t->sp, t->msum);
     SF_CHECK_LAUNCH();
-    if (sf_scan_d4(t->msum, t->mpre, n, t->scan_d4, st) != SFGPU_OK) return SFGPU_FAILURE;
     const uint32_t mb = sf_ceil_div(1u + 8u * t->split_cap, 256);
-    k_monopoles<<<mb, 256, 0, st>>>(nsplit, t->split_cap, t->nd, t->mpre);
-    SF_CHECK_LAUNCH();
+    if (s->p.math == SFGPU_MATH_EXACT && s->p.form == SFGPU_FORM_PLAIN) {
+        k_ref_leaf_sums<<<mb, 256, 0, st>>>(nsplit, t->split_cap, t->nd, t->vals, t->ordA, pos, mas);
+        SF_CHECK_LAUNCH();
+        const uint32_t sm = sf_ceil_div(std::max<uint32_t>(t->split_cap, 1), 128);
+        for (int L = (int)s->p.depth_max - 1; L >= 0; L--) {
+            k_ref_merge<<<sm, 128, 0, st>>>(L, nsplit, t->split_cap, t->split_level, t->split_node, t->nd, t->ordA,
+                                            t->ordB, pos, mas);
+            SF_CHECK_LAUNCH();
+        }
+    } else {
+        if (sf_scan_d4(t->msum, t->mpre, n, t->scan_d4, st) != SFGPU_OK) return SFGPU_FAILURE;
+        k_monopoles<<<mb, 256, 0, st>>>(nsplit, t->split_cap, t->nd, t->mpre);
+        SF_CHECK_LAUNCH();
+    }
     s->timer.end(st, tk);
     return SFGPU_OK;
 }

@@ -33,6 +33,9 @@ struct TreeWork {
     uint32_t* sbase = nullptr;
     uint32_t* split_start = nullptr;
     uint8_t* split_level = nullptr;
+    uint32_t* split_node = nullptr;  // node id of each split node
+    uint32_t* ordA = nullptr;        // EXACT monopoles: members in index order
+    uint32_t* ordB = nullptr;
     NodeArrays nd;
     float4* sp = nullptr;       // sorted bodies (x, y, z, m)
     sfd4* msum = nullptr;    // (m x, m y, m z, m) per sorted slot, FP64

@@ -1,10 +1,10 @@
 """Barnes-Hut tree build and walk on the GPU against the oracle (GPU only).
 
 Bit-exact: root cube, octree keys / membership, node count, per-body
-interaction and opening-test counts (the same cells are accepted).
-Tolerance: forces within 1e-6 (EXACT arithmetic; centre-of-mass sums are
-FP64 instead of the reference's FP32 running sums) or 1e-5 (FAST) global
-relative L2 of the reference."""
+interaction and opening-test counts (the same cells are accepted), and with
+EXACT arithmetic the forces, potentials and whole KDK steps.  FAST
+arithmetic (FP64 centres of mass, rsqrt): within 1e-5 global relative L2 of
+the reference."""
 import numpy as np
 import pytest
 
@@ -89,15 +89,22 @@ def test_tree_uniform_golden(sf, oracle32, math):
         ni, no = s.walk_stats()
         np.testing.assert_array_equal(ni, stats[:, 0])
         np.testing.assert_array_equal(no, stats[:, 1])
-        tol = 1e-6 if math == "exact" else 1e-5
-        assert rel_l2(v["acc"], d["solv_acc"]) < tol
-        assert rel_l2(v["pot"], d["solv_pot"]) < tol
+        if math == "exact":
+            np.testing.assert_array_equal(v["acc"], d["solv_acc"])
+            np.testing.assert_array_equal(v["pot"], d["solv_pot"])
+        else:
+            assert rel_l2(v["acc"], d["solv_acc"]) < 1e-5
+            assert rel_l2(v["pot"], d["solv_pot"]) < 1e-5
         for k in range(int(d["steps"])):
             s.step(k)
-        out = slab_views(s.download(), n, 13)
-        ref = slab_views(d["final_slab"], n, 13)
-        assert rel_l2(out["pos"], ref["pos"]) < 1e-6
-        assert rel_l2(out["acc"], ref["acc"]) < tol * 10
+        final = s.download()
+        if math == "exact":
+            np.testing.assert_array_equal(final, d["final_slab"])
+        else:
+            out = slab_views(final, n, 13)
+            ref = slab_views(d["final_slab"], n, 13)
+            assert rel_l2(out["pos"], ref["pos"]) < 1e-6
+            assert rel_l2(out["acc"], ref["acc"]) < 1e-4
 
 
 def test_tree_lattice_ties(sf, oracle32):
@@ -118,7 +125,8 @@ def test_tree_lattice_ties(sf, oracle32):
         _, _, stats = oracle32.walk(d["pos"], d["mas"], nodes, op)
         ni, no = s.walk_stats()
         np.testing.assert_array_equal(ni, stats[:, 0])
-        assert rel_l2(v["acc"], d["walk_acc"]) < 1e-6
+        np.testing.assert_array_equal(v["acc"], d["walk_acc"])
+        np.testing.assert_array_equal(v["pot"], d["walk_pot"])
 
 
 def test_tree_depth_overflow_flag(sf):
@@ -160,7 +168,8 @@ def test_tree_outside_and_nan_bodies(sf, oracle32):
     st, nodes = oracle32.tree_build(pos, mas, bounds, op)
     assert nin == nodes[0]["bodies"] < n
     a, pt, _ = oracle32.walk(pos, mas, nodes, op)
-    assert rel_l2(v["acc"], a) < 1e-6
+    np.testing.assert_array_equal(v["acc"], a)
+    np.testing.assert_array_equal(v["pot"], pt)
 
 
 @pytest.mark.parametrize("n,seed", [(65536, 2), (20000, 8)])
