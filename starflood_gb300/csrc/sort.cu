@@ -13,8 +13,7 @@ constexpr int RADIX_BITS = 7;
 constexpr int RADIX = 1 << RADIX_BITS;       // 128 buckets
 constexpr int SORT_WARPS = 8;
 constexpr int SORT_THREADS = SORT_WARPS * 32;
-constexpr int SORT_ITEMS = 8;
-constexpr int SORT_TILE = SORT_THREADS * SORT_ITEMS;  // 2048 keys per tile
+constexpr int SORT_TILE_MIN = SORT_THREADS * 2;              // 512 keys per tile
 constexpr int MAX_PASSES = 10;
 constexpr uint32_t FLAG_AGG = 1u << 30;
 constexpr uint32_t FLAG_INC = 2u << 30;
@@ -39,6 +38,7 @@ __global__ void __launch_bounds__(256) k_hist(const uint64_t* __restrict__ keys,
         if (sh[i]) atomicAdd(&hist[i], sh[i]);
 }
 
+template <int SORT_ITEMS>
 __global__ void __launch_bounds__(SORT_THREADS) k_onesweep(
     const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint64_t* __restrict__ kout,
     uint32_t* __restrict__ vout, uint32_t n, int shift, const uint32_t* __restrict__ hist,
@@ -86,7 +86,7 @@ __global__ void __launch_bounds__(SORT_THREADS) k_onesweep(
     uint32_t rank[SORT_ITEMS];
     uint32_t dig[SORT_ITEMS];
     const uint32_t lt = (1u << lane) - 1u;
-    const size_t wbase = (size_t)tile * SORT_TILE + (size_t)warp * (32 * SORT_ITEMS);
+    const size_t wbase = (size_t)tile * (SORT_THREADS * SORT_ITEMS) + (size_t)warp * (32 * SORT_ITEMS);
 #pragma unroll
     for (int it = 0; it < SORT_ITEMS; it++) {
         const size_t e = wbase + (size_t)it * 32 + lane;
@@ -174,7 +174,7 @@ __global__ void k_copy_pairs(const uint64_t* __restrict__ ks, const uint32_t* __
 
 int sf_sort_alloc(SortWork& w, size_t n) {
     sf_sort_free(w);
-    const size_t tiles = (n + SORT_TILE - 1) / SORT_TILE + 1;
+    const size_t tiles = (n + SORT_TILE_MIN - 1) / SORT_TILE_MIN + 1;
     SF_CUDA(cudaMalloc(&w.keys_b, sizeof(uint64_t) * (n ? n : 1)));
     SF_CUDA(cudaMalloc(&w.vals_b, sizeof(uint32_t) * (n ? n : 1)));
     SF_CUDA(cudaMalloc(&w.hist, sizeof(uint32_t) * MAX_PASSES * RADIX));
@@ -206,7 +206,9 @@ int sf_sort_pairs(uint64_t* keys, uint32_t* vals, uint32_t n, int bits, SortWork
         sf_set_error("sort: %d key bits is too many", bits);
         return SFGPU_FAILURE;
     }
-    const uint32_t tiles = sf_ceil_div(n, SORT_TILE);
+    // small inputs take small tiles so that more SMs join each pass
+    const int items = n <= (1u << 18) ? 2 : (n <= (1u << 20) ? 4 : 8);
+    const uint32_t tiles = sf_ceil_div(n, SORT_THREADS * items);
     SF_CUDA(cudaMemsetAsync(w.hist, 0, sizeof(uint32_t) * passes * RADIX, st));
     SF_CUDA(cudaMemsetAsync(w.counters, 0, sizeof(uint32_t) * passes, st));
     SF_CUDA(cudaMemsetAsync(w.status, 0, sizeof(uint32_t) * (size_t)passes * tiles * RADIX, st));
@@ -218,9 +220,16 @@ int sf_sort_pairs(uint64_t* keys, uint32_t* vals, uint32_t n, int bits, SortWork
     uint64_t* kb = w.keys_b;
     uint32_t* vb = w.vals_b;
     for (int p = 0; p < passes; p++) {
-        k_onesweep<<<tiles, SORT_THREADS, 0, st>>>(ka, va, kb, vb, n, p * RADIX_BITS, w.hist + p * RADIX,
-                                                   w.status + (size_t)p * tiles * RADIX, w.counters + p,
-                                                   d_status, enable);
+        uint32_t* stp = w.status + (size_t)p * tiles * RADIX;
+        if (items == 2)
+            k_onesweep<2><<<tiles, SORT_THREADS, 0, st>>>(ka, va, kb, vb, n, p * RADIX_BITS, w.hist + p * RADIX, stp,
+                                                          w.counters + p, d_status, enable);
+        else if (items == 4)
+            k_onesweep<4><<<tiles, SORT_THREADS, 0, st>>>(ka, va, kb, vb, n, p * RADIX_BITS, w.hist + p * RADIX, stp,
+                                                          w.counters + p, d_status, enable);
+        else
+            k_onesweep<8><<<tiles, SORT_THREADS, 0, st>>>(ka, va, kb, vb, n, p * RADIX_BITS, w.hist + p * RADIX, stp,
+                                                          w.counters + p, d_status, enable);
         SF_CHECK_LAUNCH();
         std::swap(ka, kb);
         std::swap(va, vb);

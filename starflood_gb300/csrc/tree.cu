@@ -142,8 +142,7 @@ __global__ void __launch_bounds__(FIX_THREADS) k_tie_fix(const float* __restrict
     __shared__ uint64_t cur[TIE_CAP];
     __shared__ uint32_t body[TIE_CAP];
     __shared__ uint32_t mask[TIE_CAP];
-    __shared__ uint32_t red[FIX_THREADS / 32];
-    __shared__ uint32_t s_lo, s_hi, s_changed;
+    __shared__ uint32_t s_changed;
     const uint32_t T = min(*tie_count, TIE_CAP);
     if (threadIdx.x == 0) {
         *resort = 0u;
@@ -163,81 +162,66 @@ __global__ void __launch_bounds__(FIX_THREADS) k_tie_fix(const float* __restrict
     }
     __syncthreads();
 
-    auto block_sum = [&](uint32_t v) -> uint32_t {
-        v = __reduce_add_sync(0xffffffffu, v);
-        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-        __syncthreads();
-        uint32_t tot = 0;
-        for (int w = 0; w < FIX_THREADS / 32; w++) tot += red[w];
-        __syncthreads();
-        return tot;
-    };
-
+    // Levels in order; within a level every midplane body is settled by its
+    // own thread: membership of a level-L cell can only have been changed by
+    // moves at shallower levels, collected in `moved`.
+    __shared__ uint32_t moved[TIE_CAP];
+    __shared__ uint32_t n_moved, n_moved_next;
+    if (threadIdx.x == 0) n_moved = n_moved_next = 0u;
+    __syncthreads();
     for (int L = 0; L < (int)depth_max && L < 16; L++) {
-        for (uint32_t t = 0; t < T; t++) {
-            if (!((mask[t] >> L) & 1u)) continue;  // uniform
+        for (uint32_t t = threadIdx.x; t < T; t += FIX_THREADS) {
+            if (!((mask[t] >> L) & 1u)) continue;
             const uint64_t pre = prefix_of(cur[t], L);
             const int shift = 3 * (16 - L);
-            if (threadIdx.x == 0) {
-                if (L == 0) {
-                    s_lo = 0;
-                    s_hi = nin;
-                } else {
-                    s_lo = lower_bound_shift(K, 0, nin, shift, pre);
-                    s_hi = lower_bound_shift(K, s_lo, nin, shift, pre + 1);
-                }
-            }
-            __syncthreads();
-            const uint32_t lo = s_lo, hi = s_hi;
+            const uint32_t lo = (L == 0) ? 0u : lower_bound_shift(K, 0, nin, shift, pre);
+            const uint32_t hi = (L == 0) ? nin : lower_bound_shift(K, lo, nin, shift, pre + 1);
             const uint32_t p = body[t];
-            // membership corrections from midplane bodies already moved
-            uint32_t c_in = 0, c_out = 0, r_in = 0, r_out = 0;
-            for (uint32_t u = threadIdx.x; u < T; u += FIX_THREADS) {
+            uint32_t add = 0, sub = 0, radd = 0, rsub = 0;
+            for (uint32_t m = 0; m < n_moved; m++) {
+                const uint32_t u = moved[m];
                 const bool pin = prefix_of(prov[u], L) == pre;
                 const bool cin = prefix_of(cur[u], L) == pre;
-                if (cin && !pin) { c_in++; if (body[u] < p) r_in++; }
-                if (pin && !cin) { c_out++; if (body[u] < p) r_out++; }
+                if (cin && !pin) { add++; if (body[u] < p) radd++; }
+                if (pin && !cin) { sub++; if (body[u] < p) rsub++; }
             }
-            const uint32_t add = block_sum(c_in), sub = block_sum(c_out);
-            const uint32_t radd = block_sum(r_in), rsub = block_sum(r_out);
             const uint32_t count = (hi - lo) + add - sub;
-            if (count <= leaf_cap) continue;  // node does not split: digit unused
-            // rank of p among the node's bodies in index order, decided only
-            // up to leaf_cap (early exit once enough smaller indices are seen)
+            if (count <= leaf_cap) {
+                mask[t] = 0u;  // the cell is a leaf for good: deeper digits unused
+                continue;
+            }
+            // rank of p among the cell's bodies in index order, decided up to
+            // leaf_cap (stop once enough smaller indices are seen)
             const uint32_t need = leaf_cap + rsub;
             uint32_t seen = 0;
-            for (uint32_t k0 = lo; k0 < hi; k0 += FIX_THREADS) {
-                const uint32_t k = k0 + threadIdx.x;
-                const uint32_t v = (k < hi && V[k] < p) ? 1u : 0u;
-                seen += block_sum(v);
-                if (seen >= need) break;
-            }
+            for (uint32_t k = lo; k < hi && seen < need; k++) seen += (V[k] < p) ? 1u : 0u;
             const uint32_t rank = seen + radd - rsub;
             const bool strict = rank < leaf_cap;
-            if (threadIdx.x == 0) {
-                const uint32_t q = p;
-                const float x[3] = {pos[3u * q], pos[3u * q + 1u], pos[3u * q + 2u]};
-                Cube c = cube_of(bounds, cur[t], L);
-                uint32_t o = 0;
-                for (int a = 0; a < 3; a++) {
-                    const float m = midf(c.lo[a], c.hi[a]);
-                    const bool up = strict ? (m < x[a]) : (m <= x[a]);
-                    o |= (up ? 1u : 0u) << a;
-                }
-                const uint32_t old = (uint32_t)(cur[t] >> (3 * (15 - L))) & 7u;
-                if (o != old) {
-                    uint64_t key = (L == 0 ? 0ull : (pre << (3 * (16 - L))));
-                    key |= (uint64_t)o << (3 * (15 - L));
-                    Cube cc = cube_of(bounds, key, L + 1);
-                    uint32_t tb = 0;
-                    key = descend(x, cc, key, L + 1, tb);
-                    cur[t] = key;
-                    mask[t] = (mask[t] & ((2u << L) - 1u)) | (tb & ~((2u << L) - 1u));
-                    s_changed = 1u;
-                }
+            const float x[3] = {pos[3u * p], pos[3u * p + 1u], pos[3u * p + 2u]};
+            Cube c = cube_of(bounds, cur[t], L);
+            uint32_t o = 0;
+            for (int a = 0; a < 3; a++) {
+                const float m = midf(c.lo[a], c.hi[a]);
+                const bool up = strict ? (m < x[a]) : (m <= x[a]);
+                o |= (up ? 1u : 0u) << a;
             }
-            __syncthreads();
+            const uint32_t old = (uint32_t)(cur[t] >> (3 * (15 - L))) & 7u;
+            if (o != old) {
+                uint64_t key = (L == 0 ? 0ull : (pre << (3 * (16 - L))));
+                key |= (uint64_t)o << (3 * (15 - L));
+                Cube cc = cube_of(bounds, key, L + 1);
+                uint32_t tb = 0;
+                key = descend(x, cc, key, L + 1, tb);
+                cur[t] = key;
+                mask[t] = (mask[t] & ((2u << L) - 1u)) | (tb & ~((2u << L) - 1u));
+                s_changed = 1u;
+                const uint32_t slot = atomicAdd(&n_moved_next, 1u);
+                if (slot < TIE_CAP) moved[slot] = t;
+            }
         }
+        __syncthreads();
+        if (threadIdx.x == 0) n_moved = min(n_moved_next, TIE_CAP);
+        __syncthreads();
     }
     __syncthreads();
     // write changed keys back at their sorted slots
@@ -527,6 +511,7 @@ int sf_tree_alloc(TreeWork** out, uint32_t n, const sfgpu_params& p) {
     SF_CUDA(cudaMalloc(&t->sp, sizeof(float4) * nn));
     SF_CUDA(cudaMalloc(&t->msum, sizeof(sfd4) * nn));
     SF_CUDA(cudaMalloc(&t->mpre, sizeof(sfd4) * (nn + 1)));
+    SF_CUDA(cudaMalloc(&t->walk_part, sizeof(float4) * sf_walk_scratch_floats4((uint32_t)nn)));
     if (sf_scan_reserve(t->scan_u32, (uint32_t)nn, sizeof(uint32_t)) != SFGPU_OK) return SFGPU_FAILURE;
     if (sf_scan_reserve(t->scan_d4, (uint32_t)nn, sizeof(sfd4)) != SFGPU_OK) return SFGPU_FAILURE;
     return SFGPU_OK;
@@ -553,6 +538,7 @@ void sf_tree_free(TreeWork* t) {
     cudaFree(t->nd.parent);
     cudaFree(t->nd.start);
     cudaFree(t->sp);
+    cudaFree(t->walk_part);
     cudaFree(t->msum);
     cudaFree(t->mpre);
     cudaFree(t->scan_u32.partials);

@@ -41,7 +41,10 @@ struct TreeWork {
     sfd4* msum = nullptr;    // (m x, m y, m z, m) per sorted slot, FP64
     sfd4* mpre = nullptr;    // exclusive prefix of msum (n+1)
     ScanWork scan_u32, scan_d4;
+    float4* walk_part = nullptr;  // split-walk partial sums (SPLIT x n)
 };
+
+size_t sf_walk_scratch_floats4(uint32_t n);
 
 int sf_tree_build(sfgpu_sim* s);
 int sf_walk_launch(sfgpu_sim* s);

@@ -198,11 +198,259 @@ int launch_kind(sfgpu_sim* s, bool stats) {
     return SFGPU_OK;
 }
 
+// ---- split walk (FAST / COMPENSATED) ----------------------------------------
+// The walk above runs one warp per 32 bodies: 2048 warps for 65,536 bodies,
+// about 13 per SM, each a chain of dependent node loads.  Here SPLIT warps
+// share a group of 32 bodies, warp p walking only the subtree of root octant
+// p (warp 0 also takes the root itself as a monopole for lanes that do not
+// open it).  Partial sums go to scratch and k_walk_reduce adds them in octant
+// order.  All four node vectors are loaded at once per visit, and the
+// opening test divides approximately, falling back to the IEEE divide only
+// within 2^-19 of theta, so every decision equals the reference's.
+constexpr int SPLIT = 8;
+
+__device__ __forceinline__ bool opens(const float4& G, float rx, float ry, float rz, const ForceConsts& fc,
+                                      float th_lo, float th_hi) {
+    const float ox = fsub(G.x, rx), oy = fsub(G.y, ry), oz = fsub(G.z, rz);
+    const float d2 = fadd(fadd(fmul(ox, ox), fmul(oy, oy)), fmul(oz, oz));
+    if (!(0.0f < d2)) return fc.theta <= 0.0f;
+    const float q = __fdividef(G.w, d2);
+    if (q > th_hi) return true;
+    if (q < th_lo) return false;
+    return fc.theta <= fdiv(G.w, d2);
+}
+
+template <int KIND>
+__device__ __forceinline__ void monopole(const float4& C, const float4& Lo, const float4& H, uint32_t bodies, float rx,
+                                         float ry, float rz, float mi, float eps2, KSum& ax, KSum& ay, KSum& az,
+                                         KSum& ph) {
+    float cx = C.x, cy = C.y, cz = C.z, mj = C.w;
+    if (Lo.x <= rx && rx <= Lo.w && Lo.y <= ry && ry <= H.x && Lo.z <= rz && rz <= H.y && 1u < bodies) {
+        cx = fsub(fmul(cx, mj), fmul(mi, rx));
+        cy = fsub(fmul(cy, mj), fmul(mi, ry));
+        cz = fsub(fmul(cz, mj), fmul(mi, rz));
+        mj = fsub(mj, mi);
+        const float f = (0.0f < mj) ? fdiv(1.0f, mj) : 1.0f;
+        cx = fmul(cx, f);
+        cy = fmul(cy, f);
+        cz = fmul(cz, f);
+    }
+    const float dx = cx - rx, dy = cy - ry, dz = cz - rz;
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
+    const float inv = rsqrtf(r2);
+    const float mphi = mj * inv;
+    const float f = mphi * (inv * inv);
+    if (KIND == WALK_COMP) {
+        ax.add(f * dx);
+        ay.add(f * dy);
+        az.add(f * dz);
+        ph.add(mphi);
+    } else {
+        ax.s = fmaf(f, dx, ax.s);
+        ay.s = fmaf(f, dy, ay.s);
+        az.s = fmaf(f, dz, az.s);
+        ph.s += mphi;
+    }
+}
+
+template <int KIND, bool STATS>
+__global__ void __launch_bounds__(WALK_THREADS) k_walk_split(const float4* __restrict__ sp,
+                                                             const uint32_t* __restrict__ V, uint32_t n,
+                                                             NodeArrays nd, ForceConsts fc, float th_lo, float th_hi,
+                                                             uint32_t leaf_cap, float4* __restrict__ part,
+                                                             uint32_t* __restrict__ st_int,
+                                                             uint32_t* __restrict__ st_open,
+                                                             unsigned long long* __restrict__ tot,
+                                                             uint32_t* d_status) {
+    __shared__ uint32_t s_node[WALK_WARPS][STACK];
+    __shared__ uint32_t s_mask[WALK_WARPS][STACK];
+    const int lane = threadIdx.x & 31;
+    const int w = threadIdx.x >> 5;
+    const uint32_t gw = blockIdx.x * WALK_WARPS + w;
+    const uint32_t group = gw / SPLIT;
+    const uint32_t oct = gw % SPLIT;
+    const uint32_t k = group * 32u + lane;
+    const bool live = k < n;
+    const uint32_t live_mask = __ballot_sync(0xffffffffu, live);
+    if (!live_mask) return;
+    const float4 b = live ? sp[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float rx = b.x, ry = b.y, rz = b.z, mi = b.w;
+    KSum ax{0.f, 0.f}, ay{0.f, 0.f}, az{0.f, 0.f}, ph{0.f, 0.f};
+    uint32_t n_int = 0, n_open = 0;
+    int top = 0;
+
+    {  // the root: opening test in every warp, monopole in warp 0 only
+        const float4 H = __ldg(&nd.hi[0]);
+        const float4 G = __ldg(&nd.geo[0]);
+        const float4 C = __ldg(&nd.com[0]);
+        const float4 Lo = __ldg(&nd.lo[0]);
+        const uint32_t bodies = __float_as_uint(H.z);
+        if (bodies > 0u) {
+            bool open = false;
+            if (bodies > leaf_cap && live) {
+                open = opens(G, rx, ry, rz, fc, th_lo, th_hi);
+                if (oct == 0) n_open++;
+            }
+            const uint32_t om = __ballot_sync(0xffffffffu, open);
+            if (oct == 0 && live && !open) {
+                monopole<KIND>(C, Lo, H, bodies, rx, ry, rz, mi, fc.eps2, ax, ay, az, ph);
+                n_int++;
+            }
+            const uint32_t first = __float_as_uint(H.w);
+            if (om && first != NODE_NONE) {
+                if (lane == 0) {
+                    s_node[w][0] = first + oct;
+                    s_mask[w][0] = om;
+                }
+                top = 1;
+            }
+        }
+    }
+    __syncwarp();
+    uint32_t guard = 0;
+    while (top > 0) {
+        top--;
+        const uint32_t v = s_node[w][top];
+        const uint32_t M = s_mask[w][top];
+        __syncwarp();
+        if (++guard > (1u << 26)) {
+            if (lane == 0) atomicOr(d_status, SFGPU_STATUS_WALK);
+            break;
+        }
+        const float4 H = __ldg(&nd.hi[v]);
+        const float4 G = __ldg(&nd.geo[v]);
+        const float4 C = __ldg(&nd.com[v]);
+        const float4 Lo = __ldg(&nd.lo[v]);
+        const uint32_t bodies = __float_as_uint(H.z);
+        if (bodies == 0u) continue;
+        const bool me = (M >> lane) & 1u;
+        uint32_t take = M;
+        if (bodies > leaf_cap) {
+            bool open = false;
+            if (me) {
+                open = opens(G, rx, ry, rz, fc, th_lo, th_hi);
+                n_open++;
+            }
+            const uint32_t om = __ballot_sync(0xffffffffu, open);
+            take = M & ~om;
+            if (om) {
+                const uint32_t first = __float_as_uint(H.w);
+                if (top + 8 > STACK || first == NODE_NONE) {
+                    if (lane == 0) atomicOr(d_status, SFGPU_STATUS_WALK);
+                    take = M;
+                } else {
+                    if (lane < 8) {
+                        s_node[w][top + lane] = first + 7u - (uint32_t)lane;
+                        s_mask[w][top + lane] = om;
+                    }
+                    top += 8;
+                }
+            }
+            __syncwarp();
+        }
+        if ((take >> lane) & 1u) {
+            monopole<KIND>(C, Lo, H, bodies, rx, ry, rz, mi, fc.eps2, ax, ay, az, ph);
+            n_int++;
+        }
+    }
+    if (live) {
+        if (KIND == WALK_COMP)
+            part[(size_t)oct * n + k] = make_float4(ax.s - ax.c, ay.s - ay.c, az.s - az.c, ph.s - ph.c);
+        else
+            part[(size_t)oct * n + k] = make_float4(ax.s, ay.s, az.s, ph.s);
+        if (STATS) {
+            const uint32_t p = V[k];
+            atomicAdd(&st_int[p], n_int);
+            atomicAdd(&st_open[p], n_open);
+        }
+    }
+    unsigned long long ci = n_int, co = n_open;
+    for (int o = 16; o > 0; o >>= 1) {
+        ci += __shfl_xor_sync(0xffffffffu, ci, o);
+        co += __shfl_xor_sync(0xffffffffu, co, o);
+    }
+    if (lane == 0) {
+        atomicAdd(&tot[0], ci);
+        atomicAdd(&tot[1], co);
+    }
+}
+
+// acc = G m_i sum_p S_p (S = -sum F), pot = -G sum_p phi_p, octant order.
+template <int KIND>
+__global__ void k_walk_reduce(const float4* __restrict__ part, const float4* __restrict__ sp,
+                              const uint32_t* __restrict__ V, uint32_t n, ForceConsts fc, float* __restrict__ acc,
+                              float* __restrict__ pot) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const float mi = sp[k].w;
+    const uint32_t p = V[k];
+    const float g = -fc.neg_g;
+    if (KIND == WALK_COMP) {
+        double x = 0, y = 0, z = 0, w = 0;
+        for (int o = 0; o < SPLIT; o++) {
+            const float4 t = part[(size_t)o * n + k];
+            x += t.x;
+            y += t.y;
+            z += t.z;
+            w += t.w;
+        }
+        const double scale = fc.physical ? (double)g : (double)g * (double)mi;
+        acc[3u * p + 0u] = (float)(scale * x);
+        acc[3u * p + 1u] = (float)(scale * y);
+        acc[3u * p + 2u] = (float)(scale * z);
+        pot[p] = (float)((double)fc.neg_g * w);
+    } else {
+        float4 s = part[k];
+        for (int o = 1; o < SPLIT; o++) {
+            const float4 t = part[(size_t)o * n + k];
+            s.x += t.x;
+            s.y += t.y;
+            s.z += t.z;
+            s.w += t.w;
+        }
+        const float scale = fc.physical ? g : g * mi;
+        acc[3u * p + 0u] = scale * s.x;
+        acc[3u * p + 1u] = scale * s.y;
+        acc[3u * p + 2u] = scale * s.z;
+        pot[p] = fc.neg_g * s.w;
+    }
+}
+
+template <int KIND>
+int launch_split(sfgpu_sim* s, bool stats) {
+    TreeWork* t = s->tree;
+    const ForceConsts fc = sf_force_consts(s->p);
+    const float th_lo = fc.theta * (1.0f - 1.0f / 524288.0f);
+    const float th_hi = fc.theta * (1.0f + 1.0f / 524288.0f);
+    const uint32_t groups = sf_ceil_div(s->n, 32);
+    const uint32_t grid = sf_ceil_div((uint64_t)groups * SPLIT, WALK_WARPS);
+    float* acc = s->slab + (size_t)6 * s->n;
+    float* pot = s->slab + (size_t)10 * s->n;
+    if (stats) {
+        SF_CUDA(cudaMemsetAsync(s->stat_int, 0, sizeof(uint32_t) * s->n, s->stream));
+        SF_CUDA(cudaMemsetAsync(s->stat_open, 0, sizeof(uint32_t) * s->n, s->stream));
+        k_walk_split<KIND, true><<<grid, WALK_THREADS, 0, s->stream>>>(t->sp, t->vals, s->n, t->nd, fc, th_lo, th_hi,
+                                                                       s->p.leaf_cap, t->walk_part, s->stat_int,
+                                                                       s->stat_open, s->walk_tot, s->d_status);
+    } else {
+        k_walk_split<KIND, false><<<grid, WALK_THREADS, 0, s->stream>>>(t->sp, t->vals, s->n, t->nd, fc, th_lo,
+                                                                        th_hi, s->p.leaf_cap, t->walk_part, nullptr,
+                                                                        nullptr, s->walk_tot, s->d_status);
+    }
+    SF_CHECK_LAUNCH();
+    k_walk_reduce<KIND><<<sf_ceil_div(s->n, 256), 256, 0, s->stream>>>(t->walk_part, t->sp, t->vals, s->n, fc, acc,
+                                                                       pot);
+    SF_CHECK_LAUNCH();
+    return SFGPU_OK;
+}
+
 }  // namespace
+
+size_t sf_walk_scratch_floats4(uint32_t n) { return (size_t)SPLIT * n; }
 
 int sf_walk_launch(sfgpu_sim* s) {
     const bool stats = (s->p.flags & SFGPU_FLAG_STATS) && s->stat_int;
     if (s->p.math == SFGPU_MATH_EXACT && s->p.form == SFGPU_FORM_PLAIN) return launch_kind<WALK_EXACT>(s, stats);
-    if (s->p.form == SFGPU_FORM_COMPENSATED) return launch_kind<WALK_COMP>(s, stats);
-    return launch_kind<WALK_FAST>(s, stats);
+    if (s->p.form == SFGPU_FORM_COMPENSATED) return launch_split<WALK_COMP>(s, stats);
+    return launch_split<WALK_FAST>(s, stats);
 }
