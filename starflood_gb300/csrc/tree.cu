@@ -213,10 +213,16 @@ __global__ void __launch_bounds__(FIX_THREADS) k_tie_fix(const float* __restrict
                 uint32_t tb = 0;
                 key = descend(x, cc, key, L + 1, tb);
                 cur[t] = key;
-                mask[t] = (mask[t] & ((2u << L) - 1u)) | (tb & ~((2u << L) - 1u));
+                // bit 31 marks bodies already in `moved`: each is listed once,
+                // however many levels it moves at (its correction is by its
+                // current key, so a second entry would count it twice)
+                const uint32_t listed = mask[t] & 0x80000000u;
+                mask[t] = (mask[t] & ((2u << L) - 1u)) | (tb & ~((2u << L) - 1u) & 0xFFFFu) | 0x80000000u;
                 s_changed = 1u;
-                const uint32_t slot = atomicAdd(&n_moved_next, 1u);
-                if (slot < TIE_CAP) moved[slot] = t;
+                if (!listed) {
+                    const uint32_t slot = atomicAdd(&n_moved_next, 1u);
+                    if (slot < TIE_CAP) moved[slot] = t;
+                }
             }
         }
         __syncthreads();
