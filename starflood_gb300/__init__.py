@@ -82,6 +82,7 @@ def lib():
             "sfgpu_tree_num_nodes": (i32, [vp, u32p]),
             "sfgpu_tree_export": (i32, [vp, u32p, u32p, u32p, f32p, f32p]),
             "sfgpu_gravity_pp": (i32, [P, u32, vp, vp, vp, vp, vp]),
+            "sfgpu_gravity_pp_noalloc": (i32, [P, u32, vp, vp, vp, vp, vp]),
             "sfgpu_batch_create": (i32, [C.POINTER(vp), u32, u32p, P]),
             "sfgpu_batch_destroy": (i32, [vp]),
             "sfgpu_batch_upload": (i32, [vp, vp, vp, vp]),

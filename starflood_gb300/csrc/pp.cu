@@ -258,3 +258,97 @@ int sf_stage_gravity_pp(sfgpu_sim* s) {
     return sf_pp_launch(s->p, s->n, s->slab, s->slab + (size_t)9 * s->n, acc, pot, &s->pp_part, &s->pp_part_cap,
                         s->stream, s->pos64);
 }
+
+// ---------------------------------------------------------------------------
+// PP force without allocation (sfgpu_gravity_pp_noalloc).
+//
+// For callers that cannot call cudaMalloc: the j-split partial sums that
+// sfgpu_gravity_pp keeps in a cudaMalloc'd work buffer live instead in the
+// file-scope array below, 16 MiB (NOALLOC_PARTS float4 entries), which every
+// GPU that loads this library holds until the process exits.  The number of
+// j-splits is lowered until the partials fit; N above NOALLOC_PARTS (plain
+// form) or NOALLOC_PARTS/2 (compensated form) is rejected.  Nothing in the
+// array needs clearing between calls: every partial that the reduction reads
+// is written by the same call first.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+namespace {
+constexpr size_t NOALLOC_PARTS = (size_t)1 << 20;
+static __device__ __align__(256) float4 g_noalloc_parts[NOALLOC_PARTS];
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_mutex;
+float4* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {nullptr};
+
+// Device address of g_noalloc_parts on the current device: looked up once
+// per device (the host-side symbol is not a device address).
+int noalloc_parts(float4** out) {
+    int dev = 0;
+    SF_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) {
+        sf_set_error("sfgpu_gravity_pp_noalloc: device %d out of range", dev);
+        return SFGPU_FAILURE;
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+        void* ptr = nullptr;
+        SF_CUDA(cudaGetSymbolAddress(&ptr, g_noalloc_parts));
+        g_noalloc_ptr[dev] = (float4*)ptr;
+    }
+    *out = g_noalloc_ptr[dev];
+    return SFGPU_OK;
+}
+}  // namespace
+
+extern "C" int sfgpu_gravity_pp_noalloc(const sfgpu_params* p, uint32_t n, const float* pos, const float* mas,
+                                        float* acc, float* pot, void* stream) {
+    sf_clear_error();
+    if (!p) {
+        sf_set_error("sfgpu_gravity_pp_noalloc: params is NULL");
+        return SFGPU_FAILURE;
+    }
+    if (!(p->eps > 0.0)) {
+        sf_set_error("sfgpu_gravity_pp_noalloc: eps must be > 0");
+        return SFGPU_FAILURE;
+    }
+    if (p->math == SFGPU_MATH_EXACT && p->form == SFGPU_FORM_COMPENSATED) {
+        sf_set_error("sfgpu_gravity_pp_noalloc: EXACT math applies to the PLAIN form only");
+        return SFGPU_FAILURE;
+    }
+    const bool comp = p->form == SFGPU_FORM_COMPENSATED;
+    const size_t per_split = (size_t)n * (comp ? 2 : 1);
+    if (per_split > NOALLOC_PARTS) {
+        sf_set_error("sfgpu_gravity_pp_noalloc: N = %u exceeds the maximum of %zu bodies (%s form) of the "
+                     "built-in %zu MiB work array",
+                     n, comp ? NOALLOC_PARTS / 2 : NOALLOC_PARTS, comp ? "compensated" : "plain",
+                     (NOALLOC_PARTS * sizeof(float4)) >> 20);
+        return SFGPU_FAILURE;
+    }
+    if (n == 0) return SFGPU_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    const ForceConsts fc = sf_force_consts(*p);
+    if (p->math == SFGPU_MATH_EXACT) {  // needs no work array at all
+        k_pp_exact<<<sf_ceil_div(n, EXACT_BS), EXACT_BS, 0, st>>>(pos, mas, n, fc, acc, pot);
+        SF_CHECK_LAUNCH();
+        return SFGPU_OK;
+    }
+    float4* parts = nullptr;
+    if (noalloc_parts(&parts) != SFGPU_OK) return SFGPU_FAILURE;
+    const PPShape sh = pp_shape(n);
+    uint32_t nsplit = std::min<uint32_t>(sh.nsplit, (uint32_t)(NOALLOC_PARTS / per_split));
+    uint32_t jchunk = sf_ceil_div(sf_ceil_div(n, nsplit), FAST_BS) * FAST_BS;
+    nsplit = sf_ceil_div(n, jchunk);
+    dim3 grid(sh.iblocks, nsplit);
+    if (comp)
+        k_pp_tile<FAST_BS, FAST_IPT, true><<<grid, FAST_BS, 0, st>>>(pos, mas, nullptr, n, fc.eps2, jchunk, parts);
+    else
+        k_pp_tile<FAST_BS, FAST_IPT, false><<<grid, FAST_BS, 0, st>>>(pos, mas, nullptr, n, fc.eps2, jchunk, parts);
+    SF_CHECK_LAUNCH();
+    if (comp)
+        k_pp_reduce<true><<<sf_ceil_div(n, 256), 256, 0, st>>>(parts, n, nsplit, mas, fc, acc, pot);
+    else
+        k_pp_reduce<false><<<sf_ceil_div(n, 256), 256, 0, st>>>(parts, n, nsplit, mas, fc, acc, pot);
+    SF_CHECK_LAUNCH();
+    return SFGPU_OK;
+}
