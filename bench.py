@@ -338,6 +338,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-pp", action="store_true", help="skip the N=1M PP sub-benchmark")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     args = ap.parse_args()
     rank, world, local = env_rank()
 
@@ -400,7 +401,7 @@ def main():
             "stage_ms_per_step": stage_ms, "device_status": r["status"]}
     if rank == 0:
         try:
-            line["cpu_baseline"] = cpu_bh_rate(max_seconds=10.0)
+            line["cpu_baseline"] = {"skipped": "--no-cpu"} if args.no_cpu else cpu_bh_rate(max_seconds=10.0)
         except Exception as e:  # the baseline must not hide the GPU line
             line["cpu_baseline"] = {"error": str(e)}
         if not args.no_pp:
@@ -413,7 +414,7 @@ def main():
                 ips = pp[k]["interactions_per_s"]
                 pp[k]["roofline_frac"] = ips * FLOP_INTERACTION / (peak * 1e12)
             try:
-                pp["cpu_baseline"] = cpu_pp_rate()
+                pp["cpu_baseline"] = {"skipped": "--no-cpu"} if args.no_cpu else cpu_pp_rate()
             except Exception as e:
                 pp["cpu_baseline"] = {"error": str(e)}
             pp["workload"] = "PP gravity N=1048576 Plummer a=1 M=1 eps=0.005, 20 flop/interaction"
