@@ -77,7 +77,8 @@ typedef struct {
     double   sph_alpha;   /* CUBIC: Monaghan viscosity alpha                */
     double   sph_beta;    /* CUBIC: Monaghan viscosity beta                 */
     uint32_t flags;       /* SFGPU_FLAG_*                                   */
-    uint32_t reserved[7];
+    uint32_t walk_split;  /* walk threads per body: 0 auto, 1, or 8 (one per root octant) */
+    uint32_t reserved[6];
 } sfgpu_params;
 
 /* flags */

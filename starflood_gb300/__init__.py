@@ -36,7 +36,8 @@ class Params(C.Structure):
                 ("solver", C.c_int32), ("sph", C.c_int32), ("math", C.c_int32), ("form", C.c_int32),
                 ("acc_mode", C.c_int32), ("leaf_cap", C.c_uint32), ("depth_max", C.c_uint32),
                 ("nodes_max", C.c_uint32), ("sph_gamma", C.c_double), ("sph_alpha", C.c_double),
-                ("sph_beta", C.c_double), ("flags", C.c_uint32), ("reserved", C.c_uint32 * 7)]
+                ("sph_beta", C.c_double), ("flags", C.c_uint32), ("walk_split", C.c_uint32),
+                ("reserved", C.c_uint32 * 6)]
 
 
 _lib = None

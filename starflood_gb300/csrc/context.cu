@@ -192,6 +192,7 @@ extern "C" int sfgpu_destroy(sfgpu_sim* s) {
     cudaFree(s->sums);
     cudaFree(s->d_status);
     cudaFree(s->d_step);
+    cudaFree(s->d_done);
     cudaFree(s->d_bounds);
     cudaFree(s->stat_int);
     cudaFree(s->stat_open);
@@ -248,6 +249,8 @@ extern "C" int sfgpu_create(sfgpu_sim** out, uint32_t n, const sfgpu_params* p) 
     TRY(cudaMemsetAsync(s->sums, 0, sizeof(double) * 16, s->stream));
     TRY(cudaMalloc(&s->d_status, sizeof(uint32_t)));
     TRY(cudaMemsetAsync(s->d_status, 0, sizeof(uint32_t), s->stream));
+    TRY(cudaMalloc(&s->d_done, sizeof(uint32_t) * 4));
+    TRY(cudaMemsetAsync(s->d_done, 0, sizeof(uint32_t) * 4, s->stream));
     TRY(cudaMalloc(&s->d_step, sizeof(uint32_t)));
     TRY(cudaMemsetAsync(s->d_step, 0, sizeof(uint32_t), s->stream));
     TRY(cudaMalloc(&s->d_bounds, sizeof(float) * 8));
@@ -407,7 +410,7 @@ extern "C" int sfgpu_run(sfgpu_sim* s, uint32_t first_step, uint32_t nsteps) {
         return SFGPU_OK;
     }
     if (!s->graph) {
-        // step_body advances d_step itself (k_energy_final), so one captured
+        // step_body advances d_step itself (k_kick_energy), so one captured
         // step replays correctly for any step number.
         cudaGraph_t g = nullptr;
         SF_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));

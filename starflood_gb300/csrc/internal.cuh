@@ -199,6 +199,7 @@ struct sfgpu_sim {
     double* sums = nullptr;        // [0]=T [1]=V [2]=Tcorr [3]=U [4]=mean radius ...
     uint32_t* d_status = nullptr;
     uint32_t* d_step = nullptr;
+    uint32_t* d_done = nullptr;    // last-block tickets of the fused reductions
     float* d_bounds = nullptr;     // root cube (6 floats)
     TreeWork* tree = nullptr;
     void* sph = nullptr;           // SphWork (sph.cu)
@@ -221,7 +222,6 @@ int sf_stage_tree_solve(sfgpu_sim* s, bool radius_ready);
 int sf_stage_sph(sfgpu_sim* s);
 int sf_stage_kick_drift(sfgpu_sim* s, bool want_radius);
 int sf_stage_radius(sfgpu_sim* s);
-int sf_stage_bounds(sfgpu_sim* s);
 int sf_stage_kick_energy(sfgpu_sim* s);
 int sf_sph_alloc(sfgpu_sim* s);
 void sf_sph_free(sfgpu_sim* s);

@@ -5,12 +5,12 @@
 //   k_kick_drift   kick_0 and drift for one body per thread (each component
 //                  rounded exactly as the reference: v + ((dt/2) a), x + dt v)
 //                  and, for the tree, the body's FP64 distance from the origin
-//                  summed per block in double-double;
-//   k_bounds       mean radius from the block sums, pcg4d jitter of the step
-//                  number, the jittered root cube rounded to FP32;
-//   k_kick_energy  kick_1, ken = (m/2) v^2, pen = m pot, and per-block
-//                  double-double sums of ken, pen and the corrected energies;
-//   k_energy_final adds the block sums in a fixed order.
+//                  summed per block in double-double; the last block adds the
+//                  block sums, takes the mean radius, hashes the step number
+//                  with pcg4d and writes the jittered root cube in FP32;
+//   k_kick_energy  kick_1, ken = (m/2) v^2, pen = m pot, per-block
+//                  double-double sums of ken, pen and the corrected energies,
+//                  added in block order by the last block.
 //
 // Bytes per body: kick/drift reads pos, vel, acc (36 B) and writes pos, vel
 // (24 B); kick/energy reads vel, acc, mas, pot (32 B), writes vel, ken, pen
@@ -47,10 +47,71 @@ __device__ __forceinline__ double radius64(float x, float y, float z) {
     return __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
 }
 
+// The last block to finish (ticket from an atomic counter, reset for the
+// next launch) adds up the per-block partials in block order, so the totals
+// are deterministic, and no separate single-block launch is needed.
+__device__ bool last_block(uint32_t* done) {
+    __shared__ bool s_last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const uint32_t ticket = atomicAdd(done, 1u);
+        s_last = ticket == gridDim.x - 1;
+        if (s_last) *done = 0u;
+    }
+    __syncthreads();
+    if (s_last) __threadfence();
+    return s_last;
+}
+
+template <int NV>
+__device__ void sum_partials(const double2* part, uint32_t nparts, double* out) {
+    double2 v[NV];
+    for (int k = 0; k < NV; k++) v[k] = make_double2(0.0, 0.0);
+    for (uint32_t b = threadIdx.x; b < nparts; b += SF_RED_BLOCK)
+        for (int k = 0; k < NV; k++) v[k] = dd_add(v[k], __ldcg(&part[(size_t)b * NV + k]));
+    __shared__ double2 total[NV];
+    __shared__ double2 sh[NV][SF_RED_BLOCK];
+    for (int k = 0; k < NV; k++) sh[k][threadIdx.x] = v[k];
+    __syncthreads();
+    for (int off = SF_RED_BLOCK / 2; off > 0; off >>= 1) {
+        if ((int)threadIdx.x < off)
+            for (int k = 0; k < NV; k++) sh[k][threadIdx.x] = dd_add(sh[k][threadIdx.x], sh[k][threadIdx.x + off]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int k = 0; k < NV; k++) out[k] = __dadd_rn(sh[k][0].x, sh[k][0].y);
+    (void)total;
+}
+
+// simulation.c:276-301: mean radius -> jittered root cube
+__device__ void root_cube(double sum, uint32_t n, uint32_t step, float* __restrict__ bounds, double* __restrict__ sums) {
+    const double rbar = __dmul_rn(sum, 1.0 / (double)n);
+    uint32_t a = 0x638FE17Bu + step, b = 0xB10BDCE7u, c = 0x7B8ADB9Bu, d = 0xD8C5850Eu;
+    pcg4d(a, b, c, d);
+    const uint32_t h[3] = {a, b, c};
+    for (int k = 0; k < 3; k++) {
+        const double j = __dsub_rn(__dmul_rn(2.0, __dmul_rn(K_INV_U32, (double)h[k])), 1.0);
+        const double shift = __dmul_rn(__dmul_rn(0.5, j), rbar);
+        bounds[k] = __double2float_rn(__dadd_rn(__dmul_rn(-2.000, rbar), shift));
+        bounds[3 + k] = __double2float_rn(__dadd_rn(__dmul_rn(2.000, rbar), shift));
+    }
+    sums[4] = rbar;
+}
+
+__device__ void finish_bounds(const double2* part, uint32_t n, const uint32_t* d_step, float* bounds, double* sums) {
+    __shared__ double tot[1];
+    sum_partials<1>(part, gridDim.x, tot);
+    __syncthreads();
+    if (threadIdx.x == 0) root_cube(tot[0], n, *d_step, bounds, sums);
+}
+
 __global__ void __launch_bounds__(SF_RED_BLOCK) k_kick_drift(float* __restrict__ slab, uint32_t n, float half_dt,
                                                              float dt, double* __restrict__ pos64,
                                                              double* __restrict__ vel64, double dt64,
-                                                             int want_radius, double2* __restrict__ part) {
+                                                             int want_radius, double2* __restrict__ part,
+                                                             uint32_t* done, const uint32_t* __restrict__ d_step,
+                                                             float* __restrict__ bounds, double* __restrict__ sums) {
     const uint32_t i = blockIdx.x * SF_RED_BLOCK + threadIdx.x;
     float* pos = slab;
     float* vel = slab + (size_t)3 * n;
@@ -79,47 +140,27 @@ __global__ void __launch_bounds__(SF_RED_BLOCK) k_kick_drift(float* __restrict__
         }
         if (want_radius) r[0] = make_double2(radius64(x[0], x[1], x[2]), 0.0);
     }
-    if (want_radius) block_dd_reduce<1>(r, part);
+    if (!want_radius) return;
+    block_dd_reduce<1>(r, part);
+    if (last_block(done)) finish_bounds(part, n, d_step, bounds, sums);
 }
 
 __global__ void __launch_bounds__(SF_RED_BLOCK) k_radius(const float* __restrict__ pos, uint32_t n,
-                                                         double2* __restrict__ part) {
+                                                         double2* __restrict__ part, uint32_t* done,
+                                                         const uint32_t* __restrict__ d_step,
+                                                         float* __restrict__ bounds, double* __restrict__ sums) {
     const uint32_t i = blockIdx.x * SF_RED_BLOCK + threadIdx.x;
     double2 r[1] = {make_double2(0.0, 0.0)};
     if (i < n) r[0] = make_double2(radius64(pos[3u * i], pos[3u * i + 1u], pos[3u * i + 2u]), 0.0);
     block_dd_reduce<1>(r, part);
-}
-
-// simulation.c:276-301
-__global__ void __launch_bounds__(SF_RED_BLOCK) k_bounds(const double2* __restrict__ part, uint32_t nparts,
-                                                         uint32_t n, const uint32_t* __restrict__ d_step,
-                                                         float* __restrict__ bounds, double* __restrict__ sums) {
-    double2 v[1] = {make_double2(0.0, 0.0)};
-    for (uint32_t b = threadIdx.x; b < nparts; b += SF_RED_BLOCK) v[0] = dd_add(v[0], part[b]);
-    __shared__ double2 total[1];
-    // reuse the block reducer with a one-block grid (writes total[0])
-    block_dd_reduce<1>(v, total);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        const double sum = __dadd_rn(total[0].x, total[0].y);
-        const double rbar = __dmul_rn(sum, 1.0 / (double)n);
-        uint32_t a = 0x638FE17Bu + *d_step, b = 0xB10BDCE7u, c = 0x7B8ADB9Bu, d = 0xD8C5850Eu;
-        pcg4d(a, b, c, d);
-        const uint32_t h[3] = {a, b, c};
-        for (int k = 0; k < 3; k++) {
-            const double j = __dsub_rn(__dmul_rn(2.0, __dmul_rn(K_INV_U32, (double)h[k])), 1.0);
-            const double shift = __dmul_rn(__dmul_rn(0.5, j), rbar);
-            bounds[k] = __double2float_rn(__dadd_rn(__dmul_rn(-2.000, rbar), shift));
-            bounds[3 + k] = __double2float_rn(__dadd_rn(__dmul_rn(2.000, rbar), shift));
-        }
-        sums[4] = rbar;
-    }
+    if (last_block(done)) finish_bounds(part, n, d_step, bounds, sums);
 }
 
 __global__ void __launch_bounds__(SF_RED_BLOCK) k_kick_energy(float* __restrict__ slab, uint32_t n, float half_dt,
                                                               double* __restrict__ vel64, double dt64,
                                                               float g_over_eps, int physical,
-                                                              double2* __restrict__ part) {
+                                                              double2* __restrict__ part, uint32_t* done,
+                                                              double* __restrict__ sums, uint32_t* d_step) {
     const uint32_t i = blockIdx.x * SF_RED_BLOCK + threadIdx.x;
     float* vel = slab + (size_t)3 * n;
     const float* acc = slab + (size_t)6 * n;
@@ -163,19 +204,10 @@ __global__ void __launch_bounds__(SF_RED_BLOCK) k_kick_energy(float* __restrict_
         e[3] = make_double2(upair, 0.0);
     }
     block_dd_reduce<4>(e, part);
-}
-
-__global__ void __launch_bounds__(SF_RED_BLOCK) k_energy_final(const double2* __restrict__ part, uint32_t nparts,
-                                                               double* __restrict__ sums, uint32_t* d_step) {
-    double2 v[4] = {make_double2(0, 0), make_double2(0, 0), make_double2(0, 0), make_double2(0, 0)};
-    for (uint32_t b = threadIdx.x; b < nparts; b += SF_RED_BLOCK)
-        for (int k = 0; k < 4; k++) v[k] = dd_add(v[k], part[(size_t)b * 4 + k]);
-    __shared__ double2 total[4];
-    block_dd_reduce<4>(v, total);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int k = 0; k < 4; k++) sums[k] = __dadd_rn(total[k].x, total[k].y);
-        *d_step += 1u;
+    if (last_block(done)) {
+        // simulation.c:455-497: T = sum ken, V = sum pen (FP64)
+        sum_partials<4>(part, gridDim.x, sums);
+        if (threadIdx.x == 0) *d_step += 1u;
     }
 }
 
@@ -194,8 +226,9 @@ int sf_stage_kick_drift(sfgpu_sim* s, bool want_radius) {
     const uint32_t nb = sf_ceil_div(s->n, SF_RED_BLOCK);
     if (ensure_red(s, nb * 4) != SFGPU_OK) return SFGPU_FAILURE;
     const float dt = (float)s->p.dt;
-    k_kick_drift<<<nb, SF_RED_BLOCK, 0, s->stream>>>(s->slab, s->n, 0.5f * dt, dt, s->pos64, s->vel64,
-                                                     s->p.dt, want_radius ? 1 : 0, s->red);
+    k_kick_drift<<<nb, SF_RED_BLOCK, 0, s->stream>>>(s->slab, s->n, 0.5f * dt, dt, s->pos64, s->vel64, s->p.dt,
+                                                     want_radius ? 1 : 0, s->red, s->d_done, s->d_step, s->d_bounds,
+                                                     s->sums);
     SF_CHECK_LAUNCH();
     return SFGPU_OK;
 }
@@ -203,14 +236,7 @@ int sf_stage_kick_drift(sfgpu_sim* s, bool want_radius) {
 int sf_stage_radius(sfgpu_sim* s) {
     const uint32_t nb = sf_ceil_div(s->n, SF_RED_BLOCK);
     if (ensure_red(s, nb * 4) != SFGPU_OK) return SFGPU_FAILURE;
-    k_radius<<<nb, SF_RED_BLOCK, 0, s->stream>>>(s->slab, s->n, s->red);
-    SF_CHECK_LAUNCH();
-    return SFGPU_OK;
-}
-
-int sf_stage_bounds(sfgpu_sim* s) {
-    const uint32_t nb = sf_ceil_div(s->n, SF_RED_BLOCK);
-    k_bounds<<<1, SF_RED_BLOCK, 0, s->stream>>>(s->red, nb, s->n, s->d_step, s->d_bounds, s->sums);
+    k_radius<<<nb, SF_RED_BLOCK, 0, s->stream>>>(s->slab, s->n, s->red, s->d_done, s->d_step, s->d_bounds, s->sums);
     SF_CHECK_LAUNCH();
     return SFGPU_OK;
 }
@@ -220,10 +246,9 @@ int sf_stage_kick_energy(sfgpu_sim* s) {
     if (ensure_red(s, nb * 4) != SFGPU_OK) return SFGPU_FAILURE;
     const float dt = (float)s->p.dt;
     const float g_over_eps = (float)(s->p.G / s->p.eps);
-    k_kick_energy<<<nb, SF_RED_BLOCK, 0, s->stream>>>(s->slab, s->n, 0.5f * dt, s->vel64, s->p.dt,
-                                                      g_over_eps, s->p.acc_mode == SFGPU_ACC_PHYSICAL, s->red);
-    SF_CHECK_LAUNCH();
-    k_energy_final<<<1, SF_RED_BLOCK, 0, s->stream>>>(s->red, nb, s->sums, s->d_step);
+    k_kick_energy<<<nb, SF_RED_BLOCK, 0, s->stream>>>(s->slab, s->n, 0.5f * dt, s->vel64, s->p.dt, g_over_eps,
+                                                      s->p.acc_mode == SFGPU_ACC_PHYSICAL, s->red, s->d_done + 1,
+                                                      s->sums, s->d_step);
     SF_CHECK_LAUNCH();
     return SFGPU_OK;
 }

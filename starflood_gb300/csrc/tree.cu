@@ -129,24 +129,52 @@ __device__ __forceinline__ uint32_t lower_bound_shift(const uint64_t* __restrict
     return lo;
 }
 
+// The same, probing lo+1, lo+3, lo+7, ... first: O(log d) loads when the
+// answer is d slots past lo (cells deep in the tree are short runs).
+__device__ __forceinline__ uint32_t gallop_shift(const uint64_t* __restrict__ K, uint32_t lo, uint32_t hi, int shift,
+                                                 uint64_t target) {
+    if (lo >= hi || (K[lo] >> shift) >= target) return lo;
+    uint32_t prev = lo, step = 1;
+    while (true) {
+        const uint32_t probe = prev + step;
+        if (probe >= hi || probe < prev) return lower_bound_shift(K, prev + 1, hi, shift, target);
+        if ((K[probe] >> shift) >= target) return lower_bound_shift(K, prev + 1, probe, shift, target);
+        prev = probe;
+        step <<= 1;
+    }
+}
+
+// First index in [0, hi) whose key >> shift is >= target, probing backwards
+// from hi-1, whose key is known to be >= target.
+__device__ __forceinline__ uint32_t gallop_back(const uint64_t* __restrict__ K, uint32_t hi, int shift,
+                                                uint64_t target) {
+    uint32_t cur = hi - 1, step = 1;
+    while (true) {
+        if (cur < step) return lower_bound_shift(K, 0, cur, shift, target);
+        const uint32_t probe = cur - step;
+        if ((K[probe] >> shift) < target) return lower_bound_shift(K, probe + 1, cur, shift, target);
+        cur = probe;
+        step <<= 1;
+    }
+}
+
 __device__ __forceinline__ uint64_t prefix_of(uint64_t key, int L) { return L == 0 ? 0ull : key >> (3 * (16 - L)); }
 
 // Exact digits for bodies lying on a midplane (one block; see file comment).
 constexpr int FIX_THREADS = 1024;
 __global__ void __launch_bounds__(FIX_THREADS) k_tie_fix(const float* __restrict__ pos, const float* __restrict__ bounds,
-                                                         uint64_t* __restrict__ K, const uint32_t* __restrict__ V,
+                                                         uint64_t* __restrict__ K, uint32_t* __restrict__ V,
                                                          const uint32_t* __restrict__ nin_p, const uint2* __restrict__ ties,
                                                          const uint32_t* __restrict__ tie_count, uint32_t leaf_cap,
-                                                         uint32_t depth_max, uint32_t* __restrict__ resort) {
+                                                         uint32_t depth_max, uint32_t* __restrict__ resort,
+                                                         uint64_t* __restrict__ K2, uint32_t* __restrict__ V2) {
     __shared__ uint64_t prov[TIE_CAP];
     __shared__ uint64_t cur[TIE_CAP];
     __shared__ uint32_t body[TIE_CAP];
     __shared__ uint32_t mask[TIE_CAP];
-    __shared__ uint32_t s_changed;
     const uint32_t T = min(*tie_count, TIE_CAP);
     if (threadIdx.x == 0) {
         *resort = 0u;
-        s_changed = 0u;
     }
     if (T == 0) return;
     const uint32_t nin = *nin_p;
@@ -218,7 +246,6 @@ __global__ void __launch_bounds__(FIX_THREADS) k_tie_fix(const float* __restrict
                 // current key, so a second entry would count it twice)
                 const uint32_t listed = mask[t] & 0x80000000u;
                 mask[t] = (mask[t] & ((2u << L) - 1u)) | (tb & ~((2u << L) - 1u) & 0xFFFFu) | 0x80000000u;
-                s_changed = 1u;
                 if (!listed) {
                     const uint32_t slot = atomicAdd(&n_moved_next, 1u);
                     if (slot < TIE_CAP) moved[slot] = t;
@@ -230,14 +257,79 @@ __global__ void __launch_bounds__(FIX_THREADS) k_tie_fix(const float* __restrict
         __syncthreads();
     }
     __syncthreads();
-    // write changed keys back at their sorted slots
-    for (uint32_t t = threadIdx.x; t < T; t += FIX_THREADS) {
-        if (cur[t] == prov[t]) continue;
+    const uint32_t M = n_moved;
+    if (threadIdx.x == 0) *resort = M;
+    if (M == 0) return;
+    // Restore the (key, index) order in place of a second sort: the moved
+    // bodies leave their old slots and are merged back at their new keys.
+    __shared__ uint32_t mpos[TIE_CAP];   // old slot of each moved body, ascending
+    __shared__ uint64_t mkey[TIE_CAP];   // new keys, ascending by (key, body)
+    __shared__ uint32_t mbody[TIE_CAP];
+    for (uint32_t m = threadIdx.x; m < M; m += FIX_THREADS) {
+        const uint32_t t = moved[m];
         uint32_t k = lower_bound_shift(K, 0, nin, 0, prov[t]);
-        while (k < nin && K[k] == prov[t] && V[k] != body[t]) k++;
-        if (k < nin && V[k] == body[t]) K[k] = cur[t];
+        while (k < nin && V[k] != body[t]) k++;
+        uint32_t r_key = 0;
+        for (uint32_t q = 0; q < M; q++) {
+            const uint32_t u = moved[q];
+            if (cur[u] < cur[t] || (cur[u] == cur[t] && body[u] < body[t])) r_key++;
+        }
+        mkey[r_key] = cur[t];
+        mbody[r_key] = body[t];
+        prov[t] = (uint64_t)k;  // reuse: old slot
     }
-    if (threadIdx.x == 0) *resort = s_changed;
+    __syncthreads();
+    for (uint32_t m = threadIdx.x; m < M; m += FIX_THREADS) {
+        const uint32_t t = moved[m];
+        uint32_t r = 0;
+        for (uint32_t q = 0; q < M; q++)
+            if (prov[moved[q]] < prov[t]) r++;
+        mpos[r] = (uint32_t)prov[t];
+    }
+    __syncthreads();
+    auto below_pos = [&](uint32_t k) {  // moved bodies with old slot < k
+        uint32_t lo = 0, hi = M;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (mpos[mid] < k) lo = mid + 1; else hi = mid;
+        }
+        return lo;
+    };
+    auto below_key = [&](uint64_t key, uint32_t b) {  // moved bodies with (new key, body) < (key, b)
+        uint32_t lo = 0, hi = M;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (mkey[mid] < key || (mkey[mid] == key && mbody[mid] < b)) lo = mid + 1; else hi = mid;
+        }
+        return lo;
+    };
+    for (uint32_t k = threadIdx.x; k < nin; k += FIX_THREADS) {
+        const uint32_t bp = below_pos(k);
+        if (bp < M && mpos[bp] == k) continue;  // a moved body's old slot
+        const uint64_t key = K[k];
+        const uint32_t b = V[k];
+        const uint32_t dst = k - bp + below_key(key, b);
+        K2[dst] = key;
+        V2[dst] = b;
+    }
+    for (uint32_t m = threadIdx.x; m < M; m += FIX_THREADS) {
+        // stayed bodies before the new key: binary search on (K, V), minus moved slots below it
+        const uint64_t key = mkey[m];
+        const uint32_t b = mbody[m];
+        uint32_t lo = 0, hi = nin;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (K[mid] < key || (K[mid] == key && V[mid] < b)) lo = mid + 1; else hi = mid;
+        }
+        const uint32_t dst = lo - below_pos(lo) + m;
+        K2[dst] = key;
+        V2[dst] = b;
+    }
+    __syncthreads();
+    for (uint32_t k = threadIdx.x; k < nin; k += FIX_THREADS) {
+        K[k] = K2[k];
+        V[k] = V2[k];
+    }
 }
 
 // s(k): number of split nodes whose range starts at sorted position k.
@@ -297,19 +389,6 @@ __device__ __forceinline__ void write_node(NodeArrays nd, uint32_t v, const Cube
     nd.start[v] = start;
 }
 
-__global__ void k_root(const float* __restrict__ bounds, const uint32_t* __restrict__ nin_p, uint32_t leaf_cap,
-                       uint32_t depth_max, NodeArrays nd, float third) {
-    if (blockIdx.x || threadIdx.x) return;
-    Cube c;
-    for (int a = 0; a < 3; a++) {
-        c.lo[a] = bounds[a];
-        c.hi[a] = bounds[3 + a];
-    }
-    const uint32_t nin = *nin_p;
-    const bool split = nin > leaf_cap && depth_max > 0;
-    write_node(nd, 0, c, nin, split ? 1u : NODE_NONE, 0u, 0u, third);
-}
-
 __global__ void k_split_fill(const uint64_t* __restrict__ K, const uint32_t* __restrict__ nin_p,
                              const uint32_t* __restrict__ sbase, const uint32_t* __restrict__ nsplit_p,
                              uint32_t split_cap, const uint32_t* __restrict__ split_start,
@@ -318,12 +397,20 @@ __global__ void k_split_fill(const uint64_t* __restrict__ K, const uint32_t* __r
                              uint32_t* __restrict__ split_node) {
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t ns = min(*nsplit_p, split_cap);
-    if (s >= ns) return;
     const uint32_t nin = *nin_p;
+    if (s == 0) {  // the root record (tree.c:156-159: bounds = the root cube)
+        Cube r;
+        for (int a = 0; a < 3; a++) {
+            r.lo[a] = bounds[a];
+            r.hi[a] = bounds[3 + a];
+        }
+        write_node(nd, 0, r, nin, (nin > leaf_cap && depth_max > 0) ? 1u : NODE_NONE, 0u, 0u, third);
+    }
+    if (s >= ns) return;
     const uint32_t k = split_start[s];
     const int L = split_level[s];
     const uint64_t pre = prefix_of(K[k], L);
-    const uint32_t end = (L == 0) ? nin : lower_bound_shift(K, k, nin, 3 * (16 - L), pre + 1);
+    const uint32_t end = (L == 0) ? nin : gallop_shift(K, k, nin, 3 * (16 - L), pre + 1);
     const Cube c = cube_of(bounds, K[k], L);
     float mid[3];
     for (int a = 0; a < 3; a++) mid[a] = midf(c.lo[a], c.hi[a]);
@@ -332,7 +419,7 @@ __global__ void k_split_fill(const uint64_t* __restrict__ K, const uint32_t* __r
     uint32_t self = 0;
     if (L > 0) {
         const uint64_t ppre = pre >> 3;
-        const uint32_t kp = (L == 1) ? 0u : lower_bound_shift(K, 0, k + 1, 3 * (17 - L), ppre);
+        const uint32_t kp = (L == 1) ? 0u : gallop_back(K, k + 1, 3 * (17 - L), ppre);
         const int ap = (kp == 0) ? -1 : cpl_levels(K[kp - 1], K[kp]);
         const uint32_t sp = sbase[kp] + (uint32_t)(L - 1 - (ap + 1));
         self = 1u + 8u * sp + (uint32_t)(pre & 7ull);
@@ -340,7 +427,7 @@ __global__ void k_split_fill(const uint64_t* __restrict__ K, const uint32_t* __r
     split_node[s] = self;
     uint32_t cstart = k;
     for (int o = 0; o < 8; o++) {
-        const uint32_t cend = (o == 7) ? end : lower_bound_shift(K, cstart, end, 3 * (15 - L), (pre << 3) + (uint64_t)o + 1);
+        const uint32_t cend = (o == 7) ? end : gallop_shift(K, cstart, end, 3 * (15 - L), (pre << 3) + (uint64_t)o + 1);
         const uint32_t cnt = cend - cstart;
         Cube cc;
         for (int a = 0; a < 3; a++) {
@@ -575,10 +662,8 @@ int sf_tree_build(sfgpu_sim* s) {
     s->timer.end(st, tk);
     tk = s->timer.begin(st, "tree_ties");
     k_tie_fix<<<1, FIX_THREADS, 0, st>>>(pos, s->d_bounds, t->keys, t->vals, nin, t->ties, tie_count,
-                                         s->p.leaf_cap, s->p.depth_max, resort);
+                                         s->p.leaf_cap, s->p.depth_max, resort, t->sort.keys_b, t->sort.vals_b);
     SF_CHECK_LAUNCH();
-    if (sf_sort_pairs(t->keys, t->vals, n, KEY_BITS, t->sort, st, s->d_status, nullptr, resort) != SFGPU_OK)
-        return SFGPU_FAILURE;
     s->timer.end(st, tk);
     tk = s->timer.begin(st, "tree_nodes");
     k_split_count<<<nb, 256, 0, st>>>(t->keys, n, nin, s->p.leaf_cap, s->p.depth_max, t->scount, s->d_status);
@@ -586,8 +671,6 @@ int sf_tree_build(sfgpu_sim* s) {
     if (sf_scan_u32(t->scount, t->sbase, n, nsplit, t->scan_u32, st) != SFGPU_OK) return SFGPU_FAILURE;
     k_split_emit<<<nb, 256, 0, st>>>(t->keys, n, nin, t->scount, t->sbase, nsplit, t->split_cap, t->split_start,
                                      t->split_level, t->nodes_max, s->d_status);
-    SF_CHECK_LAUNCH();
-    k_root<<<1, 32, 0, st>>>(s->d_bounds, nin, s->p.leaf_cap, s->p.depth_max, t->nd, third);
     SF_CHECK_LAUNCH();
     const uint32_t sb = sf_ceil_div(std::max<uint32_t>(t->split_cap, 1), 128);
     k_split_fill<<<sb, 128, 0, st>>>(t->keys, nin, t->sbase, nsplit, t->split_cap, t->split_start, t->split_level,
@@ -618,8 +701,8 @@ int sf_tree_build(sfgpu_sim* s) {
 
 int sf_stage_tree_solve(sfgpu_sim* s, bool radius_ready) {
     int tk = s->timer.begin(s->stream, "bounds");
+    // kick_drift already reduced the radii and set the root cube
     if (!radius_ready && sf_stage_radius(s) != SFGPU_OK) return SFGPU_FAILURE;
-    if (sf_stage_bounds(s) != SFGPU_OK) return SFGPU_FAILURE;
     s->timer.end(s->stream, tk);
     if (sf_tree_build(s) != SFGPU_OK) return SFGPU_FAILURE;
     tk = s->timer.begin(s->stream, "walk");

@@ -253,115 +253,121 @@ __device__ __forceinline__ void monopole(const float4& C, const float4& Lo, cons
     }
 }
 
-template <int KIND, bool STATS>
-__global__ void __launch_bounds__(WALK_THREADS) k_walk_split(const float4* __restrict__ sp,
-                                                             const uint32_t* __restrict__ V, uint32_t n,
-                                                             NodeArrays nd, ForceConsts fc, float th_lo, float th_hi,
-                                                             uint32_t leaf_cap, float4* __restrict__ part,
-                                                             uint32_t* __restrict__ st_int,
-                                                             uint32_t* __restrict__ st_open,
-                                                             unsigned long long* __restrict__ tot,
-                                                             uint32_t* d_status) {
-    __shared__ uint32_t s_node[WALK_WARPS][STACK];
-    __shared__ uint32_t s_mask[WALK_WARPS][STACK];
+// One thread walks one body's tree, stacklessly, in the reference's order:
+// into the first child when a cell opens, on to the next sibling (children
+// are numbered contiguously), up through the parent links when the last
+// sibling is done (gravity.c:306-579 keeps the same walk state as a path of
+// octants).  With SPLIT > 1, SPLIT warps share 32 bodies and warp o walks
+// only the subtree of root octant o; partial sums are added by
+// k_walk_reduce.
+template <int KIND, int SPLIT_, bool STATS>
+__global__ void __launch_bounds__(WALK_THREADS) k_walk_body(const float4* __restrict__ sp,
+                                                            const uint32_t* __restrict__ V, uint32_t n,
+                                                            NodeArrays nd, ForceConsts fc, float th_lo, float th_hi,
+                                                            uint32_t leaf_cap, float4* __restrict__ part,
+                                                            float* __restrict__ acc, float* __restrict__ pot,
+                                                            uint32_t* __restrict__ st_int,
+                                                            uint32_t* __restrict__ st_open,
+                                                            unsigned long long* __restrict__ tot,
+                                                            uint32_t* d_status) {
     const int lane = threadIdx.x & 31;
-    const int w = threadIdx.x >> 5;
-    const uint32_t gw = blockIdx.x * WALK_WARPS + w;
-    const uint32_t group = gw / SPLIT;
-    const uint32_t oct = gw % SPLIT;
+    const uint32_t gw = blockIdx.x * WALK_WARPS + (threadIdx.x >> 5);
+    const uint32_t group = gw / SPLIT_;
+    const uint32_t oct = gw % SPLIT_;
     const uint32_t k = group * 32u + lane;
     const bool live = k < n;
-    const uint32_t live_mask = __ballot_sync(0xffffffffu, live);
-    if (!live_mask) return;
     const float4 b = live ? sp[k] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float rx = b.x, ry = b.y, rz = b.z, mi = b.w;
     KSum ax{0.f, 0.f}, ay{0.f, 0.f}, az{0.f, 0.f}, ph{0.f, 0.f};
     uint32_t n_int = 0, n_open = 0;
-    int top = 0;
 
-    {  // the root: opening test in every warp, monopole in warp 0 only
+    if (live) {
         const float4 H = __ldg(&nd.hi[0]);
-        const float4 G = __ldg(&nd.geo[0]);
-        const float4 C = __ldg(&nd.com[0]);
-        const float4 Lo = __ldg(&nd.lo[0]);
         const uint32_t bodies = __float_as_uint(H.z);
+        const uint32_t first = __float_as_uint(H.w);
+        bool descend_root = false;
         if (bodies > 0u) {
-            bool open = false;
-            if (bodies > leaf_cap && live) {
-                open = opens(G, rx, ry, rz, fc, th_lo, th_hi);
+            if (bodies > leaf_cap) {
                 if (oct == 0) n_open++;
+                descend_root = opens(__ldg(&nd.geo[0]), rx, ry, rz, fc, th_lo, th_hi) && first != NODE_NONE;
             }
-            const uint32_t om = __ballot_sync(0xffffffffu, open);
-            if (oct == 0 && live && !open) {
-                monopole<KIND>(C, Lo, H, bodies, rx, ry, rz, mi, fc.eps2, ax, ay, az, ph);
+            if (!descend_root && oct == 0) {
+                monopole<KIND>(__ldg(&nd.com[0]), __ldg(&nd.lo[0]), H, bodies, rx, ry, rz, mi, fc.eps2, ax, ay, az,
+                               ph);
                 n_int++;
             }
-            const uint32_t first = __float_as_uint(H.w);
-            if (om && first != NODE_NONE) {
-                if (lane == 0) {
-                    s_node[w][0] = first + oct;
-                    s_mask[w][0] = om;
+        }
+        if (descend_root) {
+            // SPLIT_ == 1: walk all of the root's children; else only octant oct
+            const uint32_t stop = SPLIT_ == 1 ? 0u : first + oct;
+            uint32_t v = SPLIT_ == 1 ? first : first + oct;
+            uint32_t guard = 0;
+            while (true) {
+                if (++guard > (1u << 26)) {
+                    atomicOr(d_status, SFGPU_STATUS_WALK);
+                    break;
                 }
-                top = 1;
-            }
-        }
-    }
-    __syncwarp();
-    uint32_t guard = 0;
-    while (top > 0) {
-        top--;
-        const uint32_t v = s_node[w][top];
-        const uint32_t M = s_mask[w][top];
-        __syncwarp();
-        if (++guard > (1u << 26)) {
-            if (lane == 0) atomicOr(d_status, SFGPU_STATUS_WALK);
-            break;
-        }
-        const float4 H = __ldg(&nd.hi[v]);
-        const float4 G = __ldg(&nd.geo[v]);
-        const float4 C = __ldg(&nd.com[v]);
-        const float4 Lo = __ldg(&nd.lo[v]);
-        const uint32_t bodies = __float_as_uint(H.z);
-        if (bodies == 0u) continue;
-        const bool me = (M >> lane) & 1u;
-        uint32_t take = M;
-        if (bodies > leaf_cap) {
-            bool open = false;
-            if (me) {
-                open = opens(G, rx, ry, rz, fc, th_lo, th_hi);
-                n_open++;
-            }
-            const uint32_t om = __ballot_sync(0xffffffffu, open);
-            take = M & ~om;
-            if (om) {
-                const uint32_t first = __float_as_uint(H.w);
-                if (top + 8 > STACK || first == NODE_NONE) {
-                    if (lane == 0) atomicOr(d_status, SFGPU_STATUS_WALK);
-                    take = M;
-                } else {
-                    if (lane < 8) {
-                        s_node[w][top + lane] = first + 7u - (uint32_t)lane;
-                        s_mask[w][top + lane] = om;
+                const float4 Hv = __ldg(&nd.hi[v]);
+                const float4 G = __ldg(&nd.geo[v]);
+                const float4 C = __ldg(&nd.com[v]);
+                const float4 Lo = __ldg(&nd.lo[v]);
+                const uint32_t bv = __float_as_uint(Hv.z);
+                bool down = false;
+                if (bv > 0u) {
+                    if (bv > leaf_cap) {
+                        n_open++;
+                        const uint32_t fcv = __float_as_uint(Hv.w);
+                        down = fcv != NODE_NONE && opens(G, rx, ry, rz, fc, th_lo, th_hi);
+                        if (down) v = fcv;
+                        else if (fcv == NODE_NONE) atomicOr(d_status, SFGPU_STATUS_WALK);
                     }
-                    top += 8;
+                    if (!down) {
+                        monopole<KIND>(C, Lo, Hv, bv, rx, ry, rz, mi, fc.eps2, ax, ay, az, ph);
+                        n_int++;
+                    }
                 }
+                if (down) continue;
+                // the subtree of v is done: next sibling, or climb
+                bool done = false;
+                while (true) {
+                    if (v == stop) {
+                        done = true;
+                        break;
+                    }
+                    if (((v - 1u) & 7u) != 7u) {
+                        v += 1u;
+                        break;
+                    }
+                    v = __ldg(&nd.parent[v]);
+                }
+                if (done) break;
             }
-            __syncwarp();
-        }
-        if ((take >> lane) & 1u) {
-            monopole<KIND>(C, Lo, H, bodies, rx, ry, rz, mi, fc.eps2, ax, ay, az, ph);
-            n_int++;
         }
     }
     if (live) {
+        float4 r;
         if (KIND == WALK_COMP)
-            part[(size_t)oct * n + k] = make_float4(ax.s - ax.c, ay.s - ay.c, az.s - az.c, ph.s - ph.c);
+            r = make_float4(ax.s - ax.c, ay.s - ay.c, az.s - az.c, ph.s - ph.c);
         else
-            part[(size_t)oct * n + k] = make_float4(ax.s, ay.s, az.s, ph.s);
-        if (STATS) {
-            const uint32_t p = V[k];
-            atomicAdd(&st_int[p], n_int);
-            atomicAdd(&st_open[p], n_open);
+            r = make_float4(ax.s, ay.s, az.s, ph.s);
+        const uint32_t p = V[k];
+        if (SPLIT_ == 1) {
+            const float g = -fc.neg_g;
+            const float scale = fc.physical ? g : g * mi;
+            acc[3u * p + 0u] = scale * r.x;
+            acc[3u * p + 1u] = scale * r.y;
+            acc[3u * p + 2u] = scale * r.z;
+            pot[p] = fc.neg_g * r.w;
+            if (STATS) {
+                st_int[p] = n_int;
+                st_open[p] = n_open;
+            }
+        } else {
+            part[(size_t)oct * n + k] = r;
+            if (STATS) {
+                atomicAdd(&st_int[p], n_int);
+                atomicAdd(&st_open[p], n_open);
+            }
         }
     }
     unsigned long long ci = n_int, co = n_open;
@@ -369,7 +375,7 @@ __global__ void __launch_bounds__(WALK_THREADS) k_walk_split(const float4* __res
         ci += __shfl_xor_sync(0xffffffffu, ci, o);
         co += __shfl_xor_sync(0xffffffffu, co, o);
     }
-    if (lane == 0) {
+    if (lane == 0 && (ci | co)) {
         atomicAdd(&tot[0], ci);
         atomicAdd(&tot[1], co);
     }
@@ -416,32 +422,46 @@ __global__ void k_walk_reduce(const float4* __restrict__ part, const float4* __r
     }
 }
 
-template <int KIND>
-int launch_split(sfgpu_sim* s, bool stats) {
+template <int KIND, int SPLIT_>
+int launch_body(sfgpu_sim* s, bool stats) {
     TreeWork* t = s->tree;
     const ForceConsts fc = sf_force_consts(s->p);
     const float th_lo = fc.theta * (1.0f - 1.0f / 524288.0f);
     const float th_hi = fc.theta * (1.0f + 1.0f / 524288.0f);
     const uint32_t groups = sf_ceil_div(s->n, 32);
-    const uint32_t grid = sf_ceil_div((uint64_t)groups * SPLIT, WALK_WARPS);
+    const uint32_t grid = sf_ceil_div((uint64_t)groups * SPLIT_, WALK_WARPS);
     float* acc = s->slab + (size_t)6 * s->n;
     float* pot = s->slab + (size_t)10 * s->n;
     if (stats) {
-        SF_CUDA(cudaMemsetAsync(s->stat_int, 0, sizeof(uint32_t) * s->n, s->stream));
-        SF_CUDA(cudaMemsetAsync(s->stat_open, 0, sizeof(uint32_t) * s->n, s->stream));
-        k_walk_split<KIND, true><<<grid, WALK_THREADS, 0, s->stream>>>(t->sp, t->vals, s->n, t->nd, fc, th_lo, th_hi,
-                                                                       s->p.leaf_cap, t->walk_part, s->stat_int,
-                                                                       s->stat_open, s->walk_tot, s->d_status);
+        if (SPLIT_ > 1) {
+            SF_CUDA(cudaMemsetAsync(s->stat_int, 0, sizeof(uint32_t) * s->n, s->stream));
+            SF_CUDA(cudaMemsetAsync(s->stat_open, 0, sizeof(uint32_t) * s->n, s->stream));
+        }
+        k_walk_body<KIND, SPLIT_, true><<<grid, WALK_THREADS, 0, s->stream>>>(
+            t->sp, t->vals, s->n, t->nd, fc, th_lo, th_hi, s->p.leaf_cap, t->walk_part, acc, pot, s->stat_int,
+            s->stat_open, s->walk_tot, s->d_status);
     } else {
-        k_walk_split<KIND, false><<<grid, WALK_THREADS, 0, s->stream>>>(t->sp, t->vals, s->n, t->nd, fc, th_lo,
-                                                                        th_hi, s->p.leaf_cap, t->walk_part, nullptr,
-                                                                        nullptr, s->walk_tot, s->d_status);
+        k_walk_body<KIND, SPLIT_, false><<<grid, WALK_THREADS, 0, s->stream>>>(
+            t->sp, t->vals, s->n, t->nd, fc, th_lo, th_hi, s->p.leaf_cap, t->walk_part, acc, pot, nullptr, nullptr,
+            s->walk_tot, s->d_status);
     }
     SF_CHECK_LAUNCH();
-    k_walk_reduce<KIND><<<sf_ceil_div(s->n, 256), 256, 0, s->stream>>>(t->walk_part, t->sp, t->vals, s->n, fc, acc,
-                                                                       pot);
-    SF_CHECK_LAUNCH();
+    if (SPLIT_ > 1) {
+        k_walk_reduce<KIND><<<sf_ceil_div(s->n, 256), 256, 0, s->stream>>>(t->walk_part, t->sp, t->vals, s->n, fc,
+                                                                           acc, pot);
+        SF_CHECK_LAUNCH();
+    }
     return SFGPU_OK;
+}
+
+template <int KIND>
+int launch_fast(sfgpu_sim* s, bool stats) {
+    // split the walk over the root octants while one thread per body would
+    // leave the GPU short of warps (under ~16 warps per SM)
+    uint32_t split = s->p.walk_split;
+    if (split == 0) split = s->n <= (uint32_t)sf_num_sms() * 32u * 16u ? SPLIT : 1u;
+    if (split == 1) return launch_body<KIND, 1>(s, stats);
+    return launch_body<KIND, SPLIT>(s, stats);
 }
 
 }  // namespace
@@ -451,6 +471,6 @@ size_t sf_walk_scratch_floats4(uint32_t n) { return (size_t)SPLIT * n; }
 int sf_walk_launch(sfgpu_sim* s) {
     const bool stats = (s->p.flags & SFGPU_FLAG_STATS) && s->stat_int;
     if (s->p.math == SFGPU_MATH_EXACT && s->p.form == SFGPU_FORM_PLAIN) return launch_kind<WALK_EXACT>(s, stats);
-    if (s->p.form == SFGPU_FORM_COMPENSATED) return launch_split<WALK_COMP>(s, stats);
-    return launch_split<WALK_FAST>(s, stats);
+    if (s->p.form == SFGPU_FORM_COMPENSATED) return launch_fast<WALK_COMP>(s, stats);
+    return launch_fast<WALK_FAST>(s, stats);
 }
