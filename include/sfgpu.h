@@ -175,6 +175,11 @@ int sfgpu_gravity_part(sfgpu_sim* s);
 /* Replaces solve_sph (src/sph.c:14-282), or runs the cubic-spline SPH. */
 int sfgpu_solve_sph(sfgpu_sim* s);
 
+/* Per-body neighbour counts of the last SPH solve: REFERENCE, the bodies
+ * with fl(r^2) <= 1 in the momentum pass (src/sph.c:231, j = i included);
+ * CUBIC, the bodies with fl(r^2) < fl((2h)^2). */
+int sfgpu_sph_neighbours(sfgpu_sim* s, uint32_t* counts);
+
 /* ---- tree inspection ---------------------------------------------------- */
 /* Sorted 48-bit octree keys (3 bits per level, level 0 most significant,
  * octant bit 0 = x, 1 = y, 2 = z), the particle index of each sorted slot,

@@ -79,6 +79,7 @@ def lib():
             "sfgpu_gravity_tree": (i32, [vp]),
             "sfgpu_gravity_part": (i32, [vp]),
             "sfgpu_solve_sph": (i32, [vp]),
+            "sfgpu_sph_neighbours": (i32, [vp, u32p]),
             "sfgpu_tree_keys": (i32, [vp, C.POINTER(C.c_uint64), u32p, u32p, f32p]),
             "sfgpu_tree_num_nodes": (i32, [vp, u32p]),
             "sfgpu_tree_export": (i32, [vp, u32p, u32p, u32p, f32p, f32p]),
@@ -253,6 +254,11 @@ class Sim:
 
     def solve_sph(self):
         check(lib().sfgpu_solve_sph(self.h), "sfgpu_solve_sph")
+
+    def sph_neighbours(self):
+        a = np.zeros(self.n, np.uint32)
+        check(lib().sfgpu_sph_neighbours(self.h, a.ctypes.data_as(C.POINTER(C.c_uint32))), "sfgpu_sph_neighbours")
+        return a
 
     def tree_keys(self):
         keys = np.zeros(self.n, np.uint64)

@@ -492,6 +492,20 @@ extern "C" int sfgpu_solve_sph(sfgpu_sim* s) {
     return sf_stage_sph(s);
 }
 
+uint32_t* sf_sph_neighbour_counts(sfgpu_sim* s);
+
+extern "C" int sfgpu_sph_neighbours(sfgpu_sim* s, uint32_t* counts) {
+    sf_clear_error();
+    uint32_t* d = s ? sf_sph_neighbour_counts(s) : nullptr;
+    if (!d || !counts) {
+        sf_set_error("sfgpu_sph_neighbours needs a simulation with SPH");
+        return SFGPU_FAILURE;
+    }
+    SF_CUDA(cudaStreamSynchronize(s->stream));
+    SF_CUDA(cudaMemcpy(counts, d, sizeof(uint32_t) * s->n, cudaMemcpyDeviceToHost));
+    return SFGPU_OK;
+}
+
 extern "C" int sfgpu_synchronize(sfgpu_sim* s) {
     sf_clear_error();
     if (!s) return SFGPU_FAILURE;

@@ -205,3 +205,20 @@ def test_tree_run_graph_matches_eager(sf):
             s.run(0, 5)
             outs.append(s.download())
     np.testing.assert_array_equal(outs[0], outs[1])
+
+
+@pytest.mark.parametrize("fixture", ["tree_uniform_n4096_theta0.5_3steps.npz", "tree_lattice_ties.npz"])
+def test_tree_export_reference_numbering(sf, oracle32, fixture):
+    """node_t array in the reference's numbering, bit-identical (EXACT)."""
+    d = golden(fixture)
+    n = len(d["pos"])
+    p = sf.default_params(solver=sf.SOLVER_TREE, eps=0.01, theta=0.5, math=sf.MATH_EXACT)
+    with sf.Sim(n, p) as s:
+        s.set_state(d["pos"], d["vel"] if "vel" in d else np.zeros((n, 3), np.float32), d["mas"])
+        if "bounds" in d:
+            s.tree_build(d["bounds"])
+        else:
+            s.solve(0)
+        t = s.tree_export()
+    for k in ("parent", "bodies", "branch", "bounds", "params"):
+        np.testing.assert_array_equal(t[k], d["tree_" + k], err_msg=k)
