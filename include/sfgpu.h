@@ -179,6 +179,11 @@ int sfgpu_solve_sph(sfgpu_sim* s);
  * with fl(r^2) <= 1 in the momentum pass (src/sph.c:231, j = i included);
  * CUBIC, the bodies with fl(r^2) < fl((2h)^2). */
 int sfgpu_sph_neighbours(sfgpu_sim* s, uint32_t* counts);
+/* CUBIC SPH: specific internal energy u per body (kicked with du/dt in the
+ * leapfrog, like the velocities).  Set it after sfgpu_create; read it and the
+ * last du/dt back (either pointer may be NULL). */
+int sfgpu_sph_set_u(sfgpu_sim* s, const float* u);
+int sfgpu_sph_get_u(sfgpu_sim* s, float* u, float* dudt);
 
 /* ---- tree inspection ---------------------------------------------------- */
 /* Sorted 48-bit octree keys (3 bits per level, level 0 most significant,

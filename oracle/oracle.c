@@ -485,3 +485,107 @@ int orc_sim_step(const orc_params* p, orc_sim* s, double* T, double* V) {
     if (V) *V = vk.s;
     return status;
 }
+
+/* ---- cubic-spline SPH (no reference counterpart; FP64 oracle) --------------
+ * Kernel: Monaghan & Lattanzio (1985) M4 cubic spline in 3-D, support 2h,
+ *   W(r,h) = 1/(pi h^3) * (1 - 1.5 q^2 + 0.75 q^3)  0 <= q < 1
+ *                        * 0.25 (2 - q)^3            1 <= q < 2,  q = r/h
+ * symmetrised W_ij = (W(r,h_i) + W(r,h_j))/2 when smoothing lengths differ.
+ * Equation of state P = (gamma - 1) rho u, sound speed c = sqrt(gamma P/rho).
+ * Monaghan (1992) viscosity Pi_ij = (-alpha cbar mu + beta mu^2)/rhobar for
+ * v_ij.r_ij < 0, mu = h v_ij.r_ij/(r^2 + 0.01 h^2), h = (h_i + h_j)/2.
+ *   dv_i/dt = -sum_j m_j (P_i/rho_i^2 + P_j/rho_j^2 + Pi_ij) grad_i W_ij
+ *   du_i/dt =  sum_j m_j (P_i/rho_i^2 + Pi_ij/2) v_ij . grad_i W_ij
+ * Neighbours: j with fl32((dx^2 + dy^2) + dz^2) < fl32((2 max(h_i,h_j))^2),
+ * dx = fl32(x_i - x_j), the FP32 decision the GPU makes; physics in FP64. */
+static double cubic_w(double r, double h) {
+    const double q = r / h;
+    const double s = 1.0 / (3.14159265358979323846 * h * h * h);
+    if (q < 1.0) return s * (1.0 - 1.5 * q * q + 0.75 * q * q * q);
+    if (q < 2.0) return s * 0.25 * (2.0 - q) * (2.0 - q) * (2.0 - q);
+    return 0.0;
+}
+static double cubic_dw(double r, double h) {  /* dW/dr */
+    const double q = r / h;
+    const double s = 1.0 / (3.14159265358979323846 * h * h * h * h);
+    if (q < 1.0) return s * (-3.0 * q + 2.25 * q * q);
+    if (q < 2.0) return s * (-0.75 * (2.0 - q) * (2.0 - q));
+    return 0.0;
+}
+static int cubic_neighbour(const float* pos, const float* rad, uint32_t i, uint32_t j) {
+    volatile float dx = pos[3u * i] - pos[3u * j];
+    volatile float dy = pos[3u * i + 1u] - pos[3u * j + 1u];
+    volatile float dz = pos[3u * i + 2u] - pos[3u * j + 2u];
+    volatile float xx = dx * dx, yy = dy * dy, zz = dz * dz;
+    volatile float r2 = (xx + yy) + zz;
+    volatile float hm = rad[i] > rad[j] ? rad[i] : rad[j];
+    volatile float s = 2.0f * hm;
+    volatile float s2 = s * s;
+    return r2 < s2;
+}
+
+void orc_sph_cubic(uint32_t n, const float* pos, const float* vel, const float* mas, const float* rad,
+                   const float* u, double gamma, double alpha, double beta, double* rho, double* prs,
+                   double* acc, double* dudt, uint32_t* nbr) {
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 64)
+#endif
+    for (int64_t ii = 0; ii < (int64_t)n; ii++) {
+        const uint32_t i = (uint32_t)ii;
+        double s = 0.0;
+        uint32_t cnt = 0;
+        for (uint32_t j = 0; j < n; j++) {
+            if (!cubic_neighbour(pos, rad, i, j)) continue;
+            cnt++;
+            const double dx = (double)pos[3u * i] - pos[3u * j];
+            const double dy = (double)pos[3u * i + 1u] - pos[3u * j + 1u];
+            const double dz = (double)pos[3u * i + 2u] - pos[3u * j + 2u];
+            const double r = sqrt(dx * dx + dy * dy + dz * dz);
+            s += (double)mas[j] * 0.5 * (cubic_w(r, rad[i]) + cubic_w(r, rad[j]));
+        }
+        rho[i] = s;
+        prs[i] = (gamma - 1.0) * s * (double)u[i];
+        if (nbr) nbr[i] = cnt;
+    }
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 64)
+#endif
+    for (int64_t ii = 0; ii < (int64_t)n; ii++) {
+        const uint32_t i = (uint32_t)ii;
+        const double ci = sqrt(gamma * (gamma - 1.0) * (double)u[i]);
+        const double pi_ = rho[i] > 0.0 ? prs[i] / (rho[i] * rho[i]) : 0.0;
+        double ax = 0.0, ay = 0.0, az = 0.0, du = 0.0;
+        for (uint32_t j = 0; j < n; j++) {
+            if (j == i || !cubic_neighbour(pos, rad, i, j)) continue;
+            const double dx = (double)pos[3u * i] - pos[3u * j];
+            const double dy = (double)pos[3u * i + 1u] - pos[3u * j + 1u];
+            const double dz = (double)pos[3u * i + 2u] - pos[3u * j + 2u];
+            const double r2 = dx * dx + dy * dy + dz * dz;
+            const double r = sqrt(r2);
+            if (!(r > 0.0)) continue;
+            const double g = 0.5 * (cubic_dw(r, rad[i]) + cubic_dw(r, rad[j])) / r;  /* grad W = g r_ij */
+            const double vx = (double)vel[3u * i] - vel[3u * j];
+            const double vy = (double)vel[3u * i + 1u] - vel[3u * j + 1u];
+            const double vz = (double)vel[3u * i + 2u] - vel[3u * j + 2u];
+            const double vr = vx * dx + vy * dy + vz * dz;
+            const double pj = rho[j] > 0.0 ? prs[j] / (rho[j] * rho[j]) : 0.0;
+            double visc = 0.0;
+            if (vr < 0.0) {
+                const double h = 0.5 * ((double)rad[i] + rad[j]);
+                const double mu = h * vr / (r2 + 0.01 * h * h);
+                const double cj = sqrt(gamma * (gamma - 1.0) * (double)u[j]);
+                const double cbar = 0.5 * (ci + cj), rbar = 0.5 * (rho[i] + rho[j]);
+                visc = (-alpha * cbar * mu + beta * mu * mu) / rbar;
+            }
+            const double f = (double)mas[j] * (pi_ + pj + visc) * g;
+            ax -= f * dx;
+            ay -= f * dy;
+            az -= f * dz;
+            du += (double)mas[j] * (pi_ + 0.5 * visc) * g * vr;
+        }
+        acc[3u * i] = ax;
+        acc[3u * i + 1u] = ay;
+        acc[3u * i + 2u] = az;
+        dudt[i] = du;
+    }
+}

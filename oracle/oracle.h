@@ -95,6 +95,14 @@ void orc_sph_reference(const orc_params* p, uint32_t n, const orc_real* pos,
                        const orc_real* mas, const orc_real* rad, orc_real* rho,
                        orc_real* prs, orc_real* acc, uint32_t* nbr);
 
+/* Cubic-spline SPH with ideal-gas pressure and Monaghan viscosity (no
+ * reference counterpart; the FP64 oracle of the GPU's SFGPU_SPH_CUBIC).
+ * Inputs are the FP32 state; rho, prs, acc (SPH part only), dudt in FP64;
+ * nbr (may be NULL) gets the neighbour-set sizes (j = i included). */
+void orc_sph_cubic(uint32_t n, const float* pos, const float* vel, const float* mas, const float* rad,
+                   const float* u, double gamma, double alpha, double beta, double* rho, double* prs,
+                   double* acc, double* dudt, uint32_t* nbr);
+
 /* Simulation over one slab in the reference layout (simulation.h:17-51):
  * pos[3N] vel[3N] acc[3N] mas[N] pot[N] ken[N] pen[N] (+ rad rho prs). */
 typedef struct {

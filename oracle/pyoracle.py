@@ -67,6 +67,9 @@ class Oracle:
         L.orc_sim_dof.restype = C.c_uint32
         L.orc_sim_dof.argtypes = [C.POINTER(Params)]
         L.orc_threads.restype = C.c_int
+        fp, dp = C.POINTER(C.c_float), C.POINTER(C.c_double)
+        L.orc_sph_cubic.argtypes = [C.c_uint32, fp, fp, fp, fp, fp, C.c_double, C.c_double, C.c_double,
+                                    dp, dp, dp, dp, u32p]
 
         class Sim(C.Structure):
             _fields_ = [("step_number", C.c_uint32), ("N", C.c_uint32), ("mem", C.c_void_p),
@@ -152,6 +155,21 @@ class Oracle:
                                    prs.ctypes.data_as(self._rp), acc.ctypes.data_as(self._rp),
                                    nbr.ctypes.data_as(u32p))
         return rho, prs, acc, nbr
+
+    def sph_cubic(self, pos, vel, mas, rad, u, gamma=5.0 / 3.0, alpha=1.0, beta=2.0):
+        """Cubic-spline SPH (FP64 physics, FP32 neighbour decisions)."""
+        f = lambda a: np.ascontiguousarray(a, np.float32)
+        pos, vel, mas, rad, u = f(pos), f(vel), f(mas), f(rad), f(u)
+        n = len(pos)
+        rho, prs, dudt = np.zeros(n), np.zeros(n), np.zeros(n)
+        acc = np.zeros((n, 3))
+        nbr = np.zeros(n, np.uint32)
+        fp, dp = C.POINTER(C.c_float), C.POINTER(C.c_double)
+        self.lib.orc_sph_cubic(n, pos.ctypes.data_as(fp), vel.ctypes.data_as(fp), mas.ctypes.data_as(fp),
+                               rad.ctypes.data_as(fp), u.ctypes.data_as(fp), gamma, alpha, beta,
+                               rho.ctypes.data_as(dp), prs.ctypes.data_as(dp), acc.ctypes.data_as(dp),
+                               dudt.ctypes.data_as(dp), nbr.ctypes.data_as(u32p))
+        return rho, prs, acc, dudt, nbr
 
     # --- slab-level simulation (simulation.c) -------------------------------
     def new_sim(self, n, params: Params):

@@ -80,6 +80,8 @@ def lib():
             "sfgpu_gravity_part": (i32, [vp]),
             "sfgpu_solve_sph": (i32, [vp]),
             "sfgpu_sph_neighbours": (i32, [vp, u32p]),
+            "sfgpu_sph_set_u": (i32, [vp, f32p]),
+            "sfgpu_sph_get_u": (i32, [vp, f32p, f32p]),
             "sfgpu_tree_keys": (i32, [vp, C.POINTER(C.c_uint64), u32p, u32p, f32p]),
             "sfgpu_tree_num_nodes": (i32, [vp, u32p]),
             "sfgpu_tree_export": (i32, [vp, u32p, u32p, u32p, f32p, f32p]),
@@ -259,6 +261,17 @@ class Sim:
         a = np.zeros(self.n, np.uint32)
         check(lib().sfgpu_sph_neighbours(self.h, a.ctypes.data_as(C.POINTER(C.c_uint32))), "sfgpu_sph_neighbours")
         return a
+
+    def sph_set_u(self, u):
+        u = np.ascontiguousarray(u, np.float32)
+        check(lib().sfgpu_sph_set_u(self.h, u.ctypes.data_as(C.POINTER(C.c_float))), "sfgpu_sph_set_u")
+
+    def sph_get_u(self):
+        u = np.zeros(self.n, np.float32)
+        du = np.zeros(self.n, np.float32)
+        f = C.POINTER(C.c_float)
+        check(lib().sfgpu_sph_get_u(self.h, u.ctypes.data_as(f), du.ctypes.data_as(f)), "sfgpu_sph_get_u")
+        return u, du
 
     def tree_keys(self):
         keys = np.zeros(self.n, np.uint64)

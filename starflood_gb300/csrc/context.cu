@@ -506,6 +506,29 @@ extern "C" int sfgpu_sph_neighbours(sfgpu_sim* s, uint32_t* counts) {
     return SFGPU_OK;
 }
 
+extern "C" int sfgpu_sph_set_u(sfgpu_sim* s, const float* u) {
+    sf_clear_error();
+    if (!s || !s->u || !u) {
+        sf_set_error("sfgpu_sph_set_u needs a simulation with cubic-spline SPH");
+        return SFGPU_FAILURE;
+    }
+    SF_CUDA(cudaStreamSynchronize(s->stream));
+    SF_CUDA(cudaMemcpy(s->u, u, sizeof(float) * s->n, cudaMemcpyHostToDevice));
+    return SFGPU_OK;
+}
+
+extern "C" int sfgpu_sph_get_u(sfgpu_sim* s, float* u, float* dudt) {
+    sf_clear_error();
+    if (!s || !s->u) {
+        sf_set_error("sfgpu_sph_get_u needs a simulation with cubic-spline SPH");
+        return SFGPU_FAILURE;
+    }
+    SF_CUDA(cudaStreamSynchronize(s->stream));
+    if (u) SF_CUDA(cudaMemcpy(u, s->u, sizeof(float) * s->n, cudaMemcpyDeviceToHost));
+    if (dudt) SF_CUDA(cudaMemcpy(dudt, s->dudt, sizeof(float) * s->n, cudaMemcpyDeviceToHost));
+    return SFGPU_OK;
+}
+
 extern "C" int sfgpu_synchronize(sfgpu_sim* s) {
     sf_clear_error();
     if (!s) return SFGPU_FAILURE;

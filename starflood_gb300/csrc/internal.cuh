@@ -203,6 +203,7 @@ struct sfgpu_sim {
     float* d_bounds = nullptr;     // root cube (6 floats)
     TreeWork* tree = nullptr;
     void* sph = nullptr;           // SphWork (sph.cu)
+    void* sph_cubic = nullptr;     // CubicWork (sph_cubic.cu)
     // pinned host mirrors
     uint32_t* h_step = nullptr;
     double* h_sums = nullptr;

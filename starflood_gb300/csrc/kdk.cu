@@ -111,8 +111,10 @@ __global__ void __launch_bounds__(SF_RED_BLOCK) k_kick_drift(float* __restrict__
                                                              double* __restrict__ vel64, double dt64,
                                                              int want_radius, double2* __restrict__ part,
                                                              uint32_t* done, const uint32_t* __restrict__ d_step,
-                                                             float* __restrict__ bounds, double* __restrict__ sums) {
+                                                             float* __restrict__ bounds, double* __restrict__ sums,
+                                                             float* __restrict__ u, const float* __restrict__ dudt) {
     const uint32_t i = blockIdx.x * SF_RED_BLOCK + threadIdx.x;
+    if (u && i < n) u[i] = fadd(u[i], fmul(half_dt, dudt[i]));  // SPH internal energy, kick_0
     float* pos = slab;
     float* vel = slab + (size_t)3 * n;
     const float* acc = slab + (size_t)6 * n;
@@ -160,8 +162,10 @@ __global__ void __launch_bounds__(SF_RED_BLOCK) k_kick_energy(float* __restrict_
                                                               double* __restrict__ vel64, double dt64,
                                                               float g_over_eps, int physical,
                                                               double2* __restrict__ part, uint32_t* done,
-                                                              double* __restrict__ sums, uint32_t* d_step) {
+                                                              double* __restrict__ sums, uint32_t* d_step,
+                                                              float* __restrict__ u, const float* __restrict__ dudt) {
     const uint32_t i = blockIdx.x * SF_RED_BLOCK + threadIdx.x;
+    if (u && i < n) u[i] = fadd(u[i], fmul(half_dt, dudt[i]));  // SPH internal energy, kick_1
     float* vel = slab + (size_t)3 * n;
     const float* acc = slab + (size_t)6 * n;
     const float* mas = slab + (size_t)9 * n;
@@ -228,7 +232,7 @@ int sf_stage_kick_drift(sfgpu_sim* s, bool want_radius) {
     const float dt = (float)s->p.dt;
     k_kick_drift<<<nb, SF_RED_BLOCK, 0, s->stream>>>(s->slab, s->n, 0.5f * dt, dt, s->pos64, s->vel64, s->p.dt,
                                                      want_radius ? 1 : 0, s->red, s->d_done, s->d_step, s->d_bounds,
-                                                     s->sums);
+                                                     s->sums, s->u, s->dudt);
     SF_CHECK_LAUNCH();
     return SFGPU_OK;
 }
@@ -248,7 +252,7 @@ int sf_stage_kick_energy(sfgpu_sim* s) {
     const float g_over_eps = (float)(s->p.G / s->p.eps);
     k_kick_energy<<<nb, SF_RED_BLOCK, 0, s->stream>>>(s->slab, s->n, 0.5f * dt, s->vel64, s->p.dt, g_over_eps,
                                                       s->p.acc_mode == SFGPU_ACC_PHYSICAL, s->red, s->d_done + 1,
-                                                      s->sums, s->d_step);
+                                                      s->sums, s->d_step, s->u, s->dudt);
     SF_CHECK_LAUNCH();
     return SFGPU_OK;
 }
