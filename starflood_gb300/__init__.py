@@ -349,3 +349,75 @@ def compat_functions():
     L.sim_find.restype = C.c_void_p
     L.sim_find.argtypes = [S, C.c_int]
     return L
+
+
+class Batch:
+    """Many independent systems (sfgpu_batch): batched PP + KDK, and the
+    adjoint of a trajectory."""
+
+    def __init__(self, sizes, params: Params):
+        self.sizes = [int(x) for x in sizes]
+        off = np.zeros(len(self.sizes) + 1, np.uint32)
+        off[1:] = np.cumsum(self.sizes)
+        self.off = off
+        self.total = int(off[-1])
+        self.params = params
+        h = C.c_void_p()
+        check(lib().sfgpu_batch_create(C.byref(h), len(self.sizes), off.ctypes.data_as(C.POINTER(C.c_uint32)),
+                                       C.byref(params)), "sfgpu_batch_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().sfgpu_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def upload(self, pos, vel, mas):
+        f = lambda a: np.ascontiguousarray(a, np.float32)
+        pos, vel, mas = f(pos), f(vel), f(mas)
+        check(lib().sfgpu_batch_upload(self.h, _ptr(pos), _ptr(vel), _ptr(mas)), "sfgpu_batch_upload")
+
+    def download(self):
+        pos = np.zeros((self.total, 3), np.float32)
+        vel = np.zeros((self.total, 3), np.float32)
+        acc = np.zeros((self.total, 3), np.float32)
+        pot = np.zeros(self.total, np.float32)
+        check(lib().sfgpu_batch_download(self.h, _ptr(pos), _ptr(vel), _ptr(acc), _ptr(pot)), "download")
+        return pos, vel, acc, pot
+
+    def solve(self):
+        check(lib().sfgpu_batch_solve(self.h), "sfgpu_batch_solve")
+
+    def run(self, nsteps):
+        check(lib().sfgpu_batch_run(self.h, nsteps), "sfgpu_batch_run")
+
+    def sync(self):
+        check(lib().sfgpu_batch_synchronize(self.h), "sfgpu_batch_synchronize")
+
+    def stream(self) -> int:
+        return int(lib().sfgpu_batch_stream(self.h) or 0)
+
+    def autotune(self) -> int:
+        c = C.c_int()
+        check(lib().sfgpu_batch_autotune(self.h, C.byref(c)), "sfgpu_batch_autotune")
+        return c.value
+
+    def grad(self, nsteps, checkpoint=20):
+        gp = np.zeros((self.total, 3), np.float32)
+        gv = np.zeros((self.total, 3), np.float32)
+        loss = C.c_double()
+        check(lib().sfgpu_batch_grad(self.h, nsteps, checkpoint, _ptr(gp), _ptr(gv), C.byref(loss)),
+              "sfgpu_batch_grad")
+        return loss.value, gp, gv
