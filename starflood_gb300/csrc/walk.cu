@@ -454,14 +454,269 @@ int launch_body(sfgpu_sim* s, bool stats) {
     return SFGPU_OK;
 }
 
+// ---- group walk (FAST / COMPENSATED, the default) -----------------------------
+// A warp walks the tree for its 32 bodies (consecutive in key order), but the
+// lanes work on up to 32 stack entries (cell, mask of bodies still walking it)
+// at once, so the loads of many cells are in flight together.  Each entry is
+// classified against the bounding box of the group: with margins of 2^-12 on
+// theta, far larger than the FP32 rounding of the reference's ratio, "every
+// body accepts" (w^2 < theta d_min^2) and "every body opens"
+// (w^2 >= theta d_max^2) are certain to agree with each body's own FP32
+// decision; only the remaining "mixed" cells are tested body by body with the
+// reference's arithmetic.  Accepted (cell, mask) pairs go to a list in shared
+// memory that all 32 lanes then run through with dense monopole
+// interactions.  Every body ends up with exactly the cells the reference
+// gives it (the per-body interaction counts are checked in the tests).
+constexpr int GW_WARPS = 4;
+constexpr int GW_THREADS = GW_WARPS * 32;
+constexpr int GW_STACK = 1024;
+constexpr int GW_LIST = 256;
+
+template <int KIND>
+__device__ __forceinline__ void flush_list(const uint32_t* lnode, const uint32_t* lmask, int count, const NodeArrays& nd,
+                                           int lane, float rx, float ry, float rz, float mi, float eps2, KSum& ax,
+                                           KSum& ay, KSum& az, KSum& ph, uint32_t& n_int) {
+#pragma unroll 2
+    for (int e = 0; e < count; e++) {
+        const uint32_t v = lnode[e];
+        const uint32_t M = lmask[e];
+        const float4 C = __ldg(&nd.com[v]);
+        const float4 Lo = __ldg(&nd.lo[v]);
+        const float4 H = __ldg(&nd.hi[v]);
+        if ((M >> lane) & 1u) {
+            monopole<KIND>(C, Lo, H, __float_as_uint(H.z), rx, ry, rz, mi, eps2, ax, ay, az, ph);
+            n_int++;
+        }
+    }
+}
+
+template <int KIND, bool STATS>
+__global__ void __launch_bounds__(GW_THREADS) k_walk_group(const float4* __restrict__ sp,
+                                                           const uint32_t* __restrict__ V, uint32_t n, NodeArrays nd,
+                                                           ForceConsts fc, float th_lo, float th_hi,
+                                                           float th_acc, float th_open, uint32_t leaf_cap,
+                                                           float* __restrict__ acc, float* __restrict__ pot,
+                                                           uint32_t* __restrict__ st_int,
+                                                           uint32_t* __restrict__ st_open,
+                                                           unsigned long long* __restrict__ tot, uint32_t* d_status) {
+    __shared__ uint32_t s_node[GW_WARPS][GW_STACK];
+    __shared__ uint32_t s_mask[GW_WARPS][GW_STACK];
+    __shared__ uint32_t l_node[GW_WARPS][GW_LIST];
+    __shared__ uint32_t l_mask[GW_WARPS][GW_LIST];
+    const int lane = threadIdx.x & 31;
+    const int w = threadIdx.x >> 5;
+    uint32_t* stn = s_node[w];
+    uint32_t* stm = s_mask[w];
+    uint32_t* lsn = l_node[w];
+    uint32_t* lsm = l_mask[w];
+    const uint32_t k = (blockIdx.x * GW_WARPS + w) * 32u + lane;
+    const bool live = k < n;
+    const uint32_t live_mask = __ballot_sync(0xffffffffu, live);
+    if (!live_mask) return;
+    const float4 b = live ? sp[k] : sp[(blockIdx.x * GW_WARPS + w) * 32u];
+    const float rx = b.x, ry = b.y, rz = b.z, mi = b.w;
+    // bounding box of the group (dead lanes repeat the first body)
+    float bx0 = rx, by0 = ry, bz0 = rz, bx1 = rx, by1 = ry, bz1 = rz;
+    for (int o = 16; o > 0; o >>= 1) {
+        bx0 = fminf(bx0, __shfl_xor_sync(0xffffffffu, bx0, o));
+        by0 = fminf(by0, __shfl_xor_sync(0xffffffffu, by0, o));
+        bz0 = fminf(bz0, __shfl_xor_sync(0xffffffffu, bz0, o));
+        bx1 = fmaxf(bx1, __shfl_xor_sync(0xffffffffu, bx1, o));
+        by1 = fmaxf(by1, __shfl_xor_sync(0xffffffffu, by1, o));
+        bz1 = fmaxf(bz1, __shfl_xor_sync(0xffffffffu, bz1, o));
+    }
+    KSum ax{0.f, 0.f}, ay{0.f, 0.f}, az{0.f, 0.f}, ph{0.f, 0.f};
+    uint32_t n_int = 0, n_open = 0;
+    unsigned long long open_total = 0;
+    int top = 1, count = 0;
+    if (lane == 0) {
+        stn[0] = 0u;
+        stm[0] = live_mask;
+    }
+    __syncwarp();
+    uint32_t guard = 0;
+    while (top > 0) {
+        if (++guard > (1u << 24)) {
+            if (lane == 0) atomicOr(d_status, SFGPU_STATUS_WALK);
+            break;
+        }
+        int pops = min(32, min(top, (GW_STACK - top) / 8));
+        if (pops == 0) {  // no room for children: cannot happen with GW_STACK >> depth * 8
+            if (lane == 0) atomicOr(d_status, SFGPU_STATUS_WALK);
+            break;
+        }
+        uint32_t v = 0, M = 0;
+        if (lane < pops) {
+            v = stn[top - 1 - lane];
+            M = stm[top - 1 - lane];
+        }
+        top -= pops;
+        __syncwarp();
+        // 0 drop, 1 accept, 2 open, 3 mixed
+        int kind = 0;
+        bool internal = false;
+        float4 G = make_float4(0.f, 0.f, 0.f, 0.f);
+        uint32_t first = NODE_NONE;
+        if (lane < pops) {
+            const float4 H = __ldg(&nd.hi[v]);
+            G = __ldg(&nd.geo[v]);
+            const uint32_t bodies = __float_as_uint(H.z);
+            first = __float_as_uint(H.w);
+            internal = bodies > leaf_cap;
+            if (bodies == 0u) {
+                kind = 0;
+            } else if (bodies <= leaf_cap) {
+                kind = 1;
+            } else {
+                open_total += __popc(M);
+                // distances from the cell centre to the group's box (nearest, farthest)
+                const float ex = fmaxf(0.f, fmaxf(bx0 - G.x, G.x - bx1));
+                const float ey = fmaxf(0.f, fmaxf(by0 - G.y, G.y - by1));
+                const float ez = fmaxf(0.f, fmaxf(bz0 - G.z, G.z - bz1));
+                const float fx = fmaxf(fabsf(G.x - bx0), fabsf(G.x - bx1));
+                const float fy = fmaxf(fabsf(G.y - by0), fabsf(G.y - by1));
+                const float fz = fmaxf(fabsf(G.z - bz0), fabsf(G.z - bz1));
+                const float dmin2 = (ex * ex + ey * ey + ez * ez) * (1.0f - 1.0f / 65536.0f);
+                const float dmax2 = (fx * fx + fy * fy + fz * fz) * (1.0f + 1.0f / 65536.0f);
+                if (dmin2 > 0.0f && G.w < th_acc * dmin2) kind = 1;
+                else if (G.w >= th_open * dmax2 && first != NODE_NONE) kind = 2;
+                else kind = 3;
+            }
+        }
+        // accepted cells -> list
+        const uint32_t acc_b = __ballot_sync(0xffffffffu, kind == 1);
+        if (kind == 1) {
+            const int slot = count + __popc(acc_b & ((1u << lane) - 1u));
+            lsn[slot] = v;
+            lsm[slot] = M;
+        }
+        count += __popc(acc_b);
+        // cells every body opens -> their children
+        const uint32_t open_b = __ballot_sync(0xffffffffu, kind == 2);
+        if (kind == 2) {
+            const int base = top + 8 * __popc(open_b & ((1u << lane) - 1u));
+            for (int o = 0; o < 8; o++) {
+                stn[base + o] = first + 7u - (uint32_t)o;
+                stm[base + o] = M;
+            }
+        }
+        top += 8 * __popc(open_b);
+        __syncwarp();
+        if (count > GW_LIST - 32) {
+            flush_list<KIND>(lsn, lsm, count, nd, lane, rx, ry, rz, mi, fc.eps2, ax, ay, az, ph, n_int);
+            count = 0;
+            __syncwarp();
+        }
+        // mixed cells: the reference's test, body by body
+        uint32_t mixed = __ballot_sync(0xffffffffu, kind == 3);
+        while (mixed) {
+            const int src = __ffs(mixed) - 1;
+            mixed &= mixed - 1u;
+            const uint32_t mv = __shfl_sync(0xffffffffu, v, src);
+            const uint32_t mm = __shfl_sync(0xffffffffu, M, src);
+            const uint32_t mf = __shfl_sync(0xffffffffu, first, src);
+            const float4 mg = make_float4(__shfl_sync(0xffffffffu, G.x, src), __shfl_sync(0xffffffffu, G.y, src),
+                                          __shfl_sync(0xffffffffu, G.z, src), __shfl_sync(0xffffffffu, G.w, src));
+            const bool me = (mm >> lane) & 1u;
+            const bool op = me && mf != NODE_NONE && opens(mg, rx, ry, rz, fc, th_lo, th_hi);
+            const uint32_t om = __ballot_sync(0xffffffffu, op);
+            const uint32_t am = mm & ~om;
+            if (am && count >= GW_LIST) {
+                flush_list<KIND>(lsn, lsm, count, nd, lane, rx, ry, rz, mi, fc.eps2, ax, ay, az, ph, n_int);
+                count = 0;
+                __syncwarp();
+            }
+            if (am && lane == 0) {
+                lsn[count] = mv;
+                lsm[count] = am;
+            }
+            count += am ? 1 : 0;
+            if (om) {
+                if (lane < 8) {
+                    stn[top + lane] = mf + 7u - (uint32_t)lane;
+                    stm[top + lane] = om;
+                }
+                top += 8;
+            }
+            __syncwarp();
+        }
+        if (STATS) {  // opening tests (internal cells only) attributed to bodies
+            for (int l = 0; l < pops; l++) {
+                const bool il = __shfl_sync(0xffffffffu, internal, l);
+                const uint32_t ml = __shfl_sync(0xffffffffu, M, l);
+                if (il && ((ml >> lane) & 1u)) n_open++;
+            }
+        }
+        if (count > GW_LIST - 32) {
+            flush_list<KIND>(lsn, lsm, count, nd, lane, rx, ry, rz, mi, fc.eps2, ax, ay, az, ph, n_int);
+            count = 0;
+            __syncwarp();
+        }
+    }
+    flush_list<KIND>(lsn, lsm, count, nd, lane, rx, ry, rz, mi, fc.eps2, ax, ay, az, ph, n_int);
+    if (live) {
+        const uint32_t p = V[k];
+        float sx = ax.s, sy = ay.s, sz = az.s, sw = ph.s;
+        if (KIND == WALK_COMP) {
+            sx -= ax.c;
+            sy -= ay.c;
+            sz -= az.c;
+            sw -= ph.c;
+        }
+        const float g = -fc.neg_g;
+        const float scale = fc.physical ? g : g * mi;
+        acc[3u * p + 0u] = scale * sx;
+        acc[3u * p + 1u] = scale * sy;
+        acc[3u * p + 2u] = scale * sz;
+        pot[p] = fc.neg_g * sw;
+        if (STATS) {
+            st_int[p] = n_int;
+            st_open[p] = n_open;
+        }
+    }
+    unsigned long long ci = n_int;
+    for (int o = 16; o > 0; o >>= 1) {
+        ci += __shfl_xor_sync(0xffffffffu, ci, o);
+        open_total += __shfl_xor_sync(0xffffffffu, open_total, o);
+    }
+    if (lane == 0) {
+        atomicAdd(&tot[0], ci);
+        atomicAdd(&tot[1], open_total);
+    }
+}
+
+template <int KIND>
+int launch_group(sfgpu_sim* s, bool stats) {
+    TreeWork* t = s->tree;
+    const ForceConsts fc = sf_force_consts(s->p);
+    const float th_lo = fc.theta * (1.0f - 1.0f / 524288.0f);
+    const float th_hi = fc.theta * (1.0f + 1.0f / 524288.0f);
+    const float th_acc = fc.theta * (1.0f - 1.0f / 4096.0f);
+    const float th_open = fc.theta * (1.0f + 1.0f / 4096.0f);
+    const uint32_t grid = sf_ceil_div(sf_ceil_div(s->n, 32), GW_WARPS);
+    float* acc = s->slab + (size_t)6 * s->n;
+    float* pot = s->slab + (size_t)10 * s->n;
+    if (stats)
+        k_walk_group<KIND, true><<<grid, GW_THREADS, 0, s->stream>>>(t->sp, t->vals, s->n, t->nd, fc, th_lo, th_hi,
+                                                                     th_acc, th_open, s->p.leaf_cap, acc, pot,
+                                                                     s->stat_int, s->stat_open, s->walk_tot,
+                                                                     s->d_status);
+    else
+        k_walk_group<KIND, false><<<grid, GW_THREADS, 0, s->stream>>>(t->sp, t->vals, s->n, t->nd, fc, th_lo, th_hi,
+                                                                      th_acc, th_open, s->p.leaf_cap, acc, pot,
+                                                                      nullptr, nullptr, s->walk_tot, s->d_status);
+    SF_CHECK_LAUNCH();
+    return SFGPU_OK;
+}
+
 template <int KIND>
 int launch_fast(sfgpu_sim* s, bool stats) {
-    // split the walk over the root octants while one thread per body would
-    // leave the GPU short of warps (under ~16 warps per SM)
-    uint32_t split = s->p.walk_split;
-    if (split == 0) split = s->n <= (uint32_t)sf_num_sms() * 32u * 16u ? SPLIT : 1u;
+    // walk_split: 0 (default) group walk; 1 one thread per body; 8 one thread
+    // per body and root octant
+    const uint32_t split = s->p.walk_split;
     if (split == 1) return launch_body<KIND, 1>(s, stats);
-    return launch_body<KIND, SPLIT>(s, stats);
+    if (split == 8) return launch_body<KIND, SPLIT>(s, stats);
+    return launch_group<KIND>(s, stats);
 }
 
 }  // namespace

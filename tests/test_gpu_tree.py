@@ -172,12 +172,14 @@ def test_tree_outside_and_nan_bodies(sf, oracle32):
     np.testing.assert_array_equal(v["pot"], pt)
 
 
+@pytest.mark.parametrize("split", [0, 1, 8])
 @pytest.mark.parametrize("n,seed", [(65536, 2), (20000, 8)])
-def test_tree_fast_large(sf, oracle32, n, seed):
+def test_tree_fast_large(sf, oracle32, n, seed, split):
+    """FAST walks (group walk; one thread per body; per body and root octant)."""
     from starflood_gb300.ics import uniform_ball, plummer
     gen = uniform_ball if n == 65536 else plummer
     pos, vel, mas = gen(n, seed=seed)
-    p = sf.default_params(solver=sf.SOLVER_TREE, eps=0.01, theta=0.5, flags=sf.FLAG_STATS)
+    p = sf.default_params(solver=sf.SOLVER_TREE, eps=0.01, theta=0.5, flags=sf.FLAG_STATS, walk_split=split)
     with sf.Sim(n, p) as s:
         s.set_state(pos, vel, mas)
         s.solve(5)
