@@ -469,7 +469,7 @@ int launch_body(sfgpu_sim* s, bool stats) {
 // gives it (the per-body interaction counts are checked in the tests).
 constexpr int GW_WARPS = 4;
 constexpr int GW_THREADS = GW_WARPS * 32;
-constexpr int GW_STACK = 1024;
+constexpr int GW_STACK = 512;
 constexpr int GW_LIST = 256;
 
 template <int KIND>
@@ -490,11 +490,12 @@ __device__ __forceinline__ void flush_list(const uint32_t* lnode, const uint32_t
     }
 }
 
-template <int KIND, bool STATS>
+template <int KIND, int GSPLIT, bool STATS>
 __global__ void __launch_bounds__(GW_THREADS) k_walk_group(const float4* __restrict__ sp,
                                                            const uint32_t* __restrict__ V, uint32_t n, NodeArrays nd,
                                                            ForceConsts fc, float th_lo, float th_hi,
                                                            float th_acc, float th_open, uint32_t leaf_cap,
+                                                           float4* __restrict__ part,
                                                            float* __restrict__ acc, float* __restrict__ pot,
                                                            uint32_t* __restrict__ st_int,
                                                            uint32_t* __restrict__ st_open,
@@ -509,11 +510,14 @@ __global__ void __launch_bounds__(GW_THREADS) k_walk_group(const float4* __restr
     uint32_t* stm = s_mask[w];
     uint32_t* lsn = l_node[w];
     uint32_t* lsm = l_mask[w];
-    const uint32_t k = (blockIdx.x * GW_WARPS + w) * 32u + lane;
+    const uint32_t gw = blockIdx.x * GW_WARPS + w;
+    const uint32_t group = gw / GSPLIT;
+    const uint32_t oct = gw % GSPLIT;
+    const uint32_t k = group * 32u + lane;
     const bool live = k < n;
     const uint32_t live_mask = __ballot_sync(0xffffffffu, live);
     if (!live_mask) return;
-    const float4 b = live ? sp[k] : sp[(blockIdx.x * GW_WARPS + w) * 32u];
+    const float4 b = live ? sp[k] : sp[group * 32u];
     const float rx = b.x, ry = b.y, rz = b.z, mi = b.w;
     // bounding box of the group (dead lanes repeat the first body)
     float bx0 = rx, by0 = ry, bz0 = rz, bx1 = rx, by1 = ry, bz1 = rz;
@@ -528,10 +532,43 @@ __global__ void __launch_bounds__(GW_THREADS) k_walk_group(const float4* __restr
     KSum ax{0.f, 0.f}, ay{0.f, 0.f}, az{0.f, 0.f}, ph{0.f, 0.f};
     uint32_t n_int = 0, n_open = 0;
     unsigned long long open_total = 0;
-    int top = 1, count = 0;
-    if (lane == 0) {
-        stn[0] = 0u;
-        stm[0] = live_mask;
+    int top = 0, count = 0;
+    if (GSPLIT == 1) {
+        if (lane == 0) {
+            stn[0] = 0u;
+            stm[0] = live_mask;
+        }
+        top = 1;
+    } else {
+        // the root in every warp (exact per-body test); warp oct keeps only the
+        // subtree of root octant oct, warp 0 the root as a monopole
+        const float4 H = __ldg(&nd.hi[0]);
+        const uint32_t bodies = __float_as_uint(H.z);
+        const uint32_t first = __float_as_uint(H.w);
+        if (bodies > 0u) {
+            uint32_t om = 0u;
+            if (bodies > leaf_cap) {
+                if (oct == 0) open_total += __popc(live_mask);
+                if (STATS && oct == 0 && live) n_open++;
+                const float4 G = __ldg(&nd.geo[0]);
+                om = __ballot_sync(0xffffffffu, live && first != NODE_NONE && opens(G, rx, ry, rz, fc, th_lo, th_hi));
+            }
+            const uint32_t am = live_mask & ~om;
+            if (oct == 0 && am) {
+                if (lane == 0) {
+                    lsn[0] = 0u;
+                    lsm[0] = am;
+                }
+                count = 1;
+            }
+            if (om) {
+                if (lane == 0) {
+                    stn[0] = first + oct;
+                    stm[0] = om;
+                }
+                top = 1;
+            }
+        }
     }
     __syncwarp();
     uint32_t guard = 0;
@@ -663,15 +700,23 @@ __global__ void __launch_bounds__(GW_THREADS) k_walk_group(const float4* __restr
             sz -= az.c;
             sw -= ph.c;
         }
-        const float g = -fc.neg_g;
-        const float scale = fc.physical ? g : g * mi;
-        acc[3u * p + 0u] = scale * sx;
-        acc[3u * p + 1u] = scale * sy;
-        acc[3u * p + 2u] = scale * sz;
-        pot[p] = fc.neg_g * sw;
-        if (STATS) {
-            st_int[p] = n_int;
-            st_open[p] = n_open;
+        if (GSPLIT == 1) {
+            const float g = -fc.neg_g;
+            const float scale = fc.physical ? g : g * mi;
+            acc[3u * p + 0u] = scale * sx;
+            acc[3u * p + 1u] = scale * sy;
+            acc[3u * p + 2u] = scale * sz;
+            pot[p] = fc.neg_g * sw;
+            if (STATS) {
+                st_int[p] = n_int;
+                st_open[p] = n_open;
+            }
+        } else {
+            part[(size_t)oct * n + k] = make_float4(sx, sy, sz, sw);
+            if (STATS) {
+                atomicAdd(&st_int[p], n_int);
+                atomicAdd(&st_open[p], n_open);
+            }
         }
     }
     unsigned long long ci = n_int;
@@ -685,7 +730,7 @@ __global__ void __launch_bounds__(GW_THREADS) k_walk_group(const float4* __restr
     }
 }
 
-template <int KIND>
+template <int KIND, int GSPLIT>
 int launch_group(sfgpu_sim* s, bool stats) {
     TreeWork* t = s->tree;
     const ForceConsts fc = sf_force_consts(s->p);
@@ -693,30 +738,43 @@ int launch_group(sfgpu_sim* s, bool stats) {
     const float th_hi = fc.theta * (1.0f + 1.0f / 524288.0f);
     const float th_acc = fc.theta * (1.0f - 1.0f / 4096.0f);
     const float th_open = fc.theta * (1.0f + 1.0f / 4096.0f);
-    const uint32_t grid = sf_ceil_div(sf_ceil_div(s->n, 32), GW_WARPS);
+    const uint32_t grid = sf_ceil_div((uint64_t)sf_ceil_div(s->n, 32) * GSPLIT, GW_WARPS);
     float* acc = s->slab + (size_t)6 * s->n;
     float* pot = s->slab + (size_t)10 * s->n;
-    if (stats)
-        k_walk_group<KIND, true><<<grid, GW_THREADS, 0, s->stream>>>(t->sp, t->vals, s->n, t->nd, fc, th_lo, th_hi,
-                                                                     th_acc, th_open, s->p.leaf_cap, acc, pot,
-                                                                     s->stat_int, s->stat_open, s->walk_tot,
-                                                                     s->d_status);
-    else
-        k_walk_group<KIND, false><<<grid, GW_THREADS, 0, s->stream>>>(t->sp, t->vals, s->n, t->nd, fc, th_lo, th_hi,
-                                                                      th_acc, th_open, s->p.leaf_cap, acc, pot,
-                                                                      nullptr, nullptr, s->walk_tot, s->d_status);
+    if (stats) {
+        if (GSPLIT > 1) {
+            SF_CUDA(cudaMemsetAsync(s->stat_int, 0, sizeof(uint32_t) * s->n, s->stream));
+            SF_CUDA(cudaMemsetAsync(s->stat_open, 0, sizeof(uint32_t) * s->n, s->stream));
+        }
+        k_walk_group<KIND, GSPLIT, true><<<grid, GW_THREADS, 0, s->stream>>>(
+            t->sp, t->vals, s->n, t->nd, fc, th_lo, th_hi, th_acc, th_open, s->p.leaf_cap, t->walk_part, acc, pot,
+            s->stat_int, s->stat_open, s->walk_tot, s->d_status);
+    } else {
+        k_walk_group<KIND, GSPLIT, false><<<grid, GW_THREADS, 0, s->stream>>>(
+            t->sp, t->vals, s->n, t->nd, fc, th_lo, th_hi, th_acc, th_open, s->p.leaf_cap, t->walk_part, acc, pot,
+            nullptr, nullptr, s->walk_tot, s->d_status);
+    }
     SF_CHECK_LAUNCH();
+    if (GSPLIT > 1) {
+        k_walk_reduce<KIND><<<sf_ceil_div(s->n, 256), 256, 0, s->stream>>>(t->walk_part, t->sp, t->vals, s->n, fc,
+                                                                           acc, pot);
+        SF_CHECK_LAUNCH();
+    }
     return SFGPU_OK;
 }
 
 template <int KIND>
 int launch_fast(sfgpu_sim* s, bool stats) {
-    // walk_split: 0 (default) group walk; 1 one thread per body; 8 one thread
-    // per body and root octant
+    // walk_split: 0 (default) group walk, split over the root octants while
+    // one warp per 32 bodies would leave the SMs short of warps; 1 one
+    // thread per body; 8 one thread per body and root octant; 32 group walk
+    // without the split
     const uint32_t split = s->p.walk_split;
     if (split == 1) return launch_body<KIND, 1>(s, stats);
     if (split == 8) return launch_body<KIND, SPLIT>(s, stats);
-    return launch_group<KIND>(s, stats);
+    if (split == 32) return launch_group<KIND, 1>(s, stats);
+    if (sf_ceil_div(s->n, 32) >= (uint32_t)sf_num_sms() * 48u) return launch_group<KIND, 1>(s, stats);
+    return launch_group<KIND, SPLIT>(s, stats);
 }
 
 }  // namespace
