@@ -476,7 +476,7 @@ template <int KIND>
 __device__ __forceinline__ void flush_list(const uint32_t* lnode, const uint32_t* lmask, int count, const NodeArrays& nd,
                                            int lane, float rx, float ry, float rz, float mi, float eps2, KSum& ax,
                                            KSum& ay, KSum& az, KSum& ph, uint32_t& n_int) {
-#pragma unroll 2
+#pragma unroll 4
     for (int e = 0; e < count; e++) {
         const uint32_t v = lnode[e];
         const uint32_t M = lmask[e];
@@ -504,8 +504,12 @@ __global__ void __launch_bounds__(GW_THREADS) k_walk_group(const float4* __restr
     __shared__ uint32_t s_mask[GW_WARPS][GW_STACK];
     __shared__ uint32_t l_node[GW_WARPS][GW_LIST];
     __shared__ uint32_t l_mask[GW_WARPS][GW_LIST];
+    __shared__ float4 s_body[GW_WARPS][32];
+    __shared__ uint32_t f_node[GW_WARPS][80];  // top-level frontiers: [0,8) level 1, [8,72) level 2
+    __shared__ uint32_t f_mask[GW_WARPS][80];
     const int lane = threadIdx.x & 31;
     const int w = threadIdx.x >> 5;
+    float4* sbd = s_body[w];
     uint32_t* stn = s_node[w];
     uint32_t* stm = s_mask[w];
     uint32_t* lsn = l_node[w];
@@ -519,6 +523,7 @@ __global__ void __launch_bounds__(GW_THREADS) k_walk_group(const float4* __restr
     if (!live_mask) return;
     const float4 b = live ? sp[k] : sp[group * 32u];
     const float rx = b.x, ry = b.y, rz = b.z, mi = b.w;
+    sbd[lane] = b;
     // bounding box of the group (dead lanes repeat the first body)
     float bx0 = rx, by0 = ry, bz0 = rz, bx1 = rx, by1 = ry, bz1 = rz;
     for (int o = 16; o > 0; o >>= 1) {
@@ -540,34 +545,79 @@ __global__ void __launch_bounds__(GW_THREADS) k_walk_group(const float4* __restr
         }
         top = 1;
     } else {
-        // the root in every warp (exact per-body test); warp oct keeps only the
-        // subtree of root octant oct, warp 0 the root as a monopole
-        const float4 H = __ldg(&nd.hi[0]);
-        const uint32_t bodies = __float_as_uint(H.z);
-        const uint32_t first = __float_as_uint(H.w);
-        if (bodies > 0u) {
+        // Every warp of the group walks the top two levels itself (exact
+        // per-body tests); the up to 64 cells left at level 2 are dealt out
+        // round-robin, warp `oct` keeping cells j with j % GSPLIT == oct, so
+        // the expensive near-field cells spread over the warps.  Cells
+        // accepted above level 2 (and the opening-test totals there) belong
+        // to warp 0.
+        uint32_t* fnd = f_node[w];
+        uint32_t* fms = f_mask[w];
+        int n_in = 1, in_base = 0, out_base = 0;  // level 0 writes the 8 level-1 slots [0, 8)
+        for (int lvl = 0; lvl < 2; lvl++) {
+            uint32_t v = 0u, M = 0u, first = NODE_NONE, bodies = 0u;
+            float4 G = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (lane < n_in) {
+                v = lvl == 0 ? 0u : fnd[in_base + lane];
+                M = lvl == 0 ? live_mask : fms[in_base + lane];
+                const float4 H = __ldg(&nd.hi[v]);
+                G = __ldg(&nd.geo[v]);
+                bodies = __float_as_uint(H.z);
+                first = __float_as_uint(H.w);
+            }
+            const bool internal = lane < n_in && bodies > leaf_cap;
             uint32_t om = 0u;
-            if (bodies > leaf_cap) {
-                if (oct == 0) open_total += __popc(live_mask);
-                if (STATS && oct == 0 && live) n_open++;
-                const float4 G = __ldg(&nd.geo[0]);
-                om = __ballot_sync(0xffffffffu, live && first != NODE_NONE && opens(G, rx, ry, rz, fc, th_lo, th_hi));
-            }
-            const uint32_t am = live_mask & ~om;
-            if (oct == 0 && am) {
-                if (lane == 0) {
-                    lsn[0] = 0u;
-                    lsm[0] = am;
+            if (internal && first != NODE_NONE) {
+                uint32_t mm = M;
+                while (mm) {
+                    const int i = __ffs(mm) - 1;
+                    mm &= mm - 1u;
+                    const float4 bi = sbd[i];
+                    if (opens(G, bi.x, bi.y, bi.z, fc, th_lo, th_hi)) om |= 1u << i;
                 }
-                count = 1;
             }
+            if (internal && oct == 0) open_total += __popc(M);
+            if (STATS && oct == 0) {
+                for (int l = 0; l < n_in; l++) {
+                    const bool il = __shfl_sync(0xffffffffu, internal, l);
+                    const uint32_t ml = __shfl_sync(0xffffffffu, M, l);
+                    if (il && ((ml >> lane) & 1u)) n_open++;
+                }
+            }
+            const uint32_t am = (lane < n_in && bodies > 0u) ? (M & ~om) : 0u;
+            const uint32_t lt = (1u << lane) - 1u;
+            const uint32_t ab = __ballot_sync(0xffffffffu, am != 0u);
+            if (oct == 0) {
+                if (am) {
+                    lsn[count + __popc(ab & lt)] = v;
+                    lsm[count + __popc(ab & lt)] = am;
+                }
+                count += __popc(ab);
+            }
+            const uint32_t ob = __ballot_sync(0xffffffffu, om != 0u);
             if (om) {
-                if (lane == 0) {
-                    stn[0] = first + oct;
-                    stm[0] = om;
+                const int base = out_base + 8 * __popc(ob & lt);
+                for (int o = 0; o < 8; o++) {
+                    fnd[base + o] = first + (uint32_t)o;
+                    fms[base + o] = om;
                 }
-                top = 1;
             }
+            __syncwarp();
+            n_in = 8 * __popc(ob);
+            in_base = out_base;
+            out_base = 8;  // level 1 writes the 64 level-2 slots [8, 72)
+        }
+        // level-2 cells: this warp's share onto its stack
+        for (int j0 = 0; j0 < n_in; j0 += 32) {
+            const int j = j0 + lane;
+            const bool mine = j < n_in && (j % GSPLIT) == (int)oct;
+            const uint32_t mb = __ballot_sync(0xffffffffu, mine);
+            if (mine) {
+                const int slot = top + __popc(mb & ((1u << lane) - 1u));
+                stn[slot] = fnd[in_base + j];
+                stm[slot] = fms[in_base + j];
+            }
+            top += __popc(mb);
         }
     }
     __syncwarp();
@@ -644,37 +694,41 @@ __global__ void __launch_bounds__(GW_THREADS) k_walk_group(const float4* __restr
             count = 0;
             __syncwarp();
         }
-        // mixed cells: the reference's test, body by body
-        uint32_t mixed = __ballot_sync(0xffffffffu, kind == 3);
-        while (mixed) {
-            const int src = __ffs(mixed) - 1;
-            mixed &= mixed - 1u;
-            const uint32_t mv = __shfl_sync(0xffffffffu, v, src);
-            const uint32_t mm = __shfl_sync(0xffffffffu, M, src);
-            const uint32_t mf = __shfl_sync(0xffffffffu, first, src);
-            const float4 mg = make_float4(__shfl_sync(0xffffffffu, G.x, src), __shfl_sync(0xffffffffu, G.y, src),
-                                          __shfl_sync(0xffffffffu, G.z, src), __shfl_sync(0xffffffffu, G.w, src));
-            const bool me = (mm >> lane) & 1u;
-            const bool op = me && mf != NODE_NONE && opens(mg, rx, ry, rz, fc, th_lo, th_hi);
-            const uint32_t om = __ballot_sync(0xffffffffu, op);
-            const uint32_t am = mm & ~om;
-            if (am && count >= GW_LIST) {
-                flush_list<KIND>(lsn, lsm, count, nd, lane, rx, ry, rz, mi, fc.eps2, ax, ay, az, ph, n_int);
-                count = 0;
-                __syncwarp();
+        // mixed cells: one lane per cell runs the reference's test for each
+        // body of the cell's mask (bodies staged in shared memory), so the
+        // tests of up to 32 cells proceed side by side
+        uint32_t om = 0u;
+        if (kind == 3 && first != NODE_NONE) {
+            uint32_t mm = M;
+            while (mm) {
+                const int i = __ffs(mm) - 1;
+                mm &= mm - 1u;
+                const float4 bi = sbd[i];
+                if (opens(G, bi.x, bi.y, bi.z, fc, th_lo, th_hi)) om |= 1u << i;
             }
-            if (am && lane == 0) {
-                lsn[count] = mv;
-                lsm[count] = am;
+        }
+        const uint32_t am = (kind == 3) ? (M & ~om) : 0u;
+        const uint32_t lt = (1u << lane) - 1u;
+        const uint32_t ab = __ballot_sync(0xffffffffu, am != 0u);
+        if (am) {
+            const int slot = count + __popc(ab & lt);
+            lsn[slot] = v;
+            lsm[slot] = am;
+        }
+        count += __popc(ab);
+        const uint32_t ob = __ballot_sync(0xffffffffu, om != 0u);
+        if (om) {
+            const int base = top + 8 * __popc(ob & lt);
+            for (int o = 0; o < 8; o++) {
+                stn[base + o] = first + 7u - (uint32_t)o;
+                stm[base + o] = om;
             }
-            count += am ? 1 : 0;
-            if (om) {
-                if (lane < 8) {
-                    stn[top + lane] = mf + 7u - (uint32_t)lane;
-                    stm[top + lane] = om;
-                }
-                top += 8;
-            }
+        }
+        top += 8 * __popc(ob);
+        __syncwarp();
+        if (count > GW_LIST - 32) {
+            flush_list<KIND>(lsn, lsm, count, nd, lane, rx, ry, rz, mi, fc.eps2, ax, ay, az, ph, n_int);
+            count = 0;
             __syncwarp();
         }
         if (STATS) {  // opening tests (internal cells only) attributed to bodies
