@@ -77,7 +77,7 @@ typedef struct {
     double   sph_alpha;   /* CUBIC: Monaghan viscosity alpha                */
     double   sph_beta;    /* CUBIC: Monaghan viscosity beta                 */
     uint32_t flags;       /* SFGPU_FLAG_*                                   */
-    uint32_t walk_split;  /* walk threads per body: 0 auto, 1, or 8 (one per root octant) */
+    uint32_t walk_split;  /* walk variant: 0 group walk (default), 1 thread per body, 8 thread per body and root octant, 64 group walk over 8 warps */
     uint32_t reserved[6];
 } sfgpu_params;
 

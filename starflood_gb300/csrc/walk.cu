@@ -819,16 +819,17 @@ int launch_group(sfgpu_sim* s, bool stats) {
 
 template <int KIND>
 int launch_fast(sfgpu_sim* s, bool stats) {
-    // walk_split: 0 (default) group walk, split over the root octants while
-    // one warp per 32 bodies would leave the SMs short of warps; 1 one
-    // thread per body; 8 one thread per body and root octant; 32 group walk
-    // without the split
+    // walk_split: 0 or 32 (default) group walk; 1 one thread per body; 8 one
+    // thread per body and root octant; 64 group walk with the level-2
+    // frontier dealt over 8 warps per group.  Measured on the 65,536-body
+    // uniform sphere the plain group walk is the fastest (the split variants
+    // pay for their redundant top levels and imbalance more than they gain
+    // in occupancy).
     const uint32_t split = s->p.walk_split;
     if (split == 1) return launch_body<KIND, 1>(s, stats);
     if (split == 8) return launch_body<KIND, SPLIT>(s, stats);
-    if (split == 32) return launch_group<KIND, 1>(s, stats);
-    if (sf_ceil_div(s->n, 32) >= (uint32_t)sf_num_sms() * 48u) return launch_group<KIND, 1>(s, stats);
-    return launch_group<KIND, SPLIT>(s, stats);
+    if (split == 64) return launch_group<KIND, SPLIT>(s, stats);
+    return launch_group<KIND, 1>(s, stats);
 }
 
 }  // namespace

@@ -172,7 +172,7 @@ def test_tree_outside_and_nan_bodies(sf, oracle32):
     np.testing.assert_array_equal(v["pot"], pt)
 
 
-@pytest.mark.parametrize("split", [0, 1, 8, 32])
+@pytest.mark.parametrize("split", [0, 1, 8, 64])
 @pytest.mark.parametrize("n,seed", [(65536, 2), (20000, 8)])
 def test_tree_fast_large(sf, oracle32, n, seed, split):
     """FAST walks (group walk; one thread per body; per body and root octant)."""
