@@ -1,9 +1,12 @@
 """Benchmark: Barnes-Hut KDK steps of the 65,536-body expanding uniform sphere
 (theta = 0.5 squared criterion, leaf 8, eps = 0.01, dt = 1e-3) on one GB300,
-plus PP gravity at N = 1,048,576 (Plummer, eps = 0.005), plain and
-compensated forms.  Prints one JSON line.
+plus three sub-benchmarks in the same JSON line: PP gravity at N = 1,048,576
+(Plummer, eps = 0.005), plain and compensated forms ("pp"); Barnes-Hut +
+cubic-spline SPH on a 262,144-body Plummer gas ("sph"); 256 batched systems
+of 1024..32768 bodies, forward and adjoint ("batch").
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                  [--no-pp] [--no-sph] [--no-batch] [--no-cpu]
 
 value  particle-steps/s of K steps with the state resident in HBM, each step
        one replay of the captured CUDA graph of sim_step; the L2 is flushed
@@ -12,8 +15,9 @@ e2e    the same K steps through the drop-in sim_step() with host slabs:
        every call uploads the slab from page-locked host memory, steps and
        downloads the slab (host wall clock).
 roofline  the dominant kernel (the walk), from a CUDA-event-instrumented twin
-       run of the same K steps: algorithmic FP32 flops = 20 per monopole
-       interaction + 12 per opening test (both counted on the device).
+       run of the same K steps: algorithmic FP32 flops = 22 per monopole
+       interaction (20 force + 2 potential, the conventional count) + 12 per
+       opening test (both counted on the device), against the FP32 FMA peak.
 cpu_baseline  the CPU restatement of the reference path (oracle/, OpenMP,
        all host threads) on a bounded sample of the same workload.
 --impl reference  times that CPU path as the reference arm.
@@ -38,9 +42,10 @@ sys.path.insert(0, ROOT)
 
 N_BH = 65536
 N_PP = 1 << 20
+N_SPH = 1 << 18
 METRIC = "particle-steps/s & PP interactions/s, chosen vs plain, 1 GB300, rel err<=1e-6"
 WORKLOAD = "Barnes-Hut KDK step, N=65536 uniform unit sphere, v=0.5r, m=1/N, G=1, eps=0.01, theta=0.5, leaf=8, dt=1e-3"
-FLOP_INTERACTION = 20
+FLOP_INTERACTION = 22  # conventional count: 20 for the force, 2 more with the potential
 FLOP_OPEN = 12
 
 
@@ -113,6 +118,16 @@ def fp32_peak_tflops():
         pass
     return sms * 128 * 2 * mhz * 1e6 / 1e12, "derived: %d SMs x 128 FP32 lanes x 2 flop x %.0f MHz (%s)" % (
         sms, mhz, src)
+
+
+def hbm_peak():
+    """Measured HBM copy bandwidth (GB/s) of MEASURED_PEAKS.json, else the
+    6.8 TB/s fallback."""
+    try:
+        mp = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        return float(mp["hbm_gbs"]), "measured: hbm_gbs of MEASURED_PEAKS.json"
+    except Exception:
+        return 6800.0, "fallback: 6.8 TB/s (no MEASURED_PEAKS.json)"
 
 
 def bh_inputs(n=N_BH):
@@ -331,6 +346,252 @@ def pp_accuracy(sf):
     return errs
 
 
+# ---------------------------------------------------------------------------
+# Barnes-Hut + cubic-spline SPH, N = 262,144 Plummer gas
+# ---------------------------------------------------------------------------
+def sph_inputs(n=N_SPH):
+    from starflood_gb300.ics import plummer
+    pos, vel, mas = plummer(n, seed=7)
+    return pos, vel, mas, np.full(n, 0.05, np.float32), np.full(n, 0.05, np.float32)
+
+
+def sph_cell_tile_records(pos, h):
+    """sum over occupied cells c of sum over the 27 cells c' around c of |c'|:
+    the body records one pass streams when each cell loads its 27-cell
+    neighbourhood once (cell side 2 h (1 + 1/4096), the search radius)."""
+    side = 2.0 * float(h) * (1.0 + 1.0 / 4096.0)
+    c = np.floor(pos.astype(np.float64) / side).astype(np.int64)
+    c -= c.min(0)
+    span = c.max(0) + 3
+    key = ((c[:, 0] + 1) * span[1] + (c[:, 1] + 1)) * span[2] + (c[:, 2] + 1)
+    cells, counts = np.unique(key, return_counts=True)
+    occ = dict(zip(cells.tolist(), counts.tolist()))
+    offs = [(dx * span[1] + dy) * span[2] + dz for dx in (-1, 0, 1) for dy in (-1, 0, 1) for dz in (-1, 0, 1)]
+    total = 0
+    for k in cells.tolist():
+        total += sum(occ.get(k + o, 0) for o in offs)
+    return total
+
+
+def gpu_sph(sf, steps, warmup):
+    import ctypes as C
+    import torch
+    n = N_SPH
+    pos, vel, mas, rad, u = sph_inputs()
+    L = sf.lib()
+
+    def new_sim(flags):
+        p = sf.default_params(solver=sf.SOLVER_TREE, sph=sf.SPH_CUBIC, eps=0.01, dt=5e-4, theta=0.5,
+                              acc_mode=sf.ACC_PHYSICAL, sph_gamma=5.0 / 3.0, sph_alpha=1.0, sph_beta=2.0,
+                              flags=flags)
+        s = sf.Sim(n, p)
+        s.set_state(pos, vel, mas, rad)
+        s.sph_set_u(u)
+        s.solve(0)
+        return s
+
+    s = new_sim(0)
+    stream = s.stream()
+    ext = torch.cuda.ExternalStream(stream)
+    s.run(0, warmup + 1)
+    s.sync()
+    events = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    torch.cuda.synchronize()
+    for k in range(steps):
+        sf.check(L.sfgpu_flush_l2(C.c_void_p(stream)), "flush")
+        with torch.cuda.stream(ext):
+            events[k][0].record(ext)
+        s.run(warmup + 1 + k, 1)
+        with torch.cuda.stream(ext):
+            events[k][1].record(ext)
+    s.sync()
+    torch.cuda.synchronize()
+    total_ms = float(sum(a.elapsed_time(b) for a, b in events))
+    status = s.status()
+    mid = sf.slab_views(s.download(), n, 16)["pos"].copy()
+    s.close()
+
+    st = new_sim(sf.FLAG_TIMING)
+    st.run(0, warmup)
+    st.sync()
+    st.stage_times()
+    tsteps = max(3, steps // 5)
+    for k in range(tsteps):
+        sf.check(L.sfgpu_flush_l2(C.c_void_p(st.stream())), "flush")
+        st.step(warmup + k)
+    st.sync()
+    stages = st.stage_times()
+    pairs = float(st.sph_neighbours().astype(np.float64).sum())
+    st.close()
+
+    records = 0.5 * (sph_cell_tile_records(pos, 0.05) + sph_cell_tile_records(mid, 0.05))
+    dens_bytes = records * 16 + n * 32    # x, y, z, m per tile record; 16 B in + 16 B out per body
+    force_bytes = records * 48 + n * 32   # + vx, vy, vz, u and rho, P/rho^2, c, h per tile record
+    d_ms = stages["sph_density"][0] / max(1, stages["sph_density"][1])
+    f_ms = stages["sph_force"][0] / max(1, stages["sph_force"][1])
+    peak = hbm_peak()
+    dens_gbs = dens_bytes / (d_ms * 1e-3) / 1e9
+    force_gbs = force_bytes / (f_ms * 1e-3) / 1e9
+    dom = ("sph_force", force_gbs, force_bytes, f_ms) if f_ms >= d_ms else ("sph_density", dens_gbs, dens_bytes, d_ms)
+    return {
+        "workload": "Barnes-Hut (theta=0.5, leaf 8, eps=0.01) + cubic-spline SPH (h=0.05, gamma=5/3, u0=0.05, "
+                    "alpha=1, beta=2), N=262144 Plummer a=1 M=1 with isotropic velocities, dt=5e-4",
+        "value": n * steps / (total_ms * 1e-3), "unit": "particle-steps/s", "steps": steps,
+        "ms_per_step": total_ms / steps, "device_status": status,
+        "l2": "flushed between timed steps (256 MiB memset, untimed)",
+        "stage_ms_per_step": {k: round(v[0] / max(1, v[1]), 4) for k, v in stages.items()},
+        "neighbour_pairs_per_pass": pairs,
+        "pairs_per_s": {"density": pairs / (d_ms * 1e-3), "force": pairs / (f_ms * 1e-3)},
+        "roofline": {"kernel": "k_cubic_pass<%s>" % ("true" if dom[0] == "sph_force" else "false"),
+                     "bound": "hbm", "achieved": dom[1], "peak": peak[0], "unit": "GB/s", "frac": dom[1] / peak[0],
+                     "traffic": None, "peak_source": peak[1],
+                     "algorithmic_bytes_per_launch": dom[2], "avg_launch_ms": dom[3],
+                     "density_pass_gbs": dens_gbs, "force_pass_gbs": force_gbs,
+                     "cell_tile_records_per_pass": records},
+    }
+
+
+def cpu_sph_rate(max_seconds=20.0):
+    """The reference's own BH + SPH step (SPH mode A: Gaussian all-pairs,
+    sph.c) on a sample of the same Plummer gas, extrapolated to N = 262,144 by
+    N^2 (the all-pairs SPH passes dominate)."""
+    from oracle import build as ob
+    ob.build_oracle()
+    from oracle.pyoracle import Oracle, make_params, slab_views
+    from starflood_gb300.ics import plummer
+    n = 16384
+    pos, vel, mas = plummer(n, seed=7)
+    orc = Oracle("f32")
+    p = make_params(dt=5e-4, eps=0.01, theta=0.5, use_tree=1, use_sph=1)
+    sim, slab, _ = orc.new_sim(n, p)
+    v = slab_views(slab, n, 16)
+    v["pos"][:] = pos
+    v["vel"][:] = vel
+    v["mas"][:] = mas
+    v["rad"][:] = 0.05
+    orc.sim_solv(p, sim, 0)
+    t0 = time.perf_counter()
+    steps = 0
+    while steps < 1 or (time.perf_counter() - t0) < max_seconds and steps < 5:
+        orc.sim_step(p, sim, steps)
+        steps += 1
+    dt = (time.perf_counter() - t0) / steps
+    dt_full = dt * (N_SPH / n) ** 2
+    return {"value": N_SPH / dt_full, "unit": "particle-steps/s", "cores": orc.threads(), "kind": "port",
+            "sample": "%d sim_step calls (Barnes-Hut + reference SPH, Gaussian all-pairs) at N=%d, %.2f s each, "
+                      "scaled by N^2 to N=%d" % (steps, n, dt, N_SPH)}
+
+
+# ---------------------------------------------------------------------------
+# batched + adjoint: 256 independent uniform spheres, N log-uniform in [1024, 32768]
+# ---------------------------------------------------------------------------
+def batch_inputs():
+    from starflood_gb300.ics import log_uniform_sizes, uniform_ball
+    sizes = log_uniform_sizes(256, 1024, 32768, seed=7)
+    P, V, M = [], [], []
+    for k, n in enumerate(sizes):
+        p, v, m = uniform_ball(int(n), seed=1000 + k)
+        P.append(p)
+        V.append(v)
+        M.append(m)
+    return [int(x) for x in sizes], np.concatenate(P), np.concatenate(V), np.concatenate(M)
+
+
+def fp64_pp(pos, mas, eps, idx):
+    x = pos.astype(np.float64)
+    m = mas.astype(np.float64)
+    out = np.zeros((len(idx), 3))
+    for a in range(0, len(idx), 512):
+        ii = idx[a:a + 512]
+        d = x[None, :, :] - x[ii][:, None, :]
+        r2 = (d * d).sum(-1) + eps * eps
+        out[a:a + 512] = (d * (m[None, :] / (r2 * np.sqrt(r2)))[..., None]).sum(1) * m[ii][:, None]
+    return out
+
+
+def gpu_batch(sf, steps=200, ckpt=20):
+    import torch
+    sizes, pos, vel, mas = batch_inputs()
+    off = np.concatenate([[0], np.cumsum(sizes)])
+    inter_per_eval = float(sum(n * n for n in sizes))
+    p = sf.default_params(solver=sf.SOLVER_PP, eps=0.01, dt=1e-3)
+    out = {"workload": "256 uniform spheres, N log-uniform in [1024, 32768] (total %d), PP eps=0.01, "
+                       "%d KDK steps at dt=1e-3, loss = sum over systems of mean r^2 at the last step, "
+                       "checkpoint every %d steps" % (int(off[-1]), steps, ckpt),
+           "interactions_per_eval": inter_per_eval}
+    check_sys = [int(np.argmin(sizes)), int(np.argsort(sizes)[len(sizes) // 2])]
+    with sf.Batch(sizes, p) as b:
+        b.upload(pos, vel, mas)
+        b.solve()
+        cfg = b.autotune()
+        b.solve()
+        _, _, acc, _ = b.download()
+        errs = []
+        for k in check_sys:
+            sl = slice(off[k], off[k + 1])
+            idx = np.arange(0, sizes[k], max(1, sizes[k] // 512))
+            ref = fp64_pp(pos[sl], mas[sl], 0.01, idx)
+            errs.append(float(np.linalg.norm(acc[sl][idx] - ref) / np.linalg.norm(ref)))
+        ext = torch.cuda.ExternalStream(b.stream())
+        b.run(3)
+        b.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(ext):
+            e0.record(ext)
+        b.run(steps)
+        with torch.cuda.stream(ext):
+            e1.record(ext)
+        b.sync()
+        fwd_ms = e0.elapsed_time(e1)
+        t0 = time.perf_counter()
+        b.run(steps)
+        b.sync()
+        fwd_wall = time.perf_counter() - t0
+        b.upload(pos, vel, mas)
+        t0 = time.perf_counter()
+        loss, gp, gv = b.grad(steps, ckpt)
+        adj_s = time.perf_counter() - t0
+    out["batched"] = {"value": inter_per_eval * steps / (fwd_ms * 1e-3), "unit": "interactions/s",
+                      "particle_steps_per_s": float(off[-1]) * steps / (fwd_ms * 1e-3), "ms": fwd_ms,
+                      "wall_clock_value": inter_per_eval * steps / fwd_wall,
+                      "tile_config": cfg, "force_error_vs_fp64": max(errs),
+                      "launch": "one CUDA graph of all %d steps, persistent PP kernel per step" % steps}
+    out["adjoint"] = {"seconds": adj_s, "loss": loss, "grad_finite": bool(np.isfinite(gp).all() and np.isfinite(gv).all()),
+                      "note": "forward with checkpoints + reverse sweep with recomputation (host wall clock, "
+                              "includes the gradient download)"}
+    # plain form: one simulation per system, its own graph of the same steps
+    sims, plain_errs = [], []
+    try:
+        for k, n in enumerate(sizes):
+            sl = slice(off[k], off[k + 1])
+            s = sf.Sim(n, p)
+            s.set_state(pos[sl], vel[sl], mas[sl])
+            s.solve(0)
+            if k in check_sys:
+                a = sf.slab_views(s.download(), n, 13)["acc"]
+                idx = np.arange(0, n, max(1, n // 512))
+                ref = fp64_pp(pos[sl], mas[sl], 0.01, idx)
+                plain_errs.append(float(np.linalg.norm(a[idx] - ref) / np.linalg.norm(ref)))
+            s.run(0, 1)
+            sims.append(s)
+        for s in sims:
+            s.sync()
+        t0 = time.perf_counter()
+        for s in sims:
+            s.run(1, steps)
+        for s in sims:
+            s.sync()
+        plain_s = time.perf_counter() - t0
+    finally:
+        for s in sims:
+            s.close()
+    out["plain"] = {"value": inter_per_eval * steps / plain_s, "unit": "interactions/s", "seconds": plain_s,
+                    "force_error_vs_fp64": max(plain_errs),
+                    "launch": "one simulation per system, each a CUDA graph per step, host wall clock"}
+    out["batched_over_plain"] = out["batched"]["value"] / out["plain"]["value"]
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -339,6 +600,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-pp", action="store_true", help="skip the N=1M PP sub-benchmark")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
+    ap.add_argument("--no-sph", action="store_true", help="skip the N=262144 Barnes-Hut + SPH sub-benchmark")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched + adjoint sub-benchmark")
     args = ap.parse_args()
     rank, world, local = env_rank()
 
@@ -417,8 +680,22 @@ def main():
                 pp["cpu_baseline"] = {"skipped": "--no-cpu"} if args.no_cpu else cpu_pp_rate()
             except Exception as e:
                 pp["cpu_baseline"] = {"error": str(e)}
-            pp["workload"] = "PP gravity N=1048576 Plummer a=1 M=1 eps=0.005, 20 flop/interaction"
+            pp["workload"] = "PP gravity N=1048576 Plummer a=1 M=1 eps=0.005, %d flop/interaction" % FLOP_INTERACTION
             line["pp"] = pp
+        if not args.no_sph:
+            sph = gpu_sph(sf, max(10, min(args.steps, 50)), args.warmup)
+            try:
+                sph["cpu_baseline"] = {"skipped": "--no-cpu"} if args.no_cpu else cpu_sph_rate()
+            except Exception as e:
+                sph["cpu_baseline"] = {"error": str(e)}
+            line["sph"] = sph
+        if not args.no_batch:
+            bt = gpu_batch(sf)
+            if not args.no_cpu and isinstance(line.get("pp", {}).get("cpu_baseline"), dict) \
+                    and "value" in line["pp"]["cpu_baseline"]:
+                cpu = line["pp"]["cpu_baseline"]
+                bt["cpu_baseline"] = dict(cpu, sample=cpu["sample"] + "; the batched workload at this rate")
+            line["batch"] = bt
         print(json.dumps(line))
     if world > 1:
         dist.barrier()

@@ -212,6 +212,21 @@ int sfgpu_host_unregister(void* ptr);
  * that the next kernel starts with a cold L2. */
 int sfgpu_flush_l2(void* stream);
 
+/* ---- snapshots (src/simulation_io.c:16-149, the raw format) --------------- */
+/* The raw format is the slab itself, N*dof floats with no header, as
+ * sim_save_raw / sim_read_raw write and read it.  sfgpu_save_raw snapshots
+ * the state left by the work queued so far without waiting for it: the slab
+ * is copied to page-locked staging memory on the simulation's stream and a
+ * writer thread writes the file while later steps run (at most two
+ * snapshots in flight; a third call waits for a free buffer).
+ * sfgpu_snapshot_wait blocks until every snapshot is written and returns -1
+ * with the first write error.  sfgpu_read_raw loads a raw file (exactly
+ * N*dof floats, else -1; the reference only prints a short read) and
+ * uploads it. */
+int sfgpu_save_raw(sfgpu_sim* s, const char* filename);
+int sfgpu_snapshot_wait(sfgpu_sim* s);
+int sfgpu_read_raw(sfgpu_sim* s, const char* filename);
+
 /* ---- stateless solver calls on device arrays ---------------------------- */
 /* All pointers are device pointers in the reference layout; stream is a
  * cudaStream_t (NULL = default stream).  Work space is allocated and cached

@@ -78,6 +78,12 @@ real* sim_find(const sim_t* sim, enum sim_conf parameter);
 int sim_init(sim_t* sim, unsigned int N);
 /* src/simulation.c:189-228 */
 int sim_free(sim_t* sim);
+/* src/simulation_io.c:16-79: the slab (N*SIM_DOF reals, no header) from a
+ * file into sim->mem and the device; like the reference, a short read is
+ * reported on stderr but not failed. */
+int sim_read_raw(sim_t* sim, const char* filename);
+/* src/simulation_io.c:81-149: sim->mem (current after every call) to a file. */
+int sim_save_raw(const sim_t* sim, const char* filename);
 /* src/simulation.c:230-345 (without SOLVER_VIS) */
 int sim_solv(sim_t* sim);
 /* src/simulation.c:347-519 (without SOLVER_VIS) */

@@ -125,6 +125,8 @@ def build_reference(names: list[str] | None = None, force: bool = False) -> list
             with open(cfg, "w") as f:
                 f.write(text)
         units = ["simulation", "gravity", "sph", "log", "grid"] + (["tree"] if v["tree"] else [])
+        if not v["fp64"]:
+            units.append("simulation_io")  # the raw snapshot format
         srcs = [os.path.join(REFERENCE_SRC, u + ".c") for u in units]
         out = os.path.join(REF_OUT, "libref_%s.so" % name)
         outs.append(out)

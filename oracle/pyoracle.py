@@ -264,5 +264,13 @@ class Reference:
         return dict(parent=parent, bodies=bodies, branch=branch, bounds=bounds, params=params,
                     root_bounds=tb)
 
+    def save_raw(self, filename):
+        """src/simulation_io.c:81-149 (FP32 variants)."""
+        return self.lib.refh_save_raw(filename.encode())
+
+    def read_raw(self, filename):
+        """src/simulation_io.c:16-79 (FP32 variants)."""
+        return self.lib.refh_read_raw(filename.encode())
+
     def free(self):
         self.lib.refh_free()

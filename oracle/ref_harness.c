@@ -133,6 +133,13 @@ int refh_tree_build(unsigned int n, const real* bounds6) {
 int refh_walk(void) { return solve_gravity_part_tree(&g_sim); }
 #endif
 
+#ifndef STARFLOOD_DOUBLE_PRECISION
+/* src/simulation_io.c:16-149 on the harness's simulation (FP32 builds; the
+ * FP64 build of simulation_io.c does not compile) */
+int refh_save_raw(const char* filename) { return sim_save_raw(&g_sim, filename); }
+int refh_read_raw(const char* filename) { return sim_read_raw(&g_sim, filename); }
+#endif
+
 int refh_free(void) {
     mute();
     int rc = sim_free(&g_sim);

@@ -102,6 +102,9 @@ def lib():
             "sfgpu_host_register": (i32, [vp, C.c_size_t]),
             "sfgpu_host_unregister": (i32, [vp]),
             "sfgpu_flush_l2": (i32, [vp]),
+            "sfgpu_save_raw": (i32, [vp, C.c_char_p]),
+            "sfgpu_snapshot_wait": (i32, [vp]),
+            "sfgpu_read_raw": (i32, [vp, C.c_char_p]),
             "sfgpu_compat_configure": (i32, [P]),
             "sfgpu_compat_params": (None, [P]),
         }
@@ -232,6 +235,16 @@ class Sim:
             raise SfgpuError(last_error())
         return {names[i].decode(): (ms[i], la[i]) for i in range(m)}
 
+    def save_raw(self, filename):
+        """Queue a raw snapshot of the current state (written asynchronously)."""
+        check(lib().sfgpu_save_raw(self.h, os.fsencode(filename)), "sfgpu_save_raw")
+
+    def snapshot_wait(self):
+        check(lib().sfgpu_snapshot_wait(self.h), "sfgpu_snapshot_wait")
+
+    def read_raw(self, filename):
+        check(lib().sfgpu_read_raw(self.h, os.fsencode(filename)), "sfgpu_read_raw")
+
     def walk_stats(self):
         a = np.zeros(self.n, np.uint32)
         b = np.zeros(self.n, np.uint32)
@@ -342,6 +355,7 @@ def compat_functions():
     for name, args in (("sim_init", [S, C.c_uint]), ("sim_free", [S]), ("sim_solv", [S]), ("sim_step", [S]),
                        ("solve_gravity_part_part", [S]), ("solve_gravity_part_tree", [S]), ("solve_sph", [S]),
                        ("tree_init", [T, C.c_uint]), ("tree_free", [T]),
+                       ("sim_save_raw", [S, C.c_char_p]), ("sim_read_raw", [S, C.c_char_p]),
                        ("tree_build", [T, C.c_uint, C.c_void_p, C.c_void_p])):
         fn = getattr(L, name)
         fn.restype = C.c_int

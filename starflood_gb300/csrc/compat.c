@@ -256,6 +256,58 @@ static int solv_common(sim_t* sim, int step) {
 int sim_solv(sim_t* sim) { return solv_common(sim, 0); }
 int sim_step(sim_t* sim) { return solv_common(sim, 1); }
 
+/* src/simulation_io.c:16-79.  The raw format is the slab itself.  As in the
+ * reference, a short read is reported but not failed; the device copy
+ * follows on the next call (every call uploads the host slab). */
+int sim_read_raw(sim_t* sim, const char* filename) {
+    if (!filename) {
+        fprintf(stderr, "%s error: filename is NULL!\n", "sim_read_raw()");
+        return -1;
+    }
+    FILE* f = fopen(filename, "rb");
+    if (!f) {
+        fprintf(stderr, "%s error: fopen(\"%s\", \"%s\") ", "sim_read_raw()", filename, "rb");
+        perror("failed");
+        return -1;
+    }
+    const size_t len = (size_t)sim->N * (size_t)dof_now();
+    if (len != fread(sim->mem, sizeof(real), len, f)) {
+        fprintf(stderr, "%s error: fread(file) ", "sim_read_raw()");
+        perror("failed");
+    }
+    if (fclose(f) != 0) {
+        fprintf(stderr, "%s error: fclose(file) ", "sim_read_raw()");
+        perror("failed");
+        return -1;
+    }
+    return 0;
+}
+
+/* src/simulation_io.c:81-149: the host slab, current after every call. */
+int sim_save_raw(const sim_t* sim, const char* filename) {
+    if (!filename) {
+        fprintf(stderr, "%s error: filename is NULL!\n", "sim_save_raw()");
+        return -1;
+    }
+    FILE* f = fopen(filename, "wb");
+    if (!f) {
+        fprintf(stderr, "%s error: fopen(\"%s\", \"%s\") ", "sim_save_raw()", filename, "wb");
+        perror("failed");
+        return -1;
+    }
+    const size_t len = (size_t)sim->N * (size_t)dof_now();
+    if (len != fwrite(sim->mem, sizeof(real), len, f)) {
+        fprintf(stderr, "%s error: fwrite(file) ", "sim_save_raw()");
+        perror("failed");
+    }
+    if (fclose(f) != 0) {
+        fprintf(stderr, "%s error: fclose(file) ", "sim_save_raw()");
+        perror("failed");
+        return -1;
+    }
+    return 0;
+}
+
 int sim_solv_vis(sim_t* sim, float* render_buffer, unsigned int sizex, unsigned int sizey) {
     (void)render_buffer;
     (void)sizex;

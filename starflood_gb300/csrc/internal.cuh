@@ -172,6 +172,12 @@ void sf_sort_free(SortWork& w);
 int sf_sort_pairs(uint64_t* keys, uint32_t* vals, uint32_t n, int bits, SortWork& w,
                   cudaStream_t st, uint32_t* d_status, const uint32_t* d_n = nullptr,
                   const uint32_t* enable = nullptr);
+// The same without the final copy: the result is left in (*out_keys,
+// *out_vals), which is (keys, vals) after an even number of passes and
+// (w.keys_b, w.vals_b) after an odd one.
+int sf_sort_pairs_keep(uint64_t* keys, uint32_t* vals, uint32_t n, int bits, SortWork& w, cudaStream_t st,
+                       uint32_t* d_status, uint64_t** out_keys, uint32_t** out_vals,
+                       const uint32_t* enable = nullptr);
 
 // ---------------------------------------------------------------------------
 // simulation state
@@ -215,7 +221,9 @@ struct sfgpu_sim {
     StageTimer timer;
     cudaGraphExec_t graph = nullptr;
     bool graph_ok = true;
+    struct SnapshotWriter* snap = nullptr;  // snapshot.cu
 };
+void sf_snapshot_free(sfgpu_sim* s);
 
 // stage entry points (each queues kernels on s->stream)
 int sf_stage_gravity_pp(sfgpu_sim* s);

@@ -21,23 +21,27 @@ namespace {
 
 constexpr double K_INV_U32 = 2.3283062977608182109179324470460414886474609375e-10;  // rng.h:9
 
+// Fixed-order FP64 block sum (pairwise within each warp by shuffles, then
+// the warps in order); thread 0 writes the NV block totals.  Plain FP64 adds:
+// GB300's FP64 rate makes double-double arithmetic the bottleneck here.
 template <int NV>
-__device__ void block_dd_reduce(double2 (&v)[NV], double2* out) {
-    __shared__ double2 sh[NV][SF_RED_BLOCK];
-    const int t = threadIdx.x;
+__device__ void block_sum(double (&v)[NV], double* out) {
+    __shared__ double wsum[NV][SF_RED_BLOCK / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-    for (int k = 0; k < NV; k++) sh[k][t] = v[k];
-    __syncthreads();
-    for (int off = SF_RED_BLOCK / 2; off > 0; off >>= 1) {
-        if (t < off) {
-#pragma unroll
-            for (int k = 0; k < NV; k++) sh[k][t] = dd_add(sh[k][t], sh[k][t + off]);
-        }
-        __syncthreads();
+    for (int k = 0; k < NV; k++) {
+        double x = v[k];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) wsum[k][warp] = x;
     }
-    if (t == 0) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
 #pragma unroll
-        for (int k = 0; k < NV; k++) out[(size_t)blockIdx.x * NV + k] = sh[k][0];
+        for (int k = 0; k < NV; k++) {
+            double t = 0.0;
+            for (int w = 0; w < SF_RED_BLOCK / 32; w++) t += wsum[k][w];
+            out[(size_t)blockIdx.x * NV + k] = t;
+        }
     }
 }
 
@@ -65,23 +69,25 @@ __device__ bool last_block(uint32_t* done) {
 }
 
 template <int NV>
-__device__ void sum_partials(const double2* part, uint32_t nparts, double* out) {
-    double2 v[NV];
-    for (int k = 0; k < NV; k++) v[k] = make_double2(0.0, 0.0);
+__device__ void sum_partials(const double* part, uint32_t nparts, double* out) {
+    double v[NV];
+    for (int k = 0; k < NV; k++) v[k] = 0.0;
     for (uint32_t b = threadIdx.x; b < nparts; b += SF_RED_BLOCK)
-        for (int k = 0; k < NV; k++) v[k] = dd_add(v[k], __ldcg(&part[(size_t)b * NV + k]));
-    __shared__ double2 total[NV];
-    __shared__ double2 sh[NV][SF_RED_BLOCK];
-    for (int k = 0; k < NV; k++) sh[k][threadIdx.x] = v[k];
-    __syncthreads();
-    for (int off = SF_RED_BLOCK / 2; off > 0; off >>= 1) {
-        if ((int)threadIdx.x < off)
-            for (int k = 0; k < NV; k++) sh[k][threadIdx.x] = dd_add(sh[k][threadIdx.x], sh[k][threadIdx.x + off]);
-        __syncthreads();
+        for (int k = 0; k < NV; k++) v[k] += __ldcg(&part[(size_t)b * NV + k]);
+    __shared__ double wsum[NV][SF_RED_BLOCK / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int k = 0; k < NV; k++) {
+        double x = v[k];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) wsum[k][warp] = x;
     }
+    __syncthreads();
     if (threadIdx.x == 0)
-        for (int k = 0; k < NV; k++) out[k] = __dadd_rn(sh[k][0].x, sh[k][0].y);
-    (void)total;
+        for (int k = 0; k < NV; k++) {
+            double t = 0.0;
+            for (int w = 0; w < SF_RED_BLOCK / 32; w++) t += wsum[k][w];
+            out[k] = t;
+        }
 }
 
 // simulation.c:276-301: mean radius -> jittered root cube
@@ -99,7 +105,7 @@ __device__ void root_cube(double sum, uint32_t n, uint32_t step, float* __restri
     sums[4] = rbar;
 }
 
-__device__ void finish_bounds(const double2* part, uint32_t n, const uint32_t* d_step, float* bounds, double* sums) {
+__device__ void finish_bounds(const double* part, uint32_t n, const uint32_t* d_step, float* bounds, double* sums) {
     __shared__ double tot[1];
     sum_partials<1>(part, gridDim.x, tot);
     __syncthreads();
@@ -109,7 +115,7 @@ __device__ void finish_bounds(const double2* part, uint32_t n, const uint32_t* d
 __global__ void __launch_bounds__(SF_RED_BLOCK) k_kick_drift(float* __restrict__ slab, uint32_t n, float half_dt,
                                                              float dt, double* __restrict__ pos64,
                                                              double* __restrict__ vel64, double dt64,
-                                                             int want_radius, double2* __restrict__ part,
+                                                             int want_radius, double* __restrict__ part,
                                                              uint32_t* done, const uint32_t* __restrict__ d_step,
                                                              float* __restrict__ bounds, double* __restrict__ sums,
                                                              float* __restrict__ u, const float* __restrict__ dudt) {
@@ -118,7 +124,7 @@ __global__ void __launch_bounds__(SF_RED_BLOCK) k_kick_drift(float* __restrict__
     float* pos = slab;
     float* vel = slab + (size_t)3 * n;
     const float* acc = slab + (size_t)6 * n;
-    double2 r[1] = {make_double2(0.0, 0.0)};
+    double r[1] = {0.0};
     if (i < n) {
         float x[3];
 #pragma unroll
@@ -140,28 +146,28 @@ __global__ void __launch_bounds__(SF_RED_BLOCK) k_kick_drift(float* __restrict__
                 pos[k] = x[c];
             }
         }
-        if (want_radius) r[0] = make_double2(radius64(x[0], x[1], x[2]), 0.0);
+        if (want_radius) r[0] = radius64(x[0], x[1], x[2]);
     }
     if (!want_radius) return;
-    block_dd_reduce<1>(r, part);
+    block_sum<1>(r, part);
     if (last_block(done)) finish_bounds(part, n, d_step, bounds, sums);
 }
 
 __global__ void __launch_bounds__(SF_RED_BLOCK) k_radius(const float* __restrict__ pos, uint32_t n,
-                                                         double2* __restrict__ part, uint32_t* done,
+                                                         double* __restrict__ part, uint32_t* done,
                                                          const uint32_t* __restrict__ d_step,
                                                          float* __restrict__ bounds, double* __restrict__ sums) {
     const uint32_t i = blockIdx.x * SF_RED_BLOCK + threadIdx.x;
-    double2 r[1] = {make_double2(0.0, 0.0)};
-    if (i < n) r[0] = make_double2(radius64(pos[3u * i], pos[3u * i + 1u], pos[3u * i + 2u]), 0.0);
-    block_dd_reduce<1>(r, part);
+    double r[1] = {0.0};
+    if (i < n) r[0] = radius64(pos[3u * i], pos[3u * i + 1u], pos[3u * i + 2u]);
+    block_sum<1>(r, part);
     if (last_block(done)) finish_bounds(part, n, d_step, bounds, sums);
 }
 
 __global__ void __launch_bounds__(SF_RED_BLOCK) k_kick_energy(float* __restrict__ slab, uint32_t n, float half_dt,
                                                               double* __restrict__ vel64, double dt64,
                                                               float g_over_eps, int physical,
-                                                              double2* __restrict__ part, uint32_t* done,
+                                                              double* __restrict__ part, uint32_t* done,
                                                               double* __restrict__ sums, uint32_t* d_step,
                                                               float* __restrict__ u, const float* __restrict__ dudt) {
     const uint32_t i = blockIdx.x * SF_RED_BLOCK + threadIdx.x;
@@ -172,7 +178,7 @@ __global__ void __launch_bounds__(SF_RED_BLOCK) k_kick_energy(float* __restrict_
     const float* pot = slab + (size_t)10 * n;
     float* ken = slab + (size_t)11 * n;
     float* pen = slab + (size_t)12 * n;
-    double2 e[4] = {make_double2(0, 0), make_double2(0, 0), make_double2(0, 0), make_double2(0, 0)};
+    double e[4] = {0.0, 0.0, 0.0, 0.0};
     if (i < n) {
         float v[3];
         double v64[3];
@@ -202,12 +208,12 @@ __global__ void __launch_bounds__(SF_RED_BLOCK) k_kick_energy(float* __restrict_
         const double kin = physical ? 0.5 * (double)m * v2d : 0.5 * v2d;
         const double selfp = (double)g_over_eps * (double)m;  // G m_i / eps (the j = i term)
         const double upair = 0.5 * (double)m * ((double)pot[i] + selfp);
-        e[0] = make_double2((double)k_i, 0.0);
-        e[1] = make_double2((double)p_i, 0.0);
-        e[2] = make_double2(kin, 0.0);
-        e[3] = make_double2(upair, 0.0);
+        e[0] = (double)k_i;
+        e[1] = (double)p_i;
+        e[2] = kin;
+        e[3] = upair;
     }
-    block_dd_reduce<4>(e, part);
+    block_sum<4>(e, part);
     if (last_block(done)) {
         // simulation.c:455-497: T = sum ken, V = sum pen (FP64)
         sum_partials<4>(part, gridDim.x, sums);
@@ -231,7 +237,7 @@ int sf_stage_kick_drift(sfgpu_sim* s, bool want_radius) {
     if (ensure_red(s, nb * 4) != SFGPU_OK) return SFGPU_FAILURE;
     const float dt = (float)s->p.dt;
     k_kick_drift<<<nb, SF_RED_BLOCK, 0, s->stream>>>(s->slab, s->n, 0.5f * dt, dt, s->pos64, s->vel64, s->p.dt,
-                                                     want_radius ? 1 : 0, s->red, s->d_done, s->d_step, s->d_bounds,
+                                                     want_radius ? 1 : 0, (double*)s->red, s->d_done, s->d_step, s->d_bounds,
                                                      s->sums, s->u, s->dudt);
     SF_CHECK_LAUNCH();
     return SFGPU_OK;
@@ -240,7 +246,7 @@ int sf_stage_kick_drift(sfgpu_sim* s, bool want_radius) {
 int sf_stage_radius(sfgpu_sim* s) {
     const uint32_t nb = sf_ceil_div(s->n, SF_RED_BLOCK);
     if (ensure_red(s, nb * 4) != SFGPU_OK) return SFGPU_FAILURE;
-    k_radius<<<nb, SF_RED_BLOCK, 0, s->stream>>>(s->slab, s->n, s->red, s->d_done, s->d_step, s->d_bounds, s->sums);
+    k_radius<<<nb, SF_RED_BLOCK, 0, s->stream>>>(s->slab, s->n, (double*)s->red, s->d_done, s->d_step, s->d_bounds, s->sums);
     SF_CHECK_LAUNCH();
     return SFGPU_OK;
 }
@@ -251,7 +257,7 @@ int sf_stage_kick_energy(sfgpu_sim* s) {
     const float dt = (float)s->p.dt;
     const float g_over_eps = (float)(s->p.G / s->p.eps);
     k_kick_energy<<<nb, SF_RED_BLOCK, 0, s->stream>>>(s->slab, s->n, 0.5f * dt, s->vel64, s->p.dt, g_over_eps,
-                                                      s->p.acc_mode == SFGPU_ACC_PHYSICAL, s->red, s->d_done + 1,
+                                                      s->p.acc_mode == SFGPU_ACC_PHYSICAL, (double*)s->red, s->d_done + 1,
                                                       s->sums, s->d_step, s->u, s->dudt);
     SF_CHECK_LAUNCH();
     return SFGPU_OK;

@@ -142,6 +142,110 @@ __global__ void __launch_bounds__(BS) k_pp_tile(const float* __restrict__ pos, c
     (void)pos64;
 }
 
+// The same tile loop on Blackwell's paired FP32 instructions (fma/add/mul
+// .f32x2): two bodies per instruction, so one issue slot does two lanes'
+// worth of FP32 work and the rsqrt (MUFU) and shared-memory loads no longer
+// compete with the arithmetic for issue.  Every element is rounded exactly as
+// in k_pp_tile (same operations, same order), so the results are identical.
+// Each j is staged pre-duplicated as (x,x,y,y) and (z,z,w,w) so the paired
+// operands come straight out of one 128-bit shared load.
+template <int BS, int PAIRS, bool COMP>
+__global__ void __launch_bounds__(BS) k_pp_tile2(const float* __restrict__ pos, const float* __restrict__ mas,
+                                                 uint32_t n, float eps2, uint32_t jchunk,
+                                                 float4* __restrict__ part) {
+    __shared__ float4 sj[2][BS];
+    const uint32_t ibase = blockIdx.x * (BS * 2 * PAIRS);
+    float2 nx[PAIRS], ny[PAIRS], nz[PAIRS];
+    float2 ax[PAIRS], ay[PAIRS], az[PAIRS], ph[PAIRS];
+    float2 hx[PAIRS], hy[PAIRS], hz[PAIRS], hp[PAIRS];  // compensated totals
+    float2 lx[PAIRS], ly[PAIRS], lz[PAIRS], lp[PAIRS];
+    const float2 zero2 = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int q = 0; q < PAIRS; q++) {
+        const uint32_t i0 = ibase + (2 * q) * BS + threadIdx.x;
+        const uint32_t i1 = i0 + BS;
+        nx[q] = make_float2(i0 < n ? -pos[3u * i0] : 0.f, i1 < n ? -pos[3u * i1] : 0.f);
+        ny[q] = make_float2(i0 < n ? -pos[3u * i0 + 1u] : 0.f, i1 < n ? -pos[3u * i1 + 1u] : 0.f);
+        nz[q] = make_float2(i0 < n ? -pos[3u * i0 + 2u] : 0.f, i1 < n ? -pos[3u * i1 + 2u] : 0.f);
+        ax[q] = ay[q] = az[q] = ph[q] = zero2;
+        hx[q] = hy[q] = hz[q] = hp[q] = zero2;
+        lx[q] = ly[q] = lz[q] = lp[q] = zero2;
+    }
+    const float2 e2 = make_float2(eps2, eps2);
+    const uint32_t j0 = blockIdx.y * jchunk;
+    const uint32_t j1 = min(n, j0 + jchunk);
+    for (uint32_t jt = j0; jt < j1; jt += BS) {
+        const uint32_t j = jt + threadIdx.x;
+        float x = 0.f, y = 0.f, z = 0.f, w = 0.f;  // padding: zero mass
+        if (j < j1) {
+            x = pos[3u * j];
+            y = pos[3u * j + 1u];
+            z = pos[3u * j + 2u];
+            w = mas[j];
+        }
+        __syncthreads();
+        sj[0][threadIdx.x] = make_float4(x, x, y, y);
+        sj[1][threadIdx.x] = make_float4(z, z, w, w);
+        __syncthreads();
+#pragma unroll 4
+        for (int jj = 0; jj < BS; jj++) {
+            const float4 A = sj[0][jj];
+            const float4 B = sj[1][jj];
+            const float2 sx = make_float2(A.x, A.y), sy = make_float2(A.z, A.w);
+            const float2 sz = make_float2(B.x, B.y), sw = make_float2(B.z, B.w);
+#pragma unroll
+            for (int q = 0; q < PAIRS; q++) {
+                const float2 dx = __fadd2_rn(sx, nx[q]);
+                const float2 dy = __fadd2_rn(sy, ny[q]);
+                const float2 dz = __fadd2_rn(sz, nz[q]);
+                float2 r2 = __ffma2_rn(dz, dz, e2);
+                r2 = __ffma2_rn(dy, dy, r2);
+                r2 = __ffma2_rn(dx, dx, r2);
+                const float2 inv = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
+                const float2 mphi = __fmul2_rn(sw, inv);
+                const float2 f = __fmul2_rn(mphi, __fmul2_rn(inv, inv));
+                ax[q] = __ffma2_rn(f, dx, ax[q]);
+                ay[q] = __ffma2_rn(f, dy, ay[q]);
+                az[q] = __ffma2_rn(f, dz, az[q]);
+                ph[q] = __fadd2_rn(ph[q], mphi);
+            }
+        }
+        if (COMP) {
+#pragma unroll
+            for (int q = 0; q < PAIRS; q++) {
+                float e;
+                two_sumf(hx[q].x, ax[q].x, hx[q].x, e); lx[q].x += e;
+                two_sumf(hx[q].y, ax[q].y, hx[q].y, e); lx[q].y += e;
+                two_sumf(hy[q].x, ay[q].x, hy[q].x, e); ly[q].x += e;
+                two_sumf(hy[q].y, ay[q].y, hy[q].y, e); ly[q].y += e;
+                two_sumf(hz[q].x, az[q].x, hz[q].x, e); lz[q].x += e;
+                two_sumf(hz[q].y, az[q].y, hz[q].y, e); lz[q].y += e;
+                two_sumf(hp[q].x, ph[q].x, hp[q].x, e); lp[q].x += e;
+                two_sumf(hp[q].y, ph[q].y, hp[q].y, e); lp[q].y += e;
+                ax[q] = ay[q] = az[q] = ph[q] = zero2;
+            }
+        }
+    }
+    float4* out = part + (size_t)blockIdx.y * n * (COMP ? 2 : 1);
+#pragma unroll
+    for (int q = 0; q < PAIRS; q++) {
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const uint32_t i = ibase + (2 * q + h) * BS + threadIdx.x;
+            if (i >= n) continue;
+            if (COMP) {
+                out[i] = h ? make_float4(hx[q].y, hy[q].y, hz[q].y, hp[q].y)
+                           : make_float4(hx[q].x, hy[q].x, hz[q].x, hp[q].x);
+                out[(size_t)n + i] = h ? make_float4(lx[q].y, ly[q].y, lz[q].y, lp[q].y)
+                                       : make_float4(lx[q].x, ly[q].x, lz[q].x, lp[q].x);
+            } else {
+                out[i] = h ? make_float4(ax[q].y, ay[q].y, az[q].y, ph[q].y)
+                           : make_float4(ax[q].x, ay[q].x, az[q].x, ph[q].x);
+            }
+        }
+    }
+}
+
 template <bool COMP>
 __global__ void k_pp_reduce(const float4* __restrict__ part, uint32_t n, uint32_t nsplit,
                             const float* __restrict__ mas, ForceConsts fc, float* __restrict__ acc,

@@ -194,8 +194,10 @@ void sf_sort_free(SortWork& w) {
     w = SortWork{};
 }
 
-int sf_sort_pairs(uint64_t* keys, uint32_t* vals, uint32_t n, int bits, SortWork& w, cudaStream_t st,
-                  uint32_t* d_status, const uint32_t*, const uint32_t* enable) {
+int sf_sort_pairs_keep(uint64_t* keys, uint32_t* vals, uint32_t n, int bits, SortWork& w, cudaStream_t st,
+                       uint32_t* d_status, uint64_t** out_keys, uint32_t** out_vals, const uint32_t* enable) {
+    *out_keys = keys;
+    *out_vals = vals;
     if (n > w.cap) {
         sf_set_error("sort: %u keys exceed the work space of %zu", n, w.cap);
         return SFGPU_FAILURE;
@@ -234,6 +236,16 @@ int sf_sort_pairs(uint64_t* keys, uint32_t* vals, uint32_t n, int bits, SortWork
         std::swap(ka, kb);
         std::swap(va, vb);
     }
+    *out_keys = ka;
+    *out_vals = va;
+    return SFGPU_OK;
+}
+
+int sf_sort_pairs(uint64_t* keys, uint32_t* vals, uint32_t n, int bits, SortWork& w, cudaStream_t st,
+                  uint32_t* d_status, const uint32_t*, const uint32_t* enable) {
+    uint64_t* ka = keys;
+    uint32_t* va = vals;
+    if (sf_sort_pairs_keep(keys, vals, n, bits, w, st, d_status, &ka, &va, enable) != SFGPU_OK) return SFGPU_FAILURE;
     if (ka != keys) {
         const uint32_t cb = std::min<uint32_t>(sf_ceil_div(n, 256), (uint32_t)sf_num_sms() * 8);
         k_copy_pairs<<<cb, 256, 0, st>>>(ka, va, keys, vals, n, enable);

@@ -274,6 +274,7 @@ int sf_sph_cubic(sfgpu_sim* s) {
     cudaStream_t st = s->stream;
     float* hs = w->grid + 4;
     const uint32_t hb = std::min<uint32_t>(sf_ceil_div(n, 256), 1024);
+    int tk = s->timer.begin(st, "sph_grid");
     k_hmax<<<hb, 256, 0, st>>>(s->slab + (size_t)13 * n, n, w->done, w->grid, w->done + 1);
     SF_CHECK_LAUNCH();
     const uint32_t mask = w->tsize - 1;
@@ -287,14 +288,19 @@ int sf_sph_cubic(sfgpu_sim* s) {
     k_cell_gather<<<nb, 256, 0, st>>>(w->keys, w->vals, n, s->slab, s->u, w->grid, w->bstart, w->bend, w->px, w->pv,
                                       w->cell, hs);
     SF_CHECK_LAUNCH();
+    s->timer.end(st, tk);
     const float gamma = (float)s->p.sph_gamma, alpha = (float)s->p.sph_alpha, beta = (float)s->p.sph_beta;
     const uint32_t pb = sf_ceil_div(n, 128);
     uint32_t* nbr = sf_sph_neighbour_counts(s);
+    tk = s->timer.begin(st, "sph_density");
     k_cubic_pass<false><<<pb, 128, 0, st>>>(n, w->grid, mask, w->bstart, w->bend, w->px, w->pv, w->cell, hs, w->pd,
                                             w->vals, gamma, alpha, beta, s->slab, s->dudt, nbr);
     SF_CHECK_LAUNCH();
+    s->timer.end(st, tk);
+    tk = s->timer.begin(st, "sph_force");
     k_cubic_pass<true><<<pb, 128, 0, st>>>(n, w->grid, mask, w->bstart, w->bend, w->px, w->pv, w->cell, hs, w->pd,
                                            w->vals, gamma, alpha, beta, s->slab, s->dudt, nbr);
     SF_CHECK_LAUNCH();
+    s->timer.end(st, tk);
     return SFGPU_OK;
 }

@@ -17,7 +17,8 @@
 // most significant) with the "<=" rule, plus a mask of the levels where it sat
 // exactly on a midplane; (2) keys are radix sorted (stable, so ties keep index
 // order); (3) one block re-derives the digits of the few midplane bodies with
-// the rank rule and the keys are re-sorted when any changed; (4) split nodes
+// the rank rule, and the bodies whose digits changed are merged back into
+// the sorted order at their new keys; (4) split nodes
 // are read off the sorted keys: position k starts a split node at level L iff
 // k begins a level-L run (key[k-1] differs in the first L digits) and
 // key[k+leaf_cap] shares those L digits; an exclusive scan of the per-position
@@ -129,55 +130,67 @@ __device__ __forceinline__ uint32_t lower_bound_shift(const uint64_t* __restrict
     return lo;
 }
 
-// The same, probing lo+1, lo+3, lo+7, ... first: O(log d) loads when the
-// answer is d slots past lo (cells deep in the tree are short runs).
-__device__ __forceinline__ uint32_t gallop_shift(const uint64_t* __restrict__ K, uint32_t lo, uint32_t hi, int shift,
-                                                 uint64_t target) {
-    if (lo >= hi || (K[lo] >> shift) >= target) return lo;
-    uint32_t prev = lo, step = 1;
-    while (true) {
-        const uint32_t probe = prev + step;
-        if (probe >= hi || probe < prev) return lower_bound_shift(K, prev + 1, hi, shift, target);
-        if ((K[probe] >> shift) >= target) return lower_bound_shift(K, prev + 1, probe, shift, target);
-        prev = probe;
-        step <<= 1;
-    }
-}
-
-// First index in [0, hi) whose key >> shift is >= target, probing backwards
-// from hi-1, whose key is known to be >= target.
-__device__ __forceinline__ uint32_t gallop_back(const uint64_t* __restrict__ K, uint32_t hi, int shift,
-                                                uint64_t target) {
-    uint32_t cur = hi - 1, step = 1;
-    while (true) {
-        if (cur < step) return lower_bound_shift(K, 0, cur, shift, target);
-        const uint32_t probe = cur - step;
-        if ((K[probe] >> shift) < target) return lower_bound_shift(K, probe + 1, cur, shift, target);
-        cur = probe;
-        step <<= 1;
-    }
-}
-
 __device__ __forceinline__ uint64_t prefix_of(uint64_t key, int L) { return L == 0 ? 0ull : key >> (3 * (16 - L)); }
 
+// Sorted-key search through a table of every stride-th key in shared memory:
+// the table narrows the answer to one stride (no global loads), a binary
+// search of that stride finishes it (log2(stride) dependent loads instead of
+// log2(nin)).
+constexpr uint32_t NSAMP = 1024;
+
+struct KeySamples {
+    uint32_t stride, count, nin;
+};
+
+__device__ __forceinline__ KeySamples load_key_samples(const uint64_t* __restrict__ K, uint32_t nin,
+                                                       uint64_t* samp) {
+    KeySamples ks;
+    ks.nin = nin;
+    ks.stride = max(1u, (nin + NSAMP - 1) / NSAMP);
+    ks.count = (nin + ks.stride - 1) / ks.stride;
+    for (uint32_t j = threadIdx.x; j < ks.count; j += blockDim.x) samp[j] = K[(size_t)j * ks.stride];
+    return ks;
+}
+
+// first index in [0, nin) whose key >> shift is >= target
+__device__ __forceinline__ uint32_t search_keys(const uint64_t* __restrict__ K, const uint64_t* samp,
+                                                const KeySamples& ks, int shift, uint64_t target) {
+    uint32_t lo = 0, hi = ks.count;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if ((samp[mid] >> shift) < target) lo = mid + 1; else hi = mid;
+    }
+    if (lo == 0) return 0u;
+    const uint32_t a = (lo - 1) * ks.stride + 1;
+    const uint32_t b = (lo == ks.count) ? ks.nin : lo * ks.stride;
+    return lower_bound_shift(K, a, b, shift, target);
+}
+
 // Exact digits for bodies lying on a midplane (one block; see file comment).
+// Reads the sorted provisional keys (Ks, Vs); the bodies whose digits change
+// are listed for k_tie_merge: their old slots ascending (gpos), their new
+// (key, body) ascending (gkey, gbody), their number in *moved_out.
 constexpr int FIX_THREADS = 1024;
+
 __global__ void __launch_bounds__(FIX_THREADS) k_tie_fix(const float* __restrict__ pos, const float* __restrict__ bounds,
-                                                         uint64_t* __restrict__ K, uint32_t* __restrict__ V,
+                                                         const uint64_t* __restrict__ K, const uint32_t* __restrict__ V,
                                                          const uint32_t* __restrict__ nin_p, const uint2* __restrict__ ties,
                                                          const uint32_t* __restrict__ tie_count, uint32_t leaf_cap,
-                                                         uint32_t depth_max, uint32_t* __restrict__ resort,
-                                                         uint64_t* __restrict__ K2, uint32_t* __restrict__ V2) {
+                                                         uint32_t depth_max, uint32_t* __restrict__ moved_out,
+                                                         uint32_t* __restrict__ gpos, uint64_t* __restrict__ gkey,
+                                                         uint32_t* __restrict__ gbody) {
     __shared__ uint64_t prov[TIE_CAP];
     __shared__ uint64_t cur[TIE_CAP];
     __shared__ uint32_t body[TIE_CAP];
     __shared__ uint32_t mask[TIE_CAP];
+    __shared__ uint64_t samp[NSAMP];
     const uint32_t T = min(*tie_count, TIE_CAP);
-    if (threadIdx.x == 0) {
-        *resort = 0u;
+    if (T == 0) {
+        if (threadIdx.x == 0) *moved_out = 0u;
+        return;
     }
-    if (T == 0) return;
     const uint32_t nin = *nin_p;
+    const KeySamples ks = load_key_samples(K, nin, samp);
     for (uint32_t t = threadIdx.x; t < T; t += FIX_THREADS) {
         const uint2 e = ties[t];
         body[t] = e.x;
@@ -202,8 +215,8 @@ __global__ void __launch_bounds__(FIX_THREADS) k_tie_fix(const float* __restrict
             if (!((mask[t] >> L) & 1u)) continue;
             const uint64_t pre = prefix_of(cur[t], L);
             const int shift = 3 * (16 - L);
-            const uint32_t lo = (L == 0) ? 0u : lower_bound_shift(K, 0, nin, shift, pre);
-            const uint32_t hi = (L == 0) ? nin : lower_bound_shift(K, lo, nin, shift, pre + 1);
+            const uint32_t lo = (L == 0) ? 0u : search_keys(K, samp, ks, shift, pre);
+            const uint32_t hi = (L == 0) ? nin : search_keys(K, samp, ks, shift, pre + 1);
             const uint32_t p = body[t];
             uint32_t add = 0, sub = 0, radd = 0, rsub = 0;
             for (uint32_t m = 0; m < n_moved; m++) {
@@ -256,37 +269,66 @@ __global__ void __launch_bounds__(FIX_THREADS) k_tie_fix(const float* __restrict
         if (threadIdx.x == 0) n_moved = min(n_moved_next, TIE_CAP);
         __syncthreads();
     }
-    __syncthreads();
     const uint32_t M = n_moved;
-    if (threadIdx.x == 0) *resort = M;
-    if (M == 0) return;
-    // Restore the (key, index) order in place of a second sort: the moved
-    // bodies leave their old slots and are merged back at their new keys.
-    __shared__ uint32_t mpos[TIE_CAP];   // old slot of each moved body, ascending
-    __shared__ uint64_t mkey[TIE_CAP];   // new keys, ascending by (key, body)
-    __shared__ uint32_t mbody[TIE_CAP];
+    if (threadIdx.x == 0) *moved_out = M;
+    // the moved bodies' old slots, ranked ascending, and their new (key,
+    // body), ranked ascending
     for (uint32_t m = threadIdx.x; m < M; m += FIX_THREADS) {
         const uint32_t t = moved[m];
-        uint32_t k = lower_bound_shift(K, 0, nin, 0, prov[t]);
+        uint32_t k = search_keys(K, samp, ks, 0, prov[t]);
         while (k < nin && V[k] != body[t]) k++;
         uint32_t r_key = 0;
         for (uint32_t q = 0; q < M; q++) {
             const uint32_t u = moved[q];
             if (cur[u] < cur[t] || (cur[u] == cur[t] && body[u] < body[t])) r_key++;
         }
-        mkey[r_key] = cur[t];
-        mbody[r_key] = body[t];
-        prov[t] = (uint64_t)k;  // reuse: old slot
+        gkey[r_key] = cur[t];
+        gbody[r_key] = body[t];
+        mask[t] = k;  // reuse: old slot
     }
     __syncthreads();
     for (uint32_t m = threadIdx.x; m < M; m += FIX_THREADS) {
         const uint32_t t = moved[m];
         uint32_t r = 0;
         for (uint32_t q = 0; q < M; q++)
-            if (prov[moved[q]] < prov[t]) r++;
-        mpos[r] = (uint32_t)prov[t];
+            if (mask[moved[q]] < mask[t]) r++;
+        gpos[r] = mask[t];
+    }
+}
+
+// (K, V) = the sorted provisional (Ks, Vs) with the moved bodies taken out
+// of their old slots and merged back at their new keys; a plain copy when
+// nothing moved.  Replaces a second sort.
+constexpr int MERGE_THREADS = 256;
+
+__global__ void __launch_bounds__(MERGE_THREADS) k_tie_merge(const uint64_t* __restrict__ Ks,
+                                                             const uint32_t* __restrict__ Vs,
+                                                             uint64_t* __restrict__ K, uint32_t* __restrict__ V,
+                                                             uint32_t n, const uint32_t* __restrict__ nin_p,
+                                                             const uint32_t* __restrict__ moved,
+                                                             const uint32_t* __restrict__ gpos,
+                                                             const uint64_t* __restrict__ gkey,
+                                                             const uint32_t* __restrict__ gbody) {
+    const uint32_t M = min(*moved, TIE_CAP);
+    const uint32_t stride = gridDim.x * MERGE_THREADS;
+    const uint32_t g = blockIdx.x * MERGE_THREADS + threadIdx.x;
+    if (M == 0) {
+        for (uint32_t k = g; k < n; k += stride) {
+            K[k] = Ks[k];
+            V[k] = Vs[k];
+        }
+        return;
+    }
+    __shared__ uint32_t mpos[TIE_CAP];
+    __shared__ uint64_t mkey[TIE_CAP];
+    __shared__ uint32_t mbody[TIE_CAP];
+    for (uint32_t m = threadIdx.x; m < M; m += MERGE_THREADS) {
+        mpos[m] = gpos[m];
+        mkey[m] = gkey[m];
+        mbody[m] = gbody[m];
     }
     __syncthreads();
+    const uint32_t nin = *nin_p;
     auto below_pos = [&](uint32_t k) {  // moved bodies with old slot < k
         uint32_t lo = 0, hi = M;
         while (lo < hi) {
@@ -303,32 +345,32 @@ __global__ void __launch_bounds__(FIX_THREADS) k_tie_fix(const float* __restrict
         }
         return lo;
     };
-    for (uint32_t k = threadIdx.x; k < nin; k += FIX_THREADS) {
+    for (uint32_t k = g; k < n; k += stride) {
+        if (k >= nin) {  // bodies outside the root cube keep their slots
+            K[k] = Ks[k];
+            V[k] = Vs[k];
+            continue;
+        }
         const uint32_t bp = below_pos(k);
         if (bp < M && mpos[bp] == k) continue;  // a moved body's old slot
-        const uint64_t key = K[k];
-        const uint32_t b = V[k];
+        const uint64_t key = Ks[k];
+        const uint32_t b = Vs[k];
         const uint32_t dst = k - bp + below_key(key, b);
-        K2[dst] = key;
-        V2[dst] = b;
+        K[dst] = key;
+        V[dst] = b;
     }
-    for (uint32_t m = threadIdx.x; m < M; m += FIX_THREADS) {
-        // stayed bodies before the new key: binary search on (K, V), minus moved slots below it
+    for (uint32_t m = g; m < M; m += stride) {
+        // stayed bodies before the new key: binary search on (Ks, Vs), minus moved slots below it
         const uint64_t key = mkey[m];
         const uint32_t b = mbody[m];
         uint32_t lo = 0, hi = nin;
         while (lo < hi) {
             const uint32_t mid = (lo + hi) >> 1;
-            if (K[mid] < key || (K[mid] == key && V[mid] < b)) lo = mid + 1; else hi = mid;
+            if (Ks[mid] < key || (Ks[mid] == key && Vs[mid] < b)) lo = mid + 1; else hi = mid;
         }
         const uint32_t dst = lo - below_pos(lo) + m;
-        K2[dst] = key;
-        V2[dst] = b;
-    }
-    __syncthreads();
-    for (uint32_t k = threadIdx.x; k < nin; k += FIX_THREADS) {
-        K[k] = K2[k];
-        V[k] = V2[k];
+        K[dst] = key;
+        V[dst] = b;
     }
 }
 
@@ -389,16 +431,26 @@ __device__ __forceinline__ void write_node(NodeArrays nd, uint32_t v, const Cube
     nd.start[v] = start;
 }
 
-__global__ void k_split_fill(const uint64_t* __restrict__ K, const uint32_t* __restrict__ nin_p,
+// One split node per 8 threads, thread o writing the node of octant o: its
+// first body is the first sorted key at or past octant o of the split cell
+// (one table-narrowed search, no chain of gallops), its end the next
+// octant's start.  Thread 0 of the group also places the split node itself
+// (its id under its parent), which every thread of the group needs.
+constexpr int FILL_THREADS = 128;
+
+__global__ void __launch_bounds__(FILL_THREADS) k_split_fill(const uint64_t* __restrict__ K, const uint32_t* __restrict__ nin_p,
                              const uint32_t* __restrict__ sbase, const uint32_t* __restrict__ nsplit_p,
                              uint32_t split_cap, const uint32_t* __restrict__ split_start,
                              const uint8_t* __restrict__ split_level, const float* __restrict__ bounds,
                              uint32_t leaf_cap, uint32_t depth_max, NodeArrays nd, float third,
                              uint32_t* __restrict__ split_node) {
-    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ uint64_t samp[NSAMP];
     const uint32_t ns = min(*nsplit_p, split_cap);
     const uint32_t nin = *nin_p;
-    if (s == 0) {  // the root record (tree.c:156-159: bounds = the root cube)
+    const uint32_t g = blockIdx.x * FILL_THREADS + threadIdx.x;
+    const uint32_t s = g >> 3;
+    const uint32_t o = g & 7u;
+    if (g == 0) {  // the root record (tree.c:156-159: bounds = the root cube)
         Cube r;
         for (int a = 0; a < 3; a++) {
             r.lo[a] = bounds[a];
@@ -406,46 +458,52 @@ __global__ void k_split_fill(const uint64_t* __restrict__ K, const uint32_t* __r
         }
         write_node(nd, 0, r, nin, (nin > leaf_cap && depth_max > 0) ? 1u : NODE_NONE, 0u, 0u, third);
     }
-    if (s >= ns) return;
-    const uint32_t k = split_start[s];
-    const int L = split_level[s];
-    const uint64_t pre = prefix_of(K[k], L);
-    const uint32_t end = (L == 0) ? nin : gallop_shift(K, k, nin, 3 * (16 - L), pre + 1);
-    const Cube c = cube_of(bounds, K[k], L);
-    float mid[3];
-    for (int a = 0; a < 3; a++) mid[a] = midf(c.lo[a], c.hi[a]);
+    if ((blockIdx.x * FILL_THREADS) / 8u >= ns) return;  // the whole block is past the split nodes
+    const KeySamples ks = load_key_samples(K, nin, samp);
+    __syncthreads();
+    const bool live = s < ns;
+    uint32_t k = 0, cend = 0;
+    int L = 0;
+    uint64_t pre = 0;
+    if (live) {
+        k = split_start[s];
+        L = split_level[s];
+        pre = prefix_of(K[k], L);
+        // end of octant o = first key at or past octant o+1 (for o = 7 the
+        // next level-L cell, or nin)
+        cend = search_keys(K, samp, ks, 3 * (15 - L), (pre << 3) + (uint64_t)o + 1);
+    }
+    uint32_t cstart = __shfl_up_sync(0xffffffffu, cend, 1, 8);
+    if (o == 0) cstart = k;
+    if (!live) return;
     // node id of this split node (the children's parent); the node record
-    // itself is written by the parent's thread
+    // itself is written by the parent's group
     uint32_t self = 0;
     if (L > 0) {
-        const uint64_t ppre = pre >> 3;
-        const uint32_t kp = (L == 1) ? 0u : gallop_back(K, k + 1, 3 * (17 - L), ppre);
+        const uint32_t kp = (L == 1) ? 0u : search_keys(K, samp, ks, 3 * (17 - L), pre >> 3);
         const int ap = (kp == 0) ? -1 : cpl_levels(K[kp - 1], K[kp]);
         const uint32_t sp = sbase[kp] + (uint32_t)(L - 1 - (ap + 1));
         self = 1u + 8u * sp + (uint32_t)(pre & 7ull);
     }
-    split_node[s] = self;
-    uint32_t cstart = k;
-    for (int o = 0; o < 8; o++) {
-        const uint32_t cend = (o == 7) ? end : gallop_shift(K, cstart, end, 3 * (15 - L), (pre << 3) + (uint64_t)o + 1);
-        const uint32_t cnt = cend - cstart;
-        Cube cc;
-        for (int a = 0; a < 3; a++) {
-            const bool up = (o >> a) & 1;
-            cc.lo[a] = up ? mid[a] : c.lo[a];
-            cc.hi[a] = up ? c.hi[a] : mid[a];
-        }
-        uint32_t fc = NODE_NONE;
-        if (cnt > leaf_cap && L + 1 < (int)depth_max) {
-            const int ac = (cstart == 0) ? -1 : cpl_levels(K[cstart - 1], K[cstart]);
-            const uint32_t sid = sbase[cstart] + (uint32_t)(L + 1 - (ac + 1));
-            // beyond capacity (node overflow, flagged by k_split_emit) the
-            // child stays a leaf so nothing reads past the node arrays
-            fc = sid < split_cap ? 1u + 8u * sid : NODE_NONE;
-        }
-        write_node(nd, 1u + 8u * s + (uint32_t)o, cc, cnt, fc, self, cstart, third);
-        cstart = cend;
+    if (o == 0) split_node[s] = self;
+    const Cube c = cube_of(bounds, K[k], L);
+    const uint32_t cnt = cend - cstart;
+    Cube cc;
+    for (int a = 0; a < 3; a++) {
+        const float mid = midf(c.lo[a], c.hi[a]);
+        const bool up = (o >> a) & 1u;
+        cc.lo[a] = up ? mid : c.lo[a];
+        cc.hi[a] = up ? c.hi[a] : mid;
     }
+    uint32_t fc = NODE_NONE;
+    if (cnt > leaf_cap && L + 1 < (int)depth_max) {
+        const int ac = (cstart == 0) ? -1 : cpl_levels(K[cstart - 1], K[cstart]);
+        const uint32_t sid = sbase[cstart] + (uint32_t)(L + 1 - (ac + 1));
+        // beyond capacity (node overflow, flagged by k_split_emit) the
+        // child stays a leaf so nothing reads past the node arrays
+        fc = sid < split_cap ? 1u + 8u * sid : NODE_NONE;
+    }
+    write_node(nd, 1u + 8u * s + o, cc, cnt, fc, self, cstart, third);
 }
 
 __global__ void k_gather(const uint32_t* __restrict__ V, uint32_t n, const uint32_t* __restrict__ nin_p,
@@ -586,6 +644,9 @@ int sf_tree_alloc(TreeWork** out, uint32_t n, const sfgpu_params& p) {
     if (sf_sort_alloc(t->sort, nn) != SFGPU_OK) return SFGPU_FAILURE;
     SF_CUDA(cudaMalloc(&t->counters, sizeof(uint32_t) * 8));
     SF_CUDA(cudaMalloc(&t->ties, sizeof(uint2) * TIE_CAP));
+    SF_CUDA(cudaMalloc(&t->tie_pos, sizeof(uint32_t) * TIE_CAP));
+    SF_CUDA(cudaMalloc(&t->tie_key, sizeof(uint64_t) * TIE_CAP));
+    SF_CUDA(cudaMalloc(&t->tie_body, sizeof(uint32_t) * TIE_CAP));
     SF_CUDA(cudaMalloc(&t->scount, sizeof(uint32_t) * nn));
     SF_CUDA(cudaMalloc(&t->sbase, sizeof(uint32_t) * nn));
     SF_CUDA(cudaMalloc(&t->split_start, sizeof(uint32_t) * std::max<uint32_t>(t->split_cap, 1)));
@@ -617,6 +678,9 @@ void sf_tree_free(TreeWork* t) {
     sf_sort_free(t->sort);
     cudaFree(t->counters);
     cudaFree(t->ties);
+    cudaFree(t->tie_pos);
+    cudaFree(t->tie_key);
+    cudaFree(t->tie_body);
     cudaFree(t->scount);
     cudaFree(t->sbase);
     cudaFree(t->split_start);
@@ -658,11 +722,27 @@ int sf_tree_build(sfgpu_sim* s) {
     SF_CHECK_LAUNCH();
     s->timer.end(st, tk);
     tk = s->timer.begin(st, "tree_sort");
-    if (sf_sort_pairs(t->keys, t->vals, n, KEY_BITS, t->sort, st, s->d_status) != SFGPU_OK) return SFGPU_FAILURE;
+    // the sorted provisional keys stay in the sort's other buffer (7 passes);
+    // k_tie_merge writes the final order into (t->keys, t->vals)
+    uint64_t* ks = t->keys;
+    uint32_t* vs = t->vals;
+    if (sf_sort_pairs_keep(t->keys, t->vals, n, KEY_BITS, t->sort, st, s->d_status, &ks, &vs) != SFGPU_OK)
+        return SFGPU_FAILURE;
+    if (ks == t->keys) {  // n <= 1: nothing was sorted; merge from a copy
+        SF_CUDA(cudaMemcpyAsync(t->sort.keys_b, t->keys, sizeof(uint64_t) * n, cudaMemcpyDeviceToDevice, st));
+        SF_CUDA(cudaMemcpyAsync(t->sort.vals_b, t->vals, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st));
+        ks = t->sort.keys_b;
+        vs = t->sort.vals_b;
+    }
     s->timer.end(st, tk);
     tk = s->timer.begin(st, "tree_ties");
-    k_tie_fix<<<1, FIX_THREADS, 0, st>>>(pos, s->d_bounds, t->keys, t->vals, nin, t->ties, tie_count,
-                                         s->p.leaf_cap, s->p.depth_max, resort, t->sort.keys_b, t->sort.vals_b);
+    k_tie_fix<<<1, FIX_THREADS, 0, st>>>(pos, s->d_bounds, ks, vs, nin, t->ties, tie_count, s->p.leaf_cap,
+                                         s->p.depth_max, resort, t->tie_pos, t->tie_key, t->tie_body);
+    SF_CHECK_LAUNCH();
+    const uint32_t mgb = std::max<uint32_t>(1u, std::min<uint32_t>(sf_ceil_div(n, MERGE_THREADS),
+                                                                   (uint32_t)sf_num_sms() * 8u));
+    k_tie_merge<<<mgb, MERGE_THREADS, 0, st>>>(ks, vs, t->keys, t->vals, n, nin, resort, t->tie_pos, t->tie_key,
+                                                t->tie_body);
     SF_CHECK_LAUNCH();
     s->timer.end(st, tk);
     tk = s->timer.begin(st, "tree_nodes");
@@ -672,8 +752,8 @@ int sf_tree_build(sfgpu_sim* s) {
     k_split_emit<<<nb, 256, 0, st>>>(t->keys, n, nin, t->scount, t->sbase, nsplit, t->split_cap, t->split_start,
                                      t->split_level, t->nodes_max, s->d_status);
     SF_CHECK_LAUNCH();
-    const uint32_t sb = sf_ceil_div(std::max<uint32_t>(t->split_cap, 1), 128);
-    k_split_fill<<<sb, 128, 0, st>>>(t->keys, nin, t->sbase, nsplit, t->split_cap, t->split_start, t->split_level,
+    const uint32_t sb = sf_ceil_div((uint64_t)std::max<uint32_t>(t->split_cap, 1) * 8u, FILL_THREADS);
+    k_split_fill<<<sb, FILL_THREADS, 0, st>>>(t->keys, nin, t->sbase, nsplit, t->split_cap, t->split_start, t->split_level,
                                      s->d_bounds, s->p.leaf_cap, s->p.depth_max, t->nd, third, t->split_node);
     SF_CHECK_LAUNCH();
     s->timer.end(st, tk);

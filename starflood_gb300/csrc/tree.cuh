@@ -27,8 +27,11 @@ struct TreeWork {
     uint64_t* keys = nullptr;   // sorted keys
     uint32_t* vals = nullptr;   // body index of each sorted slot
     SortWork sort;
-    uint32_t* counters = nullptr;  // [0] bodies in cube [1] midplane bodies [2] resort [3] splits
+    uint32_t* counters = nullptr;  // [0] bodies in cube [1] midplane bodies [2] moved midplane bodies [3] splits
     uint2* ties = nullptr;
+    uint32_t* tie_pos = nullptr;   // moved midplane bodies: old slots ascending
+    uint64_t* tie_key = nullptr;   // their new keys, ascending by (key, body)
+    uint32_t* tie_body = nullptr;
     uint32_t* scount = nullptr;
     uint32_t* sbase = nullptr;
     uint32_t* split_start = nullptr;

@@ -470,16 +470,86 @@ int launch_body(sfgpu_sim* s, bool stats) {
 constexpr int GW_WARPS = 4;
 constexpr int GW_THREADS = GW_WARPS * 32;
 constexpr int GW_STACK = 512;
-constexpr int GW_LIST = 256;
+constexpr int GW_LIST = 256;  // accepted cells whose bounds miss the group box
+constexpr int GW_SLOW = 64;   // accepted cells that may contain a body (self-exclusion test)
+
+// Per-warp lists in shared memory.  The fast list holds the monopole itself
+// (centre of mass and mass, as separate arrays so that two consecutive
+// entries are one 64-bit load) and the mask of the bodies taking it; the
+// slow list holds node ids for the few accepted cells whose closed bounds
+// meet the group's box, where the reference's self-exclusion test must run.
+struct GroupLists {
+    float* x;
+    float* y;
+    float* z;
+    float* m;
+    uint32_t* msk;
+    uint32_t* qn;
+    uint32_t* qm;
+};
+
+// Fast list: every lane runs every entry, its mask bit selecting the result,
+// so the inner loop has no per-lane branch.  FAST kind evaluates two entries
+// per instruction (paired FP32), each element rounded as the scalar code
+// would; COMP kind adds each interaction to Kahan sums in list order.
+template <int KIND>
+__device__ __forceinline__ void flush_fast(const GroupLists& L, int count, int lane, float rx, float ry, float rz,
+                                           float eps2, float2& a2x, float2& a2y, float2& a2z, float2& p2,
+                                           KSum& ax, KSum& ay, KSum& az, KSum& ph, uint32_t& n_int) {
+    if (KIND == WALK_COMP) {
+        for (int e = 0; e < count; e++) {
+            const uint32_t M = L.msk[e];
+            if ((M >> lane) & 1u) {
+                const float dx = L.x[e] - rx, dy = L.y[e] - ry, dz = L.z[e] - rz;
+                const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
+                const float inv = rsqrtf(r2);
+                const float mphi = L.m[e] * inv;
+                const float f = mphi * (inv * inv);
+                ax.add(f * dx);
+                ay.add(f * dy);
+                az.add(f * dz);
+                ph.add(mphi);
+                n_int++;
+            }
+        }
+        return;
+    }
+    const float2 nrx = make_float2(-rx, -rx), nry = make_float2(-ry, -ry), nrz = make_float2(-rz, -rz);
+    const float2 e2 = make_float2(eps2, eps2);
+#pragma unroll 2
+    for (int e = 0; e < count; e += 2) {  // count is even (padded by the caller)
+        const float2 X = *reinterpret_cast<const float2*>(&L.x[e]);
+        const float2 Y = *reinterpret_cast<const float2*>(&L.y[e]);
+        const float2 Z = *reinterpret_cast<const float2*>(&L.z[e]);
+        const float2 Mj = *reinterpret_cast<const float2*>(&L.m[e]);
+        const uint2 MK = *reinterpret_cast<const uint2*>(&L.msk[e]);
+        const bool t0 = (MK.x >> lane) & 1u, t1 = (MK.y >> lane) & 1u;
+        const float2 dx = __fadd2_rn(X, nrx);
+        const float2 dy = __fadd2_rn(Y, nry);
+        const float2 dz = __fadd2_rn(Z, nrz);
+        float2 r2 = __ffma2_rn(dz, dz, e2);
+        r2 = __ffma2_rn(dy, dy, r2);
+        r2 = __ffma2_rn(dx, dx, r2);
+        const float2 inv = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
+        float2 mphi = __fmul2_rn(Mj, inv);
+        float2 f = __fmul2_rn(mphi, __fmul2_rn(inv, inv));
+        mphi = make_float2(t0 ? mphi.x : 0.f, t1 ? mphi.y : 0.f);
+        f = make_float2(t0 ? f.x : 0.f, t1 ? f.y : 0.f);
+        a2x = __ffma2_rn(f, dx, a2x);
+        a2y = __ffma2_rn(f, dy, a2y);
+        a2z = __ffma2_rn(f, dz, a2z);
+        p2 = __fadd2_rn(p2, mphi);
+        n_int += (uint32_t)t0 + (uint32_t)t1;
+    }
+}
 
 template <int KIND>
-__device__ __forceinline__ void flush_list(const uint32_t* lnode, const uint32_t* lmask, int count, const NodeArrays& nd,
-                                           int lane, float rx, float ry, float rz, float mi, float eps2, KSum& ax,
-                                           KSum& ay, KSum& az, KSum& ph, uint32_t& n_int) {
-#pragma unroll 4
+__device__ __forceinline__ void flush_slow(const GroupLists& L, int count, const NodeArrays& nd, int lane, float rx,
+                                           float ry, float rz, float mi, float eps2, KSum& ax, KSum& ay, KSum& az,
+                                           KSum& ph, uint32_t& n_int) {
     for (int e = 0; e < count; e++) {
-        const uint32_t v = lnode[e];
-        const uint32_t M = lmask[e];
+        const uint32_t v = L.qn[e];
+        const uint32_t M = L.qm[e];
         const float4 C = __ldg(&nd.com[v]);
         const float4 Lo = __ldg(&nd.lo[v]);
         const float4 H = __ldg(&nd.hi[v]);
@@ -488,6 +558,35 @@ __device__ __forceinline__ void flush_list(const uint32_t* lnode, const uint32_t
             n_int++;
         }
     }
+}
+
+// Appends the cells of the lanes with am != 0 (their C, Lo, H loaded) to the
+// fast or the slow list.
+__device__ __forceinline__ void append_cells(const GroupLists& L, uint32_t am, uint32_t v, const float4& C,
+                                             const float4& Lo, const float4& H, float bx0, float by0, float bz0,
+                                             float bx1, float by1, float bz1, int lane, int& count, int& qcount) {
+    const uint32_t lt = (1u << lane) - 1u;
+    // the reference's self-exclusion needs a body inside the closed bounds
+    // of a cell with more than one body: impossible when the bounds miss
+    // the group's box
+    const bool slow = am != 0u && __float_as_uint(H.z) > 1u && !(Lo.w < bx0 || bx1 < Lo.x || H.x < by0 ||
+                                                                  by1 < Lo.y || H.y < bz0 || bz1 < Lo.z);
+    const uint32_t sb = __ballot_sync(0xffffffffu, slow);
+    const uint32_t fb = __ballot_sync(0xffffffffu, am != 0u && !slow);
+    if (slow) {
+        const int q = qcount + __popc(sb & lt);
+        L.qn[q] = v;
+        L.qm[q] = am;
+    } else if (am) {
+        const int q = count + __popc(fb & lt);
+        L.x[q] = C.x;
+        L.y[q] = C.y;
+        L.z[q] = C.z;
+        L.m[q] = C.w;
+        L.msk[q] = am;
+    }
+    count += __popc(fb);
+    qcount += __popc(sb);
 }
 
 template <int KIND, int GSPLIT, bool STATS>
@@ -502,8 +601,13 @@ __global__ void __launch_bounds__(GW_THREADS) k_walk_group(const float4* __restr
                                                            unsigned long long* __restrict__ tot, uint32_t* d_status) {
     __shared__ uint32_t s_node[GW_WARPS][GW_STACK];
     __shared__ uint32_t s_mask[GW_WARPS][GW_STACK];
-    __shared__ uint32_t l_node[GW_WARPS][GW_LIST];
-    __shared__ uint32_t l_mask[GW_WARPS][GW_LIST];
+    __shared__ __align__(16) float l_x[GW_WARPS][GW_LIST];
+    __shared__ __align__(16) float l_y[GW_WARPS][GW_LIST];
+    __shared__ __align__(16) float l_z[GW_WARPS][GW_LIST];
+    __shared__ __align__(16) float l_m[GW_WARPS][GW_LIST];
+    __shared__ __align__(16) uint32_t l_k[GW_WARPS][GW_LIST];
+    __shared__ uint32_t q_node[GW_WARPS][GW_SLOW];
+    __shared__ uint32_t q_mask[GW_WARPS][GW_SLOW];
     __shared__ float4 s_body[GW_WARPS][32];
     __shared__ uint32_t f_node[GW_WARPS][80];  // top-level frontiers: [0,8) level 1, [8,72) level 2
     __shared__ uint32_t f_mask[GW_WARPS][80];
@@ -512,8 +616,7 @@ __global__ void __launch_bounds__(GW_THREADS) k_walk_group(const float4* __restr
     float4* sbd = s_body[w];
     uint32_t* stn = s_node[w];
     uint32_t* stm = s_mask[w];
-    uint32_t* lsn = l_node[w];
-    uint32_t* lsm = l_mask[w];
+    const GroupLists L{l_x[w], l_y[w], l_z[w], l_m[w], l_k[w], q_node[w], q_mask[w]};
     const uint32_t gw = blockIdx.x * GW_WARPS + w;
     const uint32_t group = gw / GSPLIT;
     const uint32_t oct = gw % GSPLIT;
@@ -535,9 +638,31 @@ __global__ void __launch_bounds__(GW_THREADS) k_walk_group(const float4* __restr
         bz1 = fmaxf(bz1, __shfl_xor_sync(0xffffffffu, bz1, o));
     }
     KSum ax{0.f, 0.f}, ay{0.f, 0.f}, az{0.f, 0.f}, ph{0.f, 0.f};
+    float2 a2x = make_float2(0.f, 0.f), a2y = a2x, a2z = a2x, p2 = a2x;
     uint32_t n_int = 0, n_open = 0;
     unsigned long long open_total = 0;
-    int top = 0, count = 0;
+    int top = 0, count = 0, qcount = 0;
+    auto flush = [&](bool all) {
+        if (all || count > GW_LIST - 34) {
+            if (KIND != WALK_COMP && (count & 1)) {  // pad to an even count with an entry no lane takes
+                if (lane == 0) {
+                    L.x[count] = L.y[count] = L.z[count] = 0.f;
+                    L.m[count] = 0.f;
+                    L.msk[count] = 0u;
+                }
+                count++;
+                __syncwarp();
+            }
+            flush_fast<KIND>(L, count, lane, rx, ry, rz, fc.eps2, a2x, a2y, a2z, p2, ax, ay, az, ph, n_int);
+            count = 0;
+            __syncwarp();
+        }
+        if (all || qcount > GW_SLOW - 32) {
+            flush_slow<KIND>(L, qcount, nd, lane, rx, ry, rz, mi, fc.eps2, ax, ay, az, ph, n_int);
+            qcount = 0;
+            __syncwarp();
+        }
+    };
     if (GSPLIT == 1) {
         if (lane == 0) {
             stn[0] = 0u;
@@ -556,12 +681,14 @@ __global__ void __launch_bounds__(GW_THREADS) k_walk_group(const float4* __restr
         int n_in = 1, in_base = 0, out_base = 0;  // level 0 writes the 8 level-1 slots [0, 8)
         for (int lvl = 0; lvl < 2; lvl++) {
             uint32_t v = 0u, M = 0u, first = NODE_NONE, bodies = 0u;
-            float4 G = make_float4(0.f, 0.f, 0.f, 0.f);
+            float4 G = make_float4(0.f, 0.f, 0.f, 0.f), H = G, C = G, Lo = G;
             if (lane < n_in) {
                 v = lvl == 0 ? 0u : fnd[in_base + lane];
                 M = lvl == 0 ? live_mask : fms[in_base + lane];
-                const float4 H = __ldg(&nd.hi[v]);
+                H = __ldg(&nd.hi[v]);
                 G = __ldg(&nd.geo[v]);
+                C = __ldg(&nd.com[v]);
+                Lo = __ldg(&nd.lo[v]);
                 bodies = __float_as_uint(H.z);
                 first = __float_as_uint(H.w);
             }
@@ -584,16 +711,9 @@ __global__ void __launch_bounds__(GW_THREADS) k_walk_group(const float4* __restr
                     if (il && ((ml >> lane) & 1u)) n_open++;
                 }
             }
-            const uint32_t am = (lane < n_in && bodies > 0u) ? (M & ~om) : 0u;
+            const uint32_t am = (oct == 0 && lane < n_in && bodies > 0u) ? (M & ~om) : 0u;
             const uint32_t lt = (1u << lane) - 1u;
-            const uint32_t ab = __ballot_sync(0xffffffffu, am != 0u);
-            if (oct == 0) {
-                if (am) {
-                    lsn[count + __popc(ab & lt)] = v;
-                    lsm[count + __popc(ab & lt)] = am;
-                }
-                count += __popc(ab);
-            }
+            append_cells(L, am, v, C, Lo, H, bx0, by0, bz0, bx1, by1, bz1, lane, count, qcount);
             const uint32_t ob = __ballot_sync(0xffffffffu, om != 0u);
             if (om) {
                 const int base = out_base + 8 * __popc(ob & lt);
@@ -642,10 +762,10 @@ __global__ void __launch_bounds__(GW_THREADS) k_walk_group(const float4* __restr
         // 0 drop, 1 accept, 2 open, 3 mixed
         int kind = 0;
         bool internal = false;
-        float4 G = make_float4(0.f, 0.f, 0.f, 0.f);
+        float4 G = make_float4(0.f, 0.f, 0.f, 0.f), H = G, C = G, Lo = G;
         uint32_t first = NODE_NONE;
         if (lane < pops) {
-            const float4 H = __ldg(&nd.hi[v]);
+            H = __ldg(&nd.hi[v]);
             G = __ldg(&nd.geo[v]);
             const uint32_t bodies = __float_as_uint(H.z);
             first = __float_as_uint(H.w);
@@ -669,53 +789,60 @@ __global__ void __launch_bounds__(GW_THREADS) k_walk_group(const float4* __restr
                 else if (G.w >= th_open * dmax2 && first != NODE_NONE) kind = 2;
                 else kind = 3;
             }
+            if (kind == 1 || kind == 3) {  // monopole data, in flight during the mixed tests
+                C = __ldg(&nd.com[v]);
+                Lo = __ldg(&nd.lo[v]);
+            }
         }
-        // accepted cells -> list
-        const uint32_t acc_b = __ballot_sync(0xffffffffu, kind == 1);
-        if (kind == 1) {
-            const int slot = count + __popc(acc_b & ((1u << lane) - 1u));
-            lsn[slot] = v;
-            lsm[slot] = M;
-        }
-        count += __popc(acc_b);
         // cells every body opens -> their children
+        const uint32_t lt = (1u << lane) - 1u;
         const uint32_t open_b = __ballot_sync(0xffffffffu, kind == 2);
         if (kind == 2) {
-            const int base = top + 8 * __popc(open_b & ((1u << lane) - 1u));
+            const int base = top + 8 * __popc(open_b & lt);
             for (int o = 0; o < 8; o++) {
                 stn[base + o] = first + 7u - (uint32_t)o;
                 stm[base + o] = M;
             }
         }
         top += 8 * __popc(open_b);
-        __syncwarp();
-        if (count > GW_LIST - 32) {
-            flush_list<KIND>(lsn, lsm, count, nd, lane, rx, ry, rz, mi, fc.eps2, ax, ay, az, ph, n_int);
-            count = 0;
-            __syncwarp();
-        }
-        // mixed cells: one lane per cell runs the reference's test for each
-        // body of the cell's mask (bodies staged in shared memory), so the
-        // tests of up to 32 cells proceed side by side
+        // mixed cells: the reference's test for each (cell, body) pair of
+        // the masks.  Either one lane per cell loops over its bodies, or the
+        // warp goes through the cells one at a time with one lane per body,
+        // whichever takes fewer rounds.
+        const bool mixed = kind == 3 && first != NODE_NONE;
+        const uint32_t mix_b = __ballot_sync(0xffffffffu, mixed);
         uint32_t om = 0u;
-        if (kind == 3 && first != NODE_NONE) {
-            uint32_t mm = M;
-            while (mm) {
-                const int i = __ffs(mm) - 1;
-                mm &= mm - 1u;
-                const float4 bi = sbd[i];
-                if (opens(G, bi.x, bi.y, bi.z, fc, th_lo, th_hi)) om |= 1u << i;
+        if (mix_b) {
+            const int rounds_cell = __popc(mix_b);
+            const int rounds_body = __reduce_max_sync(0xffffffffu, mixed ? (uint32_t)__popc(M) : 0u);
+            if (rounds_body <= rounds_cell) {
+                if (mixed) {
+                    uint32_t mm = M;
+                    while (mm) {
+                        const int i = __ffs(mm) - 1;
+                        mm &= mm - 1u;
+                        const float4 bi = sbd[i];
+                        if (opens(G, bi.x, bi.y, bi.z, fc, th_lo, th_hi)) om |= 1u << i;
+                    }
+                }
+            } else {
+                uint32_t cells = mix_b;
+                while (cells) {
+                    const int l = __ffs(cells) - 1;
+                    cells &= cells - 1u;
+                    const float4 Gl = make_float4(__shfl_sync(0xffffffffu, G.x, l), __shfl_sync(0xffffffffu, G.y, l),
+                                                  __shfl_sync(0xffffffffu, G.z, l), __shfl_sync(0xffffffffu, G.w, l));
+                    const uint32_t Ml = __shfl_sync(0xffffffffu, M, l);
+                    const bool t = ((Ml >> lane) & 1u) && opens(Gl, rx, ry, rz, fc, th_lo, th_hi);
+                    const uint32_t ol = __ballot_sync(0xffffffffu, t);
+                    if (lane == l) om = ol;
+                }
             }
         }
-        const uint32_t am = (kind == 3) ? (M & ~om) : 0u;
-        const uint32_t lt = (1u << lane) - 1u;
-        const uint32_t ab = __ballot_sync(0xffffffffu, am != 0u);
-        if (am) {
-            const int slot = count + __popc(ab & lt);
-            lsn[slot] = v;
-            lsm[slot] = am;
-        }
-        count += __popc(ab);
+        // accepted cells (all of the mask, or the bodies of a mixed cell
+        // that do not open it) -> lists
+        const uint32_t am = (kind == 1) ? M : ((kind == 3) ? (M & ~om) : 0u);
+        append_cells(L, am, v, C, Lo, H, bx0, by0, bz0, bx1, by1, bz1, lane, count, qcount);
         const uint32_t ob = __ballot_sync(0xffffffffu, om != 0u);
         if (om) {
             const int base = top + 8 * __popc(ob & lt);
@@ -726,11 +853,6 @@ __global__ void __launch_bounds__(GW_THREADS) k_walk_group(const float4* __restr
         }
         top += 8 * __popc(ob);
         __syncwarp();
-        if (count > GW_LIST - 32) {
-            flush_list<KIND>(lsn, lsm, count, nd, lane, rx, ry, rz, mi, fc.eps2, ax, ay, az, ph, n_int);
-            count = 0;
-            __syncwarp();
-        }
         if (STATS) {  // opening tests (internal cells only) attributed to bodies
             for (int l = 0; l < pops; l++) {
                 const bool il = __shfl_sync(0xffffffffu, internal, l);
@@ -738,13 +860,9 @@ __global__ void __launch_bounds__(GW_THREADS) k_walk_group(const float4* __restr
                 if (il && ((ml >> lane) & 1u)) n_open++;
             }
         }
-        if (count > GW_LIST - 32) {
-            flush_list<KIND>(lsn, lsm, count, nd, lane, rx, ry, rz, mi, fc.eps2, ax, ay, az, ph, n_int);
-            count = 0;
-            __syncwarp();
-        }
+        flush(false);
     }
-    flush_list<KIND>(lsn, lsm, count, nd, lane, rx, ry, rz, mi, fc.eps2, ax, ay, az, ph, n_int);
+    flush(true);
     if (live) {
         const uint32_t p = V[k];
         float sx = ax.s, sy = ay.s, sz = az.s, sw = ph.s;
@@ -753,6 +871,11 @@ __global__ void __launch_bounds__(GW_THREADS) k_walk_group(const float4* __restr
             sy -= ay.c;
             sz -= az.c;
             sw -= ph.c;
+        } else {
+            sx += a2x.x + a2x.y;
+            sy += a2y.x + a2y.y;
+            sz += a2z.x + a2z.y;
+            sw += p2.x + p2.y;
         }
         if (GSPLIT == 1) {
             const float g = -fc.neg_g;

@@ -140,11 +140,31 @@ def sph_reference():
                         mas=mas, rad=rad, eps=0.01, dt=5e-4, theta=0.5, steps=2, **out)
 
 
+def raw_snapshot():
+    """A raw snapshot (src/simulation_io.c:81-149) written by the reference
+    after 2 PP steps of 64 bodies, with the slab it holds."""
+    n = 64
+    pos, vel, mas = uniform_ball(n, seed=9)
+    ref = Reference("pp_e0.01")
+    v = ref.init(n)
+    v["pos"][:] = pos
+    v["vel"][:] = vel
+    v["mas"][:] = mas
+    assert ref.solv(0) == 0
+    for s in range(2):
+        assert ref.step(s) == 0
+    path = os.path.join(OUT, "raw_pp_n64_2steps.bin")
+    assert ref.save_raw(path) == 0
+    np.savez_compressed(os.path.join(OUT, "raw_pp_n64_2steps.npz"), slab=ref.slab.copy(), n=n, dof=ref.dof)
+    ref.free()
+
+
 def main():
     if not obuild.reference_available():
         raise SystemExit("the Starflood reference sources are needed to regenerate fixtures")
     obuild.build()
-    for f in (pp_c1, pp_plummer, pp_fp64, tree_uniform, tree_ties, tree_overflow, sph_reference):
+    for f in (pp_c1, pp_plummer, pp_fp64, tree_uniform, tree_ties, tree_overflow, sph_reference,
+              raw_snapshot):
         f()
         print("wrote", f.__name__)
 
