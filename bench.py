@@ -287,13 +287,13 @@ def gpu_bh_e2e(steps, warmup, sf, pos, vel, mas):
             "d2h_bytes_per_step": bytes_, "api": "sim_step() of include/starflood_compat.h, host slab"}
 
 
-def gpu_pp(sf, reps=2):
+def gpu_pp(sf, reps=2, n=N_PP):
     from starflood_gb300.ics import plummer
-    pos, vel, mas = plummer(N_PP, seed=5)
+    pos, vel, mas = plummer(n, seed=5)
     out = {}
     for name, form in (("plain", sf.FORM_PLAIN), ("compensated", sf.FORM_COMPENSATED)):
         p = sf.default_params(solver=sf.SOLVER_PP, eps=0.005, dt=1e-3, form=form, flags=sf.FLAG_TIMING)
-        with sf.Sim(N_PP, p) as s:
+        with sf.Sim(n, p) as s:
             s.set_state(pos, vel, mas)
             s.solve(0)
             s.sync()
@@ -302,7 +302,7 @@ def gpu_pp(sf, reps=2):
                 s.solve(0)
             s.sync()
             ms = s.stage_times()["pp"][0] / reps
-        out[name] = {"interactions_per_s": float(N_PP) * N_PP / (ms * 1e-3), "ms_per_eval": ms}
+        out[name] = {"interactions_per_s": float(n) * n / (ms * 1e-3), "ms_per_eval": ms}
     return out
 
 
@@ -592,6 +592,62 @@ def gpu_batch(sf, steps=200, ckpt=20):
     return out
 
 
+# ---------------------------------------------------------------------------
+# vis_draw: splat rasteriser, N = 65,536 bodies x 128 samples into 1920 x 1080
+# ---------------------------------------------------------------------------
+def gpu_vis(sf, reps=5, sizex=1920, sizey=1080):
+    import ctypes as C
+    import torch
+    pos, vel, mas = bh_inputs()
+    n = N_BH
+    L = sf.lib()
+    p = sf.default_params(solver=sf.SOLVER_TREE, eps=0.01, dt=1e-3, theta=0.5)
+    with sf.Sim(n, p) as s:
+        s.set_state(pos, vel, mas)
+        s.solve(0)
+        s.sync()
+        vp = (C.c_byte * 64)()
+        L.sfgpu_vis_params_default(vp)
+        da, dr = C.c_void_p(), C.c_void_p()
+        sf.check(L.sfgpu_vis_buffers_alloc(sizex, sizey, C.byref(da), C.byref(dr)), "vis buffers")
+        try:
+            ext = torch.cuda.ExternalStream(s.stream())
+            sf.check(L.sfgpu_vis_draw(s.h, vp, 0, sizex, sizey, da, dr), "vis")
+            s.sync()
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+            for k in range(reps):
+                sf.check(L.sfgpu_flush_l2(C.c_void_p(s.stream())), "flush")
+                with torch.cuda.stream(ext):
+                    ev[k][0].record(ext)
+                sf.check(L.sfgpu_vis_draw(s.h, vp, k + 1, sizex, sizey, da, dr), "vis")
+                with torch.cuda.stream(ext):
+                    ev[k][1].record(ext)
+            s.sync()
+            ms = sum(a.elapsed_time(b) for a, b in ev) / reps
+            acc = np.zeros((sizey, sizex, 4), np.int32)
+            sf.check(L.sfgpu_vis_download(s.h, sizex, sizey, da, dr, acc.ctypes.data, None), "download")
+        finally:
+            L.sfgpu_vis_buffers_free(da, dr)
+        state = sf.slab_views(s.download(), n, 13)
+    samples = n * 128
+    out = {"workload": "vis_draw of the N=65536 Barnes-Hut state, 128 samples per body, 1920x1080, shipped "
+                       "camera and tonemapping (L2 flushed before each draw)",
+           "value": samples / (ms * 1e-3), "unit": "splat samples/s", "ms_per_frame": ms,
+           "samples_in_frame": int(acc[..., 3].sum()),
+           "atomic_bytes_per_frame": int(acc[..., 3].sum()) * 16}
+    try:
+        from oracle.pyoracle import Oracle
+        orc = Oracle("f32")
+        t0 = time.perf_counter()
+        orc.vis_draw(state["pos"], state["vel"], state["pot"], 1, 1e-3, sizex, sizey)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": samples / dt, "unit": "splat samples/s", "cores": orc.threads(),
+                               "kind": "port", "sample": "one orc_vis_draw frame of the same state (%.2f s)" % dt}
+    except Exception as e:
+        out["cpu_baseline"] = {"error": str(e)}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -602,6 +658,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     ap.add_argument("--no-sph", action="store_true", help="skip the N=262144 Barnes-Hut + SPH sub-benchmark")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched + adjoint sub-benchmark")
+    ap.add_argument("--no-vis", action="store_true", help="skip the vis_draw splat sub-benchmark")
+    ap.add_argument("--only", choices=["pp", "sph"], default=None,
+                    help="run one sub-benchmark alone and print its object (profiling runs)")
+    ap.add_argument("--pp-n", type=int, default=N_PP, help="bodies of the PP sub-benchmark with --only pp")
     args = ap.parse_args()
     rank, world, local = env_rank()
 
@@ -631,6 +691,13 @@ def main():
     if world > 1:
         dist.barrier()
     import starflood_gb300 as sf
+
+    if args.only == "pp":
+        print(json.dumps({"only": "pp", "n": args.pp_n, "pp": gpu_pp(sf, n=args.pp_n)}))
+        return
+    if args.only == "sph":
+        print(json.dumps({"only": "sph", "sph": gpu_sph(sf, max(3, args.steps), args.warmup)}))
+        return
 
     r = gpu_bh(args.steps, args.warmup, sf)
     t_ms = r["total_ms"]
@@ -696,6 +763,11 @@ def main():
                 cpu = line["pp"]["cpu_baseline"]
                 bt["cpu_baseline"] = dict(cpu, sample=cpu["sample"] + "; the batched workload at this rate")
             line["batch"] = bt
+        if not args.no_vis:
+            try:
+                line["vis"] = gpu_vis(sf)
+            except Exception as e:
+                line["vis"] = {"error": str(e)}
         print(json.dumps(line))
     if world > 1:
         dist.barrier()

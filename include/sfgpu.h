@@ -227,6 +227,33 @@ int sfgpu_save_raw(sfgpu_sim* s, const char* filename);
 int sfgpu_snapshot_wait(sfgpu_sim* s);
 int sfgpu_read_raw(sfgpu_sim* s, const char* filename);
 
+/* ---- visualisation (src/visualization.c:258-740, vis_draw) -------------- */
+/* The reference's compile-time camera and image settings (config.h). */
+typedef struct sfgpu_vis_params {
+    uint32_t samples;    /* SPATIAL_SAMPLES: jittered splats per body (128) */
+    int32_t autoscaling; /* AUTOSCALING: projection divided by the mean radius (1) */
+    int32_t tonemap;     /* tanh tonemapping, as for 0 < VIS_FILE_FORMAT (1) */
+    int32_t reserved;
+    double timestep;     /* TIMESTEP_SIZE of the camera clock; < 0: the simulation's dt */
+    double exposure;     /* EXPOSURE: pixel scale 0.01 / samples * 2^exposure (-1) */
+    double ortho_scale;  /* ORTHO_SCALE: projection scale 2^ortho_scale (-1) */
+} sfgpu_vis_params;
+void sfgpu_vis_params_default(sfgpu_vis_params* vp);
+/* Splats the simulation's current state into d_atomic (int32 RGBA,
+ * 4*sizex*sizey, cleared first; alpha counts samples) and finishes it into
+ * d_render (float RGBA), both device buffers, queued on the simulation's
+ * stream without a sync.  Camera time = timestep * step_number. */
+int sfgpu_vis_draw(sfgpu_sim* s, const sfgpu_vis_params* vp, uint32_t step_number, uint32_t sizex,
+                   uint32_t sizey, int32_t* d_atomic, float* d_render);
+/* Device buffers of the right size for sfgpu_vis_draw, and their release. */
+int sfgpu_vis_buffers_alloc(uint32_t sizex, uint32_t sizey, int32_t** d_atomic, float** d_render);
+void sfgpu_vis_buffers_free(int32_t* d_atomic, float* d_render);
+/* Copies either buffer (NULL to skip) to host memory after the draw. */
+int sfgpu_vis_download(sfgpu_sim* s, uint32_t sizex, uint32_t sizey, const int32_t* d_atomic,
+                       const float* d_render, int32_t* atomic_out, float* render_out);
+/* The model matrix of vis_draw's camera at time t (visualization.c:367-411). */
+void sfgpu_vis_model_matrix(double time, float out[16]);
+
 /* ---- stateless solver calls on device arrays ---------------------------- */
 /* All pointers are device pointers in the reference layout; stream is a
  * cudaStream_t (NULL = default stream).  Work space is allocated and cached

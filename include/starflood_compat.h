@@ -78,6 +78,25 @@ real* sim_find(const sim_t* sim, enum sim_conf parameter);
 int sim_init(sim_t* sim, unsigned int N);
 /* src/simulation.c:189-228 */
 int sim_free(sim_t* sim);
+/* src/visualization.h:10-27 */
+typedef enum { IMAGE_FILETYPE_PFM, IMAGE_FILETYPE_PPM, IMAGE_FILETYPE_PNG, NUM_IMAGE_FILETYPE } image_filetype_t;
+typedef struct {
+    unsigned int sizex, sizey;
+    void* mem;
+    int32_t* atomic_buffer;
+    float* render_buffer;
+    void* binary_buffer;
+} vis_t;
+/* src/visualization.c:34-176 (plus device buffers for the GPU draw) */
+int vis_init(vis_t* vis, unsigned int sizex, unsigned int sizey);
+/* src/visualization.c:178-238 */
+int vis_free(vis_t* vis);
+/* src/visualization_io.c:170-330: PFM and PPM (PNG needs stb_image_write:
+ * reported, as a reference build without ENABLE_STB_IMAGE_WRITE does). */
+int vis_save(const vis_t* vis, const char* filename, image_filetype_t filetype);
+/* src/visualization.c:258-740 on the GPU; buffers current on return. */
+int vis_draw(const vis_t* vis, const sim_t* sim);
+
 /* src/simulation_io.c:16-79: the slab (N*SIM_DOF reals, no header) from a
  * file into sim->mem and the device; like the reference, a short read is
  * reported on stderr but not failed. */

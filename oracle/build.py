@@ -91,7 +91,7 @@ def reference_config(variant: dict) -> str:
         text = f.read()
     for off in ("SOLVER_VIS", "ENABLE_TIMING", "LOG_STATISTICS", "LOG_TIMINGS_SIM_STEP",
                 "LOG_TIMINGS_VIS_DRAW", "LOG_TIMINGS_FFT_EXEC", "ENABLE_VIS_IO_THREAD",
-                "ENABLE_STB_IMAGE_WRITE", "PAIRWISE_SOLVER_DECIMATION"):
+                "ENABLE_STB_IMAGE_WRITE", "PAIRWISE_SOLVER_DECIMATION", "ENABLE_OFFLOAD_VIS"):
         text = _set_macro(text, off, None)
     text = _set_macro(text, "TIMESTEP_SIZE", variant["dt"])
     text = _set_macro(text, "EPSILON", variant["eps"])
@@ -126,7 +126,7 @@ def build_reference(names: list[str] | None = None, force: bool = False) -> list
                 f.write(text)
         units = ["simulation", "gravity", "sph", "log", "grid"] + (["tree"] if v["tree"] else [])
         if not v["fp64"]:
-            units.append("simulation_io")  # the raw snapshot format
+            units += ["simulation_io", "visualization", "visualization_io"]  # raw snapshots, vis_draw, images
         srcs = [os.path.join(REFERENCE_SRC, u + ".c") for u in units]
         out = os.path.join(REF_OUT, "libref_%s.so" % name)
         outs.append(out)

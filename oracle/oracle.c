@@ -589,3 +589,95 @@ void orc_sph_cubic(uint32_t n, const float* pos, const float* vel, const float* 
         dudt[i] = du;
     }
 }
+
+/* ---- visualization.c:258-740: vis_draw, the atomic splat rasteriser ------- */
+#define ORC_TAU 6.28318530717958647692528676655900576839433879875021
+
+/* x86 float->int: out of range and NaN give INT_MIN (the reference's (int)). */
+static int vis_to_int(float v) { return (v >= -2147483648.0f && v < 2147483648.0f) ? (int)v : INT32_MIN; }
+
+void orc_vis_draw(uint32_t n, const float* pos, const float* vel, const float* pot, uint32_t step,
+                  double timestep, uint32_t sizex, uint32_t sizey, uint32_t samples, double exposure,
+                  double ortho_scale, int autoscale, int tonemap, int32_t* accum, float* render) {
+    /* mean radius, FP64 Kahan in index order (visualization.c:276-305) */
+    double sum = 0.0, comp = 0.0;
+    for (uint32_t i = 0; i < n; i++) {
+        const double x = pos[3u * i], y = pos[3u * i + 1u], z = pos[3u * i + 2u];
+        const double r = sqrt((x * x) + (y * y) + (z * z));
+        const double yk = r - comp;
+        volatile double t = sum + yk;
+        volatile double d = t - sum;
+        comp = d - yk;
+        sum = t;
+    }
+    const double mean = sum * (1.0 / (double)n);
+    /* camera (visualization.c:318-480): model rotation, orthographic scale */
+    const float time = (float)(timestep * (double)step);
+    float alp = 0.0f, bet = (float)ORC_TAU * 0.1250f, gam = (float)ORC_TAU * 0.0625f;
+    alp += (float)ORC_TAU * 1.000e-4f * time;
+    bet += (float)ORC_TAU * 1.000e-4f * time;
+    gam += (float)ORC_TAU * 1.000e-4f * time;
+    const float ca = cosf(alp), sa = sinf(alp), cb = cosf(bet), sb = sinf(bet), cg = cosf(gam), sg = sinf(gam);
+    const float M[16] = {ca * cb, ca * sb * sg - sa * cg, ca * sb * cg + sa * sg, 0.0f,
+                         sa * cb, sa * sb * sg + ca * cg, sa * sb * cg - ca * sg, 0.0f,
+                         -sb,     cb * sg,                cb * cg,                0.0f,
+                         0.0f,    0.0f,                   0.0f,                   1.0f};
+    float scale = (float)exp2(ortho_scale);
+    if (autoscale) scale *= (float)(1.0 / mean);
+    /* P (V M) with V = I and P = diag(scale, scale, scale, 1): every term
+     * but one of each product is an exact zero */
+    float MVP[16];
+    for (int k = 0; k < 16; k++) MVP[k] = (k < 12) ? scale * M[k] : M[k];
+    memset(accum, 0, sizeof(int32_t) * 4u * (size_t)sizex * sizey);
+    const float half_x = 0.5f * (float)sizex, half_y = 0.5f * (float)sizey;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 256)
+#endif
+    for (uint32_t i = 0; i < n; i++) {
+        const float x[4] = {pos[3u * i], pos[3u * i + 1u], pos[3u * i + 2u], 1.0f};
+        float p[2];
+        for (int r = 0; r < 2; r++) {
+            p[r] = (MVP[4 * r] * x[0]) + (MVP[4 * r + 1] * x[1]) + (MVP[4 * r + 2] * x[2]) + (MVP[4 * r + 3] * x[3]);
+            p[r] += 0.0f * vel[3u * i + (uint32_t)r];
+        }
+        const float phase = 1.000e-1f * pot[i];
+        int32_t col[3];
+        for (int c = 0; c < 3; c++) {
+            const float sh = (float)(ORC_TAU * ((double)c / 3.0));
+            col[c] = (int32_t)(100.0f * (0.5f * cosf((float)ORC_TAU * phase - sh) + 0.5f));
+        }
+        for (uint32_t smp = 0; smp < samples; smp++) {
+            uint32_t h[4] = {0xB79ABC95u + smp, 0xE0DA3F84u + i, 0xAB75F07Bu + step, 0xCF52CA01u};
+            orc_pcg4d(h);
+            const float inv = (float)2.3283062977608182109179324470460414886474609375e-10;
+            const float u2 = inv * (float)h[2], u3 = inv * (float)h[3];
+            const float rad = sqrtf(-2.0f * logf(u2));
+            const float o0 = 0.750f * (rad * cosf((float)ORC_TAU * u3));
+            const float o1 = 0.750f * (rad * sinf((float)ORC_TAU * u3));
+            const int cx = vis_to_int(o0 + -0.5f + half_y * p[0] + half_x);
+            const int cy = vis_to_int(o1 + -0.5f + half_y * p[1] + half_y);
+            if (0 <= cx && cx < (int)sizex && 0 <= cy && cy < (int)sizey) {
+                int32_t* px = accum + 4u * ((size_t)sizex * (uint32_t)cy + (uint32_t)cx);
+                for (int c = 0; c < 3; c++) {
+#ifdef _OPENMP
+#pragma omp atomic update
+#endif
+                    px[c] += col[c];
+                }
+#ifdef _OPENMP
+#pragma omp atomic update
+#endif
+                px[3] += 1;
+            }
+        }
+    }
+    const double pscale = 0.01 / (double)samples * exp2(exposure);
+    for (size_t k = 0; k < (size_t)sizex * sizey; k++) {
+        for (int c = 0; c < 3; c++) {
+            double v = pscale * (double)accum[4 * k + (size_t)c];
+            if (tonemap) v = tanh(v);
+            render[4 * k + (size_t)c] = (float)v;
+        }
+        render[4 * k + 3] = 1.0f;
+    }
+}

@@ -103,6 +103,17 @@ void orc_sph_cubic(uint32_t n, const float* pos, const float* vel, const float* 
                    const float* u, double gamma, double alpha, double beta, double* rho, double* prs,
                    double* acc, double* dudt, uint32_t* nbr);
 
+/* vis_draw's splat rasteriser (src/visualization.c:258-740) on FP32 state:
+ * mean radius (FP64 Kahan), camera matrix at time = timestep * step,
+ * `samples` pcg4d-jittered Gaussian splats per body added to the int32 RGBA
+ * buffer accum (4*sizex*sizey, cleared here), then render = tanh(accum *
+ * 0.01 / samples * 2^exposure) when tonemap is set.  Defaults of the
+ * reference's config.h: samples 128, exposure -1, ortho_scale -1, autoscale
+ * on, tonemap on.  Uses the host libm (cosf, sinf, logf, tanh). */
+void orc_vis_draw(uint32_t n, const float* pos, const float* vel, const float* pot, uint32_t step,
+                  double timestep, uint32_t sizex, uint32_t sizey, uint32_t samples, double exposure,
+                  double ortho_scale, int autoscale, int tonemap, int32_t* accum, float* render);
+
 /* Simulation over one slab in the reference layout (simulation.h:17-51):
  * pos[3N] vel[3N] acc[3N] mas[N] pot[N] ken[N] pen[N] (+ rad rho prs). */
 typedef struct {

@@ -70,6 +70,9 @@ class Oracle:
         fp, dp = C.POINTER(C.c_float), C.POINTER(C.c_double)
         L.orc_sph_cubic.argtypes = [C.c_uint32, fp, fp, fp, fp, fp, C.c_double, C.c_double, C.c_double,
                                     dp, dp, dp, dp, u32p]
+        L.orc_vis_draw.argtypes = [C.c_uint32, fp, fp, fp, C.c_uint32, C.c_double, C.c_uint32, C.c_uint32,
+                                   C.c_uint32, C.c_double, C.c_double, C.c_int, C.c_int,
+                                   C.POINTER(C.c_int32), fp]
 
         class Sim(C.Structure):
             _fields_ = [("step_number", C.c_uint32), ("N", C.c_uint32), ("mem", C.c_void_p),
@@ -155,6 +158,20 @@ class Oracle:
                                    prs.ctypes.data_as(self._rp), acc.ctypes.data_as(self._rp),
                                    nbr.ctypes.data_as(u32p))
         return rho, prs, acc, nbr
+
+    def vis_draw(self, pos, vel, pot, step, timestep, sizex, sizey, samples=128, exposure=-1.0,
+                 ortho_scale=-1.0, autoscale=1, tonemap=1):
+        """vis_draw (src/visualization.c:258-740): (accum int32 (sizey, sizex, 4),
+        render float32 (sizey, sizex, 4))."""
+        f = lambda a: np.ascontiguousarray(a, np.float32)
+        pos, vel, pot = f(pos), f(vel), f(pot)
+        accum = np.zeros((sizey, sizex, 4), np.int32)
+        render = np.zeros((sizey, sizex, 4), np.float32)
+        fp = C.POINTER(C.c_float)
+        self.lib.orc_vis_draw(len(pos), pos.ctypes.data_as(fp), vel.ctypes.data_as(fp), pot.ctypes.data_as(fp),
+                              step, timestep, sizex, sizey, samples, exposure, ortho_scale, autoscale, tonemap,
+                              accum.ctypes.data_as(C.POINTER(C.c_int32)), render.ctypes.data_as(fp))
+        return accum, render
 
     def sph_cubic(self, pos, vel, mas, rad, u, gamma=5.0 / 3.0, alpha=1.0, beta=2.0):
         """Cubic-spline SPH (FP64 physics, FP32 neighbour decisions)."""
@@ -263,6 +280,20 @@ class Reference:
         self.lib.refh_tree_bounds(tb.ctypes.data)
         return dict(parent=parent, bodies=bodies, branch=branch, bounds=bounds, params=params,
                     root_bounds=tb)
+
+    def vis_draw(self, step, sizex, sizey):
+        """src/visualization.c vis_draw of the current state (FP32 variants):
+        (accum int32 (sizey, sizex, 4), render float32 (sizey, sizex, 4))."""
+        accum = np.zeros((sizey, sizex, 4), np.int32)
+        render = np.zeros((sizey, sizex, 4), np.float32)
+        assert self.lib.refh_vis_draw(step, sizex, sizey, accum.ctypes.data, render.ctypes.data) == 0
+        return accum, render
+
+    def vis_save_ppm(self, render, filename):
+        """src/visualization_io.c vis_save(IMAGE_FILETYPE_PPM) of a render buffer."""
+        render = np.ascontiguousarray(render, np.float32)
+        sizey, sizex = render.shape[:2]
+        return self.lib.refh_vis_save(render.ctypes.data, sizex, sizey, filename.encode(), 1)
 
     def save_raw(self, filename):
         """src/simulation_io.c:81-149 (FP32 variants)."""

@@ -15,6 +15,9 @@
 #include "simulation.h"
 #include "gravity.h"
 #include "sph.h"
+#ifndef STARFLOOD_DOUBLE_PRECISION
+#include "visualization.h"
+#endif
 #ifdef ENABLE_TREE
 #include "tree.h"
 #endif
@@ -137,6 +140,41 @@ int refh_walk(void) { return solve_gravity_part_tree(&g_sim); }
 /* src/simulation_io.c:16-149 on the harness's simulation (FP32 builds; the
  * FP64 build of simulation_io.c does not compile) */
 int refh_save_raw(const char* filename) { return sim_save_raw(&g_sim, filename); }
+
+/* src/visualization_io.c:170-330: vis_save of a given render buffer (the
+ * binary buffer is sized for the configured VIS_FILE_FORMAT, 8-bit here,
+ * so only the PPM / PNG writers may be called) */
+int refh_vis_save(const f32* render_in, unsigned int sizex, unsigned int sizey, const char* filename,
+                  int filetype) {
+    vis_t vis;
+    mute();
+    int rc = vis_init(&vis, sizex, sizey);
+    if (rc == 0) {
+        memcpy(vis.render_buffer, render_in, sizeof(f32) * 4u * sizex * sizey);
+        rc = vis_save(&vis, filename, (image_filetype_t)filetype);
+        vis_free(&vis);
+    }
+    unmute();
+    return rc;
+}
+
+/* src/visualization.c:34-740: vis_draw of the harness's state at step_number
+ * into copies of the accumulation and render buffers */
+int refh_vis_draw(unsigned int step_number, unsigned int sizex, unsigned int sizey, i32* atomic_out,
+                  f32* render_out) {
+    vis_t vis;
+    mute();
+    int rc = vis_init(&vis, sizex, sizey);
+    if (rc == 0) {
+        g_sim.step_number = step_number;
+        rc = vis_draw(&vis, &g_sim);
+        memcpy(atomic_out, vis.atomic_buffer, sizeof(i32) * 4u * sizex * sizey);
+        memcpy(render_out, vis.render_buffer, sizeof(f32) * 4u * sizex * sizey);
+        vis_free(&vis);
+    }
+    unmute();
+    return rc;
+}
 int refh_read_raw(const char* filename) { return sim_read_raw(&g_sim, filename); }
 #endif
 

@@ -103,6 +103,11 @@ def lib():
             "sfgpu_host_unregister": (i32, [vp]),
             "sfgpu_flush_l2": (i32, [vp]),
             "sfgpu_save_raw": (i32, [vp, C.c_char_p]),
+            "sfgpu_vis_params_default": (None, [vp]),
+            "sfgpu_vis_draw": (i32, [vp, vp, u32, u32, u32, vp, vp]),
+            "sfgpu_vis_buffers_alloc": (i32, [u32, u32, C.POINTER(vp), C.POINTER(vp)]),
+            "sfgpu_vis_buffers_free": (None, [vp, vp]),
+            "sfgpu_vis_download": (i32, [vp, u32, u32, vp, vp, vp, vp]),
             "sfgpu_snapshot_wait": (i32, [vp]),
             "sfgpu_read_raw": (i32, [vp, C.c_char_p]),
             "sfgpu_compat_configure": (i32, [P]),
@@ -245,6 +250,25 @@ class Sim:
     def read_raw(self, filename):
         check(lib().sfgpu_read_raw(self.h, os.fsencode(filename)), "sfgpu_read_raw")
 
+    def vis_draw(self, step, sizex, sizey, samples=128):
+        """vis_draw of the current state: (accum int32 (sizey, sizex, 4),
+        render float32 (sizey, sizex, 4))."""
+        L = lib()
+        vp = (C.c_byte * 64)()
+        L.sfgpu_vis_params_default(vp)
+        C.c_uint32.from_buffer(vp, 0).value = samples
+        da, dr = C.c_void_p(), C.c_void_p()
+        check(L.sfgpu_vis_buffers_alloc(sizex, sizey, C.byref(da), C.byref(dr)), "sfgpu_vis_buffers_alloc")
+        try:
+            check(L.sfgpu_vis_draw(self.h, vp, step, sizex, sizey, da, dr), "sfgpu_vis_draw")
+            acc = np.zeros((sizey, sizex, 4), np.int32)
+            ren = np.zeros((sizey, sizex, 4), np.float32)
+            check(L.sfgpu_vis_download(self.h, sizex, sizey, da, dr, acc.ctypes.data, ren.ctypes.data),
+                  "sfgpu_vis_download")
+        finally:
+            L.sfgpu_vis_buffers_free(da, dr)
+        return acc, ren
+
     def walk_stats(self):
         a = np.zeros(self.n, np.uint32)
         b = np.zeros(self.n, np.uint32)
@@ -343,6 +367,12 @@ class SimT(C.Structure):
     _fields_ = [("step_number", C.c_uint), ("N", C.c_uint), ("mem", C.c_void_p), ("tree", TreeT)]
 
 
+class VisT(C.Structure):
+    """src/visualization.h:19-27"""
+    _fields_ = [("sizex", C.c_uint), ("sizey", C.c_uint), ("mem", C.c_void_p), ("atomic_buffer", C.c_void_p),
+                ("render_buffer", C.c_void_p), ("binary_buffer", C.c_void_p)]
+
+
 def compat_configure(p: Params):
     check(lib().sfgpu_compat_configure(C.byref(p)), "sfgpu_compat_configure")
 
@@ -352,10 +382,13 @@ def compat_functions():
     L = lib()
     S = C.POINTER(SimT)
     T = C.POINTER(TreeT)
+    V = C.POINTER(VisT)
     for name, args in (("sim_init", [S, C.c_uint]), ("sim_free", [S]), ("sim_solv", [S]), ("sim_step", [S]),
                        ("solve_gravity_part_part", [S]), ("solve_gravity_part_tree", [S]), ("solve_sph", [S]),
                        ("tree_init", [T, C.c_uint]), ("tree_free", [T]),
                        ("sim_save_raw", [S, C.c_char_p]), ("sim_read_raw", [S, C.c_char_p]),
+                       ("vis_init", [V, C.c_uint, C.c_uint]), ("vis_free", [V]),
+                       ("vis_draw", [V, S]), ("vis_save", [V, C.c_char_p, C.c_int]),
                        ("tree_build", [T, C.c_uint, C.c_void_p, C.c_void_p])):
         fn = getattr(L, name)
         fn.restype = C.c_int

@@ -21,7 +21,7 @@ LIB = os.path.join(HERE, "libsfgpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUDE, "-I" + CSRC,
               "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
-CC_FLAGS = ["-O2", "-fPIC", "-std=c11", "-Wall", "-Wextra", "-I" + INCLUDE]
+CC_FLAGS = ["-O2", "-fPIC", "-std=c11", "-Wall", "-Wextra", "-ffp-contract=off", "-I" + INCLUDE]
 
 
 def nvcc() -> str:
@@ -71,7 +71,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
                 print(o)
     if force or jobs or not os.path.exists(LIB) or _stale(LIB, objs):
         tmp = LIB + ".tmp"
-        _run([nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lpthread"])
+        _run([nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lpthread", "-lm"])
         os.replace(tmp, LIB)
     return LIB
 

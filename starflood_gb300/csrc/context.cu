@@ -180,6 +180,7 @@ extern "C" int sfgpu_destroy(sfgpu_sim* s) {
     if (!s) return SFGPU_OK;
     if (s->stream) cudaStreamSynchronize(s->stream);
     sf_snapshot_free(s);
+    sf_vis_free(s);
     if (s->graph) cudaGraphExecDestroy(s->graph);
     sf_tree_free(s->tree);
     sf_sph_free(s);

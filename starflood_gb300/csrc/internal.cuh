@@ -48,6 +48,20 @@ __device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b)
 __device__ __forceinline__ float fsqrt(float a) { return __fsqrt_rn(a); }
 
 // Kahan running sum (the idiom of src/gravity.c:521-533).
+// One MUFU instruction each (flush-to-zero): the force kernels call them on
+// r^2 + eps^2, which is positive and far above the subnormal range for any
+// eps > 0.
+__device__ __forceinline__ float rsqrt_hw(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rcp_hw(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 struct KSum {
     float s, c;
     __device__ __forceinline__ void add(float x) {
@@ -222,8 +236,10 @@ struct sfgpu_sim {
     cudaGraphExec_t graph = nullptr;
     bool graph_ok = true;
     struct SnapshotWriter* snap = nullptr;  // snapshot.cu
+    void* vis = nullptr;                    // VisScratch (vis.cu)
 };
 void sf_snapshot_free(sfgpu_sim* s);
+void sf_vis_free(sfgpu_sim* s);
 
 // stage entry points (each queues kernels on s->stream)
 int sf_stage_gravity_pp(sfgpu_sim* s);

@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(BS) k_pp_tile(const float* __restrict__ pos, c
 // in k_pp_tile (same operations, same order), so the results are identical.
 // Each j is staged pre-duplicated as (x,x,y,y) and (z,z,w,w) so the paired
 // operands come straight out of one 128-bit shared load.
-template <int BS, int PAIRS, bool COMP>
+template <int BS, int PAIRS, bool COMP, int RSQ = 0>
 __global__ void __launch_bounds__(BS) k_pp_tile2(const float* __restrict__ pos, const float* __restrict__ mas,
                                                  uint32_t n, float eps2, uint32_t jchunk,
                                                  float4* __restrict__ part) {
@@ -201,9 +201,19 @@ __global__ void __launch_bounds__(BS) k_pp_tile2(const float* __restrict__ pos, 
                 float2 r2 = __ffma2_rn(dz, dz, e2);
                 r2 = __ffma2_rn(dy, dy, r2);
                 r2 = __ffma2_rn(dx, dx, r2);
-                const float2 inv = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
+                float2 inv, inv2;
+                if (RSQ == 0) {
+                    inv = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
+                    inv2 = __fmul2_rn(inv, inv);
+                } else if (RSQ == 1) {
+                    inv = make_float2(rsqrt_hw(r2.x), rsqrt_hw(r2.y));
+                    inv2 = __fmul2_rn(inv, inv);
+                } else {  // 1/r^2 from the MUFU too: one FP32 multiply fewer
+                    inv = make_float2(rsqrt_hw(r2.x), rsqrt_hw(r2.y));
+                    inv2 = make_float2(rcp_hw(r2.x), rcp_hw(r2.y));
+                }
                 const float2 mphi = __fmul2_rn(sw, inv);
-                const float2 f = __fmul2_rn(mphi, __fmul2_rn(inv, inv));
+                const float2 f = __fmul2_rn(mphi, inv2);
                 ax[q] = __ffma2_rn(f, dx, ax[q]);
                 ay[q] = __ffma2_rn(f, dy, ay[q]);
                 az[q] = __ffma2_rn(f, dz, az[q]);

@@ -159,12 +159,32 @@ def raw_snapshot():
     ref.free()
 
 
+def vis_splat():
+    """vis_draw (src/visualization.c) of a 2048-body Plummer sphere after one
+    PP solve (potentials set), step 7, 96 x 64 pixels, shipped settings
+    (128 samples, exposure -1, ortho -1, autoscaling, tanh)."""
+    n = 2048
+    pos, vel, mas = plummer(n, seed=13)
+    ref = Reference("pp_e0.01")
+    v = ref.init(n)
+    v["pos"][:] = pos
+    v["vel"][:] = vel
+    v["mas"][:] = mas
+    assert ref.solv(0) == 0
+    accum, render = ref.vis_draw(7, 96, 64)
+    np.savez_compressed(os.path.join(OUT, "vis_plummer_n2048_96x64_step7.npz"), pos=v["pos"].copy(),
+                        vel=v["vel"].copy(), pot=v["pot"].copy(), mas=mas, step=7, timestep=1e-3,
+                        sizex=96, sizey=64, accum=accum, render=render)
+    assert ref.vis_save_ppm(render, os.path.join(OUT, "vis_plummer_n2048_96x64_step7.ppm")) == 0
+    ref.free()
+
+
 def main():
     if not obuild.reference_available():
         raise SystemExit("the Starflood reference sources are needed to regenerate fixtures")
     obuild.build()
     for f in (pp_c1, pp_plummer, pp_fp64, tree_uniform, tree_ties, tree_overflow, sph_reference,
-              raw_snapshot):
+              raw_snapshot, vis_splat):
         f()
         print("wrote", f.__name__)
 
