@@ -373,7 +373,7 @@ def sph_cell_tile_records(pos, h):
     return total
 
 
-def gpu_sph(sf, steps, warmup):
+def gpu_sph(sf, steps, warmup, sph_path=0):
     import ctypes as C
     import torch
     n = N_SPH
@@ -383,7 +383,7 @@ def gpu_sph(sf, steps, warmup):
     def new_sim(flags):
         p = sf.default_params(solver=sf.SOLVER_TREE, sph=sf.SPH_CUBIC, eps=0.01, dt=5e-4, theta=0.5,
                               acc_mode=sf.ACC_PHYSICAL, sph_gamma=5.0 / 3.0, sph_alpha=1.0, sph_beta=2.0,
-                              flags=flags)
+                              flags=flags, sph_path=sph_path)
         s = sf.Sim(n, p)
         s.set_state(pos, vel, mas, rad)
         s.sph_set_u(u)
@@ -662,6 +662,7 @@ def main():
     ap.add_argument("--only", choices=["pp", "sph"], default=None,
                     help="run one sub-benchmark alone and print its object (profiling runs)")
     ap.add_argument("--pp-n", type=int, default=N_PP, help="bodies of the PP sub-benchmark with --only pp")
+    ap.add_argument("--sph-path", type=int, default=0, help="SPH pass variant with --only sph (sfgpu_params.sph_path)")
     args = ap.parse_args()
     rank, world, local = env_rank()
 
@@ -696,7 +697,7 @@ def main():
         print(json.dumps({"only": "pp", "n": args.pp_n, "pp": gpu_pp(sf, n=args.pp_n)}))
         return
     if args.only == "sph":
-        print(json.dumps({"only": "sph", "sph": gpu_sph(sf, max(3, args.steps), args.warmup)}))
+        print(json.dumps({"only": "sph", "sph": gpu_sph(sf, max(3, args.steps), args.warmup, args.sph_path)}))
         return
 
     r = gpu_bh(args.steps, args.warmup, sf)

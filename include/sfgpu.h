@@ -78,7 +78,8 @@ typedef struct {
     double   sph_beta;    /* CUBIC: Monaghan viscosity beta                 */
     uint32_t flags;       /* SFGPU_FLAG_*                                   */
     uint32_t walk_split;  /* walk variant: 0 group walk (default), 1 thread per body, 8 thread per body and root octant, 64 group walk over 8 warps */
-    uint32_t reserved[6];
+    uint32_t sph_path;    /* CUBIC SPH passes: 0 one thread per body (default), 1 one warp per 32-body slice of a cell */
+    uint32_t reserved[5];
 } sfgpu_params;
 
 /* flags */
@@ -211,6 +212,13 @@ int sfgpu_host_unregister(void* ptr);
 /* Overwrite a 256 MiB device buffer (larger than the L2) on a stream, so
  * that the next kernel starts with a cold L2. */
 int sfgpu_flush_l2(void* stream);
+
+/* One drop-in call on a host slab (page-locked for full speed), as
+ * sim_solv / sim_step (src/simulation.c:230-519) make it: uploads the arrays
+ * the call reads (pos, vel, acc, mas; rad with SPH), runs the solve
+ * (solve_only != 0) or one graph-replayed step, downloads the whole slab and
+ * the device status word (cleared), with a single host synchronisation. */
+int sfgpu_host_step(sfgpu_sim* s, float* slab, uint32_t step_number, int solve_only, uint32_t* status);
 
 /* ---- snapshots (src/simulation_io.c:16-149, the raw format) --------------- */
 /* The raw format is the slab itself, N*dof floats with no header, as

@@ -37,7 +37,7 @@ class Params(C.Structure):
                 ("acc_mode", C.c_int32), ("leaf_cap", C.c_uint32), ("depth_max", C.c_uint32),
                 ("nodes_max", C.c_uint32), ("sph_gamma", C.c_double), ("sph_alpha", C.c_double),
                 ("sph_beta", C.c_double), ("flags", C.c_uint32), ("walk_split", C.c_uint32),
-                ("reserved", C.c_uint32 * 6)]
+                ("sph_path", C.c_uint32), ("reserved", C.c_uint32 * 5)]
 
 
 _lib = None

@@ -73,7 +73,7 @@ struct TileConfig {
     uint32_t jchunk;
 };
 // candidate shapes for the autotuner (threads per CTA, bodies per thread, j-chunk)
-const TileConfig kConfigs[] = {{128, 2, 1024}, {128, 4, 2048}, {128, 4, 4096}, {256, 2, 2048}, {128, 8, 4096}};
+const TileConfig kConfigs[] = {{128, 4, 2048}, {128, 8, 2048}, {128, 8, 4096}, {256, 4, 4096}, {128, 8, 8192}};
 constexpr int kNumConfigs = sizeof(kConfigs) / sizeof(kConfigs[0]);
 
 template <int BS, int IPT>
@@ -82,7 +82,7 @@ __global__ void __launch_bounds__(BS) k_batch_pp(const BatchItem* __restrict__ i
                                                  const uint32_t* __restrict__ part_off, uint32_t jchunk,
                                                  const float* __restrict__ pos, const float* __restrict__ mas,
                                                  float eps2, float4* __restrict__ part) {
-    __shared__ float4 sj[BS];
+    __shared__ float4 sj[2][BS];
     __shared__ uint32_t s_item;
     while (true) {
         if (threadIdx.x == 0) s_item = atomicAdd(ticket, 1u);
@@ -92,47 +92,51 @@ __global__ void __launch_bounds__(BS) k_batch_pp(const BatchItem* __restrict__ i
         if (it >= nitems) break;
         const BatchItem w = items[it];
         const uint32_t base = off[w.sys], nb = off[w.sys + 1] - base;
-        float xi[IPT], yi[IPT], zi[IPT], ax[IPT], ay[IPT], az[IPT], ph[IPT];
+        // bodies i0 + k*BS + tid, k < IPT, as IPT/2 pairs on the paired FP32
+        // instructions (pp_pair_step)
+        constexpr int PAIRS = IPT / 2;
+        float2 nx[PAIRS], ny[PAIRS], nz[PAIRS], ax[PAIRS], ay[PAIRS], az[PAIRS], ph[PAIRS];
 #pragma unroll
-        for (int k = 0; k < IPT; k++) {
-            const uint32_t i = w.i0 + k * BS + threadIdx.x;
-            const bool live = i < nb;
-            xi[k] = live ? pos[3u * (base + i)] : 0.f;
-            yi[k] = live ? pos[3u * (base + i) + 1u] : 0.f;
-            zi[k] = live ? pos[3u * (base + i) + 2u] : 0.f;
-            ax[k] = ay[k] = az[k] = ph[k] = 0.f;
+        for (int q = 0; q < PAIRS; q++) {
+            const uint32_t i0 = w.i0 + (2 * q) * BS + threadIdx.x, i1 = i0 + BS;
+            nx[q] = make_float2(i0 < nb ? -pos[3u * (base + i0)] : 0.f, i1 < nb ? -pos[3u * (base + i1)] : 0.f);
+            ny[q] = make_float2(i0 < nb ? -pos[3u * (base + i0) + 1u] : 0.f,
+                                i1 < nb ? -pos[3u * (base + i1) + 1u] : 0.f);
+            nz[q] = make_float2(i0 < nb ? -pos[3u * (base + i0) + 2u] : 0.f,
+                                i1 < nb ? -pos[3u * (base + i1) + 2u] : 0.f);
+            ax[q] = ay[q] = az[q] = ph[q] = make_float2(0.f, 0.f);
         }
+        const float2 e2 = make_float2(eps2, eps2);
         const uint32_t j1 = min(nb, w.j0 + jchunk);
         for (uint32_t jt = w.j0; jt < j1; jt += BS) {
             const uint32_t j = jt + threadIdx.x;
-            float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (j < j1) q = make_float4(pos[3u * (base + j)], pos[3u * (base + j) + 1u], pos[3u * (base + j) + 2u],
-                                        mas[base + j]);
+            float x = 0.f, y = 0.f, z = 0.f, m = 0.f;  // padding: zero mass
+            if (j < j1) {
+                x = pos[3u * (base + j)];
+                y = pos[3u * (base + j) + 1u];
+                z = pos[3u * (base + j) + 2u];
+                m = mas[base + j];
+            }
             __syncthreads();
-            sj[threadIdx.x] = q;
+            sj[0][threadIdx.x] = make_float4(x, x, y, y);
+            sj[1][threadIdx.x] = make_float4(z, z, m, m);
             __syncthreads();
-#pragma unroll 8
+#pragma unroll 4
             for (int jj = 0; jj < BS; jj++) {
-                const float4 s = sj[jj];
+                const float4 A = sj[0][jj], B = sj[1][jj];
+                const float2 sx = make_float2(A.x, A.y), sy = make_float2(A.z, A.w);
+                const float2 sz = make_float2(B.x, B.y), sw = make_float2(B.z, B.w);
 #pragma unroll
-                for (int k = 0; k < IPT; k++) {
-                    const float dx = s.x - xi[k], dy = s.y - yi[k], dz = s.z - zi[k];
-                    const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
-                    const float inv = rsqrtf(r2);
-                    const float mphi = s.w * inv;
-                    const float f = mphi * (inv * inv);
-                    ax[k] = fmaf(f, dx, ax[k]);
-                    ay[k] = fmaf(f, dy, ay[k]);
-                    az[k] = fmaf(f, dz, az[k]);
-                    ph[k] += mphi;
-                }
+                for (int q = 0; q < PAIRS; q++)
+                    pp_pair_step<2>(sx, sy, sz, sw, nx[q], ny[q], nz[q], e2, ax[q], ay[q], az[q], ph[q]);
             }
         }
         float4* out = part + part_off[w.sys] + (size_t)w.chunk * nb;
 #pragma unroll
-        for (int k = 0; k < IPT; k++) {
-            const uint32_t i = w.i0 + k * BS + threadIdx.x;
-            if (i < nb) out[i] = make_float4(ax[k], ay[k], az[k], ph[k]);
+        for (int q = 0; q < PAIRS; q++) {
+            const uint32_t i0 = w.i0 + (2 * q) * BS + threadIdx.x, i1 = i0 + BS;
+            if (i0 < nb) out[i0] = make_float4(ax[q].x, ay[q].x, az[q].x, ph[q].x);
+            if (i1 < nb) out[i1] = make_float4(ax[q].y, ay[q].y, az[q].y, ph[q].y);
         }
         __syncthreads();
     }
@@ -332,10 +336,10 @@ int batch_forces(sfgpu_batch* b, const float* pos) {
     SF_CUDA(cudaMemsetAsync(b->ticket, 0, sizeof(uint32_t), s->stream));
     const int grid = sf_num_sms() * 8;  // persistent: a few CTAs per SM
     switch (b->config) {
-        case 0: launch_pp<128, 2>(b, s->stream, pos, mas, fc.eps2, grid); break;
-        case 1: launch_pp<128, 4>(b, s->stream, pos, mas, fc.eps2, grid); break;
-        case 2: launch_pp<128, 4>(b, s->stream, pos, mas, fc.eps2, grid); break;
-        case 3: launch_pp<256, 2>(b, s->stream, pos, mas, fc.eps2, grid); break;
+        case 0: launch_pp<128, 4>(b, s->stream, pos, mas, fc.eps2, grid); break;
+        case 1: launch_pp<128, 8>(b, s->stream, pos, mas, fc.eps2, grid); break;
+        case 2: launch_pp<128, 8>(b, s->stream, pos, mas, fc.eps2, grid); break;
+        case 3: launch_pp<256, 4>(b, s->stream, pos, mas, fc.eps2, grid); break;
         default: launch_pp<128, 8>(b, s->stream, pos, mas, fc.eps2, grid); break;
     }
     SF_CHECK_LAUNCH();

@@ -230,17 +230,12 @@ static int solv_common(sim_t* sim, int step) {
     if (!dev) return SFGPU_FAILURE;
     sfgpu_params p;
     params_now(&p);
-    if (sfgpu_upload(dev, (const float*)sim->mem) != SFGPU_OK) {
-        fail_msg(fn);
-        return SFGPU_FAILURE;
-    }
-    const int rc = step ? sfgpu_step(dev, sim->step_number) : sfgpu_solve(dev, sim->step_number);
-    if (rc != SFGPU_OK || sfgpu_download(dev, (float*)sim->mem) != SFGPU_OK) {
-        fail_msg(fn);
-        return SFGPU_FAILURE;
-    }
+    /* upload, solve or one graph-replayed step, download: one host sync */
     uint32_t status = 0;
-    sfgpu_status(dev, &status);
+    if (sfgpu_host_step(dev, (float*)sim->mem, sim->step_number, !step, &status) != SFGPU_OK) {
+        fail_msg(fn);
+        return SFGPU_FAILURE;
+    }
     if (status & (SFGPU_STATUS_TREE_NODES | SFGPU_STATUS_TREE_DEPTH))
         fprintf(stderr, "tree_build() error: Exceeded maximum %s!\n",
                 (status & SFGPU_STATUS_TREE_NODES) ? "number of tree nodes" : "tree depth");

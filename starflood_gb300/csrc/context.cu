@@ -538,6 +538,31 @@ extern "C" int sfgpu_synchronize(sfgpu_sim* s) {
     return SFGPU_OK;
 }
 
+extern "C" int sfgpu_host_step(sfgpu_sim* s, float* slab, uint32_t step_number, int solve_only,
+                               uint32_t* status) {
+    sf_clear_error();
+    if (!s || !slab) {
+        sf_set_error("sfgpu_host_step: NULL argument");
+        return SFGPU_FAILURE;
+    }
+    // the arrays a solve or a step reads: pos, vel, acc, mas (0..9) and,
+    // with SPH, the smoothing lengths (13); everything comes back
+    const size_t n = s->n;
+    SF_CUDA(cudaMemcpyAsync(s->slab, slab, sizeof(float) * 10 * n, cudaMemcpyHostToDevice, s->stream));
+    if (s->dof > 13)
+        SF_CUDA(cudaMemcpyAsync(s->slab + 13 * n, slab + 13 * n, sizeof(float) * n, cudaMemcpyHostToDevice,
+                                s->stream));
+    if (refresh_fp64(s) != SFGPU_OK) return SFGPU_FAILURE;
+    const int rc = solve_only ? sfgpu_solve(s, step_number) : sfgpu_run(s, step_number, 1);
+    if (rc != SFGPU_OK) return rc;
+    SF_CUDA(cudaMemcpyAsync(slab, s->slab, sizeof(float) * s->dof * n, cudaMemcpyDeviceToHost, s->stream));
+    SF_CUDA(cudaMemcpyAsync(s->h_status, s->d_status, sizeof(uint32_t), cudaMemcpyDeviceToHost, s->stream));
+    SF_CUDA(cudaMemsetAsync(s->d_status, 0, sizeof(uint32_t), s->stream));
+    SF_CUDA(cudaStreamSynchronize(s->stream));
+    if (status) *status = *s->h_status;
+    return SFGPU_OK;
+}
+
 static int fetch_sums(sfgpu_sim* s) {
     SF_CUDA(cudaMemcpyAsync(s->h_sums, s->sums, sizeof(double) * 8, cudaMemcpyDeviceToHost, s->stream));
     SF_CUDA(cudaStreamSynchronize(s->stream));

@@ -62,6 +62,39 @@ __device__ __forceinline__ float rcp_hw(float x) {
     return y;
 }
 
+// One j (coordinates and mass duplicated into pairs) against a pair of
+// bodies (negated coordinates nx, ny, nz) on the paired FP32 instructions:
+// a += m_j d / (d^2 + eps^2)^1.5, phi += m_j / (d^2 + eps^2)^0.5 with
+// d = r_j - r_i.  RSQ 0: rsqrtf, 1/r^2 = rsqrt^2; 1: MUFU rsqrt; 2: MUFU
+// rsqrt and MUFU reciprocal (13 -> 12 FP32 operations per interaction).
+template <int RSQ>
+__device__ __forceinline__ void pp_pair_step(float2 sx, float2 sy, float2 sz, float2 sw, float2 nx, float2 ny,
+                                             float2 nz, float2 e2, float2& ax, float2& ay, float2& az, float2& ph) {
+    const float2 dx = __fadd2_rn(sx, nx);
+    const float2 dy = __fadd2_rn(sy, ny);
+    const float2 dz = __fadd2_rn(sz, nz);
+    float2 r2 = __ffma2_rn(dz, dz, e2);
+    r2 = __ffma2_rn(dy, dy, r2);
+    r2 = __ffma2_rn(dx, dx, r2);
+    float2 inv, inv2;
+    if (RSQ == 0) {
+        inv = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
+        inv2 = __fmul2_rn(inv, inv);
+    } else if (RSQ == 1) {
+        inv = make_float2(rsqrt_hw(r2.x), rsqrt_hw(r2.y));
+        inv2 = __fmul2_rn(inv, inv);
+    } else {
+        inv = make_float2(rsqrt_hw(r2.x), rsqrt_hw(r2.y));
+        inv2 = make_float2(rcp_hw(r2.x), rcp_hw(r2.y));
+    }
+    const float2 mphi = __fmul2_rn(sw, inv);
+    const float2 f = __fmul2_rn(mphi, inv2);
+    ax = __ffma2_rn(f, dx, ax);
+    ay = __ffma2_rn(f, dy, ay);
+    az = __ffma2_rn(f, dz, az);
+    ph = __fadd2_rn(ph, mphi);
+}
+
 struct KSum {
     float s, c;
     __device__ __forceinline__ void add(float x) {

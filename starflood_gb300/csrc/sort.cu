@@ -208,8 +208,11 @@ int sf_sort_pairs_keep(uint64_t* keys, uint32_t* vals, uint32_t n, int bits, Sor
         sf_set_error("sort: %d key bits is too many", bits);
         return SFGPU_FAILURE;
     }
-    // small inputs take small tiles so that more SMs join each pass
-    const int items = n <= (1u << 18) ? 2 : (n <= (1u << 20) ? 4 : 8);
+    // keys per thread, measured on GB300 (7 passes of 49-bit keys): 4 up to
+    // 2^17 keys (0.087 ms at 65,536, against 0.101 with 2 or 8), 8 above
+    // (0.128 ms at 262,144 and 0.253 ms at 1,048,576, against 0.142 / 0.291
+    // with 4): fewer, fuller tiles shorten the look-back chains
+    const int items = n <= (1u << 17) ? 4 : 8;
     const uint32_t tiles = sf_ceil_div(n, SORT_THREADS * items);
     SF_CUDA(cudaMemsetAsync(w.hist, 0, sizeof(uint32_t) * passes * RADIX, st));
     SF_CUDA(cudaMemsetAsync(w.counters, 0, sizeof(uint32_t) * passes, st));

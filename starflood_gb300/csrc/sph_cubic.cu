@@ -14,13 +14,11 @@
 // Neighbour search: cells of side 2 h_max (slightly enlarged, so that FP32
 // rounding can never put two neighbours two cells apart), hashed into a
 // table of 2^k >= 2N buckets; bodies are radix sorted by bucket, so a cell's
-// bodies are one contiguous run of records.  Each pass then works cell by
-// cell (k_cubic_tiles): the records of the 27 neighbour cells are staged in
-// shared memory by bulk asynchronous copies and every body of the centre
-// cell runs against them; bodies whose cell coordinates differ from the
-// scanned cell's (hash collisions) are skipped, so none is counted twice.
-// Bytes streamed per pass: sum over cells of the 27-cell neighbourhood's
-// records (density 32 B each, force 48 B) plus the centre records.
+// bodies are one contiguous run of records.  Each pass then works a warp per
+// 32-body slice of a cell (k_cubic_cells): the slice's bodies share their 27
+// neighbour cells, whose records the warp reads together (one broadcast load
+// per record); bodies whose cell coordinates differ from the scanned cell's
+// (hash collisions) are skipped, so none is counted twice.
 #include "internal.cuh"
 
 namespace {
@@ -41,7 +39,7 @@ struct CubicWork {
     float4* pd = nullptr;      // sorted rho, P/rho^2, c, h
     float4* ph = nullptr;      // sorted h, u, c
     uint32_t* bmix = nullptr;  // per bucket: holds more than one cell
-    uint32_t* items = nullptr; // occupied buckets
+    uint2* items = nullptr;    // (bucket, first body) of every 32-body slice
     uint32_t* counters = nullptr;  // [0] items [1] density ticket [2] force ticket
     uint64_t* cell = nullptr;  // sorted packed cell coordinates
     float* grid = nullptr;     // [0] cell side, [1] 1/side
@@ -58,8 +56,22 @@ __device__ __forceinline__ uint64_t pack_cell(int3 c) {
     };
     return (f(c.x) << (2 * CELL_BITS)) | (f(c.y) << CELL_BITS) | f(c.z);
 }
+// Bucket = the low bits of the cell's Morton code (3-way bit interleave of
+// the offset coordinates): neighbouring cells land in nearby buckets, so
+// bodies sorted by bucket are also sorted in space and consecutive threads
+// scan overlapping neighbourhoods.  Cells further apart than the table's
+// period share buckets; those buckets are filtered by cell key.
+__device__ __forceinline__ uint32_t spread3(uint32_t v) {  // low 10 bits to every third bit
+    v &= 0x3FFu;
+    v = (v | (v << 16)) & 0x030000FFu;
+    v = (v | (v << 8)) & 0x0300F00Fu;
+    v = (v | (v << 4)) & 0x030C30C3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
 __device__ __forceinline__ uint32_t bucket_of(int3 c, uint32_t mask) {
-    return ((uint32_t)c.x * 73856093u ^ (uint32_t)c.y * 19349663u ^ (uint32_t)c.z * 83492791u) & mask;
+    const uint32_t x = (uint32_t)(c.x + CELL_OFF), y = (uint32_t)(c.y + CELL_OFF), z = (uint32_t)(c.z + CELL_OFF);
+    return ((spread3(x) << 2) | (spread3(y) << 1) | spread3(z)) & mask;
 }
 
 __device__ __forceinline__ float w_cubic(float r, float h) {
@@ -148,55 +160,18 @@ __global__ void k_cell_gather(const uint64_t* __restrict__ keys, const uint32_t*
     ph[k] = make_float4(slab[(size_t)13 * n + p], uu, sqrtf(gamma * (gamma - 1.0f) * uu), 0.0f);
 }
 
-// ---- cell tiles ---------------------------------------------------------------
-// One work item per occupied bucket.  For a bucket that holds one cell (the
-// usual case with a table of >= 2N buckets), the block stages the records of
-// the 27 neighbour cells into shared memory with bulk asynchronous copies
-// (cp.async.bulk, completion counted on an mbarrier), CAP records at a time,
-// and each thread runs its centre bodies (up to MAXB) against every staged
-// record.  Neighbour buckets that hold several cells are staged whole and
-// filtered by cell key per record; a bucket whose cell is not the wanted one
-// is skipped.  Centre buckets with several cells, or with more bodies than
-// the block holds, take the per-body path (body_direct).  Records:
-// density 32 B (x,y,z,m | h,u,c,0), force 48 B (x,y,z,m | v,u | rho,P/rho^2,c,h).
-constexpr int TILE_THREADS = 128;
-constexpr int TILE_CAP = 768;
-constexpr int TILE_MAXB = 4;
-constexpr uint32_t TILE_SPIN = 1u << 22;
-
-__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                 :
-                 : "r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar))
-                 : "memory");
-}
-
-// true when the phase with this parity has completed; gives up after
-// TILE_SPIN polls (a wrong byte count; cannot happen for in-bounds copies)
-__device__ __forceinline__ bool bar_wait(uint64_t* bar, uint32_t parity) {
-    const uint32_t a = smem_addr(bar);
-    for (uint32_t it = 0; it < TILE_SPIN; it++) {
-        uint32_t done;
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-            "selp.u32 %0, 1, 0, p;\n\t}"
-            : "=r"(done)
-            : "r"(a), "r"(parity)
-            : "memory");
-        if (done) return true;
-    }
-    return false;
-}
-
-struct TileSeg {
-    uint32_t j0, cnt;    // global record range of this neighbour bucket
-    uint32_t check;      // 1: filter records by cell key
-    uint32_t pad;
-    uint64_t want;       // the neighbour cell's packed key
-};
+// ---- warp per cell ------------------------------------------------------------
+// One work item per 32-body slice of an occupied bucket.  For a bucket that
+// holds one cell (the usual case with a table of >= 2N buckets) the slice's
+// 32 bodies share their 27 neighbour cells, so the warp walks those cells'
+// records together: every record is one broadcast load for the whole warp
+// and each lane tests it against its own body.  Lanes 0..26 first look up the
+// 27 neighbour buckets side by side; a neighbour bucket that holds another
+// cell is skipped whole, one that holds several cells is filtered record by
+// record.  A centre bucket that holds several cells (hash collision) runs
+// each lane's own 27-cell scan (body_direct).  Records: density 32 B
+// (x,y,z,m | h,u,c), force 48 B (x,y,z,m | v,u | rho,P/rho^2,c,h).
+constexpr int WARP_BLOCK = 128;
 
 __device__ __forceinline__ void density_pair(const float4& a, float hi, const float4& q, float hj, float& rho,
                                              uint32_t& count) {
@@ -233,9 +208,9 @@ __device__ __forceinline__ void force_pair(const float4& a, float hi, const floa
     du += q.w * (di.y + 0.5f * visc) * g * vr;
 }
 
-// one body against its 27 neighbour cells straight from global memory
+// one body against its 27 neighbour cells, its own scan
 template <bool FORCE>
-__device__ void body_direct(uint32_t k, uint32_t mask, const float* __restrict__ grid,
+__device__ __forceinline__ void body_direct(uint32_t k, uint32_t mask, const float* __restrict__ grid,
                             const uint32_t* __restrict__ bstart, const uint32_t* __restrict__ bend,
                             const float4* __restrict__ px, const float4* __restrict__ ph,
                             const float4* __restrict__ pv, const uint64_t* __restrict__ cell,
@@ -291,197 +266,110 @@ __device__ __forceinline__ void finish_body(uint32_t k, uint32_t n, float gamma,
     }
 }
 
+// one thread per body, each scanning its own 27 cells (sf_params.sph_path 0)
 template <bool FORCE>
-__global__ void __launch_bounds__(TILE_THREADS, 4) k_cubic_tiles(
+__global__ void __launch_bounds__(128) k_cubic_body(uint32_t n, const float* __restrict__ grid, uint32_t mask,
+                                                    const uint32_t* __restrict__ bstart,
+                                                    const uint32_t* __restrict__ bend, const float4* __restrict__ px,
+                                                    const float4* __restrict__ ph, const float4* __restrict__ pv,
+                                                    const uint64_t* __restrict__ cell, float4* __restrict__ pd,
+                                                    const uint32_t* __restrict__ V, float gamma, float alpha,
+                                                    float beta, float* __restrict__ slab, float* __restrict__ dudt,
+                                                    uint32_t* __restrict__ nbr) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    float o0 = 0.f, o1 = 0.f, o2 = 0.f, o3 = 0.f;
+    uint32_t count = 0;
+    body_direct<FORCE>(k, mask, grid, bstart, bend, px, ph, pv, cell, pd, alpha, beta, o0, o1, o2, o3, count);
+    finish_body<FORCE>(k, n, gamma, ph, V, pd, slab, dudt, nbr, o0, o1, o2, o3, count);
+}
+
+template <bool FORCE>
+__global__ void __launch_bounds__(WARP_BLOCK, 4) k_cubic_cells(
     uint32_t n, const float* __restrict__ grid, uint32_t mask, const uint32_t* __restrict__ bstart,
-    const uint32_t* __restrict__ bend, const uint32_t* __restrict__ bmix, const uint32_t* __restrict__ items,
+    const uint32_t* __restrict__ bend, const uint32_t* __restrict__ bmix, const uint2* __restrict__ items,
     const uint32_t* __restrict__ nitems_p, uint32_t* __restrict__ ticket, const float4* __restrict__ px,
     const float4* __restrict__ ph, const float4* __restrict__ pv, const uint64_t* __restrict__ cell,
     float4* __restrict__ pd, const uint32_t* __restrict__ V, float gamma, float alpha, float beta,
-    float* __restrict__ slab, float* __restrict__ dudt, uint32_t* __restrict__ nbr, uint32_t* d_status) {
-    extern __shared__ __align__(16) float4 tile[];
-    float4* tA = tile;                 // x, y, z, m
-    float4* tB = tile + TILE_CAP;      // density: h, u, c | force: vx, vy, vz, u
-    float4* tC = tile + 2 * TILE_CAP;  // force: rho, P/rho^2, c, h
-    __shared__ TileSeg seg[27];
-    __shared__ uint32_t s_item;
-    __shared__ __align__(8) uint64_t bar;
-    if (threadIdx.x == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bar)) : "memory");
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    __syncthreads();
-    uint32_t phase = 0;
+    float* __restrict__ slab, float* __restrict__ dudt, uint32_t* __restrict__ nbr) {
+    const int lane = threadIdx.x & 31;
     const uint32_t nitems = *nitems_p;
     while (true) {
-        if (threadIdx.x == 0) s_item = atomicAdd(ticket, 1u);
-        __syncthreads();
-        const uint32_t it = s_item;
+        uint32_t it = 0;
+        if (lane == 0) it = atomicAdd(ticket, 1u);
+        it = __shfl_sync(0xffffffffu, it, 0);
         if (it >= nitems) break;
-        const uint32_t b = items[it];
-        const uint32_t c0 = bstart[b], c1 = bend[b];
-        const uint32_t nb = c1 - c0;
-        if (bmix[b] || nb > (uint32_t)TILE_THREADS * TILE_MAXB) {
-            for (uint32_t k = c0 + threadIdx.x; k < c1; k += TILE_THREADS) {
-                float o0 = 0.f, o1 = 0.f, o2 = 0.f, o3 = 0.f;
-                uint32_t count = 0;
-                body_direct<FORCE>(k, mask, grid, bstart, bend, px, ph, pv, cell, pd, alpha, beta, o0, o1, o2,
-                                   o3, count);
-                finish_body<FORCE>(k, n, gamma, ph, V, pd, slab, dudt, nbr, o0, o1, o2, o3, count);
+        const uint2 item = items[it];  // (bucket, first body of the slice)
+        const uint32_t b = item.x;
+        const uint32_t c1 = min(bend[b], item.y + 32u);
+        const uint32_t k = item.y + lane;
+        const bool live = k < c1;
+        float o0 = 0.f, o1 = 0.f, o2 = 0.f, o3 = 0.f;
+        uint32_t count = 0;
+        if (bmix[b]) {
+            if (live)
+                body_direct<FORCE>(k, mask, grid, bstart, bend, px, ph, pv, cell, pd, alpha, beta, o0, o1, o2, o3,
+                                   count);
+        } else {
+            const float4 a = px[live ? k : item.y];
+            const float hi = ph[live ? k : item.y].x;
+            float4 di = make_float4(0.f, 0.f, 0.f, 0.f), vi = di;
+            if (FORCE) {
+                di = pd[live ? k : item.y];
+                vi = pv[live ? k : item.y];
             }
-            __syncthreads();
-            continue;
-        }
-        // the 27 neighbour buckets, in the per-body loop's order
-        if (threadIdx.x < 27) {
-            const int t = threadIdx.x;
-            const float4 a = px[c0];
-            const int3 cc = cell_of(a.x, a.y, a.z, grid[1]);
-            const int3 c = make_int3(cc.x + (t % 3) - 1, cc.y + (t / 3) % 3 - 1, cc.z + t / 9 - 1);
-            const uint64_t want = pack_cell(c);
-            const uint32_t nbk = bucket_of(c, mask);
-            const uint32_t j0 = bstart[nbk], j1 = bend[nbk];
-            uint32_t cnt = j1 - j0, check = 0;
-            if (cnt) {
-                if (bmix[nbk]) check = 1;
-                else if (cell[j0] != want) cnt = 0;
-            }
-            seg[t] = TileSeg{j0, cnt, check, 0u, want};
-        }
-        __syncthreads();
-        // centre bodies of this thread
-        float4 a[TILE_MAXB], di[TILE_MAXB], vi[TILE_MAXB];
-        float hi[TILE_MAXB];
-        float o0[TILE_MAXB], o1[TILE_MAXB], o2[TILE_MAXB], o3[TILE_MAXB];
-        uint32_t cnt_b[TILE_MAXB];
-#pragma unroll
-        for (int q = 0; q < TILE_MAXB; q++) {
-            const uint32_t k = c0 + threadIdx.x + q * TILE_THREADS;
-            const bool live = k < c1;
-            a[q] = live ? px[k] : make_float4(0.f, 0.f, 0.f, 0.f);
-            hi[q] = live ? ph[k].x : 0.f;
-            di[q] = (FORCE && live) ? pd[k] : make_float4(0.f, 0.f, 0.f, 0.f);
-            vi[q] = (FORCE && live) ? pv[k] : make_float4(0.f, 0.f, 0.f, 0.f);
-            o0[q] = o1[q] = o2[q] = o3[q] = 0.f;
-            cnt_b[q] = 0;
-        }
-        // chunks of at most TILE_CAP staged records
-        int s_from = 0;
-        uint32_t r_from = 0;  // records of seg[s_from] already done
-        bool failed = false;
-        while (s_from < 27) {
-            // plan the chunk (every thread computes the same plan)
-            int s_to = s_from;
-            uint32_t r_to = r_from, room = TILE_CAP;
-            while (s_to < 27 && room > 0) {
-                const uint32_t left = seg[s_to].cnt - r_to;
-                const uint32_t take = min(left, room);
-                room -= take;
-                r_to += take;
-                if (r_to == seg[s_to].cnt) {
-                    s_to++;
-                    r_to = 0;
+            // lanes 0..26: neighbour bucket t's range (empty when it holds
+            // another cell) and whether its records need the cell filter
+            uint32_t j0 = 0, j1 = 0, check = 0;
+            uint64_t want = 0;
+            if (lane < 27) {
+                const float4 a0 = px[item.y];
+                const int3 cc = cell_of(a0.x, a0.y, a0.z, grid[1]);
+                const int3 c = make_int3(cc.x + (lane % 3) - 1, cc.y + (lane / 3) % 3 - 1, cc.z + lane / 9 - 1);
+                want = pack_cell(c);
+                const uint32_t nbk = bucket_of(c, mask);
+                j0 = bstart[nbk];
+                j1 = bend[nbk];
+                if (j1 > j0) {
+                    if (bmix[nbk]) check = 1;
+                    else if (cell[j0] != want) j1 = j0;
                 }
             }
-            const uint32_t staged = TILE_CAP - room;
-            if (staged > 0) {
-                if (threadIdx.x == 0) {
-                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                    const uint32_t bytes = staged * (FORCE ? 48u : 32u);
-                    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(&bar)),
-                                 "r"(bytes)
-                                 : "memory");
-                    uint32_t off = 0;
-                    int s = s_from;
-                    uint32_t r = r_from;
-                    while (off < staged) {
-                        const uint32_t take = min(seg[s].cnt - r, staged - off);
-                        if (take) {
-                            const uint32_t j = seg[s].j0 + r;
-                            bulk_g2s(tA + off, px + j, take * 16u, &bar);
-                            if (FORCE) {
-                                bulk_g2s(tB + off, pv + j, take * 16u, &bar);
-                                bulk_g2s(tC + off, pd + j, take * 16u, &bar);
-                            } else {
-                                bulk_g2s(tB + off, ph + j, take * 16u, &bar);
-                            }
-                        }
-                        off += take;
-                        r += take;
-                        if (r == seg[s].cnt) {
-                            s++;
-                            r = 0;
-                        }
+            for (int t = 0; t < 27; t++) {
+                const uint32_t s0 = __shfl_sync(0xffffffffu, j0, t);
+                const uint32_t s1 = __shfl_sync(0xffffffffu, j1, t);
+                if (s0 == s1) continue;
+                const uint32_t chk = __shfl_sync(0xffffffffu, check, t);
+                const uint64_t wt = __shfl_sync(0xffffffffu, want, t);
+#pragma unroll 2
+                for (uint32_t j = s0; j < s1; j++) {
+                    if (chk && cell[j] != wt) continue;
+                    const float4 q = px[j];
+                    if (!FORCE) {
+                        density_pair(a, hi, q, ph[j].x, o0, count);
+                    } else {
+                        const float4 vj = pv[j], dj = pd[j];
+                        if (j != k) force_pair(a, hi, di, vi, q, vj, dj, alpha, beta, o0, o1, o2, o3);
                     }
                 }
-                if (!bar_wait(&bar, phase)) {
-                    if (threadIdx.x == 0) atomicOr(d_status, SFGPU_STATUS_SPIN);
-                    failed = true;
-                    bar_wait(&bar, phase);  // let copies in flight land before the block moves on
-                }
-                phase ^= 1u;
-                if (!failed) {
-                    // run the staged records segment by segment
-                    uint32_t off = 0;
-                    int s = s_from;
-                    uint32_t r = r_from;
-                    while (off < staged) {
-                        const uint32_t take = min(seg[s].cnt - r, staged - off);
-                        const uint32_t j0 = seg[s].j0 + r;
-                        const bool check = seg[s].check;
-                        const uint64_t want = seg[s].want;
-                        for (uint32_t e = 0; e < take; e++) {
-                            const uint32_t j = j0 + e;
-                            if (check && cell[j] != want) continue;
-                            const float4 qa = tA[off + e];
-                            const float4 qb = tB[off + e];
-#pragma unroll
-                            for (int q = 0; q < TILE_MAXB; q++) {
-                                if (threadIdx.x + q * TILE_THREADS >= nb) break;
-                                if (!FORCE) {
-                                    density_pair(a[q], hi[q], qa, qb.x, o0[q], cnt_b[q]);
-                                } else if (j != c0 + threadIdx.x + q * TILE_THREADS) {
-                                    force_pair(a[q], hi[q], di[q], vi[q], qa, qb, tC[off + e], alpha, beta, o0[q],
-                                               o1[q], o2[q], o3[q]);
-                                }
-                            }
-                        }
-                        off += take;
-                        r += take;
-                        if (r == seg[s].cnt) {
-                            s++;
-                            r = 0;
-                        }
-                    }
-                }
-                __syncthreads();  // the tile is free for the next chunk
-            }
-            s_from = s_to;
-            r_from = r_to;
-            if (staged == 0) break;
-        }
-        if (!failed) {
-#pragma unroll
-            for (int q = 0; q < TILE_MAXB; q++) {
-                const uint32_t k = c0 + threadIdx.x + q * TILE_THREADS;
-                if (k < c1) finish_body<FORCE>(k, n, gamma, ph, V, pd, slab, dudt, nbr, o0[q], o1[q], o2[q], o3[q],
-                                               cnt_b[q]);
             }
         }
-        __syncthreads();
+        if (live) finish_body<FORCE>(k, n, gamma, ph, V, pd, slab, dudt, nbr, o0, o1, o2, o3, count);
     }
 }
 
-// Occupied buckets as work items, and buckets that hold more than one cell.
+// Work items (bucket, first body) for every 32-body slice of every occupied
+// bucket, and the buckets that hold more than one cell.
 __global__ void k_bucket_items(const uint64_t* __restrict__ keys, uint32_t n, const uint32_t* __restrict__ bstart,
-                               const uint64_t* __restrict__ cell, uint32_t* __restrict__ bmix,
-                               uint32_t* __restrict__ items, uint32_t* __restrict__ nitems) {
+                               const uint32_t* __restrict__ bend, const uint64_t* __restrict__ cell,
+                               uint32_t* __restrict__ bmix, uint2* __restrict__ items, uint32_t* __restrict__ nitems) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const uint32_t b = (uint32_t)keys[k];
     const uint32_t s = bstart[b];
-    if (k == s) items[atomicAdd(nitems, 1u)] = b;
-    else if (cell[k] != cell[s]) bmix[b] = 1u;
+    if (((k - s) & 31u) == 0) items[atomicAdd(nitems, 1u)] = make_uint2(b, k);
+    if (k != s && cell[k] != cell[s]) bmix[b] = 1u;
+    (void)bend;
 }
 
 }  // namespace
@@ -505,7 +393,7 @@ int sf_sph_cubic_alloc(sfgpu_sim* s) {
     SF_CUDA(cudaMalloc(&w->pd, sizeof(float4) * n));
     SF_CUDA(cudaMalloc(&w->ph, sizeof(float4) * n));
     SF_CUDA(cudaMalloc(&w->bmix, sizeof(uint32_t) * w->tsize));
-    SF_CUDA(cudaMalloc(&w->items, sizeof(uint32_t) * n));
+    SF_CUDA(cudaMalloc(&w->items, sizeof(uint2) * n));
     SF_CUDA(cudaMalloc(&w->counters, sizeof(uint32_t) * 4));
     SF_CUDA(cudaMalloc(&w->cell, sizeof(uint64_t) * n));
     SF_CUDA(cudaMalloc(&w->grid, sizeof(float) * 4 + sizeof(float) * n));
@@ -562,21 +450,31 @@ int sf_sph_cubic(sfgpu_sim* s) {
     k_cell_gather<<<nb, 256, 0, st>>>(w->keys, w->vals, n, s->slab, s->u, w->grid, w->bstart, w->bend, w->px, w->pv,
                                       w->cell, w->ph, gamma);
     SF_CHECK_LAUNCH();
-    k_bucket_items<<<nb, 256, 0, st>>>(w->keys, n, w->bstart, w->cell, w->bmix, w->items, w->counters);
+    k_bucket_items<<<nb, 256, 0, st>>>(w->keys, n, w->bstart, w->bend, w->cell, w->bmix, w->items, w->counters);
     SF_CHECK_LAUNCH();
     s->timer.end(st, tk);
     uint32_t* nbr = sf_sph_neighbour_counts(s);
-    const uint32_t tb = (uint32_t)sf_num_sms() * 4u;
+    const uint32_t tb = (uint32_t)sf_num_sms() * 8u;  // persistent warps, up to 8 blocks of 4 per SM
+    const bool warp_path = s->p.sph_path == 1;
+    const uint32_t bb = sf_ceil_div(n, 128);
     tk = s->timer.begin(st, "sph_density");
-    k_cubic_tiles<false><<<tb, TILE_THREADS, sizeof(float4) * 2 * TILE_CAP, st>>>(
-        n, w->grid, mask, w->bstart, w->bend, w->bmix, w->items, w->counters, w->counters + 1, w->px, w->ph, w->pv,
-        w->cell, w->pd, w->vals, gamma, alpha, beta, s->slab, s->dudt, nbr, s->d_status);
+    if (warp_path)
+        k_cubic_cells<false><<<tb, WARP_BLOCK, 0, st>>>(n, w->grid, mask, w->bstart, w->bend, w->bmix, w->items,
+                                                        w->counters, w->counters + 1, w->px, w->ph, w->pv, w->cell,
+                                                        w->pd, w->vals, gamma, alpha, beta, s->slab, s->dudt, nbr);
+    else
+        k_cubic_body<false><<<bb, 128, 0, st>>>(n, w->grid, mask, w->bstart, w->bend, w->px, w->ph, w->pv, w->cell,
+                                                w->pd, w->vals, gamma, alpha, beta, s->slab, s->dudt, nbr);
     SF_CHECK_LAUNCH();
     s->timer.end(st, tk);
     tk = s->timer.begin(st, "sph_force");
-    k_cubic_tiles<true><<<tb, TILE_THREADS, sizeof(float4) * 3 * TILE_CAP, st>>>(
-        n, w->grid, mask, w->bstart, w->bend, w->bmix, w->items, w->counters, w->counters + 2, w->px, w->ph, w->pv,
-        w->cell, w->pd, w->vals, gamma, alpha, beta, s->slab, s->dudt, nbr, s->d_status);
+    if (warp_path)
+        k_cubic_cells<true><<<tb, WARP_BLOCK, 0, st>>>(n, w->grid, mask, w->bstart, w->bend, w->bmix, w->items,
+                                                       w->counters, w->counters + 2, w->px, w->ph, w->pv, w->cell,
+                                                       w->pd, w->vals, gamma, alpha, beta, s->slab, s->dudt, nbr);
+    else
+        k_cubic_body<true><<<bb, 128, 0, st>>>(n, w->grid, mask, w->bstart, w->bend, w->px, w->ph, w->pv, w->cell,
+                                               w->pd, w->vals, gamma, alpha, beta, s->slab, s->dudt, nbr);
     SF_CHECK_LAUNCH();
     s->timer.end(st, tk);
     return SFGPU_OK;

@@ -23,11 +23,11 @@
 // k begins a level-L run (key[k-1] differs in the first L digits) and
 // key[k+leaf_cap] shares those L digits; an exclusive scan of the per-position
 // counts numbers the split nodes in depth-first (pre)order, and a split node s
-// owns nodes 1+8s .. 8+8s for its octants; (5) monopoles come from an FP64
-// exclusive prefix sum of (m x, m y, m z, m) over the sorted bodies.
+// owns nodes 1+8s .. 8+8s for its octants; (5) monopoles come from FP64
+// sums of (m x, m y, m z, m), built from the leaves up to the root.
 //
 // Work per body: key pass reads 12 B and writes 12 B; 7 sort passes move
-// 12 B each way; the gather reads 16 B (random) and writes 16 B + 32 B FP64.
+// 12 B each way; the gather reads 16 B (random) and writes 16 B.
 #include <algorithm>
 
 #include "internal.cuh"
@@ -506,43 +506,60 @@ __global__ void __launch_bounds__(FILL_THREADS) k_split_fill(const uint64_t* __r
     write_node(nd, 1u + 8u * s + o, cc, cnt, fc, self, cstart, third);
 }
 
-__global__ void k_gather(const uint32_t* __restrict__ V, uint32_t n, const uint32_t* __restrict__ nin_p,
-                         const float* __restrict__ pos, const float* __restrict__ mas, float4* __restrict__ sp,
-                         sfd4* __restrict__ msum) {
+__global__ void k_gather(const uint32_t* __restrict__ V, uint32_t n, const float* __restrict__ pos,
+                         const float* __restrict__ mas, float4* __restrict__ sp) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const uint32_t p = V[k];
-    const float x = pos[3u * p], y = pos[3u * p + 1u], z = pos[3u * p + 2u], m = mas[p];
-    sp[k] = make_float4(x, y, z, m);
-    if (k < *nin_p) {
-        const double md = m;
-        msum[k] = mk_d4(md * (double)x, md * (double)y, md * (double)z, md);
-    } else {
-        msum[k] = mk_d4(0, 0, 0, 0);
-    }
+    sp[k] = make_float4(pos[3u * p], pos[3u * p + 1u], pos[3u * p + 2u], mas[p]);
 }
 
-// tree.c:346-354 (centre of mass = sum(m x) / sum(m)), from FP64 prefix sums
-__global__ void k_monopoles(const uint32_t* __restrict__ nsplit_p, uint32_t split_cap, NodeArrays nd,
-                            const sfd4* __restrict__ pre) {
-    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t nn = 1u + 8u * min(*nsplit_p, split_cap);
-    if (v >= nn) return;
-    const uint32_t cnt = __float_as_uint(nd.hi[v].z);
-    const uint32_t s = nd.start[v];
-    float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
-    sfd4 d = mk_d4(0, 0, 0, 0);
-    if (cnt) {
-        const sfd4 a = pre[s], b = pre[s + cnt];
-        d = mk_d4(b.x - a.x, b.y - a.y, b.z - a.z, b.w - a.w);
-        if (d.w > 0.0) {
-            const double inv = 1.0 / d.w;
-            out = make_float4((float)(d.x * inv), (float)(d.y * inv), (float)(d.z * inv), (float)d.w);
-        } else {
-            out = make_float4((float)d.x, (float)d.y, (float)d.z, (float)d.w);
-        }
+// tree.c:346-354 (centre of mass = sum(m x) / sum(m)), with FP64 sums built
+// bottom-up in one launch: a thread per leaf sums its bodies (sorted order),
+// then climbs: the last of a node's 8 children to finish (an arrival counter
+// per node) sums the 8 children's totals in octant order and goes on to the
+// parent.  The order of every addition is fixed by the tree, not by which
+// thread arrives last.
+__device__ __forceinline__ void put_monopole(NodeArrays& nd, sfd4* nsum, uint32_t v, const sfd4& d) {
+    nsum[v] = d;
+    float4 out = make_float4((float)d.x, (float)d.y, (float)d.z, (float)d.w);
+    if (d.w > 0.0) {
+        const double inv = 1.0 / d.w;
+        out = make_float4((float)(d.x * inv), (float)(d.y * inv), (float)(d.z * inv), (float)d.w);
     }
     nd.com[v] = out;
+}
+
+__global__ void k_monopoles_up(const uint32_t* __restrict__ nsplit_p, uint32_t split_cap, NodeArrays nd,
+                               const float4* __restrict__ sp, sfd4* __restrict__ nsum, uint32_t* __restrict__ arrive) {
+    uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nn = 1u + 8u * min(*nsplit_p, split_cap);
+    if (v >= nn) return;
+    const float4 H = nd.hi[v];
+    if (__float_as_uint(H.w) != NODE_NONE) return;  // internal: its last child finishes it
+    const uint32_t cnt = __float_as_uint(H.z), s = nd.start[v];
+    sfd4 d = mk_d4(0, 0, 0, 0);
+    for (uint32_t k = 0; k < cnt; k++) {
+        const float4 b = sp[s + k];
+        const double m = b.w;
+        d = mk_d4(d.x + m * (double)b.x, d.y + m * (double)b.y, d.z + m * (double)b.z, d.w + m);
+    }
+    put_monopole(nd, nsum, v, d);
+    while (v != 0u) {
+        const uint32_t p = nd.parent[v];
+        __threadfence();
+        if (atomicAdd(&arrive[p], 1u) != 7u) return;
+        __threadfence();
+        const uint32_t fc = __float_as_uint(__ldcg(&nd.hi[p].w));
+        sfd4 t = mk_d4(0, 0, 0, 0);
+        for (uint32_t o = 0; o < 8u; o++) {
+            const double* q = reinterpret_cast<const double*>(&nsum[fc + o]);  // from L2, not a stale L1 line
+            const sfd4 c = mk_d4(__ldcg(q), __ldcg(q + 1), __ldcg(q + 2), __ldcg(q + 3));
+            t = mk_d4(t.x + c.x, t.y + c.y, t.z + c.z, t.w + c.w);
+        }
+        put_monopole(nd, nsum, p, t);
+        v = p;
+    }
 }
 
 // ---- reference-order monopoles (EXACT arithmetic) ----------------------------
@@ -663,11 +680,10 @@ int sf_tree_alloc(TreeWork** out, uint32_t n, const sfgpu_params& p) {
     SF_CUDA(cudaMalloc(&t->nd.parent, sizeof(uint32_t) * nodes));
     SF_CUDA(cudaMalloc(&t->nd.start, sizeof(uint32_t) * nodes));
     SF_CUDA(cudaMalloc(&t->sp, sizeof(float4) * nn));
-    SF_CUDA(cudaMalloc(&t->msum, sizeof(sfd4) * nn));
-    SF_CUDA(cudaMalloc(&t->mpre, sizeof(sfd4) * (nn + 1)));
+    SF_CUDA(cudaMalloc(&t->nsum, sizeof(sfd4) * nodes));
+    SF_CUDA(cudaMalloc(&t->arrive, sizeof(uint32_t) * nodes));
     SF_CUDA(cudaMalloc(&t->walk_part, sizeof(float4) * sf_walk_scratch_floats4((uint32_t)nn)));
     if (sf_scan_reserve(t->scan_u32, (uint32_t)nn, sizeof(uint32_t)) != SFGPU_OK) return SFGPU_FAILURE;
-    if (sf_scan_reserve(t->scan_d4, (uint32_t)nn, sizeof(sfd4)) != SFGPU_OK) return SFGPU_FAILURE;
     return SFGPU_OK;
 }
 
@@ -696,10 +712,9 @@ void sf_tree_free(TreeWork* t) {
     cudaFree(t->nd.start);
     cudaFree(t->sp);
     cudaFree(t->walk_part);
-    cudaFree(t->msum);
-    cudaFree(t->mpre);
+    cudaFree(t->nsum);
+    cudaFree(t->arrive);
     cudaFree(t->scan_u32.partials);
-    cudaFree(t->scan_d4.partials);
     delete t;
 }
 
@@ -758,7 +773,7 @@ int sf_tree_build(sfgpu_sim* s) {
     SF_CHECK_LAUNCH();
     s->timer.end(st, tk);
     tk = s->timer.begin(st, "tree_monopoles");
-    k_gather<<<nb, 256, 0, st>>>(t->vals, n, nin, pos, mas, t->sp, t->msum);
+    k_gather<<<nb, 256, 0, st>>>(t->vals, n, pos, mas, t->sp);
     SF_CHECK_LAUNCH();
     const uint32_t mb = sf_ceil_div(1u + 8u * t->split_cap, 256);
     if (s->p.math == SFGPU_MATH_EXACT && s->p.form == SFGPU_FORM_PLAIN) {
@@ -771,8 +786,8 @@ int sf_tree_build(sfgpu_sim* s) {
             SF_CHECK_LAUNCH();
         }
     } else {
-        if (sf_scan_d4(t->msum, t->mpre, n, t->scan_d4, st) != SFGPU_OK) return SFGPU_FAILURE;
-        k_monopoles<<<mb, 256, 0, st>>>(nsplit, t->split_cap, t->nd, t->mpre);
+        SF_CUDA(cudaMemsetAsync(t->arrive, 0, sizeof(uint32_t) * (1u + 8u * (size_t)t->split_cap), st));
+        k_monopoles_up<<<mb, 256, 0, st>>>(nsplit, t->split_cap, t->nd, t->sp, t->nsum, t->arrive);
         SF_CHECK_LAUNCH();
     }
     s->timer.end(st, tk);

@@ -41,9 +41,9 @@ struct TreeWork {
     uint32_t* ordB = nullptr;
     NodeArrays nd;
     float4* sp = nullptr;       // sorted bodies (x, y, z, m)
-    sfd4* msum = nullptr;    // (m x, m y, m z, m) per sorted slot, FP64
-    sfd4* mpre = nullptr;    // exclusive prefix of msum (n+1)
-    ScanWork scan_u32, scan_d4;
+    sfd4* nsum = nullptr;        // FP64 (m x, m y, m z, m) per node
+    uint32_t* arrive = nullptr;  // children finished, per node (bottom-up sums)
+    ScanWork scan_u32;
     float4* walk_part = nullptr;  // split-walk partial sums (SPLIT x n)
 };
 

@@ -79,8 +79,9 @@ def _cubic_sim(sf, n, pos, vel, mas, rad, u, **kw):
     return s
 
 
+@pytest.mark.parametrize("path", [0, 1])
 @pytest.mark.parametrize("n,hvar", [(4096, False), (3000, True)])
-def test_sph_cubic_vs_fp64_oracle(sf, oracle64, n, hvar):
+def test_sph_cubic_vs_fp64_oracle(sf, oracle64, n, hvar, path):
     """Cubic-spline SPH: neighbour sets bit-identical to the brute-force FP32
     enumeration; rho, dv/dt, du/dt within 1e-5 / 1e-4 of the FP64 oracle."""
     from starflood_gb300.ics import plummer
@@ -91,7 +92,7 @@ def test_sph_cubic_vs_fp64_oracle(sf, oracle64, n, hvar):
         rad[::5] = 0.07
     u = np.full(n, 0.05, np.float32)
     u[::3] = 0.08
-    with _cubic_sim(sf, n, pos, vel, mas, rad, u) as s:
+    with _cubic_sim(sf, n, pos, vel, mas, rad, u, sph_path=path) as s:
         s.gravity_part()
         s.sync()
         grav = slab_views(s.download(), n, 16)["acc"].copy()

@@ -194,6 +194,31 @@ def test_tree_fast_large(sf, oracle32, n, seed, split):
     assert rel_l2(v["pot"], pt) < 1e-5
 
 
+@pytest.mark.parametrize("leaf", [16, 4])
+def test_tree_other_leaf_capacity(sf, oracle32, leaf):
+    """Leaf capacities other than the reference's 8 (its node_t holds 8
+    bodies, so these are checked against the restatement only): the same
+    cells, per-body interaction counts identical, forces within 1e-5."""
+    from starflood_gb300.ics import uniform_ball
+    n = 20000
+    pos, vel, mas = uniform_ball(n, seed=31)
+    p = sf.default_params(solver=sf.SOLVER_TREE, eps=0.01, theta=0.5, flags=sf.FLAG_STATS, leaf_cap=leaf)
+    with sf.Sim(n, p) as s:
+        s.set_state(pos, vel, mas)
+        s.solve(3)
+        assert s.status() == 0
+        v = slab_views(s.download(), n, 13)
+        ni, no = s.walk_stats()
+        nn = s.num_nodes()
+    op = make_params(eps=0.01, theta=0.5, use_tree=1, leaf_cap=leaf)
+    st, nodes = oracle32.tree_build(pos, mas, oracle32.root_bounds(pos, 3), op)
+    assert st == 0 and nn == len(nodes)
+    a, pt, stats = oracle32.walk(pos, mas, nodes, op)
+    np.testing.assert_array_equal(ni, stats[:, 0])
+    assert rel_l2(v["acc"], a) < 1e-5
+    assert rel_l2(v["pot"], pt) < 1e-5
+
+
 def test_tree_run_graph_matches_eager(sf):
     from starflood_gb300.ics import uniform_ball
     n = 8192
