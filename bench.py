@@ -306,6 +306,27 @@ def gpu_pp(sf, reps=2, n=N_PP):
     return out
 
 
+def pp_energy_drift(sf, steps=20):
+    """Relative drift of the corrected total energy (kinetic + pair potential,
+    FP64 sums) over `steps` KDK steps at dt = 1e-3 of the N = 1,048,576
+    Plummer sphere, plain FP32 state against the compensated form (FP64
+    state, compensated forces)."""
+    from starflood_gb300.ics import plummer
+    pos, vel, mas = plummer(N_PP, seed=5)
+    out = {"steps": steps}
+    for name, form in (("plain", sf.FORM_PLAIN), ("compensated", sf.FORM_COMPENSATED)):
+        p = sf.default_params(solver=sf.SOLVER_PP, eps=0.005, dt=1e-3, form=form)
+        with sf.Sim(N_PP, p) as s:
+            s.set_state(pos, vel, mas)
+            s.solve(0)
+            s.run(0, 1)
+            e0 = s.energies_corrected()[2]
+            s.run(1, steps - 1)
+            e1 = s.energies_corrected()[2]
+        out[name] = {"E_first": e0, "E_last": e1, "relative_drift": abs(e1 - e0) / abs(e0)}
+    return out
+
+
 def pp_accuracy(sf):
     """Force error of plain vs compensated against the FP64 oracle on a seeded
     8192-body subsample of the N=1,048,576 Plummer sphere (i in the sample,
@@ -741,6 +762,10 @@ def main():
                 pp["force_error_vs_fp64"] = pp_accuracy(sf)
             except Exception as e:
                 pp["force_error_vs_fp64"] = {"error": str(e)}
+            try:
+                pp["energy_drift_20_steps"] = pp_energy_drift(sf)
+            except Exception as e:
+                pp["energy_drift_20_steps"] = {"error": str(e)}
             for k in ("plain", "compensated"):
                 ips = pp[k]["interactions_per_s"]
                 pp[k]["roofline_frac"] = ips * FLOP_INTERACTION / (peak * 1e12)

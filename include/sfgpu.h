@@ -220,6 +220,12 @@ int sfgpu_flush_l2(void* stream);
  * the device status word (cleared), with a single host synchronisation. */
 int sfgpu_host_step(sfgpu_sim* s, float* slab, uint32_t step_number, int solve_only, uint32_t* status);
 
+/* initcond_generate (src/initcond.c:11-255) on the device: the reference's
+ * default initial conditions (uniform unit ball, its mass formula, Gaussian
+ * speeds of 1e-4 plus a 4e-3 sqrt(8 pi G / 3) expansion, rad 0.1 with SPH)
+ * written into the device slab (pos, vel, mas, rad), queued on the stream. */
+int sfgpu_initcond(sfgpu_sim* s);
+
 /* ---- snapshots (src/simulation_io.c:16-149, the raw format) --------------- */
 /* The raw format is the slab itself, N*dof floats with no header, as
  * sim_save_raw / sim_read_raw write and read it.  sfgpu_save_raw snapshots

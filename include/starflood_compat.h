@@ -78,6 +78,10 @@ real* sim_find(const sim_t* sim, enum sim_conf parameter);
 int sim_init(sim_t* sim, unsigned int N);
 /* src/simulation.c:189-228 */
 int sim_free(sim_t* sim);
+/* src/initcond.c:11-255: the reference's default initial conditions,
+ * generated on the GPU; the host arrays are current on return. */
+int initcond_generate(sim_t* sim);
+
 /* src/visualization.h:10-27 */
 typedef enum { IMAGE_FILETYPE_PFM, IMAGE_FILETYPE_PPM, IMAGE_FILETYPE_PNG, NUM_IMAGE_FILETYPE } image_filetype_t;
 typedef struct {

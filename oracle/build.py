@@ -126,7 +126,7 @@ def build_reference(names: list[str] | None = None, force: bool = False) -> list
                 f.write(text)
         units = ["simulation", "gravity", "sph", "log", "grid"] + (["tree"] if v["tree"] else [])
         if not v["fp64"]:
-            units += ["simulation_io", "visualization", "visualization_io"]  # raw snapshots, vis_draw, images
+            units += ["simulation_io", "visualization", "visualization_io", "initcond"]  # I/O, vis, ICs
         srcs = [os.path.join(REFERENCE_SRC, u + ".c") for u in units]
         out = os.path.join(REF_OUT, "libref_%s.so" % name)
         outs.append(out)

@@ -681,3 +681,52 @@ void orc_vis_draw(uint32_t n, const float* pos, const float* vel, const float* p
         render[4 * k + 3] = 1.0f;
     }
 }
+
+/* ---- initcond.c:11-255: initcond_generate ------------------------------- */
+#define ORC_PI_4_3 4.18879020478639098461685784437267051226289253250014
+#define ORC_PI_8_3 8.37758040957278196923371568874534102452578506500028
+#define ORC_INV_PCG 2.3283062977608182109179324470460414886474609375e-10
+
+static void orc_unit_direction(uint32_t a, uint32_t b, double* x, double* y, double* z) {
+    const double r0 = ORC_INV_PCG * (double)a, r1 = ORC_INV_PCG * (double)b;
+    const double phi = ORC_TAU * r0, the = acos(2.0 * r1 - 1.0);
+    const double cp = cos(phi), sp = sin(phi), ct = cos(the), st = sin(the);
+    *x = cp * st;
+    *y = sp * st;
+    *z = ct;
+}
+
+void orc_initcond(uint32_t n, double G, float* pos, float* vel, float* mas, float* rad) {
+    const double radius = 1.000;
+    const double volume = ORC_PI_4_3 * (radius * radius);
+    const double body_mass = volume / (double)n;
+    for (uint32_t i = 0; i < n; i++) {
+        mas[i] = (float)body_mass;
+        if (rad) rad[i] = 0.100f;
+        uint32_t s[4] = {0xD88D5EFDu + i, 0x203F83D3u, 0x710BE493u, 0xA294E7F1u};
+        orc_pcg4d(s);
+        double p[3];
+        orc_unit_direction(s[0], s[1], &p[0], &p[1], &p[2]);
+        const double r2 = ORC_INV_PCG * (double)s[2];
+        for (int k = 0; k < 3; k++) pos[3u * i + (uint32_t)k] = (float)(p[k] * (radius * cbrt(r2)));
+    }
+    for (uint32_t i = 0; i < n; i++) {
+        const double p[3] = {pos[3u * i], pos[3u * i + 1u], pos[3u * i + 2u]};
+        uint32_t s[4] = {0x4AFDC7CFu + i, 0xAE8D7CF2u, 0xE4827F00u, 0xE44CA389u};
+        orc_pcg4d(s);
+        double r[4];
+        for (int k = 0; k < 4; k++) r[k] = ORC_INV_PCG * (double)s[k];
+        double g[3] = {sqrt(-2.0 * log(r[0])) * cos(ORC_TAU * r[1]), sqrt(-2.0 * log(r[0])) * sin(ORC_TAU * r[1]),
+                       sqrt(-2.0 * log(r[2])) * cos(ORC_TAU * r[3])};
+        for (int k = 0; k < 3; k++) g[k] *= 1.000e-4;
+        const double speed = sqrt((g[0] * g[0]) + (g[1] * g[1]) + (g[2] * g[2]));
+        orc_pcg4d(s);
+        double v[3];
+        orc_unit_direction(s[0], s[1], &v[0], &v[1], &v[2]);
+        for (int k = 0; k < 3; k++) {
+            v[k] *= speed;
+            v[k] += 4.000e-3 * sqrt(ORC_PI_8_3 * G) * p[k];
+            vel[3u * i + (uint32_t)k] = (float)v[k];
+        }
+    }
+}

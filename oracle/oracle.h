@@ -103,6 +103,12 @@ void orc_sph_cubic(uint32_t n, const float* pos, const float* vel, const float* 
                    const float* u, double gamma, double alpha, double beta, double* rho, double* prs,
                    double* acc, double* dudt, uint32_t* nbr);
 
+/* initcond_generate (src/initcond.c:11-255), FP64 with the host libm:
+ * uniform unit ball from pcg4d, mass (4/3) pi / N (the reference's radius^2
+ * formula at radius 1), Gaussian speeds (sigma 1e-4) plus the expansion
+ * 4e-3 sqrt(8 pi G / 3) x; rad (may be NULL) = 0.1. */
+void orc_initcond(uint32_t n, double G, float* pos, float* vel, float* mas, float* rad);
+
 /* vis_draw's splat rasteriser (src/visualization.c:258-740) on FP32 state:
  * mean radius (FP64 Kahan), camera matrix at time = timestep * step,
  * `samples` pcg4d-jittered Gaussian splats per body added to the int32 RGBA

@@ -70,6 +70,7 @@ class Oracle:
         fp, dp = C.POINTER(C.c_float), C.POINTER(C.c_double)
         L.orc_sph_cubic.argtypes = [C.c_uint32, fp, fp, fp, fp, fp, C.c_double, C.c_double, C.c_double,
                                     dp, dp, dp, dp, u32p]
+        L.orc_initcond.argtypes = [C.c_uint32, C.c_double, fp, fp, fp, fp]
         L.orc_vis_draw.argtypes = [C.c_uint32, fp, fp, fp, C.c_uint32, C.c_double, C.c_uint32, C.c_uint32,
                                    C.c_uint32, C.c_double, C.c_double, C.c_int, C.c_int,
                                    C.POINTER(C.c_int32), fp]
@@ -158,6 +159,17 @@ class Oracle:
                                    prs.ctypes.data_as(self._rp), acc.ctypes.data_as(self._rp),
                                    nbr.ctypes.data_as(u32p))
         return rho, prs, acc, nbr
+
+    def initcond(self, n, G=1.0, sph=False):
+        """initcond_generate (src/initcond.c:11-255): (pos (n,3), vel (n,3), mas, rad or None)."""
+        pos = np.zeros((n, 3), np.float32)
+        vel = np.zeros((n, 3), np.float32)
+        mas = np.zeros(n, np.float32)
+        rad = np.zeros(n, np.float32) if sph else None
+        fp = C.POINTER(C.c_float)
+        self.lib.orc_initcond(n, G, pos.ctypes.data_as(fp), vel.ctypes.data_as(fp), mas.ctypes.data_as(fp),
+                              rad.ctypes.data_as(fp) if sph else None)
+        return pos, vel, mas, rad
 
     def vis_draw(self, pos, vel, pot, step, timestep, sizex, sizey, samples=128, exposure=-1.0,
                  ortho_scale=-1.0, autoscale=1, tonemap=1):
@@ -294,6 +306,10 @@ class Reference:
         render = np.ascontiguousarray(render, np.float32)
         sizey, sizex = render.shape[:2]
         return self.lib.refh_vis_save(render.ctypes.data, sizex, sizey, filename.encode(), 1)
+
+    def initcond(self):
+        """src/initcond.c initcond_generate on the current simulation (FP32 variants)."""
+        return self.lib.refh_initcond()
 
     def save_raw(self, filename):
         """src/simulation_io.c:81-149 (FP32 variants)."""

@@ -16,6 +16,7 @@
 #include "gravity.h"
 #include "sph.h"
 #ifndef STARFLOOD_DOUBLE_PRECISION
+#include "initcond.h"
 #include "visualization.h"
 #endif
 #ifdef ENABLE_TREE
@@ -140,6 +141,9 @@ int refh_walk(void) { return solve_gravity_part_tree(&g_sim); }
 /* src/simulation_io.c:16-149 on the harness's simulation (FP32 builds; the
  * FP64 build of simulation_io.c does not compile) */
 int refh_save_raw(const char* filename) { return sim_save_raw(&g_sim, filename); }
+
+/* src/initcond.c:11-255 on the harness's simulation */
+int refh_initcond(void) { return initcond_generate(&g_sim); }
 
 /* src/visualization_io.c:170-330: vis_save of a given render buffer (the
  * binary buffer is sized for the configured VIS_FILE_FORMAT, 8-bit here,

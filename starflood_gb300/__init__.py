@@ -103,6 +103,8 @@ def lib():
             "sfgpu_host_unregister": (i32, [vp]),
             "sfgpu_flush_l2": (i32, [vp]),
             "sfgpu_save_raw": (i32, [vp, C.c_char_p]),
+            "sfgpu_initcond": (i32, [vp]),
+            "sfgpu_host_step": (i32, [vp, vp, u32, i32, u32p]),
             "sfgpu_vis_params_default": (None, [vp]),
             "sfgpu_vis_draw": (i32, [vp, vp, u32, u32, u32, vp, vp]),
             "sfgpu_vis_buffers_alloc": (i32, [u32, u32, C.POINTER(vp), C.POINTER(vp)]),
@@ -239,6 +241,10 @@ class Sim:
         if m < 0:
             raise SfgpuError(last_error())
         return {names[i].decode(): (ms[i], la[i]) for i in range(m)}
+
+    def initcond(self):
+        """initcond_generate (src/initcond.c) into the device slab."""
+        check(lib().sfgpu_initcond(self.h), "sfgpu_initcond")
 
     def save_raw(self, filename):
         """Queue a raw snapshot of the current state (written asynchronously)."""
@@ -387,7 +393,7 @@ def compat_functions():
                        ("solve_gravity_part_part", [S]), ("solve_gravity_part_tree", [S]), ("solve_sph", [S]),
                        ("tree_init", [T, C.c_uint]), ("tree_free", [T]),
                        ("sim_save_raw", [S, C.c_char_p]), ("sim_read_raw", [S, C.c_char_p]),
-                       ("vis_init", [V, C.c_uint, C.c_uint]), ("vis_free", [V]),
+                       ("vis_init", [V, C.c_uint, C.c_uint]), ("vis_free", [V]), ("initcond_generate", [S]),
                        ("vis_draw", [V, S]), ("vis_save", [V, C.c_char_p, C.c_int]),
                        ("tree_build", [T, C.c_uint, C.c_void_p, C.c_void_p])):
         fn = getattr(L, name)

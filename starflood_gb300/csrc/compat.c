@@ -251,6 +251,18 @@ static int solv_common(sim_t* sim, int step) {
 int sim_solv(sim_t* sim) { return solv_common(sim, 0); }
 int sim_step(sim_t* sim) { return solv_common(sim, 1); }
 
+/* src/initcond.c:11-255 on the device, then the slab back to the host */
+int initcond_generate(sim_t* sim) {
+    sfgpu_sim* dev = dev_of(sim, "initcond_generate()");
+    if (!dev) return SFGPU_FAILURE;
+    if (sfgpu_upload(dev, (const float*)sim->mem) != SFGPU_OK || sfgpu_initcond(dev) != SFGPU_OK ||
+        sfgpu_download(dev, (float*)sim->mem) != SFGPU_OK) {
+        fail_msg("initcond_generate()");
+        return SFGPU_FAILURE;
+    }
+    return SFGPU_OK;
+}
+
 /* src/simulation_io.c:16-79.  The raw format is the slab itself.  As in the
  * reference, a short read is reported but not failed; the device copy
  * follows on the next call (every call uploads the host slab). */

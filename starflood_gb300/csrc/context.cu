@@ -304,6 +304,8 @@ static int refresh_fp64(sfgpu_sim* s) {
     return SFGPU_OK;
 }
 
+int sf_refresh_fp64(sfgpu_sim* s) { return refresh_fp64(s); }
+
 extern "C" int sfgpu_upload_arrays(sfgpu_sim* s, const float* slab, uint32_t first, uint32_t count) {
     sf_clear_error();
     if (!s || !slab || first + count > s->dof) {

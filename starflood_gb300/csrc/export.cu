@@ -28,7 +28,7 @@ __global__ void k_trigger(const uint32_t* __restrict__ nsplit_p, uint32_t split_
     if (warp >= ns) return;
     const uint32_t v = split_node[warp];
     const uint32_t s0 = nd.start[v];
-    const uint32_t cnt = __float_as_uint(nd.hi[v].z);
+    const uint32_t cnt = __float_as_uint(nd.hi[NODE_REC * v].z);
     uint32_t best[TOPK];
     int nb = 0;
     for (uint32_t a = lane; a < cnt; a += 32) {  // each lane keeps its cap+1 smallest
@@ -82,7 +82,7 @@ __global__ void k_export(uint32_t nn, NodeArrays nd, const uint32_t* __restrict_
     const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= nn) return;
     const uint32_t R = ref_id(v, rank);
-    const float4 Lo = nd.lo[v], H = nd.hi[v], C = nd.com[v];
+    const float4 Lo = nd.lo[NODE_REC * v], H = nd.hi[NODE_REC * v], C = nd.com[NODE_REC * v];
     const uint32_t cnt = __float_as_uint(H.z);
     const uint32_t first = __float_as_uint(H.w);
     parent[R] = v == 0 ? 0u : ref_id(nd.parent[v], rank);

@@ -47,7 +47,6 @@ __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b)
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
 __device__ __forceinline__ float fsqrt(float a) { return __fsqrt_rn(a); }
 
-// Kahan running sum (the idiom of src/gravity.c:521-533).
 // One MUFU instruction each (flush-to-zero): the force kernels call them on
 // r^2 + eps^2, which is positive and far above the subnormal range for any
 // eps > 0.
@@ -95,6 +94,7 @@ __device__ __forceinline__ void pp_pair_step(float2 sx, float2 sy, float2 sz, fl
     ph = __fadd2_rn(ph, mphi);
 }
 
+// Kahan running sum (the idiom of src/gravity.c:521-533).
 struct KSum {
     float s, c;
     __device__ __forceinline__ void add(float x) {
@@ -130,6 +130,53 @@ __device__ __forceinline__ void two_sumf(float a, float b, float& s, float& e) {
     const float bp = fsub(s, a);
     e = fadd(fsub(a, fsub(s, bp)), fsub(b, bp));
 }
+// Float-float numbers (hi + lo, about 48 significant bits) for sums that
+// need more than FP32 but should not run on GB300's FP64 pipe, which issues
+// about one FP64 operation per SM per cycle against 128 FP32.
+struct ff {
+    float hi, lo;
+};
+__device__ __forceinline__ ff ff_add(ff a, ff b) {
+    float s, e;
+    two_sumf(a.hi, b.hi, s, e);
+    e = fadd(e, fadd(a.lo, b.lo));
+    const float h = fadd(s, e);  // fast two-sum: |s| >= |e|
+    return ff{h, fsub(e, fsub(h, s))};
+}
+__device__ __forceinline__ ff ff_from(float v) { return ff{v, 0.0f}; }
+__device__ __forceinline__ ff ff_from_double(double v) {
+    const float h = (float)v;
+    return ff{h, (float)(v - (double)h)};
+}
+__device__ __forceinline__ double ff_to_double(ff a) { return (double)a.hi + (double)a.lo; }
+// x^2 exactly (two-product with one FMA)
+__device__ __forceinline__ ff ff_sqr(float x) {
+    const float p = fmul(x, x);
+    return ff{p, __fmaf_rn(x, x, -p)};
+}
+// square root of a float-float to about 46 bits: one Newton correction of
+// the FP32 root (the residual a - s^2 computed exactly with a two-product)
+__device__ __forceinline__ ff ff_sqrt(ff a) {
+    const float s = __fsqrt_rn(a.hi);
+    if (!(s > 0.0f)) return ff{s, 0.0f};
+    const float p = fmul(s, s), pe = __fmaf_rn(s, s, -p);
+    const float res = fadd(fsub(fsub(a.hi, p), pe), a.lo);
+    const float t = __fdiv_rn(res, fmul(2.0f, s));
+    const float h = fadd(s, t);
+    return ff{h, fsub(t, fsub(h, s))};
+}
+// warp sum (fixed order) of NV float-float values; lane 0 gets the totals
+template <int NV>
+__device__ __forceinline__ void ff_warp_sum(ff (&v)[NV]) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+            const ff w{__shfl_down_sync(0xffffffffu, v[k].hi, o), __shfl_down_sync(0xffffffffu, v[k].lo, o)};
+            v[k] = ff_add(v[k], w);
+        }
+}
+
 // double-double accumulate (hi, lo) += (b_hi, b_lo)
 __device__ __forceinline__ double2 dd_add(double2 a, double2 b) {
     double s, e;
@@ -195,8 +242,6 @@ int sf_scan_reserve(ScanWork& w, uint32_t n, size_t elem);
 int sf_scan_u32(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* d_total, ScanWork& w,
                 cudaStream_t st, const uint32_t* d_n = nullptr);
 // exclusive scan of n sfd4 values; out has n+1 entries (out[n] = total).
-int sf_scan_d4(const sfd4* in, sfd4* out, uint32_t n, ScanWork& w, cudaStream_t st,
-               const uint32_t* d_n = nullptr);
 
 // ---------------------------------------------------------------------------
 // radix sort of (u64 key, u32 value) pairs on the low `bits` key bits (sort.cu)
@@ -272,6 +317,7 @@ struct sfgpu_sim {
     void* vis = nullptr;                    // VisScratch (vis.cu)
 };
 void sf_snapshot_free(sfgpu_sim* s);
+int sf_refresh_fp64(sfgpu_sim* s);  // FP64 state (COMPENSATED) from the FP32 slab
 void sf_vis_free(sfgpu_sim* s);
 
 // stage entry points (each queues kernels on s->stream)

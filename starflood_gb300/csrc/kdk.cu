@@ -4,12 +4,13 @@
 //
 //   k_kick_drift   kick_0 and drift for one body per thread (each component
 //                  rounded exactly as the reference: v + ((dt/2) a), x + dt v)
-//                  and, for the tree, the body's FP64 distance from the origin
-//                  summed per block in double-double; the last block adds the
+//                  and, for the tree, the body's distance from the origin (to
+//                  FP64-like precision in float-float arithmetic) summed per
+//                  block; the last block adds the
 //                  block sums, takes the mean radius, hashes the step number
 //                  with pcg4d and writes the jittered root cube in FP32;
 //   k_kick_energy  kick_1, ken = (m/2) v^2, pen = m pot, per-block
-//                  double-double sums of ken, pen and the corrected energies,
+//                  float-float sums of ken, pen and the corrected energies,
 //                  added in block order by the last block.
 //
 // Bytes per body: kick/drift reads pos, vel, acc (36 B) and writes pos, vel
@@ -21,19 +22,17 @@ namespace {
 
 constexpr double K_INV_U32 = 2.3283062977608182109179324470460414886474609375e-10;  // rng.h:9
 
-// Fixed-order FP64 block sum (pairwise within each warp by shuffles, then
-// the warps in order); thread 0 writes the NV block totals.  Plain FP64 adds:
-// GB300's FP64 rate makes double-double arithmetic the bottleneck here.
+// Block sum of NV per-thread values in a fixed order: float-float within
+// each warp (shuffles), then the 8 warp totals in FP64 by thread 0, which
+// writes the NV block totals.  Only the last step touches the FP64 pipe.
 template <int NV>
-__device__ void block_sum(double (&v)[NV], double* out) {
+__device__ void block_sum(ff (&v)[NV], double* out) {
     __shared__ double wsum[NV][SF_RED_BLOCK / 32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    ff_warp_sum<NV>(v);
+    if (lane == 0)
 #pragma unroll
-    for (int k = 0; k < NV; k++) {
-        double x = v[k];
-        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-        if (lane == 0) wsum[k][warp] = x;
-    }
+        for (int k = 0; k < NV; k++) wsum[k][warp] = ff_to_double(v[k]);
     __syncthreads();
     if (threadIdx.x == 0) {
 #pragma unroll
@@ -45,10 +44,10 @@ __device__ void block_sum(double (&v)[NV], double* out) {
     }
 }
 
-__device__ __forceinline__ double radius64(float x, float y, float z) {
-    // simulation.c:253-260: sqrt((x*x)+(y*y)+(z*z)) in FP64
-    const double dx = x, dy = y, dz = z;
-    return __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+// simulation.c:253-260: sqrt((x*x)+(y*y)+(z*z)), the reference's FP64 value
+// to about 46 bits, in float-float arithmetic on the FP32 pipe
+__device__ __forceinline__ ff radius_ff(float x, float y, float z) {
+    return ff_sqrt(ff_add(ff_add(ff_sqr(x), ff_sqr(y)), ff_sqr(z)));
 }
 
 // The last block to finish (ticket from an atomic counter, reset for the
@@ -124,7 +123,7 @@ __global__ void __launch_bounds__(SF_RED_BLOCK) k_kick_drift(float* __restrict__
     float* pos = slab;
     float* vel = slab + (size_t)3 * n;
     const float* acc = slab + (size_t)6 * n;
-    double r[1] = {0.0};
+    ff r[1] = {ff{0.0f, 0.0f}};
     if (i < n) {
         float x[3];
 #pragma unroll
@@ -146,7 +145,7 @@ __global__ void __launch_bounds__(SF_RED_BLOCK) k_kick_drift(float* __restrict__
                 pos[k] = x[c];
             }
         }
-        if (want_radius) r[0] = radius64(x[0], x[1], x[2]);
+        if (want_radius) r[0] = radius_ff(x[0], x[1], x[2]);
     }
     if (!want_radius) return;
     block_sum<1>(r, part);
@@ -158,8 +157,8 @@ __global__ void __launch_bounds__(SF_RED_BLOCK) k_radius(const float* __restrict
                                                          const uint32_t* __restrict__ d_step,
                                                          float* __restrict__ bounds, double* __restrict__ sums) {
     const uint32_t i = blockIdx.x * SF_RED_BLOCK + threadIdx.x;
-    double r[1] = {0.0};
-    if (i < n) r[0] = radius64(pos[3u * i], pos[3u * i + 1u], pos[3u * i + 2u]);
+    ff r[1] = {ff{0.0f, 0.0f}};
+    if (i < n) r[0] = radius_ff(pos[3u * i], pos[3u * i + 1u], pos[3u * i + 2u]);
     block_sum<1>(r, part);
     if (last_block(done)) finish_bounds(part, n, d_step, bounds, sums);
 }
@@ -178,7 +177,7 @@ __global__ void __launch_bounds__(SF_RED_BLOCK) k_kick_energy(float* __restrict_
     const float* pot = slab + (size_t)10 * n;
     float* ken = slab + (size_t)11 * n;
     float* pen = slab + (size_t)12 * n;
-    double e[4] = {0.0, 0.0, 0.0, 0.0};
+    ff e[4] = {ff{0.f, 0.f}, ff{0.f, 0.f}, ff{0.f, 0.f}, ff{0.f, 0.f}};
     if (i < n) {
         float v[3];
         double v64[3];
@@ -203,15 +202,18 @@ __global__ void __launch_bounds__(SF_RED_BLOCK) k_kick_energy(float* __restrict_
         ken[i] = k_i;
         pen[i] = p_i;
         // corrected totals: kinetic term of the integrated dynamics and the
-        // pair potential without self terms, each pair once
-        const double v2d = v64[0] * v64[0] + v64[1] * v64[1] + v64[2] * v64[2];
-        const double kin = physical ? 0.5 * (double)m * v2d : 0.5 * v2d;
-        const double selfp = (double)g_over_eps * (double)m;  // G m_i / eps (the j = i term)
-        const double upair = 0.5 * (double)m * ((double)pot[i] + selfp);
-        e[0] = (double)k_i;
-        e[1] = (double)p_i;
-        e[2] = kin;
-        e[3] = upair;
+        // pair potential without self terms, each pair once (FP32 per body;
+        // FP64 velocities in the precision form)
+        if (vel64) {
+            const double v2d = v64[0] * v64[0] + v64[1] * v64[1] + v64[2] * v64[2];
+            e[2] = ff_from_double(physical ? 0.5 * (double)m * v2d : 0.5 * v2d);
+        } else {
+            e[2] = ff_from(physical ? fmul(fmul(0.5f, m), v2) : fmul(0.5f, v2));
+        }
+        const float selfp = fmul(g_over_eps, m);  // G m_i / eps (the j = i term)
+        e[3] = ff_from(fmul(fmul(0.5f, m), fadd(pot[i], selfp)));
+        e[0] = ff_from(k_i);
+        e[1] = ff_from(p_i);
     }
     block_sum<4>(e, part);
     if (last_block(done)) {

@@ -23,11 +23,11 @@
 // k begins a level-L run (key[k-1] differs in the first L digits) and
 // key[k+leaf_cap] shares those L digits; an exclusive scan of the per-position
 // counts numbers the split nodes in depth-first (pre)order, and a split node s
-// owns nodes 1+8s .. 8+8s for its octants; (5) monopoles come from FP64
-// sums of (m x, m y, m z, m), built from the leaves up to the root.
+// owns nodes 1+8s .. 8+8s for its octants; (5) monopoles come from exact
+// fixed-point prefix sums of (m x, m y, m z, m) over the sorted bodies.
 //
 // Work per body: key pass reads 12 B and writes 12 B; 7 sort passes move
-// 12 B each way; the gather reads 16 B (random) and writes 16 B.
+// 12 B each way; the gather reads 16 B (random) and writes 16 B + 32 B of fixed-point sums.
 #include <algorithm>
 
 #include "internal.cuh"
@@ -88,11 +88,17 @@ __device__ uint64_t descend(const float x[3], Cube c, uint64_t key, int from, ui
     return key;
 }
 
-__global__ void k_keys(const float* __restrict__ pos, uint32_t n, const float* __restrict__ bounds,
-                       uint64_t* __restrict__ keys, uint32_t* __restrict__ vals, uint32_t* __restrict__ nin,
-                       uint2* __restrict__ ties, uint32_t* __restrict__ tie_count, uint32_t* d_status) {
+__global__ void k_keys(const float* __restrict__ pos, const float* __restrict__ mas, uint32_t n,
+                       const float* __restrict__ bounds, uint64_t* __restrict__ keys, uint32_t* __restrict__ vals,
+                       uint32_t* __restrict__ nin, uint2* __restrict__ ties, uint32_t* __restrict__ tie_count,
+                       uint32_t* __restrict__ mmax, uint32_t* d_status) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     bool inside = false;
+    // largest |mass| (its bits: non-negative floats order as integers), the
+    // scale of the monopoles' fixed-point sums
+    uint32_t mb = i < n ? (__float_as_uint(mas[i]) & 0x7FFFFFFFu) : 0u;
+    mb = __reduce_max_sync(0xffffffffu, mb);
+    if ((threadIdx.x & 31) == 0 && mb) atomicMax(mmax, mb);
     if (i < n) {
         const float x[3] = {pos[3u * i], pos[3u * i + 1u], pos[3u * i + 2u]};
         Cube c;
@@ -424,9 +430,9 @@ __device__ __forceinline__ void write_node(NodeArrays nd, uint32_t v, const Cube
     const float mx = midf(c.lo[0], c.hi[0]), my = midf(c.lo[1], c.hi[1]), mz = midf(c.lo[2], c.hi[2]);
     // gravity.c:370-374: w = (1/3) * ((dx + dy) + dz), compared as w*w
     const float w = fmul(third, fadd(fadd(fsub(c.hi[0], c.lo[0]), fsub(c.hi[1], c.lo[1])), fsub(c.hi[2], c.lo[2])));
-    nd.geo[v] = make_float4(mx, my, mz, fmul(w, w));
-    nd.lo[v] = make_float4(c.lo[0], c.lo[1], c.lo[2], c.hi[0]);
-    nd.hi[v] = make_float4(c.hi[1], c.hi[2], __uint_as_float(bodies), __uint_as_float(first_child));
+    nd.geo[NODE_REC * v] = make_float4(mx, my, mz, fmul(w, w));
+    nd.lo[NODE_REC * v] = make_float4(c.lo[0], c.lo[1], c.lo[2], c.hi[0]);
+    nd.hi[NODE_REC * v] = make_float4(c.hi[1], c.hi[2], __uint_as_float(bodies), __uint_as_float(first_child));
     nd.parent[v] = parent;
     nd.start[v] = start;
 }
@@ -506,60 +512,173 @@ __global__ void __launch_bounds__(FILL_THREADS) k_split_fill(const uint64_t* __r
     write_node(nd, 1u + 8u * s + o, cc, cnt, fc, self, cstart, third);
 }
 
-__global__ void k_gather(const uint32_t* __restrict__ V, uint32_t n, const float* __restrict__ pos,
-                         const float* __restrict__ mas, float4* __restrict__ sp) {
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    const uint32_t p = V[k];
-    sp[k] = make_float4(pos[3u * p], pos[3u * p + 1u], pos[3u * p + 2u], mas[p]);
+// Monopoles from exact integer sums.  m x, m y, m z and m of every body are
+// turned into 64-bit fixed-point integers whose scales (powers of two) are
+// set from N, the largest mass and the root cube's extent so that no sum of
+// up to N bodies can overflow; the quantisation is 2^-(62 - log2 N) of the
+// largest term, far below FP64 rounding of the same sums.  Integer sums are
+// exact and associative, so prefix differences are exact, any summation
+// order gives the same bits, and nothing runs on GB300's slow FP64 pipe
+// except one division per node.
+struct FixScale {
+    int kx, km;  // q(m x) = m x 2^kx, q(m) = m 2^km
+};
+
+__device__ __forceinline__ int ceil_log2_u32(uint32_t v) { return v <= 1u ? 0 : 32 - __clz(v - 1u); }
+
+__device__ __forceinline__ FixScale fix_scale(uint32_t n, uint32_t mmax_bits, const float* __restrict__ bounds) {
+    float xmax = 0.0f;
+    for (int k = 0; k < 6; k++) xmax = fmaxf(xmax, fabsf(bounds[k]));
+    int em = 0, ex = 0;
+    frexpf(__uint_as_float(mmax_bits), &em);  // m_max < 2^em
+    frexpf(xmax, &ex);                        // |x| <= xmax < 2^ex
+    const int room = 62 - ceil_log2_u32(n);
+    FixScale f;
+    f.kx = room - em - ex;
+    f.km = room - em;
+    return f;
 }
 
-// tree.c:346-354 (centre of mass = sum(m x) / sum(m)), with FP64 sums built
-// bottom-up in one launch: a thread per leaf sums its bodies (sorted order),
-// then climbs: the last of a node's 8 children to finish (an arrival counter
-// per node) sums the 8 children's totals in octant order and goes on to the
-// parent.  The order of every addition is fixed by the tree, not by which
-// thread arrives last.
-__device__ __forceinline__ void put_monopole(NodeArrays& nd, sfd4* nsum, uint32_t v, const sfd4& d) {
-    nsum[v] = d;
-    float4 out = make_float4((float)d.x, (float)d.y, (float)d.z, (float)d.w);
-    if (d.w > 0.0) {
-        const double inv = 1.0 / d.w;
-        out = make_float4((float)(d.x * inv), (float)(d.y * inv), (float)(d.z * inv), (float)d.w);
+// round(M * 2^s) for |M| < 2^48
+__device__ __forceinline__ long long shift_round(long long M, int s) {
+    if (s >= 0) return M << s;
+    if (s <= -63) return 0;
+    return (M + (1ll << (-s - 1))) >> (-s);
+}
+
+// exact m * x * 2^k as a rounded integer: 24-bit mantissas multiplied in int64
+__device__ __forceinline__ long long fix_mul(float m, float x, int k) {
+    int em = 0, ex = 0;
+    const float fm = frexpf(m, &em), fx = frexpf(x, &ex);  // m = fm 2^em, fm in [0.5, 1)
+    const long long Mm = (long long)(fm * 16777216.0f), Mx = (long long)(fx * 16777216.0f);
+    return shift_round(Mm * Mx, em + ex - 48 + k);
+}
+
+struct fix4 {
+    long long x, y, z, m;
+};
+
+// Sorted bodies for the walk, and the fixed-point prefix sums of (m x, m y,
+// m z, m) over the sorted slots (zero outside the root cube), in two levels:
+// pre[k] = the sum over the slots of k's 32-slot chunk before k (a warp scan),
+// cpre[c] = the sum over the chunks before c (the last block to finish scans
+// the chunk totals, so no separate launch), cpre[nc] = the total.
+constexpr int GATHER_THREADS = 256;
+
+__device__ __forceinline__ long long warp_incl_scan(long long x, int lane) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const long long y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
     }
-    nd.com[v] = out;
+    return x;
 }
 
-__global__ void k_monopoles_up(const uint32_t* __restrict__ nsplit_p, uint32_t split_cap, NodeArrays nd,
-                               const float4* __restrict__ sp, sfd4* __restrict__ nsum, uint32_t* __restrict__ arrive) {
-    uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(GATHER_THREADS) k_gather(const uint32_t* __restrict__ V, uint32_t n,
+                                                           const uint32_t* __restrict__ nin_p,
+                                                           const uint32_t* __restrict__ mmax,
+                                                           const float* __restrict__ bounds,
+                                                           const float* __restrict__ pos,
+                                                           const float* __restrict__ mas, float4* __restrict__ sp,
+                                                           fix4* __restrict__ pre, fix4* __restrict__ cpre,
+                                                           uint32_t* done) {
+    const uint32_t k = blockIdx.x * GATHER_THREADS + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    long long q[4] = {0, 0, 0, 0};
+    if (k < n) {
+        const uint32_t p = V[k];
+        const float x = pos[3u * p], y = pos[3u * p + 1u], z = pos[3u * p + 2u], w = mas[p];
+        sp[k] = make_float4(x, y, z, w);
+        if (k < *nin_p) {
+            const FixScale f = fix_scale(n, *mmax, bounds);
+            q[0] = fix_mul(w, x, f.kx);
+            q[1] = fix_mul(w, y, f.kx);
+            q[2] = fix_mul(w, z, f.kx);
+            q[3] = fix_mul(w, 1.0f, f.km);
+        }
+    }
+    long long incl[4];
+#pragma unroll
+    for (int c = 0; c < 4; c++) incl[c] = warp_incl_scan(q[c], lane);
+    if (k < n) pre[k] = fix4{incl[0] - q[0], incl[1] - q[1], incl[2] - q[2], incl[3] - q[3]};
+    if (lane == 31 && (k & ~31u) < n) cpre[k >> 5] = fix4{incl[0], incl[1], incl[2], incl[3]};  // chunk total
+    // the last block: exclusive scan of the chunk totals, in place
+    __shared__ bool s_last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        s_last = atomicAdd(done, 1u) == gridDim.x - 1;
+        if (s_last) *done = 0u;
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    const uint32_t nc = (n + 31u) >> 5;
+    __shared__ long long wsum[4][GATHER_THREADS / 32];
+    long long carry[4] = {0, 0, 0, 0};
+    for (uint32_t c0 = 0; c0 < nc; c0 += GATHER_THREADS) {
+        const uint32_t c = c0 + threadIdx.x;
+        long long v[4] = {0, 0, 0, 0};
+        if (c < nc) {
+            const long long* t = reinterpret_cast<const long long*>(&cpre[c]);
+            for (int j = 0; j < 4; j++) v[j] = __ldcg(t + j);
+        }
+        long long in[4];
+        for (int j = 0; j < 4; j++) {
+            in[j] = warp_incl_scan(v[j], lane);
+            if (lane == 31) wsum[j][threadIdx.x >> 5] = in[j];
+        }
+        __syncthreads();
+        long long ex[4], tot[4];
+        for (int j = 0; j < 4; j++) {
+            long long w = 0, all = 0;
+            for (int u = 0; u < GATHER_THREADS / 32; u++) {
+                if (u < (int)(threadIdx.x >> 5)) w += wsum[j][u];
+                all += wsum[j][u];
+            }
+            ex[j] = carry[j] + w + in[j] - v[j];
+            tot[j] = all;
+        }
+        if (c < nc) cpre[c] = fix4{ex[0], ex[1], ex[2], ex[3]};
+        for (int j = 0; j < 4; j++) carry[j] += tot[j];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) cpre[nc] = fix4{carry[0], carry[1], carry[2], carry[3]};
+}
+
+// sum over the sorted slots [0, i)
+__device__ __forceinline__ fix4 slot_prefix(const fix4* __restrict__ pre, const fix4* __restrict__ cpre, uint32_t i,
+                                            uint32_t n) {
+    if (i >= n) return cpre[(n + 31u) >> 5];
+    const fix4 a = cpre[i >> 5], b = pre[i];
+    return fix4{a.x + b.x, a.y + b.y, a.z + b.z, a.m + b.m};
+}
+
+// tree.c:346-354: centre of mass = sum(m x) / sum(m), from the exact sums
+__global__ void k_monopoles(const uint32_t* __restrict__ nsplit_p, uint32_t split_cap, NodeArrays nd, uint32_t n,
+                            const uint32_t* __restrict__ mmax, const float* __restrict__ bounds,
+                            const fix4* __restrict__ msum, const fix4* __restrict__ cpre) {
+    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t nn = 1u + 8u * min(*nsplit_p, split_cap);
     if (v >= nn) return;
-    const float4 H = nd.hi[v];
-    if (__float_as_uint(H.w) != NODE_NONE) return;  // internal: its last child finishes it
-    const uint32_t cnt = __float_as_uint(H.z), s = nd.start[v];
-    sfd4 d = mk_d4(0, 0, 0, 0);
-    for (uint32_t k = 0; k < cnt; k++) {
-        const float4 b = sp[s + k];
-        const double m = b.w;
-        d = mk_d4(d.x + m * (double)b.x, d.y + m * (double)b.y, d.z + m * (double)b.z, d.w + m);
-    }
-    put_monopole(nd, nsum, v, d);
-    while (v != 0u) {
-        const uint32_t p = nd.parent[v];
-        __threadfence();
-        if (atomicAdd(&arrive[p], 1u) != 7u) return;
-        __threadfence();
-        const uint32_t fc = __float_as_uint(__ldcg(&nd.hi[p].w));
-        sfd4 t = mk_d4(0, 0, 0, 0);
-        for (uint32_t o = 0; o < 8u; o++) {
-            const double* q = reinterpret_cast<const double*>(&nsum[fc + o]);  // from L2, not a stale L1 line
-            const sfd4 c = mk_d4(__ldcg(q), __ldcg(q + 1), __ldcg(q + 2), __ldcg(q + 3));
-            t = mk_d4(t.x + c.x, t.y + c.y, t.z + c.z, t.w + c.w);
+    const uint32_t cnt = __float_as_uint(nd.hi[NODE_REC * v].z);
+    const uint32_t s = nd.start[v];
+    float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (cnt) {
+        const fix4 a = slot_prefix(msum, cpre, s, n), b = slot_prefix(msum, cpre, s + cnt, n);
+        const long long sx = b.x - a.x, sy = b.y - a.y, sz = b.z - a.z, sm = b.m - a.m;
+        const FixScale f = fix_scale(n, *mmax, bounds);
+        const double m = ldexp((double)sm, -f.km);
+        if (sm > 0) {
+            const double inv = ldexp(1.0 / (double)sm, f.km - f.kx);  // 2^km / (sm 2^kx)
+            out = make_float4((float)((double)sx * inv), (float)((double)sy * inv), (float)((double)sz * inv),
+                              (float)m);
+        } else {
+            out = make_float4((float)ldexp((double)sx, -f.kx), (float)ldexp((double)sy, -f.kx),
+                              (float)ldexp((double)sz, -f.kx), (float)m);
         }
-        put_monopole(nd, nsum, p, t);
-        v = p;
     }
+    nd.com[NODE_REC * v] = out;
 }
 
 // ---- reference-order monopoles (EXACT arithmetic) ----------------------------
@@ -580,7 +699,7 @@ __global__ void k_ref_leaf_sums(const uint32_t* __restrict__ nsplit_p, uint32_t 
     const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t nn = 1u + 8u * min(*nsplit_p, split_cap);
     if (v >= nn) return;
-    const float4 H = nd.hi[v];
+    const float4 H = nd.hi[NODE_REC * v];
     if (__float_as_uint(H.w) != NODE_NONE) return;  // split node: merged later
     const uint32_t cnt = __float_as_uint(H.z);
     const uint32_t s0 = nd.start[v];
@@ -602,7 +721,7 @@ __global__ void k_ref_leaf_sums(const uint32_t* __restrict__ nsplit_p, uint32_t 
         sz = fadd(sz, fmul(m, pos[3u * p + 2u]));
         sm = fadd(sm, m);
     }
-    nd.com[v] = cnt ? ref_com(sx, sy, sz, sm) : make_float4(0.f, 0.f, 0.f, 0.f);
+    nd.com[NODE_REC * v] = cnt ? ref_com(sx, sy, sz, sm) : make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
 __global__ void k_ref_merge(int level, const uint32_t* __restrict__ nsplit_p, uint32_t split_cap,
@@ -616,10 +735,10 @@ __global__ void k_ref_merge(int level, const uint32_t* __restrict__ nsplit_p, ui
     uint32_t cur[8], end[8];
     for (int o = 0; o < 8; o++) {
         cur[o] = nd.start[fc + o];
-        end[o] = cur[o] + __float_as_uint(nd.hi[fc + o].z);
+        end[o] = cur[o] + __float_as_uint(nd.hi[NODE_REC * (fc + o)].z);
     }
     const uint32_t s0 = nd.start[v];
-    const uint32_t cnt = __float_as_uint(nd.hi[v].z);
+    const uint32_t cnt = __float_as_uint(nd.hi[NODE_REC * v].z);
     float sx = 0.f, sy = 0.f, sz = 0.f, sm = 0.f;
     for (uint32_t a = 0; a < cnt; a++) {
         int best = -1;
@@ -643,7 +762,7 @@ __global__ void k_ref_merge(int level, const uint32_t* __restrict__ nsplit_p, ui
         sm = fadd(sm, m);
     }
     for (uint32_t a = 0; a < cnt; a++) X[s0 + a] = Y[s0 + a];
-    nd.com[v] = ref_com(sx, sy, sz, sm);
+    nd.com[NODE_REC * v] = ref_com(sx, sy, sz, sm);
 }
 
 }  // namespace
@@ -660,6 +779,7 @@ int sf_tree_alloc(TreeWork** out, uint32_t n, const sfgpu_params& p) {
     SF_CUDA(cudaMalloc(&t->vals, sizeof(uint32_t) * nn));
     if (sf_sort_alloc(t->sort, nn) != SFGPU_OK) return SFGPU_FAILURE;
     SF_CUDA(cudaMalloc(&t->counters, sizeof(uint32_t) * 8));
+    SF_CUDA(cudaMemset(t->counters, 0, sizeof(uint32_t) * 8));
     SF_CUDA(cudaMalloc(&t->ties, sizeof(uint2) * TIE_CAP));
     SF_CUDA(cudaMalloc(&t->tie_pos, sizeof(uint32_t) * TIE_CAP));
     SF_CUDA(cudaMalloc(&t->tie_key, sizeof(uint64_t) * TIE_CAP));
@@ -673,15 +793,15 @@ int sf_tree_alloc(TreeWork** out, uint32_t n, const sfgpu_params& p) {
         SF_CUDA(cudaMalloc(&t->ordA, sizeof(uint32_t) * nn));
         SF_CUDA(cudaMalloc(&t->ordB, sizeof(uint32_t) * nn));
     }
-    SF_CUDA(cudaMalloc(&t->nd.geo, sizeof(float4) * nodes));
-    SF_CUDA(cudaMalloc(&t->nd.lo, sizeof(float4) * nodes));
-    SF_CUDA(cudaMalloc(&t->nd.hi, sizeof(float4) * nodes));
-    SF_CUDA(cudaMalloc(&t->nd.com, sizeof(float4) * nodes));
+    SF_CUDA(cudaMalloc(&t->nd.geo, sizeof(float4) * NODE_REC * nodes));  // one 64-byte record per node
+    t->nd.lo = t->nd.geo + 1;
+    t->nd.hi = t->nd.geo + 2;
+    t->nd.com = t->nd.geo + 3;
     SF_CUDA(cudaMalloc(&t->nd.parent, sizeof(uint32_t) * nodes));
     SF_CUDA(cudaMalloc(&t->nd.start, sizeof(uint32_t) * nodes));
     SF_CUDA(cudaMalloc(&t->sp, sizeof(float4) * nn));
-    SF_CUDA(cudaMalloc(&t->nsum, sizeof(sfd4) * nodes));
-    SF_CUDA(cudaMalloc(&t->arrive, sizeof(uint32_t) * nodes));
+    SF_CUDA(cudaMalloc(&t->msum, 32 * nn));              // fix4 per sorted slot
+    SF_CUDA(cudaMalloc(&t->cpre, 32 * (nn / 32 + 2)));   // fix4 per 32 slots, + the total
     SF_CUDA(cudaMalloc(&t->walk_part, sizeof(float4) * sf_walk_scratch_floats4((uint32_t)nn)));
     if (sf_scan_reserve(t->scan_u32, (uint32_t)nn, sizeof(uint32_t)) != SFGPU_OK) return SFGPU_FAILURE;
     return SFGPU_OK;
@@ -705,15 +825,12 @@ void sf_tree_free(TreeWork* t) {
     cudaFree(t->ordA);
     cudaFree(t->ordB);
     cudaFree(t->nd.geo);
-    cudaFree(t->nd.lo);
-    cudaFree(t->nd.hi);
-    cudaFree(t->nd.com);
     cudaFree(t->nd.parent);
     cudaFree(t->nd.start);
     cudaFree(t->sp);
     cudaFree(t->walk_part);
-    cudaFree(t->nsum);
-    cudaFree(t->arrive);
+    cudaFree(t->msum);
+    cudaFree(t->cpre);
     cudaFree(t->scan_u32.partials);
     delete t;
 }
@@ -730,10 +847,11 @@ int sf_tree_build(sfgpu_sim* s) {
     uint32_t* tie_count = t->counters + 1;
     uint32_t* resort = t->counters + 2;
     uint32_t* nsplit = t->counters + 3;
-    SF_CUDA(cudaMemsetAsync(t->counters, 0, sizeof(uint32_t) * 4, st));
+    SF_CUDA(cudaMemsetAsync(t->counters, 0, sizeof(uint32_t) * 6, st));
     const uint32_t nb = sf_ceil_div(n, 256);
     int tk = s->timer.begin(st, "tree_keys");
-    k_keys<<<nb, 256, 0, st>>>(pos, n, s->d_bounds, t->keys, t->vals, nin, t->ties, tie_count, s->d_status);
+    k_keys<<<nb, 256, 0, st>>>(pos, mas, n, s->d_bounds, t->keys, t->vals, nin, t->ties, tie_count, t->counters + 4,
+                               s->d_status);
     SF_CHECK_LAUNCH();
     s->timer.end(st, tk);
     tk = s->timer.begin(st, "tree_sort");
@@ -773,7 +891,10 @@ int sf_tree_build(sfgpu_sim* s) {
     SF_CHECK_LAUNCH();
     s->timer.end(st, tk);
     tk = s->timer.begin(st, "tree_monopoles");
-    k_gather<<<nb, 256, 0, st>>>(t->vals, n, pos, mas, t->sp);
+    k_gather<<<sf_ceil_div(n, GATHER_THREADS), GATHER_THREADS, 0, st>>>(t->vals, n, nin, t->counters + 4,
+                                                                       s->d_bounds, pos, mas, t->sp,
+                                                                       (fix4*)t->msum, (fix4*)t->cpre,
+                                                                       t->counters + 5);
     SF_CHECK_LAUNCH();
     const uint32_t mb = sf_ceil_div(1u + 8u * t->split_cap, 256);
     if (s->p.math == SFGPU_MATH_EXACT && s->p.form == SFGPU_FORM_PLAIN) {
@@ -786,8 +907,8 @@ int sf_tree_build(sfgpu_sim* s) {
             SF_CHECK_LAUNCH();
         }
     } else {
-        SF_CUDA(cudaMemsetAsync(t->arrive, 0, sizeof(uint32_t) * (1u + 8u * (size_t)t->split_cap), st));
-        k_monopoles_up<<<mb, 256, 0, st>>>(nsplit, t->split_cap, t->nd, t->sp, t->nsum, t->arrive);
+        k_monopoles<<<mb, 256, 0, st>>>(nsplit, t->split_cap, t->nd, n, t->counters + 4, s->d_bounds,
+                                        (const fix4*)t->msum, (const fix4*)t->cpre);
         SF_CHECK_LAUNCH();
     }
     s->timer.end(st, tk);

@@ -13,11 +13,15 @@ constexpr uint32_t NODE_NONE = 0xFFFFFFFFu;
 //   parent, start (first sorted body)       export and monopoles
 // Nodes are numbered: root 0; the children of the s-th split node in
 // depth-first preorder are 1+8s .. 8+8s, in octant order.
+// Each node is one 64-byte record of four float4 (geo, lo, hi, com), so the
+// walk reads a node from a single cache line: node v's field X is
+// nd.X[NODE_REC * v], the four pointers being offsets 0..3 into the records.
+constexpr uint32_t NODE_REC = 4;
 struct NodeArrays {
-    float4* geo = nullptr;
-    float4* lo = nullptr;
-    float4* hi = nullptr;
-    float4* com = nullptr;
+    float4* geo = nullptr;  // cell centre, w^2
+    float4* lo = nullptr;   // min x, y, z, max x
+    float4* hi = nullptr;   // max y, z, bodies, first child
+    float4* com = nullptr;  // centre of mass, mass
     uint32_t* parent = nullptr;
     uint32_t* start = nullptr;
 };
@@ -27,7 +31,7 @@ struct TreeWork {
     uint64_t* keys = nullptr;   // sorted keys
     uint32_t* vals = nullptr;   // body index of each sorted slot
     SortWork sort;
-    uint32_t* counters = nullptr;  // [0] bodies in cube [1] midplane bodies [2] moved midplane bodies [3] splits
+    uint32_t* counters = nullptr;  // [0] bodies in cube [1] midplane bodies [2] moved midplane bodies [3] splits [4] max mass bits [5] gather's last-block ticket
     uint2* ties = nullptr;
     uint32_t* tie_pos = nullptr;   // moved midplane bodies: old slots ascending
     uint64_t* tie_key = nullptr;   // their new keys, ascending by (key, body)
@@ -41,8 +45,8 @@ struct TreeWork {
     uint32_t* ordB = nullptr;
     NodeArrays nd;
     float4* sp = nullptr;       // sorted bodies (x, y, z, m)
-    sfd4* nsum = nullptr;        // FP64 (m x, m y, m z, m) per node
-    uint32_t* arrive = nullptr;  // children finished, per node (bottom-up sums)
+    void* msum = nullptr;   // fixed-point (m x, m y, m z, m) per sorted slot (tree.cu fix4)
+    void* cpre = nullptr;   // exclusive prefix of msum per 32 slots, then the total
     ScanWork scan_u32;
     float4* walk_part = nullptr;  // split-walk partial sums (SPLIT x n)
 };

@@ -60,13 +60,13 @@ __global__ void __launch_bounds__(WALK_THREADS) k_walk(const float4* __restrict_
             if (lane == 0) atomicOr(d_status, SFGPU_STATUS_WALK);
             break;
         }
-        const float4 H = nd.hi[v];
+        const float4 H = nd.hi[NODE_REC * v];
         const uint32_t bodies = __float_as_uint(H.z);
         if (bodies == 0u) continue;  // gravity.c:324-328
         const bool me = (M >> lane) & 1u;
         uint32_t take = M;
         if (bodies > leaf_cap) {
-            const float4 G = nd.geo[v];
+            const float4 G = nd.geo[NODE_REC * v];
             bool open = false;
             if (me) {
                 // gravity.c:352-377, 448: open when theta <= (w*w)/d2
@@ -94,8 +94,8 @@ __global__ void __launch_bounds__(WALK_THREADS) k_walk(const float4* __restrict_
             __syncwarp();
         }
         if ((take >> lane) & 1u) {
-            const float4 C = nd.com[v];
-            const float4 Lo = nd.lo[v];
+            const float4 C = nd.com[NODE_REC * v];
+            const float4 Lo = nd.lo[NODE_REC * v];
             float cx = C.x, cy = C.y, cz = C.z, mj = C.w;
             // gravity.c:473-490: take body i out of a cell that contains it
             if (Lo.x <= rx && rx <= Lo.w && Lo.y <= ry && ry <= H.x && Lo.z <= rz && rz <= H.y && 1u < bodies) {
@@ -282,17 +282,17 @@ __global__ void __launch_bounds__(WALK_THREADS) k_walk_body(const float4* __rest
     uint32_t n_int = 0, n_open = 0;
 
     if (live) {
-        const float4 H = __ldg(&nd.hi[0]);
+        const float4 H = __ldg(&nd.hi[NODE_REC * 0]);
         const uint32_t bodies = __float_as_uint(H.z);
         const uint32_t first = __float_as_uint(H.w);
         bool descend_root = false;
         if (bodies > 0u) {
             if (bodies > leaf_cap) {
                 if (oct == 0) n_open++;
-                descend_root = opens(__ldg(&nd.geo[0]), rx, ry, rz, fc, th_lo, th_hi) && first != NODE_NONE;
+                descend_root = opens(__ldg(&nd.geo[NODE_REC * 0]), rx, ry, rz, fc, th_lo, th_hi) && first != NODE_NONE;
             }
             if (!descend_root && oct == 0) {
-                monopole<KIND>(__ldg(&nd.com[0]), __ldg(&nd.lo[0]), H, bodies, rx, ry, rz, mi, fc.eps2, ax, ay, az,
+                monopole<KIND>(__ldg(&nd.com[NODE_REC * 0]), __ldg(&nd.lo[NODE_REC * 0]), H, bodies, rx, ry, rz, mi, fc.eps2, ax, ay, az,
                                ph);
                 n_int++;
             }
@@ -307,10 +307,10 @@ __global__ void __launch_bounds__(WALK_THREADS) k_walk_body(const float4* __rest
                     atomicOr(d_status, SFGPU_STATUS_WALK);
                     break;
                 }
-                const float4 Hv = __ldg(&nd.hi[v]);
-                const float4 G = __ldg(&nd.geo[v]);
-                const float4 C = __ldg(&nd.com[v]);
-                const float4 Lo = __ldg(&nd.lo[v]);
+                const float4 Hv = __ldg(&nd.hi[NODE_REC * v]);
+                const float4 G = __ldg(&nd.geo[NODE_REC * v]);
+                const float4 C = __ldg(&nd.com[NODE_REC * v]);
+                const float4 Lo = __ldg(&nd.lo[NODE_REC * v]);
                 const uint32_t bv = __float_as_uint(Hv.z);
                 bool down = false;
                 if (bv > 0u) {
@@ -550,9 +550,9 @@ __device__ __forceinline__ void flush_slow(const GroupLists& L, int count, const
     for (int e = 0; e < count; e++) {
         const uint32_t v = L.qn[e];
         const uint32_t M = L.qm[e];
-        const float4 C = __ldg(&nd.com[v]);
-        const float4 Lo = __ldg(&nd.lo[v]);
-        const float4 H = __ldg(&nd.hi[v]);
+        const float4 C = __ldg(&nd.com[NODE_REC * v]);
+        const float4 Lo = __ldg(&nd.lo[NODE_REC * v]);
+        const float4 H = __ldg(&nd.hi[NODE_REC * v]);
         if ((M >> lane) & 1u) {
             monopole<KIND>(C, Lo, H, __float_as_uint(H.z), rx, ry, rz, mi, eps2, ax, ay, az, ph);
             n_int++;
@@ -685,10 +685,10 @@ __global__ void __launch_bounds__(GW_THREADS) k_walk_group(const float4* __restr
             if (lane < n_in) {
                 v = lvl == 0 ? 0u : fnd[in_base + lane];
                 M = lvl == 0 ? live_mask : fms[in_base + lane];
-                H = __ldg(&nd.hi[v]);
-                G = __ldg(&nd.geo[v]);
-                C = __ldg(&nd.com[v]);
-                Lo = __ldg(&nd.lo[v]);
+                H = __ldg(&nd.hi[NODE_REC * v]);
+                G = __ldg(&nd.geo[NODE_REC * v]);
+                C = __ldg(&nd.com[NODE_REC * v]);
+                Lo = __ldg(&nd.lo[NODE_REC * v]);
                 bodies = __float_as_uint(H.z);
                 first = __float_as_uint(H.w);
             }
@@ -765,8 +765,12 @@ __global__ void __launch_bounds__(GW_THREADS) k_walk_group(const float4* __restr
         float4 G = make_float4(0.f, 0.f, 0.f, 0.f), H = G, C = G, Lo = G;
         uint32_t first = NODE_NONE;
         if (lane < pops) {
-            H = __ldg(&nd.hi[v]);
-            G = __ldg(&nd.geo[v]);
+            // the whole node record in one round trip (the monopole half is
+            // needed by every accepted or mixed cell, most of the entries)
+            H = __ldg(&nd.hi[NODE_REC * v]);
+            G = __ldg(&nd.geo[NODE_REC * v]);
+            C = __ldg(&nd.com[NODE_REC * v]);
+            Lo = __ldg(&nd.lo[NODE_REC * v]);
             const uint32_t bodies = __float_as_uint(H.z);
             first = __float_as_uint(H.w);
             internal = bodies > leaf_cap;
@@ -788,10 +792,6 @@ __global__ void __launch_bounds__(GW_THREADS) k_walk_group(const float4* __restr
                 if (dmin2 > 0.0f && G.w < th_acc * dmin2) kind = 1;
                 else if (G.w >= th_open * dmax2 && first != NODE_NONE) kind = 2;
                 else kind = 3;
-            }
-            if (kind == 1 || kind == 3) {  // monopole data, in flight during the mixed tests
-                C = __ldg(&nd.com[v]);
-                Lo = __ldg(&nd.lo[v]);
             }
         }
         // cells every body opens -> their children

@@ -179,12 +179,23 @@ def vis_splat():
     ref.free()
 
 
+def initcond_c1():
+    """initcond_generate (src/initcond.c) of 4096 bodies, G = 1."""
+    n = 4096
+    ref = Reference("pp_e0.01")
+    v = ref.init(n)
+    assert ref.initcond() == 0
+    np.savez_compressed(os.path.join(OUT, "initcond_n4096.npz"), pos=v["pos"].copy(), vel=v["vel"].copy(),
+                        mas=v["mas"].copy(), G=1.0)
+    ref.free()
+
+
 def main():
     if not obuild.reference_available():
         raise SystemExit("the Starflood reference sources are needed to regenerate fixtures")
     obuild.build()
     for f in (pp_c1, pp_plummer, pp_fp64, tree_uniform, tree_ties, tree_overflow, sph_reference,
-              raw_snapshot, vis_splat):
+              raw_snapshot, vis_splat, initcond_c1):
         f()
         print("wrote", f.__name__)
 
