@@ -47,6 +47,7 @@ METRIC = "particle-steps/s & PP interactions/s, chosen vs plain, 1 GB300, rel er
 WORKLOAD = "Barnes-Hut KDK step, N=65536 uniform unit sphere, v=0.5r, m=1/N, G=1, eps=0.01, theta=0.5, leaf=8, dt=1e-3"
 FLOP_INTERACTION = 22  # conventional count: 20 for the force, 2 more with the potential
 FLOP_OPEN = 12
+BH_EXTRA = {}  # extra sfgpu_params of the Barnes-Hut workload (--walk-split)
 
 
 def env_rank():
@@ -189,7 +190,7 @@ def gpu_bh(steps, warmup, sf):
     L = sf.lib()
 
     def new_sim(flags):
-        p = sf.default_params(solver=sf.SOLVER_TREE, eps=0.01, dt=1e-3, theta=0.5, flags=flags)
+        p = sf.default_params(solver=sf.SOLVER_TREE, eps=0.01, dt=1e-3, theta=0.5, flags=flags, **BH_EXTRA)
         s = sf.Sim(n, p)
         s.set_state(pos, vel, mas)
         s.solve(0)
@@ -227,7 +228,7 @@ def gpu_bh(steps, warmup, sf):
     s.close()
 
     # kernels per step: one eager (uncaptured) step
-    p0 = sf.default_params(solver=sf.SOLVER_TREE, eps=0.01, dt=1e-3, theta=0.5, flags=sf.FLAG_NOGRAPH)
+    p0 = sf.default_params(solver=sf.SOLVER_TREE, eps=0.01, dt=1e-3, theta=0.5, flags=sf.FLAG_NOGRAPH, **BH_EXTRA)
     with sf.Sim(n, p0) as s2:
         s2.set_state(pos, vel, mas)
         s2.solve(0)
@@ -262,7 +263,7 @@ def gpu_bh_e2e(steps, warmup, sf, pos, vel, mas):
     import ctypes as C
     n = N_BH
     L = sf.compat_functions()
-    sf.compat_configure(sf.default_params(solver=sf.SOLVER_TREE, eps=0.01, dt=1e-3, theta=0.5))
+    sf.compat_configure(sf.default_params(solver=sf.SOLVER_TREE, eps=0.01, dt=1e-3, theta=0.5, **BH_EXTRA))
     sim = sf.SimT()
     sf.check(L.sim_init(C.byref(sim), n), "sim_init")
     dof = 13
@@ -669,6 +670,111 @@ def gpu_vis(sf, reps=5, sizex=1920, sizey=1080):
     return out
 
 
+def gpu_pm(sf, reps=5, side=256):
+    """Particle-mesh grid: the deposit (128 jittered samples per body) of the
+    N=65536 Barnes-Hut state and grid_solve_fft on the reference's 256^3 grid
+    over [-2, 2]^3 (GRID_SIZE 8).  The solve's compulsory HBM traffic: the
+    R2C transform reads side^3 x 4 B and writes the half spectrum (side^2 x
+    (side/2+1) x 8 B), the product reads it and the stencil's spectrum and
+    writes it back, the C2R transform reads it and writes side^3 x 4 B."""
+    import torch
+    pos, vel, mas = bh_inputs()
+    n = N_BH
+    p = sf.default_params(solver=sf.SOLVER_TREE, eps=0.01, dt=1e-3, theta=0.5)
+    cells = side ** 3
+    half = side * side * (side // 2 + 1)
+    solve_bytes = 4 * cells + 8 * half + 3 * 8 * half + 8 * half + 4 * cells
+    with sf.Sim(n, p) as s:
+        s.set_state(pos, vel, mas)
+        s.sync()
+        ext = torch.cuda.ExternalStream(s.stream())
+        with sf.Grid(side, (-2.0, -2.0, -2.0), (2.0, 2.0, 2.0), G=1.0, stream=s.stream()) as g:
+            g.deposit(s, 0)
+            g.solve_fft()
+            g.synchronize()
+            ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(reps)]
+            for k in range(reps):
+                sf.check(sf.lib().sfgpu_flush_l2(s.stream()), "flush")
+                with torch.cuda.stream(ext):
+                    ev[k][0].record(ext)
+                g.deposit(s, k + 1)
+                with torch.cuda.stream(ext):
+                    ev[k][1].record(ext)
+                g.solve_fft()
+                with torch.cuda.stream(ext):
+                    ev[k][2].record(ext)
+            g.synchronize()
+            dep = sum(e[0].elapsed_time(e[1]) for e in ev) / reps
+            sol = sum(e[1].elapsed_time(e[2]) for e in ev) / reps
+            samp, acc = g.download(counts=True)
+    gbs = solve_bytes / (sol * 1e-3) / 1e9
+    peak, src = hbm_peak()
+    out = {"workload": "deposit of the N=65536 Barnes-Hut state (128 samples per body) + grid_solve_fft on a "
+                       "256^3 grid over [-2,2]^3 (R2C/C2R cuFFT, stencil spectrum cached; L2 flushed each rep)",
+           "value": cells / (sol * 1e-3), "unit": "grid cells solved/s", "solve_ms": sol, "deposit_ms": dep,
+           "deposit_samples_per_s": n * 128 / (dep * 1e-3), "samples_on_grid": int(acc.sum()),
+           "roofline": {"kernel": "grid_solve_fft (cuFFT R2C + k_grid_mul + cuFFT C2R)", "bound": "hbm",
+                        "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                        "algorithmic_bytes": solve_bytes, "peak_source": src},
+           "potential_centre": float(samp[side // 2, side // 2, side // 2])}
+    try:
+        from oracle.pyoracle import Oracle
+        orc = Oracle("f32")
+        sub = 8192
+        t0 = time.perf_counter()
+        orc.grid_deposit(side, (-2.0, -2.0, -2.0), (2.0, 2.0, 2.0), pos[:sub], 1)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": sub * 128 / dt, "unit": "deposit samples/s", "cores": orc.threads(),
+                               "kind": "port", "sample": "orc_grid_deposit of %d bodies (%.2f s); the reference's "
+                               "FFT solve needs FFTW, absent here, so it has no CPU timing" % (sub, dt)}
+    except Exception as e:
+        out["cpu_baseline"] = {"error": str(e)}
+    return out
+
+
+def profiled_traffic(name):
+    """DRAM bytes per launch recorded in a profiles/ summary (the line
+    'dram bytes per launch: N'), or None."""
+    import re
+    try:
+        m = re.search(r"dram bytes per launch:\s*([0-9]+)", open(os.path.join(ROOT, "profiles", name)).read())
+        return int(m.group(1)) if m else None
+    except OSError:
+        return None
+
+
+def kdk_roofline(stages, n):
+    """The two leapfrog kernels against the HBM copy bandwidth: kick+drift
+    reads pos, vel, acc and writes pos, vel (60 B per body), kick+energies
+    reads vel, acc, mas, pot and writes vel, ken, pen (52 B per body)."""
+    peak, src = hbm_peak()
+    out = {"bound": "hbm", "unit": "GB/s", "peak": peak, "peak_source": src}
+    for key, b in (("kick_drift", 60), ("kick_energy", 52)):
+        if key in stages and stages[key][1]:
+            ms = stages[key][0] / stages[key][1]
+            gbs = b * n / (ms * 1e-3) / 1e9
+            out[key] = {"bytes_per_body": b, "ms": ms, "achieved": gbs, "frac": gbs / peak}
+    return out
+
+
+def max_over_ranks(t_ms, world):
+    """The slowest rank's timed region (the job ends when it does); the
+    process group is gloo, so this runs on host tensors."""
+    if world <= 1:
+        return t_ms
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([t_ms], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(world, n, steps, t_ms):
+    """Whole-job particle-steps/s: every rank runs its own replica of n bodies
+    for `steps` steps (weak scaling), all within the slowest rank's time."""
+    return world * n * steps / (t_ms * 1e-3)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -680,11 +786,18 @@ def main():
     ap.add_argument("--no-sph", action="store_true", help="skip the N=262144 Barnes-Hut + SPH sub-benchmark")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched + adjoint sub-benchmark")
     ap.add_argument("--no-vis", action="store_true", help="skip the vis_draw splat sub-benchmark")
-    ap.add_argument("--only", choices=["pp", "sph"], default=None,
+    ap.add_argument("--no-pm", action="store_true", help="skip the particle-mesh grid sub-benchmark")
+    ap.add_argument("--walk-split", type=int, default=0, help="Barnes-Hut walk variant (sfgpu_params.walk_split)")
+    ap.add_argument("--walk-group", type=int, default=0, help="bodies per warp of the group walk (sfgpu_params.walk_group)")
+    ap.add_argument("--only", choices=["pp", "sph", "pm"], default=None,
                     help="run one sub-benchmark alone and print its object (profiling runs)")
     ap.add_argument("--pp-n", type=int, default=N_PP, help="bodies of the PP sub-benchmark with --only pp")
     ap.add_argument("--sph-path", type=int, default=0, help="SPH pass variant with --only sph (sfgpu_params.sph_path)")
     args = ap.parse_args()
+    if args.walk_split:
+        BH_EXTRA["walk_split"] = args.walk_split
+    if args.walk_group:
+        BH_EXTRA["walk_group"] = args.walk_group
     rank, world, local = env_rank()
 
     if args.impl == "reference":
@@ -717,17 +830,17 @@ def main():
     if args.only == "pp":
         print(json.dumps({"only": "pp", "n": args.pp_n, "pp": gpu_pp(sf, n=args.pp_n)}))
         return
+    if args.only == "pm":
+        print(json.dumps({"only": "pm", "pm": gpu_pm(sf)}))
+        return
     if args.only == "sph":
         print(json.dumps({"only": "sph", "sph": gpu_sph(sf, max(3, args.steps), args.warmup, args.sph_path)}))
         return
 
     r = gpu_bh(args.steps, args.warmup, sf)
     t_ms = r["total_ms"]
-    if world > 1:
-        t = torch.tensor([t_ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_ms = float(t.item())
-    value = world * N_BH * args.steps / (t_ms * 1e-3)
+    t_ms = max_over_ranks(t_ms, world)
+    value = job_value(world, N_BH, args.steps, t_ms)
 
     peak, peak_src = fp32_peak_tflops()
     walk_ms, walk_launches = r["stages"].get("walk", (0.0, 0))
@@ -746,11 +859,15 @@ def main():
             "clocks": r["clocks"], "e2e": r["e2e"], "gpu_launches": r["per_step"] * args.steps,
             "roofline": {"kernel": "k_walk (Barnes-Hut walk)", "bound": "fp32", "achieved": achieved,
                          "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
-                         "traffic": None, "peak_source": peak_src,
+                         "traffic": profiled_traffic("walk_group_uniform65536.md"),
+                         "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum per launch, "
+                                           "profiles/walk_group_uniform65536.md (ncu)",
+                         "peak_source": peak_src,
                          "flops_per_launch": flops_per_launch, "avg_launch_ms": walk_avg_ms,
                          "interactions_per_step": r["n_int"] / max(1, walk_launches),
                          "opening_tests_per_step": r["n_open"] / max(1, walk_launches)},
-            "stage_ms_per_step": stage_ms, "device_status": r["status"]}
+            "stage_ms_per_step": stage_ms, "device_status": r["status"],
+            "kdk": kdk_roofline(r["stages"], N_BH)}
     if rank == 0:
         try:
             line["cpu_baseline"] = {"skipped": "--no-cpu"} if args.no_cpu else cpu_bh_rate(max_seconds=10.0)
@@ -794,6 +911,11 @@ def main():
                 line["vis"] = gpu_vis(sf)
             except Exception as e:
                 line["vis"] = {"error": str(e)}
+        if not args.no_pm:
+            try:
+                line["pm"] = gpu_pm(sf)
+            except Exception as e:
+                line["pm"] = {"error": str(e)}
         print(json.dumps(line))
     if world > 1:
         dist.barrier()

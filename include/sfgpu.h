@@ -77,9 +77,10 @@ typedef struct {
     double   sph_alpha;   /* CUBIC: Monaghan viscosity alpha                */
     double   sph_beta;    /* CUBIC: Monaghan viscosity beta                 */
     uint32_t flags;       /* SFGPU_FLAG_*                                   */
-    uint32_t walk_split;  /* walk variant: 0 group walk (default), 1 thread per body, 8 thread per body and root octant, 64 group walk over 8 warps */
+    uint32_t walk_split;  /* walk variant: 0 group walk (default), 1 thread per body, 8 thread per body and root octant, 64 32-body group walk over 8 warps */
     uint32_t sph_path;    /* CUBIC SPH passes: 0 one thread per body (default), 1 one warp per 32-body slice of a cell */
-    uint32_t reserved[5];
+    uint32_t walk_group;  /* bodies per warp of the group walk: 0 the default (16), 8, 16 or 32 */
+    uint32_t reserved[4];
 } sfgpu_params;
 
 /* flags */
@@ -322,6 +323,45 @@ int sfgpu_batch_grad(sfgpu_batch* b, uint32_t nsteps, uint32_t checkpoint, float
 /* Single VJP of the softened PP force: given cotangents abar (total, 3) of
  * the accelerations, accumulate xbar += (d acc / d pos)^T abar. Device ptrs. */
 int sfgpu_batch_force_vjp(sfgpu_batch* b, const float* d_abar, float* d_xbar);
+
+/* ---- particle-mesh grid (src/grid.c, src/gravity.c:116-238) -------------- */
+/* A cubic grid of side^3 FP32 samples over [bounds_min, bounds_max], x
+ * fastest (index side*side*z + side*y + x), resident in HBM.  The
+ * reference's grid is a compile-time option (ENABLE_GRID / ENABLE_FFT,
+ * config.h:48-55) whose deposit (solve_gravity_part_mesh) is compiled out. */
+typedef struct sfgpu_grid sfgpu_grid;
+/* Replaces grid_init (src/grid.c:26-159): side in [1, 256], else -1 as the
+ * reference.  The stencil -G/|x| and its spectrum are computed here, once.
+ * Every grid call is queued on `stream` (a cudaStream_t, NULL = default).
+ * Needs cuFFT (libcufft.so.12), loaded on first use; without it the call
+ * fails with a message and the rest of the library is unaffected. */
+int sfgpu_grid_create(sfgpu_grid** out, uint32_t side, const float bounds_min[3], const float bounds_max[3],
+                      double G, void* stream);
+/* Replaces grid_free (src/grid.c:161-188). */
+int sfgpu_grid_destroy(sfgpu_grid* g);
+/* grid_samp (src/grid.c:190-194): the device array of side^3 samples. */
+float* sfgpu_grid_samp(sfgpu_grid* g);
+/* The device array of side^3 int32 deposit counts. */
+int32_t* sfgpu_grid_accum(sfgpu_grid* g);
+void* sfgpu_grid_stream(sfgpu_grid* g);
+uint32_t sfgpu_grid_side(const sfgpu_grid* g);
+/* The deposit of solve_gravity_part_mesh (src/gravity.c:137-227): each of
+ * the n bodies (device pos, 3n floats) is sampled `samples` times (the
+ * reference's GRID_SAMPLES: 128) with pcg4d-seeded Gaussian offsets of sigma
+ * 0.5 cell; counts land in the accum array, samp = count / samples. */
+int sfgpu_grid_deposit_arrays(sfgpu_grid* g, uint32_t n, const float* pos, uint32_t step_number,
+                              uint32_t samples);
+/* The same over a simulation's current positions, ordered after the
+ * simulation's queued work (and its later work after the deposit). */
+int sfgpu_grid_deposit(sfgpu_grid* g, sfgpu_sim* s, uint32_t step_number, uint32_t samples);
+/* Replaces grid_solve_fft (src/grid.c:197-536): samp <- the real part of
+ * the unnormalised inverse transform of DFT(samp) * DFT(stencil), rolled by
+ * side/2 along every axis.  Asynchronous. */
+int sfgpu_grid_solve_fft(sfgpu_grid* g);
+/* Host copies of samp (and the counts; either may be NULL), synchronous. */
+int sfgpu_grid_upload(sfgpu_grid* g, const float* samp);
+int sfgpu_grid_download(sfgpu_grid* g, float* samp, int32_t* accum);
+int sfgpu_grid_synchronize(sfgpu_grid* g);
 
 #ifdef __cplusplus
 }

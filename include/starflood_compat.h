@@ -101,6 +101,33 @@ int vis_save(const vis_t* vis, const char* filename, image_filetype_t filetype);
 /* src/visualization.c:258-740 on the GPU; buffers current on return. */
 int vis_draw(const vis_t* vis, const sim_t* sim);
 
+/* src/grid.h:11-24 as built with ENABLE_FFT.  mem: side^3 FP32 samples, then
+ * side^3 int32 deposit counts; mem_fft0: the device grid (opaque);
+ * mem_fft1, mem_fft2: unused (NULL). */
+typedef struct {
+    unsigned int dim[3];
+    real bounds_min[3];
+    real bounds_max[3];
+    void* mem;
+    void* mem_fft0;
+    void* mem_fft1;
+    void* mem_fft2;
+} grid_t;
+/* src/grid.c:26-159 (side 1..256, else -1); G from sfgpu_compat_configure */
+int grid_init(grid_t* grid, unsigned int side_length, const real* bounds_min, const real* bounds_max);
+/* src/grid.c:161-188 */
+int grid_free(grid_t* grid);
+/* src/grid.c:190-194 */
+real* grid_samp(const grid_t* grid);
+/* src/grid.c:197-536 on the GPU (cuFFT); grid_samp() current on return. */
+int grid_solve_fft(const grid_t* grid);
+/* src/gravity.c:116-238: deposit of the bodies' positions (128 jittered
+ * samples each, seeded by sim->step_number) into the counts and samples,
+ * then grid_solve_fft.  The reference compiles this function out and reads
+ * the grid from sim_t (ENABLE_GRID); this sim_t has no grid member, so the
+ * grid is an argument. */
+int solve_gravity_part_mesh(const sim_t* sim, grid_t* grid);
+
 /* src/simulation_io.c:16-79: the slab (N*SIM_DOF reals, no header) from a
  * file into sim->mem and the device; like the reference, a short read is
  * reported on stderr but not failed. */

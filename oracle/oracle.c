@@ -14,6 +14,7 @@
 
 #include <math.h>
 #include <stddef.h>
+#include <stdlib.h>
 #include <string.h>
 
 #ifdef _OPENMP
@@ -729,4 +730,138 @@ void orc_initcond(uint32_t n, double G, float* pos, float* vel, float* mas, floa
             vel[3u * i + (uint32_t)k] = (float)v[k];
         }
     }
+}
+
+/* ---- gravity.c:116-230 (compiled out by #if 0 in the reference) and
+ * grid.c:197-536: the particle-mesh grid ----------------------------------- */
+void orc_grid_deposit(uint32_t side, const float bmin[3], const float bmax[3], uint32_t n, const float* pos,
+                      uint32_t step, uint32_t samples, int32_t* accum, float* poten) {
+    const size_t cells = (size_t)side * side * side;
+    const float wid[3] = {bmax[0] - bmin[0], bmax[1] - bmin[1], bmax[2] - bmin[2]};
+    memset(accum, 0, sizeof(int32_t) * cells);
+#pragma omp parallel for schedule(dynamic, 256)
+    for (uint32_t i = 0; i < n; i++) {
+        float pl[3];
+        for (int k = 0; k < 3; k++) pl[k] = (pos[3u * i + (uint32_t)k] - bmin[k]) / wid[k];
+        for (uint32_t j = 0; j < samples; j++) {
+            uint32_t s[4] = {0xB79ABC95u + j, 0xE0DA3F84u + i, 0xAB75F07Bu + step, 0xCF52CA01u};
+            orc_pcg4d(s);
+            orc_pcg4d(s);
+            float r[4];
+            for (int k = 0; k < 4; k++) r[k] = (float)ORC_INV_PCG * (float)s[k];
+            const float g[3] = {sqrtf(-2.0f * logf(r[0])) * cosf((float)ORC_TAU * r[1]),
+                                sqrtf(-2.0f * logf(r[0])) * sinf((float)ORC_TAU * r[1]),
+                                sqrtf(-2.0f * logf(r[2])) * cosf((float)ORC_TAU * r[3])};
+            int c[3];
+            for (int k = 0; k < 3; k++) c[k] = vis_to_int(0.500f * g[k] + (float)side * pl[k] + 0.5f);
+            if (0 <= c[0] && c[0] < (int)side && 0 <= c[1] && c[1] < (int)side && 0 <= c[2] && c[2] < (int)side) {
+                const size_t idx = (size_t)side * side * (uint32_t)c[2] + (size_t)side * (uint32_t)c[1] + (uint32_t)c[0];
+#pragma omp atomic update
+                accum[idx] += 1;
+            }
+        }
+    }
+    const double inv = 1.0 / (double)samples;
+    for (size_t i = 0; i < cells; i++) poten[i] = (float)(inv * (double)accum[i]);
+}
+
+/* grid.c:281-315: the FP32 stencil -G / |x| at the cell corners. */
+void orc_grid_stencil(uint32_t side, const float bmin[3], const float bmax[3], double G, float* out) {
+    const float wid[3] = {bmax[0] - bmin[0], bmax[1] - bmin[1], bmax[2] - bmin[2]};
+    for (uint32_t z = 0; z < side; z++)
+        for (uint32_t y = 0; y < side; y++)
+            for (uint32_t x = 0; x < side; x++) {
+                const float p[3] = {wid[0] * ((float)x / (float)side) + bmin[0],
+                                    wid[1] * ((float)y / (float)side) + bmin[1],
+                                    wid[2] * ((float)z / (float)side) + bmin[2]};
+                const float r2 = (p[0] * p[0]) + (p[1] * p[1]) + (p[2] * p[2]);
+                const float inv = 0.0f < r2 ? 1.0f / sqrtf(r2) : 0.0f;
+                out[(size_t)side * side * z + (size_t)side * y + x] = (float)(-G) * inv;
+            }
+}
+
+/* In-place 1-D DFT of every line of a side^3 complex field along one axis
+ * (stride 1, side or side^2), by the definition with an FP64 twiddle
+ * table; sign -1 forward, +1 backward (unnormalised, as FFTW_BACKWARD). */
+static void grid_dft_axis(uint32_t side, double* re, double* im, size_t stride, int sign) {
+    const size_t cells = (size_t)side * side * side;
+    double* wr = (double*)malloc(sizeof(double) * side);
+    double* wi = (double*)malloc(sizeof(double) * side);
+    for (uint32_t m = 0; m < side; m++) {
+        wr[m] = cos(ORC_TAU * (double)m / (double)side);
+        wi[m] = (double)sign * sin(ORC_TAU * (double)m / (double)side);
+    }
+    const size_t lines = cells / side;
+#pragma omp parallel
+    {
+        double* tr = (double*)malloc(sizeof(double) * side);
+        double* ti = (double*)malloc(sizeof(double) * side);
+#pragma omp for schedule(static)
+        for (size_t l = 0; l < lines; l++) {
+            /* line l: the cells whose index has the axis digit zeroed */
+            const size_t lo = l % stride, hi = l / stride;
+            const size_t base = hi * stride * side + lo;
+            for (uint32_t k = 0; k < side; k++) {
+                double sr = 0.0, si = 0.0;
+                uint32_t m = 0; /* j * k mod side */
+                for (uint32_t j = 0; j < side; j++, m = (m + k >= side) ? m + k - side : m + k) {
+                    const double xr = re[base + j * stride], xi = im[base + j * stride];
+                    sr += xr * wr[m] - xi * wi[m];
+                    si += xr * wi[m] + xi * wr[m];
+                }
+                tr[k] = sr;
+                ti[k] = si;
+            }
+            for (uint32_t k = 0; k < side; k++) {
+                re[base + k * stride] = tr[k];
+                im[base + k * stride] = ti[k];
+            }
+        }
+        free(tr);
+        free(ti);
+    }
+    free(wr);
+    free(wi);
+}
+
+static void grid_dft3(uint32_t side, double* re, double* im, int sign) {
+    grid_dft_axis(side, re, im, 1, sign);
+    grid_dft_axis(side, re, im, side, sign);
+    grid_dft_axis(side, re, im, (size_t)side * side, sign);
+}
+
+void orc_grid_solve_fft(uint32_t side, const float bmin[3], const float bmax[3], double G, const float* samp,
+                        double* out) {
+    const size_t cells = (size_t)side * side * side;
+    float* st = (float*)malloc(sizeof(float) * cells);
+    double* sr = (double*)calloc(cells, sizeof(double));
+    double* si = (double*)calloc(cells, sizeof(double));
+    double* fr = (double*)calloc(cells, sizeof(double));
+    double* fi = (double*)calloc(cells, sizeof(double));
+    orc_grid_stencil(side, bmin, bmax, G, st);
+    for (size_t i = 0; i < cells; i++) {
+        sr[i] = st[i];
+        fr[i] = samp[i];
+    }
+    grid_dft3(side, sr, si, -1);
+    grid_dft3(side, fr, fi, -1);
+    for (size_t i = 0; i < cells; i++) {
+        const double a = fr[i], b = fi[i];
+        fr[i] = a * sr[i] - b * si[i];
+        fi[i] = a * si[i] + b * sr[i];
+    }
+    grid_dft3(side, fr, fi, +1);
+    const uint32_t h = side / 2u;
+    for (uint32_t z = 0; z < side; z++)
+        for (uint32_t y = 0; y < side; y++)
+            for (uint32_t x = 0; x < side; x++) {
+                const size_t src = (size_t)side * side * ((z + h) % side) + (size_t)side * ((y + h) % side) +
+                                   (x + h) % side;
+                out[(size_t)side * side * z + (size_t)side * y + x] = fr[src];
+            }
+    free(st);
+    free(sr);
+    free(si);
+    free(fr);
+    free(fi);
 }

@@ -120,6 +120,22 @@ void orc_vis_draw(uint32_t n, const float* pos, const float* vel, const float* p
                   double timestep, uint32_t sizex, uint32_t sizey, uint32_t samples, double exposure,
                   double ortho_scale, int autoscale, int tonemap, int32_t* accum, float* render);
 
+/* The particle-mesh deposit of solve_gravity_part_mesh (src/gravity.c:116-230,
+ * compiled out by #if 0 in the reference): `samples` samples per body, each
+ * two pcg4d rounds of {0xB79ABC95+j, 0xE0DA3F84+i, 0xAB75F07B+step,
+ * 0xCF52CA01} turned into a Gaussian offset of sigma 0.5 cell by Box-Muller
+ * (host libm logf, cosf, sinf), counted into accum (side^3 int32, x
+ * fastest); poten = (float)(count / samples).  FP32 as the reference. */
+void orc_grid_deposit(uint32_t side, const float bmin[3], const float bmax[3], uint32_t n, const float* pos,
+                      uint32_t step, uint32_t samples, int32_t* accum, float* poten);
+/* grid.c:281-315: the stencil -G / |x| sampled at the cell corners, FP32. */
+void orc_grid_stencil(uint32_t side, const float bmin[3], const float bmax[3], double G, float* out);
+/* grid_solve_fft (src/grid.c:197-536) in FP64 by the DFT's definition:
+ * IDFT(DFT(samp) * DFT(stencil)) unnormalised (FFTW_BACKWARD), rolled by
+ * side/2 along every axis, real part. */
+void orc_grid_solve_fft(uint32_t side, const float bmin[3], const float bmax[3], double G, const float* samp,
+                        double* out);
+
 /* Simulation over one slab in the reference layout (simulation.h:17-51):
  * pos[3N] vel[3N] acc[3N] mas[N] pot[N] ken[N] pen[N] (+ rad rho prs). */
 typedef struct {

@@ -74,6 +74,10 @@ class Oracle:
         L.orc_vis_draw.argtypes = [C.c_uint32, fp, fp, fp, C.c_uint32, C.c_double, C.c_uint32, C.c_uint32,
                                    C.c_uint32, C.c_double, C.c_double, C.c_int, C.c_int,
                                    C.POINTER(C.c_int32), fp]
+        L.orc_grid_deposit.argtypes = [C.c_uint32, fp, fp, C.c_uint32, fp, C.c_uint32, C.c_uint32,
+                                       C.POINTER(C.c_int32), fp]
+        L.orc_grid_stencil.argtypes = [C.c_uint32, fp, fp, C.c_double, fp]
+        L.orc_grid_solve_fft.argtypes = [C.c_uint32, fp, fp, C.c_double, fp, dp]
 
         class Sim(C.Structure):
             _fields_ = [("step_number", C.c_uint32), ("N", C.c_uint32), ("mem", C.c_void_p),
@@ -184,6 +188,37 @@ class Oracle:
                               step, timestep, sizex, sizey, samples, exposure, ortho_scale, autoscale, tonemap,
                               accum.ctypes.data_as(C.POINTER(C.c_int32)), render.ctypes.data_as(fp))
         return accum, render
+
+    def grid_deposit(self, side, bmin, bmax, pos, step, samples=128):
+        """The particle-mesh deposit (src/gravity.c:116-230): (accum int32
+        (side, side, side), poten float32 of the same shape), index [z, y, x]."""
+        fp = C.POINTER(C.c_float)
+        pos = np.ascontiguousarray(pos, np.float32)
+        lo, hi = np.asarray(bmin, np.float32), np.asarray(bmax, np.float32)
+        accum = np.zeros((side, side, side), np.int32)
+        poten = np.zeros((side, side, side), np.float32)
+        self.lib.orc_grid_deposit(side, lo.ctypes.data_as(fp), hi.ctypes.data_as(fp), len(pos),
+                                  pos.ctypes.data_as(fp), step, samples,
+                                  accum.ctypes.data_as(C.POINTER(C.c_int32)), poten.ctypes.data_as(fp))
+        return accum, poten
+
+    def grid_stencil(self, side, bmin, bmax, G=1.0):
+        """grid.c:281-315: the FP32 stencil -G/|x| at the cell corners, [z, y, x]."""
+        fp = C.POINTER(C.c_float)
+        lo, hi = np.asarray(bmin, np.float32), np.asarray(bmax, np.float32)
+        out = np.zeros((side, side, side), np.float32)
+        self.lib.orc_grid_stencil(side, lo.ctypes.data_as(fp), hi.ctypes.data_as(fp), G, out.ctypes.data_as(fp))
+        return out
+
+    def grid_solve_fft(self, side, bmin, bmax, samp, G=1.0):
+        """grid_solve_fft (src/grid.c:197-536) in FP64 by the DFT definition."""
+        fp = C.POINTER(C.c_float)
+        lo, hi = np.asarray(bmin, np.float32), np.asarray(bmax, np.float32)
+        samp = np.ascontiguousarray(samp, np.float32)
+        out = np.zeros((side, side, side), np.float64)
+        self.lib.orc_grid_solve_fft(side, lo.ctypes.data_as(fp), hi.ctypes.data_as(fp), G,
+                                    samp.ctypes.data_as(fp), out.ctypes.data_as(C.POINTER(C.c_double)))
+        return out
 
     def sph_cubic(self, pos, vel, mas, rad, u, gamma=5.0 / 3.0, alpha=1.0, beta=2.0):
         """Cubic-spline SPH (FP64 physics, FP32 neighbour decisions)."""

@@ -37,7 +37,8 @@ class Params(C.Structure):
                 ("acc_mode", C.c_int32), ("leaf_cap", C.c_uint32), ("depth_max", C.c_uint32),
                 ("nodes_max", C.c_uint32), ("sph_gamma", C.c_double), ("sph_alpha", C.c_double),
                 ("sph_beta", C.c_double), ("flags", C.c_uint32), ("walk_split", C.c_uint32),
-                ("sph_path", C.c_uint32), ("reserved", C.c_uint32 * 5)]
+                ("sph_path", C.c_uint32), ("walk_group", C.c_uint32),
+                ("reserved", C.c_uint32 * 4)]
 
 
 _lib = None
@@ -112,6 +113,18 @@ def lib():
             "sfgpu_vis_download": (i32, [vp, u32, u32, vp, vp, vp, vp]),
             "sfgpu_snapshot_wait": (i32, [vp]),
             "sfgpu_read_raw": (i32, [vp, C.c_char_p]),
+            "sfgpu_grid_create": (i32, [C.POINTER(vp), u32, f32p, f32p, C.c_double, vp]),
+            "sfgpu_grid_destroy": (i32, [vp]),
+            "sfgpu_grid_samp": (vp, [vp]),
+            "sfgpu_grid_accum": (vp, [vp]),
+            "sfgpu_grid_stream": (vp, [vp]),
+            "sfgpu_grid_side": (u32, [vp]),
+            "sfgpu_grid_deposit_arrays": (i32, [vp, u32, vp, u32, u32]),
+            "sfgpu_grid_deposit": (i32, [vp, vp, u32, u32]),
+            "sfgpu_grid_solve_fft": (i32, [vp]),
+            "sfgpu_grid_upload": (i32, [vp, vp]),
+            "sfgpu_grid_download": (i32, [vp, vp, vp]),
+            "sfgpu_grid_synchronize": (i32, [vp]),
             "sfgpu_compat_configure": (i32, [P]),
             "sfgpu_compat_params": (None, [P]),
         }
@@ -346,6 +359,67 @@ class Sim:
         return dict(parent=parent, bodies=bodies, branch=branch, bounds=bounds, params=params)
 
 
+class Grid:
+    """A particle-mesh grid (sfgpu_grid): side^3 FP32 samples over
+    [bounds_min, bounds_max], resident in HBM; arrays are indexed [z, y, x]."""
+
+    def __init__(self, side: int, bounds_min=(-2.0, -2.0, -2.0), bounds_max=(2.0, 2.0, 2.0), G=1.0, stream=None):
+        self.side = int(side)
+        lo = np.ascontiguousarray(bounds_min, np.float32)
+        hi = np.ascontiguousarray(bounds_max, np.float32)
+        f = C.POINTER(C.c_float)
+        h = C.c_void_p()
+        check(lib().sfgpu_grid_create(C.byref(h), self.side, lo.ctypes.data_as(f), hi.ctypes.data_as(f), G,
+                                      stream), "sfgpu_grid_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().sfgpu_grid_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def stream(self):
+        return lib().sfgpu_grid_stream(self.h)
+
+    @property
+    def samp_ptr(self):
+        return lib().sfgpu_grid_samp(self.h)
+
+    def upload(self, samp):
+        a = np.ascontiguousarray(samp, np.float32).reshape(-1)
+        assert a.size == self.side ** 3
+        check(lib().sfgpu_grid_upload(self.h, _ptr(a)), "sfgpu_grid_upload")
+
+    def download(self, counts=False):
+        d = self.side
+        samp = np.zeros((d, d, d), np.float32)
+        acc = np.zeros((d, d, d), np.int32) if counts else None
+        check(lib().sfgpu_grid_download(self.h, _ptr(samp), _ptr(acc) if counts else None), "sfgpu_grid_download")
+        return (samp, acc) if counts else samp
+
+    def deposit(self, sim: "Sim", step: int, samples: int = 128):
+        check(lib().sfgpu_grid_deposit(self.h, sim.h, step, samples), "sfgpu_grid_deposit")
+
+    def deposit_arrays(self, n: int, d_pos, step: int, samples: int = 128):
+        check(lib().sfgpu_grid_deposit_arrays(self.h, n, d_pos, step, samples), "sfgpu_grid_deposit_arrays")
+
+    def solve_fft(self):
+        check(lib().sfgpu_grid_solve_fft(self.h), "sfgpu_grid_solve_fft")
+
+    def synchronize(self):
+        check(lib().sfgpu_grid_synchronize(self.h), "sfgpu_grid_synchronize")
+
+
 def slab_views(slab: np.ndarray, n: int, dof_: int):
     """Views of a slab in the reference layout (src/simulation.h:17-51)."""
     v = {"pos": slab[0:3 * n].reshape(n, 3), "vel": slab[3 * n:6 * n].reshape(n, 3),
@@ -383,12 +457,27 @@ def compat_configure(p: Params):
     check(lib().sfgpu_compat_configure(C.byref(p)), "sfgpu_compat_configure")
 
 
+class GridT(C.Structure):
+    """src/grid.h:11-24 (ENABLE_FFT layout)."""
+    _fields_ = [("dim", C.c_uint * 3), ("bounds_min", C.c_float * 3), ("bounds_max", C.c_float * 3),
+                ("mem", C.c_void_p), ("mem_fft0", C.c_void_p), ("mem_fft1", C.c_void_p), ("mem_fft2", C.c_void_p)]
+
+
 def compat_functions():
     """The drop-in entry points with their C signatures."""
     L = lib()
     S = C.POINTER(SimT)
     T = C.POINTER(TreeT)
     V = C.POINTER(VisT)
+    G = C.POINTER(GridT)
+    fp = C.POINTER(C.c_float)
+    for name, args in (("grid_init", [G, C.c_uint, fp, fp]), ("grid_free", [G]), ("grid_solve_fft", [G]),
+                       ("solve_gravity_part_mesh", [S, G])):
+        fn = getattr(L, name)
+        fn.restype = C.c_int
+        fn.argtypes = args
+    L.grid_samp.restype = C.c_void_p
+    L.grid_samp.argtypes = [G]
     for name, args in (("sim_init", [S, C.c_uint]), ("sim_free", [S]), ("sim_solv", [S]), ("sim_step", [S]),
                        ("solve_gravity_part_part", [S]), ("solve_gravity_part_tree", [S]), ("solve_sph", [S]),
                        ("tree_init", [T, C.c_uint]), ("tree_free", [T]),

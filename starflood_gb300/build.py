@@ -71,7 +71,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
                 print(o)
     if force or jobs or not os.path.exists(LIB) or _stale(LIB, objs):
         tmp = LIB + ".tmp"
-        _run([nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lpthread", "-lm"])
+        _run([nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lpthread", "-lm", "-ldl"])
         os.replace(tmp, LIB)
     return LIB
 

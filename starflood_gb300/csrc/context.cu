@@ -170,6 +170,10 @@ static int validate(const sfgpu_params* p) {
         sf_set_error("unknown sph mode %d", p->sph);
         return SFGPU_FAILURE;
     }
+    if (p->walk_group != 0 && p->walk_group != 8 && p->walk_group != 16 && p->walk_group != 32) {
+        sf_set_error("walk_group must be 0, 8, 16 or 32");
+        return SFGPU_FAILURE;
+    }
     return SFGPU_OK;
 }
 

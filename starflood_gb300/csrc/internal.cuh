@@ -254,7 +254,10 @@ struct SortWork {
     uint32_t* counters = nullptr;  // [passes] tile tickets
     size_t cap = 0;
     size_t tiles_cap = 0;
+    uint32_t flags = 0;            // SORT_NO_BUCKETS: always the tile passes
 };
+constexpr uint32_t SORT_NO_BUCKETS = 1u;
+constexpr uint32_t BUCKET_SORT_MAX = 1u << 17;  // sf_sort_pairs* use one pass + per-bucket CTAs up to here
 int sf_sort_alloc(SortWork& w, size_t n);
 void sf_sort_free(SortWork& w);
 // Sorts keys/vals in place (result back in keys/vals).  d_n (device, may be

@@ -19,6 +19,7 @@ constexpr uint32_t FLAG_AGG = 1u << 30;
 constexpr uint32_t FLAG_INC = 2u << 30;
 constexpr uint32_t VALUE_MASK = (1u << 30) - 1u;
 constexpr uint32_t SPIN_LIMIT = 1u << 24;
+constexpr int LOOKBACK = 16;  // predecessor words read per look-back round
 
 __global__ void __launch_bounds__(256) k_hist(const uint64_t* __restrict__ keys, uint32_t n, int passes,
                                               uint32_t* __restrict__ hist, const uint32_t* enable) {
@@ -118,7 +119,10 @@ __global__ void __launch_bounds__(SORT_THREADS) k_onesweep(
     }
     __syncthreads();
 
-    // decoupled look-back across tiles, one digit per thread
+    // decoupled look-back across tiles, one digit per thread; each round
+    // reads the next LOOKBACK predecessors' words at once (independent loads,
+    // one memory latency per round instead of one per tile) and sums them
+    // nearest first up to the first inclusive prefix or unpublished tile
     if (threadIdx.x < RADIX) {
         const int d = threadIdx.x;
         volatile uint32_t* st = status;
@@ -129,19 +133,29 @@ __global__ void __launch_bounds__(SORT_THREADS) k_onesweep(
             st[(size_t)tile * RADIX + d] = FLAG_AGG | tcount[d];
             int64_t look = (int64_t)tile - 1;
             uint32_t spins = 0;
-            while (look >= 0) {
-                const uint32_t w = st[(size_t)look * RADIX + d];
-                const uint32_t flag = w & ~VALUE_MASK;
-                if (flag == 0u) {
-                    if (++spins > SPIN_LIMIT) {
-                        atomicOr(d_status, SFGPU_STATUS_SPIN);
-                        break;
+            bool done = false;
+            while (!done) {
+                uint32_t w[LOOKBACK];
+#pragma unroll
+                for (int b = 0; b < LOOKBACK; b++)
+                    w[b] = (look - b >= 0) ? st[(size_t)(look - b) * RADIX + d] : 0u;
+                bool stalled = false;
+#pragma unroll
+                for (int b = 0; b < LOOKBACK; b++) {
+                    if (done || stalled) continue;
+                    const uint32_t flag = w[b] & ~VALUE_MASK;
+                    if (flag == 0u) {
+                        stalled = true;
+                        continue;
                     }
-                    continue;
+                    prefix += w[b] & VALUE_MASK;
+                    look--;
+                    if (flag == FLAG_INC) done = true;
                 }
-                prefix += w & VALUE_MASK;
-                if (flag == FLAG_INC) break;
-                look--;
+                if (stalled && ++spins > SPIN_LIMIT) {
+                    atomicOr(d_status, SFGPU_STATUS_SPIN);
+                    break;
+                }
             }
             __threadfence();
             st[(size_t)tile * RADIX + d] = FLAG_INC | ((prefix + tcount[d]) & VALUE_MASK);
@@ -159,6 +173,187 @@ __global__ void __launch_bounds__(SORT_THREADS) k_onesweep(
         vout[pos] = val[it];
     }
 }
+
+// ---- small sorts: one pass on the top digit, then every bucket in one CTA ----
+// After a tile pass on the most significant digit, the pairs of bucket b
+// (keys whose top digit is b) are contiguous.  One CTA per bucket finishes
+// the low digits with stable LSD passes in its own shared memory: per pass,
+// warps rank consecutive 32-key rounds (warp match), counts are prefixed
+// over warps and digits, and every pair moves to its place in the other
+// buffer; __syncthreads separate the steps, so no pass needs a grid-wide
+// wait.  A bucket larger than BK_CAP runs the same passes through global
+// memory in BK_CAP-pair chunks (slower, still exact).
+constexpr int BK_THREADS = 1024;
+constexpr int BK_WARPS = BK_THREADS / 32;
+constexpr int BK_ITEMS = 8;
+constexpr uint32_t BK_CAP = BK_THREADS * BK_ITEMS;  // 8192 pairs, 12 B each, two buffers
+
+struct BucketScratch {
+    uint32_t* wcnt;   // [BK_WARPS][RADIX] per-warp counts, then their exclusive prefix
+    uint32_t* gsum;   // [8][RADIX] warp-group totals / digit scan scratch
+    uint32_t* run;    // [RADIX] running start of each digit in the destination
+};
+
+// One stable pass over [0, size) of src into dst (shared memory), chunk by
+// chunk of BK_CAP pairs; digit = (key >> shift) & 127.
+__device__ void bucket_pass(const uint64_t* src_k, const uint32_t* src_v, uint64_t* dst_k, uint32_t* dst_v,
+                            uint32_t size, int shift, const BucketScratch& sc) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t lt = (1u << lane) - 1u;
+    // digit totals of the whole range -> exclusive digit starts
+    if (threadIdx.x < RADIX) sc.run[threadIdx.x] = 0u;
+    __syncthreads();
+    for (uint32_t e = threadIdx.x; e < size; e += BK_THREADS)
+        atomicAdd(&sc.run[(uint32_t)(src_k[e] >> shift) & (RADIX - 1)], 1u);
+    __syncthreads();
+    if (threadIdx.x < RADIX) {
+        const uint32_t v = sc.run[threadIdx.x];
+        uint32_t x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        sc.gsum[threadIdx.x] = x;
+        sc.run[threadIdx.x] = x - v;  // exclusive within the warp; earlier warps added below
+    }
+    __syncthreads();
+    if (threadIdx.x < RADIX) {
+        uint32_t add = 0;
+        for (int w = 0; w < (int)(threadIdx.x >> 5); w++) add += sc.gsum[w * 32 + 31];
+        sc.run[threadIdx.x] += add;
+    }
+    __syncthreads();
+    for (uint32_t c0 = 0; c0 < size; c0 += BK_CAP) {
+        const uint32_t csize = min(BK_CAP, size - c0);
+        const uint32_t rounds = (csize + BK_THREADS - 1) / BK_THREADS;  // rounds per warp
+        for (int i = threadIdx.x; i < BK_WARPS * RADIX; i += BK_THREADS) sc.wcnt[i] = 0u;
+        __syncthreads();
+        uint32_t dig[BK_ITEMS], rank[BK_ITEMS];
+        uint32_t* wc = sc.wcnt + warp * RADIX;
+#pragma unroll
+        for (int it = 0; it < BK_ITEMS; it++) {
+            dig[it] = 0xFFFFu;
+            rank[it] = 0u;
+            if ((uint32_t)it < rounds) {
+                const uint32_t e = (uint32_t)warp * 32u * rounds + (uint32_t)it * 32u + (uint32_t)lane;
+                const bool ok = e < csize;
+                const uint32_t d = ok ? (uint32_t)(src_k[c0 + e] >> shift) & (RADIX - 1) : 0u;
+                const uint32_t peers = __match_any_sync(0xffffffffu, ok ? d : (0x10000u + lane));
+                uint32_t pre = 0;
+                if (ok) pre = wc[d];
+                __syncwarp();
+                if (ok && (peers & lt) == 0u) wc[d] = pre + __popc(peers);
+                __syncwarp();
+                if (ok) {
+                    dig[it] = d;
+                    rank[it] = pre + __popc(peers & lt);
+                }
+            }
+        }
+        __syncthreads();
+        // per digit: exclusive prefix over the 32 warps (8 groups of 4)
+        {
+            const int d = threadIdx.x & (RADIX - 1), q = threadIdx.x >> 7;
+            uint32_t r = 0;
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const uint32_t c = sc.wcnt[(4 * q + j) * RADIX + d];
+                sc.wcnt[(4 * q + j) * RADIX + d] = r;
+                r += c;
+            }
+            sc.gsum[q * RADIX + d] = r;
+        }
+        __syncthreads();
+        {
+            const int d = threadIdx.x & (RADIX - 1), q = threadIdx.x >> 7;
+            uint32_t add = 0;
+#pragma unroll
+            for (int j = 0; j < 8; j++) add += j < q ? sc.gsum[j * RADIX + d] : 0u;
+#pragma unroll
+            for (int j = 0; j < 4; j++) sc.wcnt[(4 * q + j) * RADIX + d] += add;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int it = 0; it < BK_ITEMS; it++) {
+            if (dig[it] == 0xFFFFu) continue;
+            const uint32_t e = (uint32_t)warp * 32u * rounds + (uint32_t)it * 32u + (uint32_t)lane;
+            const uint32_t P = sc.run[dig[it]] + sc.wcnt[warp * RADIX + dig[it]] + rank[it];
+            dst_k[P] = src_k[c0 + e];
+            dst_v[P] = src_v[c0 + e];
+        }
+        __syncthreads();
+        // the chunk's digit counts advance the running starts
+        if (threadIdx.x < RADIX) {
+            uint32_t tot = 0;
+#pragma unroll
+            for (int j = 0; j < 8; j++) tot += sc.gsum[j * RADIX + threadIdx.x];
+            sc.run[threadIdx.x] += tot;
+        }
+        __syncthreads();
+    }
+}
+
+// Bucket blockIdx.x of (Kb, Vb) -> its sorted low digits in (K, V).
+// A bucket larger than BK_CAP is left alone and raises *big, which enables
+// the full tile passes queued after this kernel.
+__global__ void __launch_bounds__(BK_THREADS, 1) k_bucket_sort(const uint64_t* __restrict__ Kb,
+                                                               const uint32_t* __restrict__ Vb,
+                                                               uint64_t* __restrict__ K, uint32_t* __restrict__ V,
+                                                               const uint32_t* __restrict__ hist_top,
+                                                               int low_passes, uint32_t* big, const uint32_t* enable) {
+    if (enable && *enable == 0u) return;
+    extern __shared__ __align__(16) unsigned char bk_smem[];
+    uint64_t* k0 = reinterpret_cast<uint64_t*>(bk_smem);
+    uint64_t* k1 = k0 + BK_CAP;
+    uint32_t* v0 = reinterpret_cast<uint32_t*>(k1 + BK_CAP);
+    uint32_t* v1 = v0 + BK_CAP;
+    BucketScratch sc;
+    sc.wcnt = v1 + BK_CAP;
+    sc.gsum = sc.wcnt + BK_WARPS * RADIX;
+    sc.run = sc.gsum + 8 * RADIX;
+    __shared__ uint32_t s_range[2];
+    const uint32_t b = blockIdx.x;
+    if (threadIdx.x < 32) {
+        uint32_t start = 0;
+        for (uint32_t j = threadIdx.x; j < b; j += 32) start += hist_top[j];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) start += __shfl_xor_sync(0xffffffffu, start, o);
+        if (threadIdx.x == 0) {
+            s_range[0] = start;
+            s_range[1] = hist_top[b];
+        }
+    }
+    __syncthreads();
+    const uint32_t start = s_range[0], size = s_range[1];
+    if (size == 0u) return;
+    if (size > BK_CAP) {
+        if (threadIdx.x == 0) atomicOr(big, 1u);
+        return;
+    }
+    for (uint32_t e = threadIdx.x; e < size; e += BK_THREADS) {
+        k0[e] = Kb[start + e];
+        v0[e] = Vb[start + e];
+    }
+    __syncthreads();
+    uint64_t *ka = k0, *kb = k1;
+    uint32_t *va = v0, *vb = v1;
+    for (int p = 0; p < low_passes; p++) {
+        bucket_pass(ka, va, kb, vb, size, p * RADIX_BITS, sc);
+        uint64_t* tk = ka;
+        ka = kb;
+        kb = tk;
+        uint32_t* tv = va;
+        va = vb;
+        vb = tv;
+    }
+    for (uint32_t e = threadIdx.x; e < size; e += BK_THREADS) {
+        K[start + e] = ka[e];
+        V[start + e] = va[e];
+    }
+}
+
+size_t bucket_sort_smem() { return (size_t)BK_CAP * 24 + sizeof(uint32_t) * (BK_WARPS * RADIX + 8 * RADIX + RADIX); }
 
 __global__ void k_copy_pairs(const uint64_t* __restrict__ ks, const uint32_t* __restrict__ vs,
                              uint64_t* __restrict__ kd, uint32_t* __restrict__ vd, uint32_t n,
@@ -179,7 +374,7 @@ int sf_sort_alloc(SortWork& w, size_t n) {
     SF_CUDA(cudaMalloc(&w.vals_b, sizeof(uint32_t) * (n ? n : 1)));
     SF_CUDA(cudaMalloc(&w.hist, sizeof(uint32_t) * MAX_PASSES * RADIX));
     SF_CUDA(cudaMalloc(&w.status, sizeof(uint32_t) * MAX_PASSES * tiles * RADIX));
-    SF_CUDA(cudaMalloc(&w.counters, sizeof(uint32_t) * MAX_PASSES));
+    SF_CUDA(cudaMalloc(&w.counters, sizeof(uint32_t) * (MAX_PASSES + 1)));  // + the bucket overflow flag
     w.cap = n;
     w.tiles_cap = tiles;
     return SFGPU_OK;
@@ -207,6 +402,54 @@ int sf_sort_pairs_keep(uint64_t* keys, uint32_t* vals, uint32_t n, int bits, Sor
     if (passes > MAX_PASSES) {
         sf_set_error("sort: %d key bits is too many", bits);
         return SFGPU_FAILURE;
+    }
+    // small arrays (where the per-pass tile look-back chains cost more than
+    // the data movement): one tile pass on the top digit, then one CTA per
+    // bucket for the rest; the result is left in (keys, vals)
+    if (n <= BUCKET_SORT_MAX && passes >= 2 && passes < MAX_PASSES && !(w.flags & SORT_NO_BUCKETS)) {
+        static bool smem_set = false;
+        if (!smem_set) {
+            SF_CUDA(cudaFuncSetAttribute(k_bucket_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)bucket_sort_smem()));
+            smem_set = true;
+        }
+        const int items = 4;
+        const uint32_t tiles = sf_ceil_div(n, SORT_THREADS * items);
+        uint32_t* big = w.counters + MAX_PASSES;
+        // pass slot 0: the top digit; slots 1..passes: the gated fallback
+        SF_CUDA(cudaMemsetAsync(w.hist, 0, sizeof(uint32_t) * passes * RADIX, st));
+        SF_CUDA(cudaMemsetAsync(w.counters, 0, sizeof(uint32_t) * (MAX_PASSES + 1), st));
+        SF_CUDA(cudaMemsetAsync(w.status, 0, sizeof(uint32_t) * (size_t)(passes + 1) * tiles * RADIX, st));
+        const uint32_t hb = std::min<uint32_t>(sf_ceil_div(n, 256 * 8), (uint32_t)sf_num_sms() * 4);
+        k_hist<<<hb, 256, 0, st>>>(keys, n, passes, w.hist, enable);
+        SF_CHECK_LAUNCH();
+        const int top = passes - 1;
+        k_onesweep<4><<<tiles, SORT_THREADS, 0, st>>>(keys, vals, w.keys_b, w.vals_b, n, top * RADIX_BITS,
+                                                      w.hist + top * RADIX, w.status, w.counters, d_status, enable);
+        SF_CHECK_LAUNCH();
+        k_bucket_sort<<<RADIX, BK_THREADS, bucket_sort_smem(), st>>>(w.keys_b, w.vals_b, keys, vals,
+                                                                     w.hist + top * RADIX, top, big, enable);
+        SF_CHECK_LAUNCH();
+        // fallback (only if a bucket overflowed): every pass from the top
+        // pass's output, which holds all pairs; ends in (keys, vals)
+        uint64_t* ka = w.keys_b;
+        uint32_t* va = w.vals_b;
+        uint64_t* kb = keys;
+        uint32_t* vb = vals;
+        for (int p = 0; p < passes; p++) {
+            k_onesweep<4><<<tiles, SORT_THREADS, 0, st>>>(ka, va, kb, vb, n, p * RADIX_BITS, w.hist + p * RADIX,
+                                                          w.status + (size_t)(p + 1) * tiles * RADIX,
+                                                          w.counters + p + 1, d_status, big);
+            SF_CHECK_LAUNCH();
+            std::swap(ka, kb);
+            std::swap(va, vb);
+        }
+        if (ka != keys) {
+            const uint32_t cb = std::min<uint32_t>(sf_ceil_div(n, 256), (uint32_t)sf_num_sms() * 8);
+            k_copy_pairs<<<cb, 256, 0, st>>>(ka, va, keys, vals, n, big);
+            SF_CHECK_LAUNCH();
+        }
+        return SFGPU_OK;
     }
     // keys per thread, measured on GB300 (7 passes of 49-bit keys): 4 up to
     // 2^17 keys (0.087 ms at 65,536, against 0.101 with 2 or 8), 8 above

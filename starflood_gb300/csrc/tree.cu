@@ -172,6 +172,57 @@ __device__ __forceinline__ uint32_t search_keys(const uint64_t* __restrict__ K, 
     return lower_bound_shift(K, a, b, shift, target);
 }
 
+// First index in [from, end) whose key >> shift is >= target, where
+// K[from] >> shift < target: probes from+1, from+3, from+7, ... then bisects
+// the last gap, O(log d) loads for an answer d slots away.
+__device__ __forceinline__ uint32_t gallop_up(const uint64_t* __restrict__ K, uint32_t from, uint32_t end, int shift,
+                                              uint64_t target) {
+    uint32_t prev = from, step = 1;
+    while (true) {
+        const uint32_t probe = prev + step;
+        if (probe >= end || probe < prev) return lower_bound_shift(K, prev + 1, end, shift, target);
+        if ((K[probe] >> shift) >= target) return lower_bound_shift(K, prev + 1, probe, shift, target);
+        prev = probe;
+        step <<= 1;
+    }
+}
+// First index in [0, from] whose key >> shift is >= target, where
+// K[from] >> shift >= target: probes from-1, from-2, from-4, ... backwards.
+__device__ __forceinline__ uint32_t gallop_down(const uint64_t* __restrict__ K, uint32_t from, int shift,
+                                                uint64_t target) {
+    uint32_t cur = from, step = 1;
+    while (true) {
+        if (cur < step) return lower_bound_shift(K, 0, cur, shift, target);
+        const uint32_t probe = cur - step;
+        if ((K[probe] >> shift) < target) return lower_bound_shift(K, probe + 1, cur, shift, target);
+        cur = probe;
+        step <<= 1;
+    }
+}
+
+// The run of keys with K[i] >> shift == pre around `home` (whose key has that
+// prefix): the TIE_WIN neighbours on each side are loaded at once (one memory
+// latency; deep cells rarely hold more), and only a run reaching past them
+// is galloped further.
+constexpr int TIE_WIN = 8;
+__device__ __forceinline__ void run_near(const uint64_t* __restrict__ K, uint32_t home, uint32_t end, int shift,
+                                         uint64_t pre, uint32_t& lo, uint32_t& hi) {
+    uint32_t eqa = 0u, eqb = 0u;
+#pragma unroll
+    for (int j = 0; j < TIE_WIN; j++) {
+        const bool ina = home >= (uint32_t)(j + 1);
+        const bool inb = home + 1u + (uint32_t)j < end;
+        const uint64_t ka = ina ? K[home - 1u - (uint32_t)j] : 0ull;
+        const uint64_t kb = inb ? K[home + 1u + (uint32_t)j] : 0ull;
+        eqa |= (uint32_t)(ina && (ka >> shift) == pre) << j;
+        eqb |= (uint32_t)(inb && (kb >> shift) == pre) << j;
+    }
+    // sorted keys: the equal neighbours on each side are a prefix of the bits
+    const int dl = __ffs(~eqa) - 1, du = __ffs(~eqb) - 1;
+    lo = dl < TIE_WIN ? home - (uint32_t)dl : gallop_down(K, home - TIE_WIN, shift, pre);
+    hi = du < TIE_WIN ? home + 1u + (uint32_t)du : gallop_up(K, home + TIE_WIN, end, shift, pre + 1);
+}
+
 // Exact digits for bodies lying on a midplane (one block; see file comment).
 // Reads the sorted provisional keys (Ks, Vs); the bodies whose digits change
 // are listed for k_tie_merge: their old slots ascending (gpos), their new
@@ -190,6 +241,7 @@ __global__ void __launch_bounds__(FIX_THREADS) k_tie_fix(const float* __restrict
     __shared__ uint32_t body[TIE_CAP];
     __shared__ uint32_t mask[TIE_CAP];
     __shared__ uint64_t samp[NSAMP];
+    __shared__ uint32_t home[TIE_CAP];  // a sorted slot holding the body's provisional key
     const uint32_t T = min(*tie_count, TIE_CAP);
     if (T == 0) {
         if (threadIdx.x == 0) *moved_out = 0u;
@@ -208,6 +260,52 @@ __global__ void __launch_bounds__(FIX_THREADS) k_tie_fix(const float* __restrict
         cur[t] = prov[t];
     }
     __syncthreads();
+    for (uint32_t t = threadIdx.x; t < T; t += FIX_THREADS) home[t] = search_keys(K, samp, ks, 0, prov[t]);
+    __syncthreads();
+
+    // Speculation: while no body moves, every cell count is the provisional
+    // one, so each body settles its own tie levels in order without waiting
+    // for the others (the usual case: deep ties inside leaves).  A body that
+    // would move ends the speculation; the level-by-level pass below then
+    // decides everything from scratch.
+    __shared__ int s_move;
+    if (threadIdx.x == 0) s_move = 0;
+    __syncthreads();
+    for (uint32_t t = threadIdx.x; t < T; t += FIX_THREADS) {
+        const uint32_t mk = mask[t];
+        const uint32_t p = body[t];
+        for (int L = 0; L < (int)depth_max && L < 16; L++) {
+            if (!((mk >> L) & 1u)) continue;
+            uint32_t lo = 0u, hi = nin;
+            if (L > 0) run_near(K, home[t], nin, 3 * (16 - L), prefix_of(prov[t], L), lo, hi);
+            if (hi - lo <= leaf_cap) break;  // a leaf: deeper digits unused
+            uint32_t seen = 0;
+            for (uint32_t k = lo; k < hi && seen < leaf_cap; k += 4) {
+                uint32_t v4[4];
+#pragma unroll
+                for (int j = 0; j < 4; j++) v4[j] = (k + (uint32_t)j < hi) ? V[k + (uint32_t)j] : 0xFFFFFFFFu;
+#pragma unroll
+                for (int j = 0; j < 4; j++) seen += (v4[j] < p) ? 1u : 0u;
+            }
+            const bool strict = seen < leaf_cap;
+            const float x[3] = {pos[3u * p], pos[3u * p + 1u], pos[3u * p + 2u]};
+            const Cube c = cube_of(bounds, prov[t], L);
+            uint32_t o = 0;
+            for (int a = 0; a < 3; a++) {
+                const float m = midf(c.lo[a], c.hi[a]);
+                o |= ((strict ? (m < x[a]) : (m <= x[a])) ? 1u : 0u) << a;
+            }
+            if (o != ((uint32_t)(prov[t] >> (3 * (15 - L))) & 7u)) {
+                s_move = 1;
+                break;
+            }
+        }
+    }
+    __syncthreads();
+    if (!s_move) {
+        if (threadIdx.x == 0) *moved_out = 0u;
+        return;
+    }
 
     // Levels in order; within a level every midplane body is settled by its
     // own thread: membership of a level-L cell can only have been changed by
@@ -221,8 +319,17 @@ __global__ void __launch_bounds__(FIX_THREADS) k_tie_fix(const float* __restrict
             if (!((mask[t] >> L) & 1u)) continue;
             const uint64_t pre = prefix_of(cur[t], L);
             const int shift = 3 * (16 - L);
-            const uint32_t lo = (L == 0) ? 0u : search_keys(K, samp, ks, shift, pre);
-            const uint32_t hi = (L == 0) ? nin : search_keys(K, samp, ks, shift, pre + 1);
+            // the level-L cell's slots: galloped from the body's own slot while
+            // it has not moved (deep cells are short runs), else searched
+            uint32_t lo = 0u, hi = nin;
+            if (L > 0) {
+                if (prefix_of(prov[t], L) == pre) {
+                    run_near(K, home[t], nin, shift, pre, lo, hi);
+                } else {
+                    lo = search_keys(K, samp, ks, shift, pre);
+                    hi = search_keys(K, samp, ks, shift, pre + 1);
+                }
+            }
             const uint32_t p = body[t];
             uint32_t add = 0, sub = 0, radd = 0, rsub = 0;
             for (uint32_t m = 0; m < n_moved; m++) {
@@ -241,7 +348,13 @@ __global__ void __launch_bounds__(FIX_THREADS) k_tie_fix(const float* __restrict
             // leaf_cap (stop once enough smaller indices are seen)
             const uint32_t need = leaf_cap + rsub;
             uint32_t seen = 0;
-            for (uint32_t k = lo; k < hi && seen < need; k++) seen += (V[k] < p) ? 1u : 0u;
+            for (uint32_t k = lo; k < hi && seen < need; k += 4) {  // four independent loads a round
+                uint32_t v4[4];
+#pragma unroll
+                for (int j = 0; j < 4; j++) v4[j] = (k + (uint32_t)j < hi) ? V[k + (uint32_t)j] : 0xFFFFFFFFu;
+#pragma unroll
+                for (int j = 0; j < 4; j++) seen += (v4[j] < p) ? 1u : 0u;
+            }
             const uint32_t rank = seen + radd - rsub;
             const bool strict = rank < leaf_cap;
             const float x[3] = {pos[3u * p], pos[3u * p + 1u], pos[3u * p + 2u]};

@@ -467,10 +467,15 @@ int launch_body(sfgpu_sim* s, bool stats) {
 // memory that all 32 lanes then run through with dense monopole
 // interactions.  Every body ends up with exactly the cells the reference
 // gives it (the per-body interaction counts are checked in the tests).
+// Bodies per group of the group walk unless sfgpu_params.walk_group says
+// otherwise.  On the 65,536-body uniform sphere (one GB300): 32 bodies
+// 0.157 ms, 16 bodies 0.137 ms per walk.
+constexpr uint32_t WALK_GROUP_DEFAULT = 16;
 constexpr int GW_WARPS = 4;
 constexpr int GW_THREADS = GW_WARPS * 32;
 constexpr int GW_STACK = 512;
-constexpr int GW_LIST = 256;  // accepted cells whose bounds miss the group box
+constexpr int GW_LIST = 128;  // accepted cells whose bounds miss the group box
+constexpr int GW_MIN_BLOCKS = 7;  // resident blocks per SM the register budget is cut for
 constexpr int GW_SLOW = 64;   // accepted cells that may contain a body (self-exclusion test)
 
 // Per-warp lists in shared memory.  The fast list holds the monopole itself
@@ -492,12 +497,16 @@ struct GroupLists {
 // so the inner loop has no per-lane branch.  FAST kind evaluates two entries
 // per instruction (paired FP32), each element rounded as the scalar code
 // would; COMP kind adds each interaction to Kahan sums in list order.
-template <int KIND>
-__device__ __forceinline__ void flush_fast(const GroupLists& L, int count, int lane, float rx, float ry, float rz,
-                                           float eps2, float2& a2x, float2& a2y, float2& a2z, float2& p2,
+// With 16- or 8-body groups the 2 or 4 sub-warps hold the same bodies and
+// take entries in turn (FAST: entry pairs), `lane` being the body slot and
+// `half` the sub-warp.
+template <int KIND, int GB>
+__device__ __forceinline__ void flush_fast(const GroupLists& L, int count, int lane, int half, float rx, float ry,
+                                           float rz, float eps2, float2& a2x, float2& a2y, float2& a2z, float2& p2,
                                            KSum& ax, KSum& ay, KSum& az, KSum& ph, uint32_t& n_int) {
+    constexpr int H = 32 / GB;  // half-warps sharing the list
     if (KIND == WALK_COMP) {
-        for (int e = 0; e < count; e++) {
+        for (int e = half; e < count; e += H) {
             const uint32_t M = L.msk[e];
             if ((M >> lane) & 1u) {
                 const float dx = L.x[e] - rx, dy = L.y[e] - ry, dz = L.z[e] - rz;
@@ -517,7 +526,7 @@ __device__ __forceinline__ void flush_fast(const GroupLists& L, int count, int l
     const float2 nrx = make_float2(-rx, -rx), nry = make_float2(-ry, -ry), nrz = make_float2(-rz, -rz);
     const float2 e2 = make_float2(eps2, eps2);
 #pragma unroll 2
-    for (int e = 0; e < count; e += 2) {  // count is even (padded by the caller)
+    for (int e = 2 * half; e < count; e += 2 * H) {  // count is a multiple of 2H (padded by the caller)
         const float2 X = *reinterpret_cast<const float2*>(&L.x[e]);
         const float2 Y = *reinterpret_cast<const float2*>(&L.y[e]);
         const float2 Z = *reinterpret_cast<const float2*>(&L.z[e]);
@@ -543,11 +552,11 @@ __device__ __forceinline__ void flush_fast(const GroupLists& L, int count, int l
     }
 }
 
-template <int KIND>
-__device__ __forceinline__ void flush_slow(const GroupLists& L, int count, const NodeArrays& nd, int lane, float rx,
-                                           float ry, float rz, float mi, float eps2, KSum& ax, KSum& ay, KSum& az,
-                                           KSum& ph, uint32_t& n_int) {
-    for (int e = 0; e < count; e++) {
+template <int KIND, int GB>
+__device__ __forceinline__ void flush_slow(const GroupLists& L, int count, const NodeArrays& nd, int lane, int half,
+                                           float rx, float ry, float rz, float mi, float eps2, KSum& ax, KSum& ay,
+                                           KSum& az, KSum& ph, uint32_t& n_int) {
+    for (int e = half; e < count; e += 32 / GB) {
         const uint32_t v = L.qn[e];
         const uint32_t M = L.qm[e];
         const float4 C = __ldg(&nd.com[NODE_REC * v]);
@@ -589,8 +598,8 @@ __device__ __forceinline__ void append_cells(const GroupLists& L, uint32_t am, u
     qcount += __popc(sb);
 }
 
-template <int KIND, int GSPLIT, bool STATS>
-__global__ void __launch_bounds__(GW_THREADS) k_walk_group(const float4* __restrict__ sp,
+template <int KIND, int GSPLIT, int GB, bool STATS>
+__global__ void __launch_bounds__(GW_THREADS, GW_MIN_BLOCKS) k_walk_group(const float4* __restrict__ sp,
                                                            const uint32_t* __restrict__ V, uint32_t n, NodeArrays nd,
                                                            ForceConsts fc, float th_lo, float th_hi,
                                                            float th_acc, float th_open, uint32_t leaf_cap,
@@ -609,24 +618,30 @@ __global__ void __launch_bounds__(GW_THREADS) k_walk_group(const float4* __restr
     __shared__ uint32_t q_node[GW_WARPS][GW_SLOW];
     __shared__ uint32_t q_mask[GW_WARPS][GW_SLOW];
     __shared__ float4 s_body[GW_WARPS][32];
-    __shared__ uint32_t f_node[GW_WARPS][80];  // top-level frontiers: [0,8) level 1, [8,72) level 2
-    __shared__ uint32_t f_mask[GW_WARPS][80];
+    constexpr int FRONT = GSPLIT > 1 ? 80 : 1;
+    __shared__ uint32_t f_node[GW_WARPS][FRONT];  // top-level frontiers: [0,8) level 1, [8,72) level 2
+    __shared__ uint32_t f_mask[GW_WARPS][FRONT];
     const int lane = threadIdx.x & 31;
     const int w = threadIdx.x >> 5;
     float4* sbd = s_body[w];
     uint32_t* stn = s_node[w];
     uint32_t* stm = s_mask[w];
     const GroupLists L{l_x[w], l_y[w], l_z[w], l_m[w], l_k[w], q_node[w], q_mask[w]};
+    static_assert(GB == 32 || ((GB == 16 || GB == 8) && GSPLIT == 1), "8- and 16-body groups walk unsplit");
     const uint32_t gw = blockIdx.x * GW_WARPS + w;
     const uint32_t group = gw / GSPLIT;
     const uint32_t oct = gw % GSPLIT;
-    const uint32_t k = group * 32u + lane;
+    // body slot of the lane (both half-warps hold the same 16 bodies when GB = 16)
+    const int bl = lane & (GB - 1), half = lane / GB;
+    const uint32_t body_bits = GB == 32 ? 0xffffffffu : (1u << GB) - 1u;
+    const uint32_t k = group * (uint32_t)GB + (uint32_t)bl;
     const bool live = k < n;
-    const uint32_t live_mask = __ballot_sync(0xffffffffu, live);
+    const uint32_t live_mask = __ballot_sync(0xffffffffu, live) & body_bits;
     if (!live_mask) return;
-    const float4 b = live ? sp[k] : sp[group * 32u];
+    const float4 b = live ? sp[k] : sp[group * (uint32_t)GB];
     const float rx = b.x, ry = b.y, rz = b.z, mi = b.w;
-    sbd[lane] = b;
+    if (half == 0) sbd[bl] = b;
+    __syncwarp();
     // bounding box of the group (dead lanes repeat the first body)
     float bx0 = rx, by0 = ry, bz0 = rz, bx1 = rx, by1 = ry, bz1 = rz;
     for (int o = 16; o > 0; o >>= 1) {
@@ -643,22 +658,24 @@ __global__ void __launch_bounds__(GW_THREADS) k_walk_group(const float4* __restr
     unsigned long long open_total = 0;
     int top = 0, count = 0, qcount = 0;
     auto flush = [&](bool all) {
-        if (all || count > GW_LIST - 34) {
-            if (KIND != WALK_COMP && (count & 1)) {  // pad to an even count with an entry no lane takes
-                if (lane == 0) {
-                    L.x[count] = L.y[count] = L.z[count] = 0.f;
-                    L.m[count] = 0.f;
-                    L.msk[count] = 0u;
-                }
-                count++;
-                __syncwarp();
+        if (all || count > GW_LIST - 36) {
+            // FAST: pad to a multiple of 2 (4 with two half-warps) with
+            // entries no lane takes
+            constexpr int PAD = KIND == WALK_COMP ? 1 : 2 * (32 / GB);
+            const int padded = (count + PAD - 1) / PAD * PAD;
+            if (lane < padded - count) {
+                L.x[count + lane] = L.y[count + lane] = L.z[count + lane] = 0.f;
+                L.m[count + lane] = 0.f;
+                L.msk[count + lane] = 0u;
             }
-            flush_fast<KIND>(L, count, lane, rx, ry, rz, fc.eps2, a2x, a2y, a2z, p2, ax, ay, az, ph, n_int);
+            count = padded;
+            __syncwarp();
+            flush_fast<KIND, GB>(L, count, bl, half, rx, ry, rz, fc.eps2, a2x, a2y, a2z, p2, ax, ay, az, ph, n_int);
             count = 0;
             __syncwarp();
         }
         if (all || qcount > GW_SLOW - 32) {
-            flush_slow<KIND>(L, qcount, nd, lane, rx, ry, rz, mi, fc.eps2, ax, ay, az, ph, n_int);
+            flush_slow<KIND, GB>(L, qcount, nd, bl, half, rx, ry, rz, mi, fc.eps2, ax, ay, az, ph, n_int);
             qcount = 0;
             __syncwarp();
         }
@@ -813,7 +830,8 @@ __global__ void __launch_bounds__(GW_THREADS) k_walk_group(const float4* __restr
         const uint32_t mix_b = __ballot_sync(0xffffffffu, mixed);
         uint32_t om = 0u;
         if (mix_b) {
-            const int rounds_cell = __popc(mix_b);
+            constexpr int H = 32 / GB;  // sub-warps, each testing one cell per round
+            const int rounds_cell = (__popc(mix_b) + H - 1) / H;
             const int rounds_body = __reduce_max_sync(0xffffffffu, mixed ? (uint32_t)__popc(M) : 0u);
             if (rounds_body <= rounds_cell) {
                 if (mixed) {
@@ -826,16 +844,25 @@ __global__ void __launch_bounds__(GW_THREADS) k_walk_group(const float4* __restr
                     }
                 }
             } else {
+                // sub-warp h takes the h-th remaining mixed cell, one lane per body
                 uint32_t cells = mix_b;
                 while (cells) {
-                    const int l = __ffs(cells) - 1;
-                    cells &= cells - 1u;
-                    const float4 Gl = make_float4(__shfl_sync(0xffffffffu, G.x, l), __shfl_sync(0xffffffffu, G.y, l),
-                                                  __shfl_sync(0xffffffffu, G.z, l), __shfl_sync(0xffffffffu, G.w, l));
-                    const uint32_t Ml = __shfl_sync(0xffffffffu, M, l);
-                    const bool t = ((Ml >> lane) & 1u) && opens(Gl, rx, ry, rz, fc, th_lo, th_hi);
+                    uint32_t c = cells;
+                    for (int j = 0; j < half; j++) c &= c - 1u;
+                    const int l = c ? __ffs(c) - 1 : -1;
+                    const int src = l < 0 ? 0 : l;
+                    const float4 Gl = make_float4(__shfl_sync(0xffffffffu, G.x, src), __shfl_sync(0xffffffffu, G.y, src),
+                                                  __shfl_sync(0xffffffffu, G.z, src), __shfl_sync(0xffffffffu, G.w, src));
+                    const uint32_t Ml = __shfl_sync(0xffffffffu, M, src);
+                    const bool t = l >= 0 && ((Ml >> bl) & 1u) && opens(Gl, rx, ry, rz, fc, th_lo, th_hi);
                     const uint32_t ol = __ballot_sync(0xffffffffu, t);
-                    if (lane == l) om = ol;
+#pragma unroll
+                    for (int h = 0; h < H; h++) {
+                        const int lh = __shfl_sync(0xffffffffu, l, h * GB);
+                        if (lane == lh) om = (ol >> (h * GB)) & body_bits;
+                    }
+#pragma unroll
+                    for (int h = 0; h < H; h++) cells &= cells - 1u;
                 }
             }
         }
@@ -857,26 +884,35 @@ __global__ void __launch_bounds__(GW_THREADS) k_walk_group(const float4* __restr
             for (int l = 0; l < pops; l++) {
                 const bool il = __shfl_sync(0xffffffffu, internal, l);
                 const uint32_t ml = __shfl_sync(0xffffffffu, M, l);
-                if (il && ((ml >> lane) & 1u)) n_open++;
+                if (il && half == 0 && ((ml >> bl) & 1u)) n_open++;
             }
         }
         flush(false);
     }
     flush(true);
-    if (live) {
+    float sx = ax.s, sy = ay.s, sz = az.s, sw = ph.s;
+    if (KIND == WALK_COMP) {
+        sx -= ax.c;
+        sy -= ay.c;
+        sz -= az.c;
+        sw -= ph.c;
+    } else {
+        sx += a2x.x + a2x.y;
+        sy += a2y.x + a2y.y;
+        sz += a2z.x + a2z.y;
+        sw += p2.x + p2.y;
+    }
+    uint32_t n_int_body = n_int;
+#pragma unroll
+    for (int o = 16; o >= GB; o >>= 1) {  // the sub-warps' shares of the same bodies
+        sx += __shfl_xor_sync(0xffffffffu, sx, o);
+        sy += __shfl_xor_sync(0xffffffffu, sy, o);
+        sz += __shfl_xor_sync(0xffffffffu, sz, o);
+        sw += __shfl_xor_sync(0xffffffffu, sw, o);
+        n_int_body += __shfl_xor_sync(0xffffffffu, n_int_body, o);
+    }
+    if (live && half == 0) {
         const uint32_t p = V[k];
-        float sx = ax.s, sy = ay.s, sz = az.s, sw = ph.s;
-        if (KIND == WALK_COMP) {
-            sx -= ax.c;
-            sy -= ay.c;
-            sz -= az.c;
-            sw -= ph.c;
-        } else {
-            sx += a2x.x + a2x.y;
-            sy += a2y.x + a2y.y;
-            sz += a2z.x + a2z.y;
-            sw += p2.x + p2.y;
-        }
         if (GSPLIT == 1) {
             const float g = -fc.neg_g;
             const float scale = fc.physical ? g : g * mi;
@@ -885,13 +921,13 @@ __global__ void __launch_bounds__(GW_THREADS) k_walk_group(const float4* __restr
             acc[3u * p + 2u] = scale * sz;
             pot[p] = fc.neg_g * sw;
             if (STATS) {
-                st_int[p] = n_int;
+                st_int[p] = n_int_body;
                 st_open[p] = n_open;
             }
         } else {
             part[(size_t)oct * n + k] = make_float4(sx, sy, sz, sw);
             if (STATS) {
-                atomicAdd(&st_int[p], n_int);
+                atomicAdd(&st_int[p], n_int_body);
                 atomicAdd(&st_open[p], n_open);
             }
         }
@@ -907,7 +943,7 @@ __global__ void __launch_bounds__(GW_THREADS) k_walk_group(const float4* __restr
     }
 }
 
-template <int KIND, int GSPLIT>
+template <int KIND, int GSPLIT, int GB = 32>
 int launch_group(sfgpu_sim* s, bool stats) {
     TreeWork* t = s->tree;
     const ForceConsts fc = sf_force_consts(s->p);
@@ -915,7 +951,7 @@ int launch_group(sfgpu_sim* s, bool stats) {
     const float th_hi = fc.theta * (1.0f + 1.0f / 524288.0f);
     const float th_acc = fc.theta * (1.0f - 1.0f / 4096.0f);
     const float th_open = fc.theta * (1.0f + 1.0f / 4096.0f);
-    const uint32_t grid = sf_ceil_div((uint64_t)sf_ceil_div(s->n, 32) * GSPLIT, GW_WARPS);
+    const uint32_t grid = sf_ceil_div((uint64_t)sf_ceil_div(s->n, GB) * GSPLIT, GW_WARPS);
     float* acc = s->slab + (size_t)6 * s->n;
     float* pot = s->slab + (size_t)10 * s->n;
     if (stats) {
@@ -923,11 +959,11 @@ int launch_group(sfgpu_sim* s, bool stats) {
             SF_CUDA(cudaMemsetAsync(s->stat_int, 0, sizeof(uint32_t) * s->n, s->stream));
             SF_CUDA(cudaMemsetAsync(s->stat_open, 0, sizeof(uint32_t) * s->n, s->stream));
         }
-        k_walk_group<KIND, GSPLIT, true><<<grid, GW_THREADS, 0, s->stream>>>(
+        k_walk_group<KIND, GSPLIT, GB, true><<<grid, GW_THREADS, 0, s->stream>>>(
             t->sp, t->vals, s->n, t->nd, fc, th_lo, th_hi, th_acc, th_open, s->p.leaf_cap, t->walk_part, acc, pot,
             s->stat_int, s->stat_open, s->walk_tot, s->d_status);
     } else {
-        k_walk_group<KIND, GSPLIT, false><<<grid, GW_THREADS, 0, s->stream>>>(
+        k_walk_group<KIND, GSPLIT, GB, false><<<grid, GW_THREADS, 0, s->stream>>>(
             t->sp, t->vals, s->n, t->nd, fc, th_lo, th_hi, th_acc, th_open, s->p.leaf_cap, t->walk_part, acc, pot,
             nullptr, nullptr, s->walk_tot, s->d_status);
     }
@@ -942,17 +978,19 @@ int launch_group(sfgpu_sim* s, bool stats) {
 
 template <int KIND>
 int launch_fast(sfgpu_sim* s, bool stats) {
-    // walk_split: 0 or 32 (default) group walk; 1 one thread per body; 8 one
-    // thread per body and root octant; 64 group walk with the level-2
-    // frontier dealt over 8 warps per group.  Measured on the 65,536-body
-    // uniform sphere the plain group walk is the fastest (the split variants
-    // pay for their redundant top levels and imbalance more than they gain
-    // in occupancy).
+    // walk_split: 0 or 32 (default) group walk of walk_group bodies per warp
+    // (0 = the default size, 8, 16 or 32); 1 one thread per body; 8 one
+    // thread per body and root octant; 64 32-body group walk with the
+    // level-2 frontier dealt over 8 warps per group.  The split variants pay
+    // for their redundant top levels and imbalance more than they gain.
     const uint32_t split = s->p.walk_split;
     if (split == 1) return launch_body<KIND, 1>(s, stats);
     if (split == 8) return launch_body<KIND, SPLIT>(s, stats);
     if (split == 64) return launch_group<KIND, SPLIT>(s, stats);
-    return launch_group<KIND, 1>(s, stats);
+    const uint32_t gb = s->p.walk_group ? s->p.walk_group : WALK_GROUP_DEFAULT;
+    if (gb == 8) return launch_group<KIND, 1, 8>(s, stats);
+    if (gb == 16) return launch_group<KIND, 1, 16>(s, stats);
+    return launch_group<KIND, 1, 32>(s, stats);
 }
 
 }  // namespace

@@ -172,14 +172,16 @@ def test_tree_outside_and_nan_bodies(sf, oracle32):
     np.testing.assert_array_equal(v["pot"], pt)
 
 
-@pytest.mark.parametrize("split", [0, 1, 8, 64])
+@pytest.mark.parametrize("split,group", [(0, 0), (0, 8), (0, 16), (0, 32), (1, 0), (8, 0), (64, 0)])
 @pytest.mark.parametrize("n,seed", [(65536, 2), (20000, 8)])
-def test_tree_fast_large(sf, oracle32, n, seed, split):
-    """FAST walks (group walk; one thread per body; per body and root octant)."""
+def test_tree_fast_large(sf, oracle32, n, seed, split, group):
+    """FAST walks (group walk of 8, 16, 32 bodies; one thread per body; per
+    body and root octant; 32-body groups split over 8 warps)."""
     from starflood_gb300.ics import uniform_ball, plummer
     gen = uniform_ball if n == 65536 else plummer
     pos, vel, mas = gen(n, seed=seed)
-    p = sf.default_params(solver=sf.SOLVER_TREE, eps=0.01, theta=0.5, flags=sf.FLAG_STATS, walk_split=split)
+    p = sf.default_params(solver=sf.SOLVER_TREE, eps=0.01, theta=0.5, flags=sf.FLAG_STATS, walk_split=split,
+                          walk_group=group)
     with sf.Sim(n, p) as s:
         s.set_state(pos, vel, mas)
         s.solve(5)
