@@ -231,19 +231,6 @@ struct StageTimer {
 };
 
 // ---------------------------------------------------------------------------
-// 3-phase exclusive scans (scan.cu)
-// ---------------------------------------------------------------------------
-struct ScanWork {
-    void* partials = nullptr;   // per-block sums
-    size_t cap_blocks = 0;
-};
-int sf_scan_reserve(ScanWork& w, uint32_t n, size_t elem);
-// exclusive scan of n uint32 values (out may alias in), total written to *d_total.
-int sf_scan_u32(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* d_total, ScanWork& w,
-                cudaStream_t st, const uint32_t* d_n = nullptr);
-// exclusive scan of n sfd4 values; out has n+1 entries (out[n] = total).
-
-// ---------------------------------------------------------------------------
 // radix sort of (u64 key, u32 value) pairs on the low `bits` key bits (sort.cu)
 // ---------------------------------------------------------------------------
 struct SortWork {

@@ -21,6 +21,24 @@ constexpr uint32_t VALUE_MASK = (1u << 30) - 1u;
 constexpr uint32_t SPIN_LIMIT = 1u << 24;
 constexpr int LOOKBACK = 16;  // predecessor words read per look-back round
 
+// The lanes of the warp holding the same 7-bit digit as this one (only this
+// lane when !ok): the intersection of one ballot per digit bit, a fixed
+// count of single-cycle votes.
+__device__ __forceinline__ uint32_t digit_peers(uint32_t d, bool ok, int lane) {
+#ifdef SORT_PEERS_MATCH
+    return __match_any_sync(0xffffffffu, ok ? d : (0x10000u + (uint32_t)lane));
+#else
+    uint32_t m = __ballot_sync(0xffffffffu, ok);
+#pragma unroll
+    for (int b = 0; b < RADIX_BITS; b++) {
+        const uint32_t bit = (d >> b) & 1u;
+        const uint32_t bb = __ballot_sync(0xffffffffu, bit != 0u);
+        m &= bit ? bb : ~bb;
+    }
+    return ok ? m : (1u << lane);
+#endif
+}
+
 __global__ void __launch_bounds__(256) k_hist(const uint64_t* __restrict__ keys, uint32_t n, int passes,
                                               uint32_t* __restrict__ hist, const uint32_t* enable) {
     if (enable && *enable == 0u) return;
@@ -96,7 +114,7 @@ __global__ void __launch_bounds__(SORT_THREADS) k_onesweep(
         val[it] = ok ? vin[e] : 0u;
         const uint32_t d = (uint32_t)(key[it] >> shift) & (RADIX - 1);
         dig[it] = ok ? d : 0xFFFFu;
-        const uint32_t peers = __match_any_sync(0xffffffffu, ok ? d : (0x10000u + lane));
+        const uint32_t peers = digit_peers(d, ok, lane);
         uint32_t pre = 0;
         if (ok) pre = wcnt[warp][d];
         __syncwarp();
@@ -190,111 +208,96 @@ constexpr uint32_t BK_CAP = BK_THREADS * BK_ITEMS;  // 8192 pairs, 12 B each, tw
 
 struct BucketScratch {
     uint32_t* wcnt;   // [BK_WARPS][RADIX] per-warp counts, then their exclusive prefix
-    uint32_t* gsum;   // [8][RADIX] warp-group totals / digit scan scratch
-    uint32_t* run;    // [RADIX] running start of each digit in the destination
+    uint32_t* gsum;   // [8][RADIX] warp-group totals
+    uint32_t* run;    // [RADIX] start of each digit in the destination
+    uint32_t* wtot;   // [4] digit-scan warp totals
 };
 
-// One stable pass over [0, size) of src into dst (shared memory), chunk by
-// chunk of BK_CAP pairs; digit = (key >> shift) & 127.
-__device__ void bucket_pass(const uint64_t* src_k, const uint32_t* src_v, uint64_t* dst_k, uint32_t* dst_v,
-                            uint32_t size, int shift, const BucketScratch& sc) {
+// One stable pass over [0, size <= BK_CAP) of src into dst (shared memory);
+// digit = (key >> shift) & 127.  Warp w ranks positions [w 32 R, (w+1) 32 R)
+// in R = ceil(size / 1024) rounds of 32 consecutive keys.
+__device__ __forceinline__ void bucket_pass(const uint64_t* src_k, const uint32_t* src_v, uint64_t* dst_k,
+                                            uint32_t* dst_v, uint32_t size, int shift, const BucketScratch& sc) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t lt = (1u << lane) - 1u;
-    // digit totals of the whole range -> exclusive digit starts
-    if (threadIdx.x < RADIX) sc.run[threadIdx.x] = 0u;
+    const uint32_t rounds = (size + BK_THREADS - 1) / BK_THREADS;
+    for (int i = threadIdx.x; i < BK_WARPS * RADIX; i += BK_THREADS) sc.wcnt[i] = 0u;
     __syncthreads();
-    for (uint32_t e = threadIdx.x; e < size; e += BK_THREADS)
-        atomicAdd(&sc.run[(uint32_t)(src_k[e] >> shift) & (RADIX - 1)], 1u);
-    __syncthreads();
-    if (threadIdx.x < RADIX) {
-        const uint32_t v = sc.run[threadIdx.x];
-        uint32_t x = v;
+    uint32_t dig[BK_ITEMS], rank[BK_ITEMS];
+    uint32_t* wc = sc.wcnt + warp * RADIX;
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane >= o) x += y;
-        }
-        sc.gsum[threadIdx.x] = x;
-        sc.run[threadIdx.x] = x - v;  // exclusive within the warp; earlier warps added below
-    }
-    __syncthreads();
-    if (threadIdx.x < RADIX) {
-        uint32_t add = 0;
-        for (int w = 0; w < (int)(threadIdx.x >> 5); w++) add += sc.gsum[w * 32 + 31];
-        sc.run[threadIdx.x] += add;
-    }
-    __syncthreads();
-    for (uint32_t c0 = 0; c0 < size; c0 += BK_CAP) {
-        const uint32_t csize = min(BK_CAP, size - c0);
-        const uint32_t rounds = (csize + BK_THREADS - 1) / BK_THREADS;  // rounds per warp
-        for (int i = threadIdx.x; i < BK_WARPS * RADIX; i += BK_THREADS) sc.wcnt[i] = 0u;
-        __syncthreads();
-        uint32_t dig[BK_ITEMS], rank[BK_ITEMS];
-        uint32_t* wc = sc.wcnt + warp * RADIX;
-#pragma unroll
-        for (int it = 0; it < BK_ITEMS; it++) {
-            dig[it] = 0xFFFFu;
-            rank[it] = 0u;
-            if ((uint32_t)it < rounds) {
-                const uint32_t e = (uint32_t)warp * 32u * rounds + (uint32_t)it * 32u + (uint32_t)lane;
-                const bool ok = e < csize;
-                const uint32_t d = ok ? (uint32_t)(src_k[c0 + e] >> shift) & (RADIX - 1) : 0u;
-                const uint32_t peers = __match_any_sync(0xffffffffu, ok ? d : (0x10000u + lane));
-                uint32_t pre = 0;
-                if (ok) pre = wc[d];
-                __syncwarp();
-                if (ok && (peers & lt) == 0u) wc[d] = pre + __popc(peers);
-                __syncwarp();
-                if (ok) {
-                    dig[it] = d;
-                    rank[it] = pre + __popc(peers & lt);
-                }
-            }
-        }
-        __syncthreads();
-        // per digit: exclusive prefix over the 32 warps (8 groups of 4)
-        {
-            const int d = threadIdx.x & (RADIX - 1), q = threadIdx.x >> 7;
-            uint32_t r = 0;
-#pragma unroll
-            for (int j = 0; j < 4; j++) {
-                const uint32_t c = sc.wcnt[(4 * q + j) * RADIX + d];
-                sc.wcnt[(4 * q + j) * RADIX + d] = r;
-                r += c;
-            }
-            sc.gsum[q * RADIX + d] = r;
-        }
-        __syncthreads();
-        {
-            const int d = threadIdx.x & (RADIX - 1), q = threadIdx.x >> 7;
-            uint32_t add = 0;
-#pragma unroll
-            for (int j = 0; j < 8; j++) add += j < q ? sc.gsum[j * RADIX + d] : 0u;
-#pragma unroll
-            for (int j = 0; j < 4; j++) sc.wcnt[(4 * q + j) * RADIX + d] += add;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int it = 0; it < BK_ITEMS; it++) {
-            if (dig[it] == 0xFFFFu) continue;
+    for (int it = 0; it < BK_ITEMS; it++) {
+        dig[it] = 0xFFFFu;
+        rank[it] = 0u;
+        if ((uint32_t)it < rounds) {
             const uint32_t e = (uint32_t)warp * 32u * rounds + (uint32_t)it * 32u + (uint32_t)lane;
-            const uint32_t P = sc.run[dig[it]] + sc.wcnt[warp * RADIX + dig[it]] + rank[it];
-            dst_k[P] = src_k[c0 + e];
-            dst_v[P] = src_v[c0 + e];
+            const bool ok = e < size;
+            const uint32_t d = ok ? (uint32_t)(src_k[e] >> shift) & (RADIX - 1) : 0u;
+            const uint32_t peers = digit_peers(d, ok, lane);
+            uint32_t pre = 0;
+            if (ok) pre = wc[d];
+            __syncwarp();
+            if (ok && (peers & lt) == 0u) wc[d] = pre + __popc(peers);
+            __syncwarp();
+            if (ok) {
+                dig[it] = d;
+                rank[it] = pre + __popc(peers & lt);
+            }
         }
-        __syncthreads();
-        // the chunk's digit counts advance the running starts
-        if (threadIdx.x < RADIX) {
-            uint32_t tot = 0;
-#pragma unroll
-            for (int j = 0; j < 8; j++) tot += sc.gsum[j * RADIX + threadIdx.x];
-            sc.run[threadIdx.x] += tot;
-        }
-        __syncthreads();
     }
+    __syncthreads();
+    // per digit: exclusive prefix over the 32 warps (8 groups of 4)
+    const int d = threadIdx.x & (RADIX - 1), q = threadIdx.x >> 7;
+    {
+        uint32_t r = 0;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const uint32_t c = sc.wcnt[(4 * q + j) * RADIX + d];
+            sc.wcnt[(4 * q + j) * RADIX + d] = r;
+            r += c;
+        }
+        sc.gsum[q * RADIX + d] = r;
+    }
+    __syncthreads();
+    {
+        uint32_t add = 0, tot = 0;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const uint32_t g = sc.gsum[j * RADIX + d];
+            add += j < q ? g : 0u;
+            tot += g;
+        }
+#pragma unroll
+        for (int j = 0; j < 4; j++) sc.wcnt[(4 * q + j) * RADIX + d] += add;
+        if (q == 0) {  // digit totals -> exclusive digit starts (warps 0-3, one digit per thread)
+            uint32_t x = tot;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            sc.run[d] = x - tot;
+            if (lane == 31) sc.wtot[warp] = x;
+        }
+    }
+    __syncthreads();
+    if (q == 0 && warp > 0) {
+        uint32_t add = 0;
+        for (int w = 0; w < warp; w++) add += sc.wtot[w];
+        sc.run[d] += add;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int it = 0; it < BK_ITEMS; it++) {
+        if (dig[it] == 0xFFFFu) continue;
+        const uint32_t e = (uint32_t)warp * 32u * rounds + (uint32_t)it * 32u + (uint32_t)lane;
+        const uint32_t P = sc.run[dig[it]] + sc.wcnt[warp * RADIX + dig[it]] + rank[it];
+        dst_k[P] = src_k[e];
+        dst_v[P] = src_v[e];
+    }
+    __syncthreads();
 }
 
-// Bucket blockIdx.x of (Kb, Vb) -> its sorted low digits in (K, V).
 // A bucket larger than BK_CAP is left alone and raises *big, which enables
 // the full tile passes queued after this kernel.
 __global__ void __launch_bounds__(BK_THREADS, 1) k_bucket_sort(const uint64_t* __restrict__ Kb,
@@ -304,14 +307,16 @@ __global__ void __launch_bounds__(BK_THREADS, 1) k_bucket_sort(const uint64_t* _
                                                                int low_passes, uint32_t* big, const uint32_t* enable) {
     if (enable && *enable == 0u) return;
     extern __shared__ __align__(16) unsigned char bk_smem[];
+    __shared__ uint32_t s_wcnt[BK_WARPS * RADIX], s_gsum[8 * RADIX], s_run[RADIX], s_wtot[4];
     uint64_t* k0 = reinterpret_cast<uint64_t*>(bk_smem);
     uint64_t* k1 = k0 + BK_CAP;
     uint32_t* v0 = reinterpret_cast<uint32_t*>(k1 + BK_CAP);
     uint32_t* v1 = v0 + BK_CAP;
     BucketScratch sc;
-    sc.wcnt = v1 + BK_CAP;
-    sc.gsum = sc.wcnt + BK_WARPS * RADIX;
-    sc.run = sc.gsum + 8 * RADIX;
+    sc.wcnt = s_wcnt;
+    sc.gsum = s_gsum;
+    sc.run = s_run;
+    sc.wtot = s_wtot;
     __shared__ uint32_t s_range[2];
     const uint32_t b = blockIdx.x;
     if (threadIdx.x < 32) {
@@ -353,7 +358,7 @@ __global__ void __launch_bounds__(BK_THREADS, 1) k_bucket_sort(const uint64_t* _
     }
 }
 
-size_t bucket_sort_smem() { return (size_t)BK_CAP * 24 + sizeof(uint32_t) * (BK_WARPS * RADIX + 8 * RADIX + RADIX); }
+size_t bucket_sort_smem() { return (size_t)BK_CAP * 24; }  // + 21 KB of static scratch
 
 __global__ void k_copy_pairs(const uint64_t* __restrict__ ks, const uint32_t* __restrict__ vs,
                              uint64_t* __restrict__ kd, uint32_t* __restrict__ vd, uint32_t n,

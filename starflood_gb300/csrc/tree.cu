@@ -493,48 +493,119 @@ __global__ void __launch_bounds__(MERGE_THREADS) k_tie_merge(const uint64_t* __r
     }
 }
 
-// s(k): number of split nodes whose range starts at sorted position k.
-__global__ void k_split_count(const uint64_t* __restrict__ K, uint32_t n, const uint32_t* __restrict__ nin_p,
-                              uint32_t leaf_cap, uint32_t depth_max, uint32_t* __restrict__ scount,
-                              uint32_t* d_status) {
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    const uint32_t nin = *nin_p;
-    if (k >= nin) {
-        scount[k] = 0;
-        return;
-    }
-    const uint64_t key = K[k];
-    const int a = (k == 0) ? -1 : cpl_levels(K[k - 1], key);
-    int b = -1;
-    if (k + leaf_cap < nin) {
-        const int c = cpl_levels(key, K[k + leaf_cap]);
-        if (c >= (int)depth_max && a < (int)depth_max) atomicOr(d_status, SFGPU_STATUS_TREE_DEPTH);
-        b = min(c, (int)depth_max - 1);
-    }
-    scount[k] = (uint32_t)max(0, b - a);
-}
+// Split nodes from the sorted keys, in one pass: s(k), the number of split
+// nodes whose range starts at sorted position k, is the run of levels L
+// with "k begins a level-L run (K[k-1] differs in the first L digits) and
+// K[k+leaf_cap] shares them"; split nodes are numbered by the exclusive
+// prefix of s (depth-first preorder), each tile of positions taking its
+// prefix from the tiles before it through a decoupled look-back, and every
+// split node is written out as (start position, level) right away.
+constexpr int SS_THREADS = 256;
+constexpr int SS_ITEMS = 4;
+constexpr uint32_t SS_TILE = SS_THREADS * SS_ITEMS;
+constexpr uint32_t SS_AGG = 1u << 30, SS_INC = 2u << 30, SS_VAL = (1u << 30) - 1u;
 
-__global__ void k_split_emit(const uint64_t* __restrict__ K, uint32_t n, const uint32_t* __restrict__ nin_p,
-                             const uint32_t* __restrict__ scount, const uint32_t* __restrict__ sbase,
-                             const uint32_t* __restrict__ nsplit_p, uint32_t split_cap,
-                             uint32_t* __restrict__ split_start, uint8_t* __restrict__ split_level,
-                             uint32_t nodes_max, uint32_t* d_status) {
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k == 0) {
-        const uint64_t total = 1ull + 8ull * (uint64_t)*nsplit_p;
-        if (total >= nodes_max || *nsplit_p > split_cap) atomicOr(d_status, SFGPU_STATUS_TREE_NODES);
-    }
-    if (k >= n || k >= *nin_p) return;
-    const uint32_t c = scount[k];
-    if (!c) return;
-    const int a = (k == 0) ? -1 : cpl_levels(K[k - 1], K[k]);
-    for (uint32_t j = 0; j < c; j++) {
-        const uint32_t id = sbase[k] + j;
-        if (id < split_cap) {
-            split_start[id] = k;
-            split_level[id] = (uint8_t)(a + 1 + (int)j);
+__global__ void __launch_bounds__(SS_THREADS) k_split_scan(
+    const uint64_t* __restrict__ K, uint32_t n, const uint32_t* __restrict__ nin_p, uint32_t leaf_cap,
+    uint32_t depth_max, uint32_t* __restrict__ sbase, uint32_t* __restrict__ split_start,
+    uint8_t* __restrict__ split_level, uint32_t split_cap, uint32_t* __restrict__ nsplit_p, uint32_t nodes_max,
+    uint32_t* tile_status, uint32_t* ticket, uint32_t* d_status) {
+    __shared__ uint32_t s_tile, s_prefix;
+    __shared__ uint32_t wsum[SS_THREADS / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);  // tiles in launch order: the look-back cannot wait on an unstarted tile
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint32_t ntiles = (n + SS_TILE - 1) / SS_TILE;
+    const uint32_t nin = *nin_p;
+    const uint32_t k0 = tile * SS_TILE + (uint32_t)threadIdx.x * SS_ITEMS;
+    uint32_t c[SS_ITEMS];
+    int lv[SS_ITEMS];
+    uint32_t tsum = 0;
+#pragma unroll
+    for (int i = 0; i < SS_ITEMS; i++) {
+        const uint32_t k = k0 + (uint32_t)i;
+        c[i] = 0u;
+        lv[i] = -1;
+        if (k < nin) {
+            const uint64_t key = K[k];
+            const int a = (k == 0) ? -1 : cpl_levels(K[k - 1], key);
+            int b = -1;
+            if (k + leaf_cap < nin) {
+                const int cl = cpl_levels(key, K[k + leaf_cap]);
+                if (cl >= (int)depth_max && a < (int)depth_max) atomicOr(d_status, SFGPU_STATUS_TREE_DEPTH);
+                b = min(cl, (int)depth_max - 1);
+            }
+            c[i] = (uint32_t)max(0, b - a);
+            lv[i] = a;
         }
+        tsum += c[i];
+    }
+    // block exclusive scan of the per-thread sums
+    uint32_t x = tsum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[warp] = x;
+    __syncthreads();
+    uint32_t wbefore = 0, agg = 0;
+#pragma unroll
+    for (int w = 0; w < SS_THREADS / 32; w++) {
+        wbefore += w < warp ? wsum[w] : 0u;
+        agg += wsum[w];
+    }
+    const uint32_t excl = wbefore + x - tsum;
+    // decoupled look-back over the preceding tiles (warp 0, 32 tiles a round)
+    if (warp == 0) {
+        volatile uint32_t* st = tile_status;
+        uint32_t prefix = 0;
+        if (tile == 0) {
+            if (lane == 0) st[0] = SS_INC | (agg & SS_VAL);
+        } else {
+            if (lane == 0) st[tile] = SS_AGG | (agg & SS_VAL);
+            int64_t look = (int64_t)tile - 1;
+            uint32_t spins = 0;
+            while (true) {
+                const int64_t j = look - lane;
+                const uint32_t w = j >= 0 ? st[j] : 0u;
+                const uint32_t fl = w & ~SS_VAL;
+                const uint32_t inc = __ballot_sync(0xffffffffu, j >= 0 && fl == SS_INC);
+                const uint32_t gap = __ballot_sync(0xffffffffu, j >= 0 && fl == 0u);
+                const int fi = inc ? __ffs(inc) - 1 : 32, fz = gap ? __ffs(gap) - 1 : 32;
+                const int take = fi < fz ? fi + 1 : fz;  // the nearest words up to an inclusive one or a gap
+                prefix += __reduce_add_sync(0xffffffffu, lane < take ? (w & SS_VAL) : 0u);
+                if (fi < fz) break;
+                look -= take;
+                if (fz < 32 && ++spins > (1u << 24)) {
+                    if (lane == 0) atomicOr(d_status, SFGPU_STATUS_SPIN);
+                    break;
+                }
+            }
+            if (lane == 0) st[tile] = SS_INC | ((prefix + agg) & SS_VAL);
+        }
+        if (lane == 0) s_prefix = prefix;
+    }
+    __syncthreads();
+    uint32_t run = s_prefix + excl;
+#pragma unroll
+    for (int i = 0; i < SS_ITEMS; i++) {
+        const uint32_t k = k0 + (uint32_t)i;
+        if (k < n) sbase[k] = run;
+        for (uint32_t j = 0; j < c[i]; j++) {
+            const uint32_t id = run + j;
+            if (id < split_cap) {
+                split_start[id] = k;
+                split_level[id] = (uint8_t)(lv[i] + 1 + (int)j);
+            }
+        }
+        run += c[i];
+    }
+    if (tile == ntiles - 1 && threadIdx.x == 0) {  // the total, and tree.c:224's node limit
+        const uint32_t total = s_prefix + agg;
+        *nsplit_p = total;
+        if (1ull + 8ull * (uint64_t)total >= nodes_max || total > split_cap) atomicOr(d_status, SFGPU_STATUS_TREE_NODES);
     }
 }
 
@@ -891,13 +962,16 @@ int sf_tree_alloc(TreeWork** out, uint32_t n, const sfgpu_params& p) {
     SF_CUDA(cudaMalloc(&t->keys, sizeof(uint64_t) * nn));
     SF_CUDA(cudaMalloc(&t->vals, sizeof(uint32_t) * nn));
     if (sf_sort_alloc(t->sort, nn) != SFGPU_OK) return SFGPU_FAILURE;
-    SF_CUDA(cudaMalloc(&t->counters, sizeof(uint32_t) * 8));
-    SF_CUDA(cudaMemset(t->counters, 0, sizeof(uint32_t) * 8));
+    // counters: [0] bodies inside, [1] ties, [2] moved, [3] split nodes,
+    // [4] largest mass bits, [5] gather ticket, [6] split-scan ticket, [7]
+    // unused, then one look-back word per split-scan tile
+    const size_t ncount = 8 + (nn + SS_TILE - 1) / SS_TILE;
+    SF_CUDA(cudaMalloc(&t->counters, sizeof(uint32_t) * ncount));
+    SF_CUDA(cudaMemset(t->counters, 0, sizeof(uint32_t) * ncount));
     SF_CUDA(cudaMalloc(&t->ties, sizeof(uint2) * TIE_CAP));
     SF_CUDA(cudaMalloc(&t->tie_pos, sizeof(uint32_t) * TIE_CAP));
     SF_CUDA(cudaMalloc(&t->tie_key, sizeof(uint64_t) * TIE_CAP));
     SF_CUDA(cudaMalloc(&t->tie_body, sizeof(uint32_t) * TIE_CAP));
-    SF_CUDA(cudaMalloc(&t->scount, sizeof(uint32_t) * nn));
     SF_CUDA(cudaMalloc(&t->sbase, sizeof(uint32_t) * nn));
     SF_CUDA(cudaMalloc(&t->split_start, sizeof(uint32_t) * std::max<uint32_t>(t->split_cap, 1)));
     SF_CUDA(cudaMalloc(&t->split_level, sizeof(uint8_t) * std::max<uint32_t>(t->split_cap, 1)));
@@ -916,7 +990,6 @@ int sf_tree_alloc(TreeWork** out, uint32_t n, const sfgpu_params& p) {
     SF_CUDA(cudaMalloc(&t->msum, 32 * nn));              // fix4 per sorted slot
     SF_CUDA(cudaMalloc(&t->cpre, 32 * (nn / 32 + 2)));   // fix4 per 32 slots, + the total
     SF_CUDA(cudaMalloc(&t->walk_part, sizeof(float4) * sf_walk_scratch_floats4((uint32_t)nn)));
-    if (sf_scan_reserve(t->scan_u32, (uint32_t)nn, sizeof(uint32_t)) != SFGPU_OK) return SFGPU_FAILURE;
     return SFGPU_OK;
 }
 
@@ -930,7 +1003,6 @@ void sf_tree_free(TreeWork* t) {
     cudaFree(t->tie_pos);
     cudaFree(t->tie_key);
     cudaFree(t->tie_body);
-    cudaFree(t->scount);
     cudaFree(t->sbase);
     cudaFree(t->split_start);
     cudaFree(t->split_level);
@@ -944,7 +1016,6 @@ void sf_tree_free(TreeWork* t) {
     cudaFree(t->walk_part);
     cudaFree(t->msum);
     cudaFree(t->cpre);
-    cudaFree(t->scan_u32.partials);
     delete t;
 }
 
@@ -960,7 +1031,7 @@ int sf_tree_build(sfgpu_sim* s) {
     uint32_t* tie_count = t->counters + 1;
     uint32_t* resort = t->counters + 2;
     uint32_t* nsplit = t->counters + 3;
-    SF_CUDA(cudaMemsetAsync(t->counters, 0, sizeof(uint32_t) * 6, st));
+    SF_CUDA(cudaMemsetAsync(t->counters, 0, sizeof(uint32_t) * (8 + sf_ceil_div(n, SS_TILE)), st));
     const uint32_t nb = sf_ceil_div(n, 256);
     int tk = s->timer.begin(st, "tree_keys");
     k_keys<<<nb, 256, 0, st>>>(pos, mas, n, s->d_bounds, t->keys, t->vals, nin, t->ties, tie_count, t->counters + 4,
@@ -992,11 +1063,10 @@ int sf_tree_build(sfgpu_sim* s) {
     SF_CHECK_LAUNCH();
     s->timer.end(st, tk);
     tk = s->timer.begin(st, "tree_nodes");
-    k_split_count<<<nb, 256, 0, st>>>(t->keys, n, nin, s->p.leaf_cap, s->p.depth_max, t->scount, s->d_status);
-    SF_CHECK_LAUNCH();
-    if (sf_scan_u32(t->scount, t->sbase, n, nsplit, t->scan_u32, st) != SFGPU_OK) return SFGPU_FAILURE;
-    k_split_emit<<<nb, 256, 0, st>>>(t->keys, n, nin, t->scount, t->sbase, nsplit, t->split_cap, t->split_start,
-                                     t->split_level, t->nodes_max, s->d_status);
+    k_split_scan<<<sf_ceil_div(n, SS_TILE), SS_THREADS, 0, st>>>(t->keys, n, nin, s->p.leaf_cap, s->p.depth_max,
+                                                                  t->sbase, t->split_start, t->split_level,
+                                                                  t->split_cap, nsplit, t->nodes_max,
+                                                                  t->counters + 8, t->counters + 6, s->d_status);
     SF_CHECK_LAUNCH();
     const uint32_t sb = sf_ceil_div((uint64_t)std::max<uint32_t>(t->split_cap, 1) * 8u, FILL_THREADS);
     k_split_fill<<<sb, FILL_THREADS, 0, st>>>(t->keys, nin, t->sbase, nsplit, t->split_cap, t->split_start, t->split_level,

@@ -36,7 +36,6 @@ struct TreeWork {
     uint32_t* tie_pos = nullptr;   // moved midplane bodies: old slots ascending
     uint64_t* tie_key = nullptr;   // their new keys, ascending by (key, body)
     uint32_t* tie_body = nullptr;
-    uint32_t* scount = nullptr;
     uint32_t* sbase = nullptr;
     uint32_t* split_start = nullptr;
     uint8_t* split_level = nullptr;
@@ -47,7 +46,6 @@ struct TreeWork {
     float4* sp = nullptr;       // sorted bodies (x, y, z, m)
     void* msum = nullptr;   // fixed-point (m x, m y, m z, m) per sorted slot (tree.cu fix4)
     void* cpre = nullptr;   // exclusive prefix of msum per 32 slots, then the total
-    ScanWork scan_u32;
     float4* walk_part = nullptr;  // split-walk partial sums (SPLIT x n)
 };
 
