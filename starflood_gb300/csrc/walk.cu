@@ -474,9 +474,9 @@ constexpr uint32_t WALK_GROUP_DEFAULT = 16;
 constexpr int GW_WARPS = 4;
 constexpr int GW_THREADS = GW_WARPS * 32;
 constexpr int GW_STACK = 512;
-constexpr int GW_LIST = 128;  // accepted cells whose bounds miss the group box
+constexpr int GW_LIST = 112;  // accepted cells whose bounds miss the group box
 constexpr int GW_MIN_BLOCKS = 7;  // resident blocks per SM the register budget is cut for
-constexpr int GW_SLOW = 64;   // accepted cells that may contain a body (self-exclusion test)
+constexpr int GW_SLOW = 48;   // accepted cells that may contain a body (self-exclusion test)
 
 // Per-warp lists in shared memory.  The fast list holds the monopole itself
 // (centre of mass and mass, as separate arrays so that two consecutive
@@ -500,7 +500,9 @@ struct GroupLists {
 // With 16- or 8-body groups the 2 or 4 sub-warps hold the same bodies and
 // take entries in turn (FAST: entry pairs), `lane` being the body slot and
 // `half` the sub-warp.
-template <int KIND, int GB>
+// COUNT: count each body's interactions here (per-body statistics);
+// otherwise the caller counts whole entries as they are listed.
+template <int KIND, int GB, bool COUNT>
 __device__ __forceinline__ void flush_fast(const GroupLists& L, int count, int lane, int half, float rx, float ry,
                                            float rz, float eps2, float2& a2x, float2& a2y, float2& a2z, float2& p2,
                                            KSum& ax, KSum& ay, KSum& az, KSum& ph, uint32_t& n_int) {
@@ -518,7 +520,7 @@ __device__ __forceinline__ void flush_fast(const GroupLists& L, int count, int l
                 ay.add(f * dy);
                 az.add(f * dz);
                 ph.add(mphi);
-                n_int++;
+                if (COUNT) n_int++;
             }
         }
         return;
@@ -530,9 +532,11 @@ __device__ __forceinline__ void flush_fast(const GroupLists& L, int count, int l
         const float2 X = *reinterpret_cast<const float2*>(&L.x[e]);
         const float2 Y = *reinterpret_cast<const float2*>(&L.y[e]);
         const float2 Z = *reinterpret_cast<const float2*>(&L.z[e]);
-        const float2 Mj = *reinterpret_cast<const float2*>(&L.m[e]);
+        const float2 M2 = *reinterpret_cast<const float2*>(&L.m[e]);
         const uint2 MK = *reinterpret_cast<const uint2*>(&L.msk[e]);
         const bool t0 = (MK.x >> lane) & 1u, t1 = (MK.y >> lane) & 1u;
+        // a body not taking an entry sees it massless: its terms are +0
+        const float2 Mj = make_float2(t0 ? M2.x : 0.f, t1 ? M2.y : 0.f);
         const float2 dx = __fadd2_rn(X, nrx);
         const float2 dy = __fadd2_rn(Y, nry);
         const float2 dz = __fadd2_rn(Z, nrz);
@@ -540,19 +544,17 @@ __device__ __forceinline__ void flush_fast(const GroupLists& L, int count, int l
         r2 = __ffma2_rn(dy, dy, r2);
         r2 = __ffma2_rn(dx, dx, r2);
         const float2 inv = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
-        float2 mphi = __fmul2_rn(Mj, inv);
-        float2 f = __fmul2_rn(mphi, __fmul2_rn(inv, inv));
-        mphi = make_float2(t0 ? mphi.x : 0.f, t1 ? mphi.y : 0.f);
-        f = make_float2(t0 ? f.x : 0.f, t1 ? f.y : 0.f);
+        const float2 mphi = __fmul2_rn(Mj, inv);
+        const float2 f = __fmul2_rn(mphi, __fmul2_rn(inv, inv));
         a2x = __ffma2_rn(f, dx, a2x);
         a2y = __ffma2_rn(f, dy, a2y);
         a2z = __ffma2_rn(f, dz, a2z);
         p2 = __fadd2_rn(p2, mphi);
-        n_int += (uint32_t)t0 + (uint32_t)t1;
+        if (COUNT) n_int += (uint32_t)t0 + (uint32_t)t1;
     }
 }
 
-template <int KIND, int GB>
+template <int KIND, int GB, bool COUNT>
 __device__ __forceinline__ void flush_slow(const GroupLists& L, int count, const NodeArrays& nd, int lane, int half,
                                            float rx, float ry, float rz, float mi, float eps2, KSum& ax, KSum& ay,
                                            KSum& az, KSum& ph, uint32_t& n_int) {
@@ -564,7 +566,7 @@ __device__ __forceinline__ void flush_slow(const GroupLists& L, int count, const
         const float4 H = __ldg(&nd.hi[NODE_REC * v]);
         if ((M >> lane) & 1u) {
             monopole<KIND>(C, Lo, H, __float_as_uint(H.z), rx, ry, rz, mi, eps2, ax, ay, az, ph);
-            n_int++;
+            if (COUNT) n_int++;
         }
     }
 }
@@ -618,6 +620,9 @@ __global__ void __launch_bounds__(GW_THREADS, GW_MIN_BLOCKS) k_walk_group(const 
     __shared__ uint32_t q_node[GW_WARPS][GW_SLOW];
     __shared__ uint32_t q_mask[GW_WARPS][GW_SLOW];
     __shared__ float4 s_body[GW_WARPS][32];
+    __shared__ float4 s_mg[GW_WARPS][32];     // a round's mixed cells: centre and w^2,
+    __shared__ uint32_t s_mm[GW_WARPS][32];   // the bodies walking them,
+    __shared__ uint32_t s_om[GW_WARPS][32];   // and the bodies that open them
     constexpr int FRONT = GSPLIT > 1 ? 80 : 1;
     __shared__ uint32_t f_node[GW_WARPS][FRONT];  // top-level frontiers: [0,8) level 1, [8,72) level 2
     __shared__ uint32_t f_mask[GW_WARPS][FRONT];
@@ -670,12 +675,13 @@ __global__ void __launch_bounds__(GW_THREADS, GW_MIN_BLOCKS) k_walk_group(const 
             }
             count = padded;
             __syncwarp();
-            flush_fast<KIND, GB>(L, count, bl, half, rx, ry, rz, fc.eps2, a2x, a2y, a2z, p2, ax, ay, az, ph, n_int);
+            flush_fast<KIND, GB, STATS>(L, count, bl, half, rx, ry, rz, fc.eps2, a2x, a2y, a2z, p2, ax, ay, az, ph,
+                                        n_int);
             count = 0;
             __syncwarp();
         }
         if (all || qcount > GW_SLOW - 32) {
-            flush_slow<KIND, GB>(L, qcount, nd, bl, half, rx, ry, rz, mi, fc.eps2, ax, ay, az, ph, n_int);
+            flush_slow<KIND, GB, STATS>(L, qcount, nd, bl, half, rx, ry, rz, mi, fc.eps2, ax, ay, az, ph, n_int);
             qcount = 0;
             __syncwarp();
         }
@@ -731,6 +737,7 @@ __global__ void __launch_bounds__(GW_THREADS, GW_MIN_BLOCKS) k_walk_group(const 
             const uint32_t am = (oct == 0 && lane < n_in && bodies > 0u) ? (M & ~om) : 0u;
             const uint32_t lt = (1u << lane) - 1u;
             append_cells(L, am, v, C, Lo, H, bx0, by0, bz0, bx1, by1, bz1, lane, count, qcount);
+            if (!STATS) n_int += __popc(am);
             const uint32_t ob = __ballot_sync(0xffffffffu, om != 0u);
             if (om) {
                 const int base = out_base + 8 * __popc(ob & lt);
@@ -844,32 +851,34 @@ __global__ void __launch_bounds__(GW_THREADS, GW_MIN_BLOCKS) k_walk_group(const 
                     }
                 }
             } else {
-                // sub-warp h takes the h-th remaining mixed cell, one lane per body
-                uint32_t cells = mix_b;
-                while (cells) {
-                    uint32_t c = cells;
-                    for (int j = 0; j < half; j++) c &= c - 1u;
-                    const int l = c ? __ffs(c) - 1 : -1;
-                    const int src = l < 0 ? 0 : l;
-                    const float4 Gl = make_float4(__shfl_sync(0xffffffffu, G.x, src), __shfl_sync(0xffffffffu, G.y, src),
-                                                  __shfl_sync(0xffffffffu, G.z, src), __shfl_sync(0xffffffffu, G.w, src));
-                    const uint32_t Ml = __shfl_sync(0xffffffffu, M, src);
-                    const bool t = l >= 0 && ((Ml >> bl) & 1u) && opens(Gl, rx, ry, rz, fc, th_lo, th_hi);
-                    const uint32_t ol = __ballot_sync(0xffffffffu, t);
-#pragma unroll
-                    for (int h = 0; h < H; h++) {
-                        const int lh = __shfl_sync(0xffffffffu, l, h * GB);
-                        if (lane == lh) om = (ol >> (h * GB)) & body_bits;
-                    }
-#pragma unroll
-                    for (int h = 0; h < H; h++) cells &= cells - 1u;
+                // the mixed cells staged in shared memory in lane order;
+                // sub-warp h tests cell j H + h in round j, one lane per body
+                const int nmix = __popc(mix_b);
+                const int slot = __popc(mix_b & lt);
+                if (mixed) {
+                    s_mg[w][slot] = G;
+                    s_mm[w][slot] = M;
                 }
+                __syncwarp();
+                for (int j0 = 0; j0 < nmix; j0 += H) {  // the same trip count on every lane
+                    const int j = j0 + half;
+                    bool t = false;
+                    if (j < nmix) {
+                        const uint32_t Mj = s_mm[w][j];
+                        t = ((Mj >> bl) & 1u) && opens(s_mg[w][j], rx, ry, rz, fc, th_lo, th_hi);
+                    }
+                    const uint32_t ol = __ballot_sync(0xffffffffu, t);
+                    if (bl == 0 && j < nmix) s_om[w][j] = (ol >> (half * GB)) & body_bits;
+                }
+                __syncwarp();
+                if (mixed) om = s_om[w][slot];
             }
         }
         // accepted cells (all of the mask, or the bodies of a mixed cell
         // that do not open it) -> lists
         const uint32_t am = (kind == 1) ? M : ((kind == 3) ? (M & ~om) : 0u);
         append_cells(L, am, v, C, Lo, H, bx0, by0, bz0, bx1, by1, bz1, lane, count, qcount);
+        if (!STATS) n_int += __popc(am);
         const uint32_t ob = __ballot_sync(0xffffffffu, om != 0u);
         if (om) {
             const int base = top + 8 * __popc(ob & lt);

@@ -251,3 +251,26 @@ def test_tree_export_reference_numbering(sf, oracle32, fixture):
         t = s.tree_export()
     for k in ("parent", "bodies", "branch", "bounds", "params"):
         np.testing.assert_array_equal(t[k], d["tree_" + k], err_msg=k)
+
+
+@pytest.mark.parametrize("group", [8, 16, 32])
+def test_walk_totals_match_per_body_counts(sf, group):
+    """The device totals of a walk without per-body statistics (what the
+    benchmark's flop count uses) equal the sums of the per-body counts."""
+    from starflood_gb300.ics import uniform_ball
+    n = 20000
+    pos, vel, mas = uniform_ball(n, seed=13)
+    totals = []
+    for flags in (0, sf.FLAG_STATS):
+        p = sf.default_params(solver=sf.SOLVER_TREE, eps=0.01, theta=0.5, flags=flags, walk_group=group)
+        with sf.Sim(n, p) as s:
+            s.set_state(pos, vel, mas)
+            s.solve(3)
+            s.walk_totals()  # reset by reading
+            s.solve(3)
+            ti, to = s.walk_totals()
+            if flags:
+                ni, no = s.walk_stats()
+                assert (int(ni.sum()), int(no.sum())) == (ti, to)
+            totals.append((ti, to))
+    assert totals[0] == totals[1]
