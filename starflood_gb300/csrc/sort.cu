@@ -5,6 +5,8 @@
 // order, rank their keys with warp match/ballot, and chain their per-digit
 // offsets through a decoupled look-back over the preceding tiles.  All waits
 // are bounded and report SFGPU_STATUS_SPIN instead of hanging.
+#include <cooperative_groups.h>
+
 #include "internal.cuh"
 
 namespace {
@@ -57,23 +59,22 @@ __global__ void __launch_bounds__(256) k_hist(const uint64_t* __restrict__ keys,
         if (sh[i]) atomicAdd(&hist[i], sh[i]);
 }
 
+// One tile of one pass: tile `tile` of (kin, vin) ranked and scattered into
+// (kout, vout); `tile` is a ticket taken in launch order, or the block index
+// when every tile is resident (cooperative launch).
 template <int SORT_ITEMS>
-__global__ void __launch_bounds__(SORT_THREADS) k_onesweep(
-    const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint64_t* __restrict__ kout,
-    uint32_t* __restrict__ vout, uint32_t n, int shift, const uint32_t* __restrict__ hist,
-    uint32_t* status, uint32_t* counter, uint32_t* d_status, const uint32_t* enable) {
-    if (enable && *enable == 0u) return;
-    __shared__ uint32_t s_tile;
+__device__ __forceinline__ void onesweep_tile(const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin,
+                                              uint64_t* __restrict__ kout, uint32_t* __restrict__ vout, uint32_t n,
+                                              int shift, const uint32_t* __restrict__ hist, uint32_t* status,
+                                              uint32_t tile, uint32_t* d_status) {
     __shared__ uint32_t wcnt[SORT_WARPS][RADIX];
     __shared__ uint32_t base[RADIX];
     __shared__ uint32_t toff[RADIX];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
 
-    if (threadIdx.x == 0) s_tile = atomicAdd(counter, 1u);
     for (int i = threadIdx.x; i < SORT_WARPS * RADIX; i += SORT_THREADS) (&wcnt[0][0])[i] = 0u;
     __syncthreads();
-    const uint32_t tile = s_tile;
 
     // exclusive scan of the global digit histogram (warps 0..3, 32 digits each)
     if (threadIdx.x < RADIX) {
@@ -190,6 +191,50 @@ __global__ void __launch_bounds__(SORT_THREADS) k_onesweep(
         kout[pos] = key[it];
         vout[pos] = val[it];
     }
+}
+
+template <int SORT_ITEMS>
+__global__ void __launch_bounds__(SORT_THREADS) k_onesweep(
+    const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint64_t* __restrict__ kout,
+    uint32_t* __restrict__ vout, uint32_t n, int shift, const uint32_t* __restrict__ hist,
+    uint32_t* status, uint32_t* counter, uint32_t* d_status, const uint32_t* enable) {
+    if (enable && *enable == 0u) return;
+    __shared__ uint32_t s_tile;
+    if (threadIdx.x == 0) s_tile = atomicAdd(counter, 1u);
+    __syncthreads();
+    onesweep_tile<SORT_ITEMS>(kin, vin, kout, vout, n, shift, hist, status, s_tile, d_status);
+}
+
+// Every pass of the tile sort in one cooperative launch (all tiles resident,
+// a grid barrier between passes), from (k0, v0) ping-ponging with (k1, v1);
+// the result ends in (k1, v1) (copied there when the pass count is even).
+// Returns at once (the whole grid, before any barrier) unless *enable.
+template <int SORT_ITEMS>
+__global__ void __launch_bounds__(SORT_THREADS) k_onesweep_all(uint64_t* k0, uint32_t* v0, uint64_t* k1,
+                                                               uint32_t* v1, uint32_t n, int passes,
+                                                               const uint32_t* __restrict__ hist, uint32_t* status,
+                                                               uint32_t* d_status, const uint32_t* enable) {
+    if (*enable == 0u) return;
+    cooperative_groups::grid_group grid = cooperative_groups::this_grid();
+    const uint32_t tiles = gridDim.x;
+    uint64_t *ka = k0, *kb = k1;
+    uint32_t *va = v0, *vb = v1;
+    for (int p = 0; p < passes; p++) {
+        onesweep_tile<SORT_ITEMS>(ka, va, kb, vb, n, p * RADIX_BITS, hist + p * RADIX,
+                                  status + (size_t)p * tiles * RADIX, blockIdx.x, d_status);
+        grid.sync();
+        uint64_t* tk = ka;
+        ka = kb;
+        kb = tk;
+        uint32_t* tv = va;
+        va = vb;
+        vb = tv;
+    }
+    if (ka != k1)
+        for (uint32_t i = blockIdx.x * SORT_THREADS + threadIdx.x; i < n; i += tiles * SORT_THREADS) {
+            k1[i] = ka[i];
+            v1[i] = va[i];
+        }
 }
 
 // ---- small sorts: one pass on the top digit, then every bucket in one CTA ----
@@ -436,22 +481,22 @@ int sf_sort_pairs_keep(uint64_t* keys, uint32_t* vals, uint32_t n, int bits, Sor
                                                                      w.hist + top * RADIX, top, big, enable);
         SF_CHECK_LAUNCH();
         // fallback (only if a bucket overflowed): every pass from the top
-        // pass's output, which holds all pairs; ends in (keys, vals)
-        uint64_t* ka = w.keys_b;
-        uint32_t* va = w.vals_b;
-        uint64_t* kb = keys;
-        uint32_t* vb = vals;
-        for (int p = 0; p < passes; p++) {
-            k_onesweep<4><<<tiles, SORT_THREADS, 0, st>>>(ka, va, kb, vb, n, p * RADIX_BITS, w.hist + p * RADIX,
-                                                          w.status + (size_t)(p + 1) * tiles * RADIX,
-                                                          w.counters + p + 1, d_status, big);
-            SF_CHECK_LAUNCH();
-            std::swap(ka, kb);
-            std::swap(va, vb);
-        }
-        if (ka != keys) {
-            const uint32_t cb = std::min<uint32_t>(sf_ceil_div(n, 256), (uint32_t)sf_num_sms() * 8);
-            k_copy_pairs<<<cb, 256, 0, st>>>(ka, va, keys, vals, n, big);
+        // pass's output, which holds all pairs, in one cooperative launch
+        // (tiles <= 128 blocks, all resident); ends in (keys, vals)
+        {
+            uint64_t* k0 = w.keys_b;
+            uint32_t* v0 = w.vals_b;
+            uint64_t* k1 = keys;
+            uint32_t* v1 = vals;
+            uint32_t nn = n;
+            int np = passes;
+            const uint32_t* hh = w.hist;
+            uint32_t* ss = w.status + (size_t)tiles * RADIX;
+            uint32_t* ds = d_status;
+            const uint32_t* en = big;
+            void* args[] = {&k0, &v0, &k1, &v1, &nn, &np, &hh, &ss, &ds, &en};
+            SF_CUDA(cudaLaunchCooperativeKernel((const void*)k_onesweep_all<4>, dim3(tiles), dim3(SORT_THREADS), args, 0,
+                                                st));
             SF_CHECK_LAUNCH();
         }
         return SFGPU_OK;
