@@ -282,7 +282,9 @@ extern "C" int sfgpu_create(sfgpu_sim** out, uint32_t n, const sfgpu_params* p) 
             s->pp_part_cap = need;
         }
     }
-    s->red_cap = 4 * sf_ceil_div(n, SF_RED_BLOCK) + 8;
+    // per-block partials: the KDK kernels (4 per 256 bodies) and the walk's
+    // fused kick (4 per 16 bodies at the smallest group size)
+    s->red_cap = 4 * sf_ceil_div(n, 16) + 8;
     TRY(cudaMalloc(&s->red, sizeof(double2) * s->red_cap));
     TRY(cudaStreamSynchronize(s->stream));
 #undef TRY
@@ -373,10 +375,18 @@ static int step_body(sfgpu_sim* s) {
     int tk = s->timer.begin(s->stream, "kick_drift");
     if (sf_stage_kick_drift(s, tree) != SFGPU_OK) return SFGPU_FAILURE;
     s->timer.end(s->stream, tk);
-    if (solve_body(s, true) != SFGPU_OK) return SFGPU_FAILURE;
-    tk = s->timer.begin(s->stream, "kick_energy");
-    if (sf_stage_kick_energy(s) != SFGPU_OK) return SFGPU_FAILURE;
-    s->timer.end(s->stream, tk);
+    // without SPH the walk's epilogue may apply kick_1 and the energies
+    // itself (sets kicked); SPH forces come after the walk, so not then
+    s->fuse_kick = tree && s->p.sph == SFGPU_SPH_OFF;
+    s->kicked = false;
+    const int rc = solve_body(s, true);
+    s->fuse_kick = false;
+    if (rc != SFGPU_OK) return SFGPU_FAILURE;
+    if (!s->kicked) {
+        tk = s->timer.begin(s->stream, "kick_energy");
+        if (sf_stage_kick_energy(s) != SFGPU_OK) return SFGPU_FAILURE;
+        s->timer.end(s->stream, tk);
+    }
     return SFGPU_OK;
 }
 

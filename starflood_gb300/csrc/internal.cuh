@@ -303,6 +303,8 @@ struct sfgpu_sim {
     StageTimer timer;
     cudaGraphExec_t graph = nullptr;
     bool graph_ok = true;
+    bool fuse_kick = false;        // set by a step: the walk may do kick_1 and the energies
+    bool kicked = false;           // ... and did
     struct SnapshotWriter* snap = nullptr;  // snapshot.cu
     void* vis = nullptr;                    // VisScratch (vis.cu)
 };

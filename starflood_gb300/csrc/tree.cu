@@ -621,81 +621,6 @@ __device__ __forceinline__ void write_node(NodeArrays nd, uint32_t v, const Cube
     nd.start[v] = start;
 }
 
-// One split node per 8 threads, thread o writing the node of octant o: its
-// first body is the first sorted key at or past octant o of the split cell
-// (one table-narrowed search, no chain of gallops), its end the next
-// octant's start.  Thread 0 of the group also places the split node itself
-// (its id under its parent), which every thread of the group needs.
-constexpr int FILL_THREADS = 128;
-
-__global__ void __launch_bounds__(FILL_THREADS) k_split_fill(const uint64_t* __restrict__ K, const uint32_t* __restrict__ nin_p,
-                             const uint32_t* __restrict__ sbase, const uint32_t* __restrict__ nsplit_p,
-                             uint32_t split_cap, const uint32_t* __restrict__ split_start,
-                             const uint8_t* __restrict__ split_level, const float* __restrict__ bounds,
-                             uint32_t leaf_cap, uint32_t depth_max, NodeArrays nd, float third,
-                             uint32_t* __restrict__ split_node) {
-    __shared__ uint64_t samp[NSAMP];
-    const uint32_t ns = min(*nsplit_p, split_cap);
-    const uint32_t nin = *nin_p;
-    const uint32_t g = blockIdx.x * FILL_THREADS + threadIdx.x;
-    const uint32_t s = g >> 3;
-    const uint32_t o = g & 7u;
-    if (g == 0) {  // the root record (tree.c:156-159: bounds = the root cube)
-        Cube r;
-        for (int a = 0; a < 3; a++) {
-            r.lo[a] = bounds[a];
-            r.hi[a] = bounds[3 + a];
-        }
-        write_node(nd, 0, r, nin, (nin > leaf_cap && depth_max > 0) ? 1u : NODE_NONE, 0u, 0u, third);
-    }
-    if ((blockIdx.x * FILL_THREADS) / 8u >= ns) return;  // the whole block is past the split nodes
-    const KeySamples ks = load_key_samples(K, nin, samp);
-    __syncthreads();
-    const bool live = s < ns;
-    uint32_t k = 0, cend = 0;
-    int L = 0;
-    uint64_t pre = 0;
-    if (live) {
-        k = split_start[s];
-        L = split_level[s];
-        pre = prefix_of(K[k], L);
-        // end of octant o = first key at or past octant o+1 (for o = 7 the
-        // next level-L cell, or nin)
-        cend = search_keys(K, samp, ks, 3 * (15 - L), (pre << 3) + (uint64_t)o + 1);
-    }
-    uint32_t cstart = __shfl_up_sync(0xffffffffu, cend, 1, 8);
-    if (o == 0) cstart = k;
-    if (!live) return;
-    // node id of this split node (the children's parent); the node record
-    // itself is written by the parent's group
-    uint32_t self = 0;
-    if (L > 0) {
-        const uint32_t kp = (L == 1) ? 0u : search_keys(K, samp, ks, 3 * (17 - L), pre >> 3);
-        const int ap = (kp == 0) ? -1 : cpl_levels(K[kp - 1], K[kp]);
-        const uint32_t sp = sbase[kp] + (uint32_t)(L - 1 - (ap + 1));
-        self = 1u + 8u * sp + (uint32_t)(pre & 7ull);
-    }
-    if (o == 0) split_node[s] = self;
-    const Cube c = cube_of(bounds, K[k], L);
-    const uint32_t cnt = cend - cstart;
-    Cube cc;
-    for (int a = 0; a < 3; a++) {
-        const float mid = midf(c.lo[a], c.hi[a]);
-        const bool up = (o >> a) & 1u;
-        cc.lo[a] = up ? mid : c.lo[a];
-        cc.hi[a] = up ? c.hi[a] : mid;
-    }
-    uint32_t fc = NODE_NONE;
-    if (cnt > leaf_cap && L + 1 < (int)depth_max) {
-        const int ac = (cstart == 0) ? -1 : cpl_levels(K[cstart - 1], K[cstart]);
-        const uint32_t sid = sbase[cstart] + (uint32_t)(L + 1 - (ac + 1));
-        // beyond capacity (node overflow, flagged by k_split_emit) the
-        // child stays a leaf so nothing reads past the node arrays
-        fc = sid < split_cap ? 1u + 8u * sid : NODE_NONE;
-    }
-    write_node(nd, 1u + 8u * s + o, cc, cnt, fc, self, cstart, third);
-}
-
 // Monopoles from exact integer sums.  m x, m y, m z and m of every body are
 // turned into 64-bit fixed-point integers whose scales (powers of two) are
 // set from N, the largest mass and the root cube's extent so that no sum of
@@ -839,30 +764,102 @@ __device__ __forceinline__ fix4 slot_prefix(const fix4* __restrict__ pre, const 
 }
 
 // tree.c:346-354: centre of mass = sum(m x) / sum(m), from the exact sums
-__global__ void k_monopoles(const uint32_t* __restrict__ nsplit_p, uint32_t split_cap, NodeArrays nd, uint32_t n,
-                            const uint32_t* __restrict__ mmax, const float* __restrict__ bounds,
-                            const fix4* __restrict__ msum, const fix4* __restrict__ cpre) {
-    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t nn = 1u + 8u * min(*nsplit_p, split_cap);
-    if (v >= nn) return;
-    const uint32_t cnt = __float_as_uint(nd.hi[NODE_REC * v].z);
-    const uint32_t s = nd.start[v];
-    float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (cnt) {
-        const fix4 a = slot_prefix(msum, cpre, s, n), b = slot_prefix(msum, cpre, s + cnt, n);
-        const long long sx = b.x - a.x, sy = b.y - a.y, sz = b.z - a.z, sm = b.m - a.m;
-        const FixScale f = fix_scale(n, *mmax, bounds);
-        const double m = ldexp((double)sm, -f.km);
-        if (sm > 0) {
-            const double inv = ldexp(1.0 / (double)sm, f.km - f.kx);  // 2^km / (sm 2^kx)
-            out = make_float4((float)((double)sx * inv), (float)((double)sy * inv), (float)((double)sz * inv),
-                              (float)m);
-        } else {
-            out = make_float4((float)ldexp((double)sx, -f.kx), (float)ldexp((double)sy, -f.kx),
-                              (float)ldexp((double)sz, -f.kx), (float)m);
-        }
+// over the sorted slots [s, s + cnt)
+__device__ __forceinline__ float4 node_monopole(uint32_t s, uint32_t cnt, uint32_t n, const uint32_t* __restrict__ mmax,
+                                                const float* __restrict__ bounds, const fix4* __restrict__ msum,
+                                                const fix4* __restrict__ cpre) {
+    if (!cnt) return make_float4(0.f, 0.f, 0.f, 0.f);
+    const fix4 a = slot_prefix(msum, cpre, s, n), b = slot_prefix(msum, cpre, s + cnt, n);
+    const long long sx = b.x - a.x, sy = b.y - a.y, sz = b.z - a.z, sm = b.m - a.m;
+    const FixScale f = fix_scale(n, *mmax, bounds);
+    const double m = ldexp((double)sm, -f.km);
+    if (sm > 0) {
+        const double inv = ldexp(1.0 / (double)sm, f.km - f.kx);  // 2^km / (sm 2^kx)
+        return make_float4((float)((double)sx * inv), (float)((double)sy * inv), (float)((double)sz * inv),
+                           (float)m);
     }
-    nd.com[NODE_REC * v] = out;
+    return make_float4((float)ldexp((double)sx, -f.kx), (float)ldexp((double)sy, -f.kx),
+                       (float)ldexp((double)sz, -f.kx), (float)m);
+}
+
+// One split node per 8 threads, thread o writing the node of octant o: its
+// first body is the first sorted key at or past octant o of the split cell
+// (one table-narrowed search, no chain of gallops), its end the next
+// octant's start.  Thread 0 of the group also places the split node itself
+// (its id under its parent), which every thread of the group needs.  With
+// the fixed-point prefix sums (msum non-NULL) every node written also gets
+// its monopole here.
+constexpr int FILL_THREADS = 128;
+
+__global__ void __launch_bounds__(FILL_THREADS) k_split_fill(const uint64_t* __restrict__ K, const uint32_t* __restrict__ nin_p,
+                             const uint32_t* __restrict__ sbase, const uint32_t* __restrict__ nsplit_p,
+                             uint32_t split_cap, const uint32_t* __restrict__ split_start,
+                             const uint8_t* __restrict__ split_level, const float* __restrict__ bounds,
+                             uint32_t leaf_cap, uint32_t depth_max, NodeArrays nd, float third,
+                             uint32_t* __restrict__ split_node, uint32_t n, const uint32_t* __restrict__ mmax,
+                             const fix4* __restrict__ msum, const fix4* __restrict__ cpre) {
+    __shared__ uint64_t samp[NSAMP];
+    const uint32_t ns = min(*nsplit_p, split_cap);
+    const uint32_t nin = *nin_p;
+    const uint32_t g = blockIdx.x * FILL_THREADS + threadIdx.x;
+    const uint32_t s = g >> 3;
+    const uint32_t o = g & 7u;
+    if (g == 0) {  // the root record (tree.c:156-159: bounds = the root cube)
+        Cube r;
+        for (int a = 0; a < 3; a++) {
+            r.lo[a] = bounds[a];
+            r.hi[a] = bounds[3 + a];
+        }
+        write_node(nd, 0, r, nin, (nin > leaf_cap && depth_max > 0) ? 1u : NODE_NONE, 0u, 0u, third);
+        if (msum) nd.com[0] = node_monopole(0u, nin, n, mmax, bounds, msum, cpre);
+    }
+    if ((blockIdx.x * FILL_THREADS) / 8u >= ns) return;  // the whole block is past the split nodes
+    const KeySamples ks = load_key_samples(K, nin, samp);
+    __syncthreads();
+    const bool live = s < ns;
+    uint32_t k = 0, cend = 0;
+    int L = 0;
+    uint64_t pre = 0;
+    if (live) {
+        k = split_start[s];
+        L = split_level[s];
+        pre = prefix_of(K[k], L);
+        // end of octant o = first key at or past octant o+1 (for o = 7 the
+        // next level-L cell, or nin)
+        cend = search_keys(K, samp, ks, 3 * (15 - L), (pre << 3) + (uint64_t)o + 1);
+    }
+    uint32_t cstart = __shfl_up_sync(0xffffffffu, cend, 1, 8);
+    if (o == 0) cstart = k;
+    if (!live) return;
+    // node id of this split node (the children's parent); the node record
+    // itself is written by the parent's group
+    uint32_t self = 0;
+    if (L > 0) {
+        const uint32_t kp = (L == 1) ? 0u : search_keys(K, samp, ks, 3 * (17 - L), pre >> 3);
+        const int ap = (kp == 0) ? -1 : cpl_levels(K[kp - 1], K[kp]);
+        const uint32_t sp = sbase[kp] + (uint32_t)(L - 1 - (ap + 1));
+        self = 1u + 8u * sp + (uint32_t)(pre & 7ull);
+    }
+    if (o == 0) split_node[s] = self;
+    const Cube c = cube_of(bounds, K[k], L);
+    const uint32_t cnt = cend - cstart;
+    Cube cc;
+    for (int a = 0; a < 3; a++) {
+        const float mid = midf(c.lo[a], c.hi[a]);
+        const bool up = (o >> a) & 1u;
+        cc.lo[a] = up ? mid : c.lo[a];
+        cc.hi[a] = up ? c.hi[a] : mid;
+    }
+    uint32_t fc = NODE_NONE;
+    if (cnt > leaf_cap && L + 1 < (int)depth_max) {
+        const int ac = (cstart == 0) ? -1 : cpl_levels(K[cstart - 1], K[cstart]);
+        const uint32_t sid = sbase[cstart] + (uint32_t)(L + 1 - (ac + 1));
+        // beyond capacity (node overflow, flagged by k_split_emit) the
+        // child stays a leaf so nothing reads past the node arrays
+        fc = sid < split_cap ? 1u + 8u * sid : NODE_NONE;
+    }
+    write_node(nd, 1u + 8u * s + o, cc, cnt, fc, self, cstart, third);
+    if (msum) nd.com[NODE_REC * (1u + 8u * s + o)] = node_monopole(cstart, cnt, n, mmax, bounds, msum, cpre);
 }
 
 // ---- reference-order monopoles (EXACT arithmetic) ----------------------------
@@ -1062,6 +1059,14 @@ int sf_tree_build(sfgpu_sim* s) {
                                                 t->tie_body);
     SF_CHECK_LAUNCH();
     s->timer.end(st, tk);
+    const bool exact = s->p.math == SFGPU_MATH_EXACT && s->p.form == SFGPU_FORM_PLAIN;
+    tk = s->timer.begin(st, "tree_monopoles");
+    k_gather<<<sf_ceil_div(n, GATHER_THREADS), GATHER_THREADS, 0, st>>>(t->vals, n, nin, t->counters + 4,
+                                                                       s->d_bounds, pos, mas, t->sp,
+                                                                       (fix4*)t->msum, (fix4*)t->cpre,
+                                                                       t->counters + 5);
+    SF_CHECK_LAUNCH();
+    s->timer.end(st, tk);
     tk = s->timer.begin(st, "tree_nodes");
     k_split_scan<<<sf_ceil_div(n, SS_TILE), SS_THREADS, 0, st>>>(t->keys, n, nin, s->p.leaf_cap, s->p.depth_max,
                                                                   t->sbase, t->split_start, t->split_level,
@@ -1070,17 +1075,14 @@ int sf_tree_build(sfgpu_sim* s) {
     SF_CHECK_LAUNCH();
     const uint32_t sb = sf_ceil_div((uint64_t)std::max<uint32_t>(t->split_cap, 1) * 8u, FILL_THREADS);
     k_split_fill<<<sb, FILL_THREADS, 0, st>>>(t->keys, nin, t->sbase, nsplit, t->split_cap, t->split_start, t->split_level,
-                                     s->d_bounds, s->p.leaf_cap, s->p.depth_max, t->nd, third, t->split_node);
+                                     s->d_bounds, s->p.leaf_cap, s->p.depth_max, t->nd, third, t->split_node, n,
+                                     t->counters + 4, exact ? nullptr : (const fix4*)t->msum,
+                                     (const fix4*)t->cpre);
     SF_CHECK_LAUNCH();
     s->timer.end(st, tk);
-    tk = s->timer.begin(st, "tree_monopoles");
-    k_gather<<<sf_ceil_div(n, GATHER_THREADS), GATHER_THREADS, 0, st>>>(t->vals, n, nin, t->counters + 4,
-                                                                       s->d_bounds, pos, mas, t->sp,
-                                                                       (fix4*)t->msum, (fix4*)t->cpre,
-                                                                       t->counters + 5);
-    SF_CHECK_LAUNCH();
-    const uint32_t mb = sf_ceil_div(1u + 8u * t->split_cap, 256);
-    if (s->p.math == SFGPU_MATH_EXACT && s->p.form == SFGPU_FORM_PLAIN) {
+    if (exact) {
+        tk = s->timer.begin(st, "tree_monopoles");
+        const uint32_t mb = sf_ceil_div(1u + 8u * t->split_cap, 256);
         k_ref_leaf_sums<<<mb, 256, 0, st>>>(nsplit, t->split_cap, t->nd, t->vals, t->ordA, pos, mas);
         SF_CHECK_LAUNCH();
         const uint32_t sm = sf_ceil_div(std::max<uint32_t>(t->split_cap, 1), 128);
@@ -1089,12 +1091,8 @@ int sf_tree_build(sfgpu_sim* s) {
                                             t->ordB, pos, mas);
             SF_CHECK_LAUNCH();
         }
-    } else {
-        k_monopoles<<<mb, 256, 0, st>>>(nsplit, t->split_cap, t->nd, n, t->counters + 4, s->d_bounds,
-                                        (const fix4*)t->msum, (const fix4*)t->cpre);
-        SF_CHECK_LAUNCH();
+        s->timer.end(st, tk);
     }
-    s->timer.end(st, tk);
     return SFGPU_OK;
 }
 

@@ -600,7 +600,110 @@ __device__ __forceinline__ void append_cells(const GroupLists& L, uint32_t am, u
     qcount += __popc(sb);
 }
 
-template <int KIND, int GSPLIT, int GB, bool STATS>
+// kick_1 of sim_step and the energies (simulation.c:420-497), applied by the
+// walk's epilogue to each body as soon as its force is known, when no SPH
+// force follows the walk: one pass and one launch fewer per step.  The
+// per-body arithmetic is k_kick_energy's; the block partials (float-float
+// within warps, FP64 across them) are added in block order by the last
+// block, which also advances the device step counter.
+struct WalkKick {
+    float* vel;
+    float* ken;
+    float* pen;
+    double* vel64;      // FP64 velocities (precision form) or NULL
+    double dt64;
+    float half_dt;
+    float g_over_eps;   // G / eps: the self term of the corrected potential
+    int physical;
+    double* part;       // [gridDim.x][4]
+    uint32_t* done;     // last-block ticket
+    double* sums;       // [0] T, [1] V, [2] corrected kinetic, [3] corrected potential
+    uint32_t* d_step;
+};
+
+__device__ __forceinline__ void walk_kick_body(const WalkKick& wk, uint32_t p, float mi, const float a[3], float potp,
+                                               ff (&e)[4]) {
+    float v[3];
+    double v64[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        const size_t q = 3u * (size_t)p + c;
+        if (wk.vel64) {
+            v64[c] = wk.vel64[q] + 0.5 * wk.dt64 * (double)a[c];
+            wk.vel64[q] = v64[c];
+            v[c] = (float)v64[c];
+        } else {
+            v[c] = fadd(wk.vel[q], fmul(wk.half_dt, a[c]));  // simulation.c:424
+            v64[c] = v[c];
+        }
+        wk.vel[q] = v[c];
+    }
+    // simulation.c:443-450
+    const float v2 = fadd(fadd(fmul(v[0], v[0]), fmul(v[1], v[1])), fmul(v[2], v[2]));
+    const float k_i = fmul(fmul(0.5f, mi), v2);
+    const float p_i = fmul(mi, potp);
+    wk.ken[p] = k_i;
+    wk.pen[p] = p_i;
+    if (wk.vel64) {
+        const double v2d = v64[0] * v64[0] + v64[1] * v64[1] + v64[2] * v64[2];
+        e[2] = ff_from_double(wk.physical ? 0.5 * (double)mi * v2d : 0.5 * v2d);
+    } else {
+        e[2] = ff_from(wk.physical ? fmul(fmul(0.5f, mi), v2) : fmul(0.5f, v2));
+    }
+    e[3] = ff_from(fmul(fmul(0.5f, mi), fadd(potp, fmul(wk.g_over_eps, mi))));
+    e[0] = ff_from(k_i);
+    e[1] = ff_from(p_i);
+}
+
+// Block partials of e (every thread of the block calls this), then the last
+// block's ordered FP64 totals.
+__device__ void walk_kick_reduce(const WalkKick& wk, ff (&e)[4]) {
+    __shared__ double wsum[4][GW_WARPS];
+    __shared__ bool s_last;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    ff_warp_sum<4>(e);
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < 4; k++) wsum[k][warp] = ff_to_double(e[k]);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            double t = 0.0;
+            for (int u = 0; u < GW_WARPS; u++) t += wsum[k][u];
+            wk.part[(size_t)blockIdx.x * 4 + k] = t;
+        }
+        __threadfence();
+        s_last = atomicAdd(wk.done, 1u) == gridDim.x - 1;
+        if (s_last) *wk.done = 0u;
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    double v[4] = {0.0, 0.0, 0.0, 0.0};
+    for (uint32_t q = threadIdx.x; q < gridDim.x; q += GW_THREADS)
+#pragma unroll
+        for (int k = 0; k < 4; k++) v[k] += __ldcg(&wk.part[(size_t)q * 4 + k]);
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        double x = v[k];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) wsum[k][warp] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            double t = 0.0;
+            for (int u = 0; u < GW_WARPS; u++) t += wsum[k][u];
+            wk.sums[k] = t;
+        }
+        *wk.d_step += 1u;
+    }
+}
+
+template <int KIND, int GSPLIT, int GB, bool STATS, bool KICK = false>
 __global__ void __launch_bounds__(GW_THREADS, GW_MIN_BLOCKS) k_walk_group(const float4* __restrict__ sp,
                                                            const uint32_t* __restrict__ V, uint32_t n, NodeArrays nd,
                                                            ForceConsts fc, float th_lo, float th_hi,
@@ -609,7 +712,8 @@ __global__ void __launch_bounds__(GW_THREADS, GW_MIN_BLOCKS) k_walk_group(const 
                                                            float* __restrict__ acc, float* __restrict__ pot,
                                                            uint32_t* __restrict__ st_int,
                                                            uint32_t* __restrict__ st_open,
-                                                           unsigned long long* __restrict__ tot, uint32_t* d_status) {
+                                                           unsigned long long* __restrict__ tot, uint32_t* d_status,
+                                                           WalkKick wk) {
     __shared__ uint32_t s_node[GW_WARPS][GW_STACK];
     __shared__ uint32_t s_mask[GW_WARPS][GW_STACK];
     __shared__ __align__(16) float l_x[GW_WARPS][GW_LIST];
@@ -642,8 +746,10 @@ __global__ void __launch_bounds__(GW_THREADS, GW_MIN_BLOCKS) k_walk_group(const 
     const uint32_t k = group * (uint32_t)GB + (uint32_t)bl;
     const bool live = k < n;
     const uint32_t live_mask = __ballot_sync(0xffffffffu, live) & body_bits;
-    if (!live_mask) return;
-    const float4 b = live ? sp[k] : sp[group * (uint32_t)GB];
+    // with the fused kick every warp reaches the block reduction; a warp
+    // past the last body walks nothing
+    if (!live_mask && !KICK) return;
+    const float4 b = sp[live ? k : min(group * (uint32_t)GB, n - 1u)];
     const float rx = b.x, ry = b.y, rz = b.z, mi = b.w;
     if (half == 0) sbd[bl] = b;
     __syncwarp();
@@ -691,7 +797,7 @@ __global__ void __launch_bounds__(GW_THREADS, GW_MIN_BLOCKS) k_walk_group(const 
             stn[0] = 0u;
             stm[0] = live_mask;
         }
-        top = 1;
+        top = live_mask ? 1 : 0;
     } else {
         // Every warp of the group walks the top two levels itself (exact
         // per-body tests); the up to 64 cells left at level 2 are dealt out
@@ -920,15 +1026,18 @@ __global__ void __launch_bounds__(GW_THREADS, GW_MIN_BLOCKS) k_walk_group(const 
         sw += __shfl_xor_sync(0xffffffffu, sw, o);
         n_int_body += __shfl_xor_sync(0xffffffffu, n_int_body, o);
     }
+    ff e[4] = {ff{0.f, 0.f}, ff{0.f, 0.f}, ff{0.f, 0.f}, ff{0.f, 0.f}};
     if (live && half == 0) {
         const uint32_t p = V[k];
         if (GSPLIT == 1) {
             const float g = -fc.neg_g;
             const float scale = fc.physical ? g : g * mi;
-            acc[3u * p + 0u] = scale * sx;
-            acc[3u * p + 1u] = scale * sy;
-            acc[3u * p + 2u] = scale * sz;
+            const float a[3] = {scale * sx, scale * sy, scale * sz};
+            acc[3u * p + 0u] = a[0];
+            acc[3u * p + 1u] = a[1];
+            acc[3u * p + 2u] = a[2];
             pot[p] = fc.neg_g * sw;
+            if (KICK) walk_kick_body(wk, p, mi, a, fc.neg_g * sw, e);
             if (STATS) {
                 st_int[p] = n_int_body;
                 st_open[p] = n_open;
@@ -950,6 +1059,7 @@ __global__ void __launch_bounds__(GW_THREADS, GW_MIN_BLOCKS) k_walk_group(const 
         atomicAdd(&tot[0], ci);
         atomicAdd(&tot[1], open_total);
     }
+    if (KICK) walk_kick_reduce(wk, e);
 }
 
 template <int KIND, int GSPLIT, int GB = 32>
@@ -970,11 +1080,29 @@ int launch_group(sfgpu_sim* s, bool stats) {
         }
         k_walk_group<KIND, GSPLIT, GB, true><<<grid, GW_THREADS, 0, s->stream>>>(
             t->sp, t->vals, s->n, t->nd, fc, th_lo, th_hi, th_acc, th_open, s->p.leaf_cap, t->walk_part, acc, pot,
-            s->stat_int, s->stat_open, s->walk_tot, s->d_status);
+            s->stat_int, s->stat_open, s->walk_tot, s->d_status, WalkKick{});
+    } else if (GSPLIT == 1 && s->fuse_kick && s->red_cap * 2u >= grid * 4u) {
+        WalkKick wk;
+        wk.vel = s->slab + (size_t)3 * s->n;
+        wk.ken = s->slab + (size_t)11 * s->n;
+        wk.pen = s->slab + (size_t)12 * s->n;
+        wk.vel64 = s->vel64;
+        wk.dt64 = s->p.dt;
+        wk.half_dt = 0.5f * (float)s->p.dt;
+        wk.g_over_eps = (float)(s->p.G / s->p.eps);
+        wk.physical = s->p.acc_mode == SFGPU_ACC_PHYSICAL;
+        wk.part = (double*)s->red;
+        wk.done = s->d_done + 1;
+        wk.sums = s->sums;
+        wk.d_step = s->d_step;
+        k_walk_group<KIND, GSPLIT, GB, false, true><<<grid, GW_THREADS, 0, s->stream>>>(
+            t->sp, t->vals, s->n, t->nd, fc, th_lo, th_hi, th_acc, th_open, s->p.leaf_cap, t->walk_part, acc, pot,
+            nullptr, nullptr, s->walk_tot, s->d_status, wk);
+        s->kicked = true;
     } else {
         k_walk_group<KIND, GSPLIT, GB, false><<<grid, GW_THREADS, 0, s->stream>>>(
             t->sp, t->vals, s->n, t->nd, fc, th_lo, th_hi, th_acc, th_open, s->p.leaf_cap, t->walk_part, acc, pot,
-            nullptr, nullptr, s->walk_tot, s->d_status);
+            nullptr, nullptr, s->walk_tot, s->d_status, WalkKick{});
     }
     SF_CHECK_LAUNCH();
     if (GSPLIT > 1) {
