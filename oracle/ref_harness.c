@@ -1,6 +1,6 @@
 /*
  * ref_harness.c -- drives the unmodified Starflood reference (compiled in
- * place from its own sources by oracle/build_ref.py) so that its results can
+ * place from its own sources by oracle/build.py) so that its results can
  * be captured as golden vectors.
  *
  * TEST INFRASTRUCTURE ONLY.  Compiled against the reference headers with a
