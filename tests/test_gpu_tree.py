@@ -274,3 +274,32 @@ def test_walk_totals_match_per_body_counts(sf, group):
                 assert (int(ni.sum()), int(no.sum())) == (ti, to)
             totals.append((ti, to))
     assert totals[0] == totals[1]
+
+
+def test_tree_clustered_bucket_overflow(sf, oracle32):
+    """60 % of 65,536 bodies in a sphere of radius 0.02: the sort's top-digit
+    bucket holding the cluster exceeds one CTA's shared memory, so the tree
+    keys go through the sort's cooperative fallback; membership, node count
+    and per-body interaction counts must still be the reference's."""
+    from starflood_gb300.ics import uniform_ball
+    n = 65536
+    pos, vel, mas = uniform_ball(n, seed=21)
+    rng = np.random.default_rng(21)
+    m = int(0.6 * n)
+    d = rng.normal(size=(m, 3))
+    d *= (0.02 * rng.random(m) ** (1.0 / 3.0) / np.linalg.norm(d, axis=1))[:, None]
+    pos[:m] = (np.array([0.3, 0.3, 0.3]) + d).astype(np.float32)
+    p = sf.default_params(solver=sf.SOLVER_TREE, eps=0.01, theta=0.5, flags=sf.FLAG_STATS)
+    with sf.Sim(n, p) as s:
+        s.set_state(pos, vel, mas)
+        s.solve(2)
+        assert s.status() == 0
+        v = slab_views(s.download(), n, 13)
+        op = make_params(eps=0.01, theta=0.5, use_tree=1)
+        st, nodes = oracle32.tree_build(pos, mas, oracle32.root_bounds(pos, 2), op)
+        assert s.num_nodes() == len(nodes)
+        check_membership(s, nodes, n)
+        a, pt, stats = oracle32.walk(pos, mas, nodes, op)
+        ni, no = s.walk_stats()
+        np.testing.assert_array_equal(ni, stats[:, 0])
+        assert rel_l2(v["acc"], a) < 1e-5
