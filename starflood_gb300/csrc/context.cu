@@ -206,6 +206,9 @@ extern "C" int sfgpu_destroy(sfgpu_sim* s) {
     cudaFreeHost(s->h_step);
     cudaFreeHost(s->h_sums);
     cudaFreeHost(s->h_status);
+    if (s->ev_fork) cudaEventDestroy(s->ev_fork);
+    if (s->ev_join) cudaEventDestroy(s->ev_join);
+    if (s->aux) cudaStreamDestroy(s->aux);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
     return SFGPU_OK;
@@ -242,6 +245,9 @@ extern "C" int sfgpu_create(sfgpu_sim** out, uint32_t n, const sfgpu_params* p) 
     } while (0)
     TRY(cudaGetDevice(&s->device));
     TRY(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+    TRY(cudaStreamCreateWithFlags(&s->aux, cudaStreamNonBlocking));
+    TRY(cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming));
+    TRY(cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming));
     const size_t slab_bytes = sizeof(float) * (size_t)n * s->dof;
     TRY(cudaMalloc(&s->slab, slab_bytes));
     TRY(cudaMemsetAsync(s->slab, 0, slab_bytes, s->stream));  // simulation.c:118

@@ -273,6 +273,8 @@ struct sfgpu_sim {
     sfgpu_params p{};
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t aux = nullptr;        // a second stream for independent stages of a step
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     float* slab = nullptr;         // N*dof, reference layout
     double* pos64 = nullptr;       // COMPENSATED: FP64 positions (3N)
     double* vel64 = nullptr;       // COMPENSATED: FP64 velocities (3N)

@@ -1060,19 +1060,31 @@ int sf_tree_build(sfgpu_sim* s) {
     SF_CHECK_LAUNCH();
     s->timer.end(st, tk);
     const bool exact = s->p.math == SFGPU_MATH_EXACT && s->p.form == SFGPU_FORM_PLAIN;
+    // the gather (bodies and prefix sums in sorted order) and the split
+    // scan (from the sorted keys) are independent: the gather runs on the
+    // second stream, joined before the node records need its sums (with
+    // per-stage timing both stay on the main stream)
+    const bool fork = !s->timer.enabled;
+    cudaStream_t gs = fork ? s->aux : st;
+    if (fork) {
+        SF_CUDA(cudaEventRecord(s->ev_fork, st));
+        SF_CUDA(cudaStreamWaitEvent(gs, s->ev_fork, 0));
+    }
     tk = s->timer.begin(st, "tree_monopoles");
-    k_gather<<<sf_ceil_div(n, GATHER_THREADS), GATHER_THREADS, 0, st>>>(t->vals, n, nin, t->counters + 4,
+    k_gather<<<sf_ceil_div(n, GATHER_THREADS), GATHER_THREADS, 0, gs>>>(t->vals, n, nin, t->counters + 4,
                                                                        s->d_bounds, pos, mas, t->sp,
                                                                        (fix4*)t->msum, (fix4*)t->cpre,
                                                                        t->counters + 5);
     SF_CHECK_LAUNCH();
     s->timer.end(st, tk);
+    if (fork) SF_CUDA(cudaEventRecord(s->ev_join, gs));
     tk = s->timer.begin(st, "tree_nodes");
     k_split_scan<<<sf_ceil_div(n, SS_TILE), SS_THREADS, 0, st>>>(t->keys, n, nin, s->p.leaf_cap, s->p.depth_max,
                                                                   t->sbase, t->split_start, t->split_level,
                                                                   t->split_cap, nsplit, t->nodes_max,
                                                                   t->counters + 8, t->counters + 6, s->d_status);
     SF_CHECK_LAUNCH();
+    if (fork) SF_CUDA(cudaStreamWaitEvent(st, s->ev_join, 0));
     const uint32_t sb = sf_ceil_div((uint64_t)std::max<uint32_t>(t->split_cap, 1) * 8u, FILL_THREADS);
     k_split_fill<<<sb, FILL_THREADS, 0, st>>>(t->keys, nin, t->sbase, nsplit, t->split_cap, t->split_start, t->split_level,
                                      s->d_bounds, s->p.leaf_cap, s->p.depth_max, t->nd, third, t->split_node, n,
