@@ -217,8 +217,11 @@ int sfgpu_flush_l2(void* stream);
 /* One drop-in call on a host slab (page-locked for full speed), as
  * sim_solv / sim_step (src/simulation.c:230-519) make it: uploads the arrays
  * the call reads (pos, vel, acc, mas; rad with SPH), runs the solve
- * (solve_only != 0) or one graph-replayed step, downloads the whole slab and
- * the device status word (cleared), with a single host synchronisation. */
+ * (solve_only != 0) or one step, downloads the whole slab and the device
+ * status word (cleared), with a single host synchronisation.  For a
+ * page-locked slab the copies and the step are one captured CUDA graph
+ * (recaptured when the slab pointer or the call kind changes), so a call
+ * is one graph launch. */
 int sfgpu_host_step(sfgpu_sim* s, float* slab, uint32_t step_number, int solve_only, uint32_t* status);
 
 /* initcond_generate (src/initcond.c:11-255) on the device: the reference's

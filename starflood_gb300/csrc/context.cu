@@ -186,6 +186,8 @@ extern "C" int sfgpu_destroy(sfgpu_sim* s) {
     sf_snapshot_free(s);
     sf_vis_free(s);
     if (s->graph) cudaGraphExecDestroy(s->graph);
+    if (s->host_graph) cudaGraphExecDestroy(s->host_graph);
+    cudaFreeHost(s->h_step_in);
     sf_tree_free(s->tree);
     sf_sph_free(s);
     cudaFree(s->slab);
@@ -270,6 +272,7 @@ extern "C" int sfgpu_create(sfgpu_sim** out, uint32_t n, const sfgpu_params* p) 
     TRY(cudaMalloc(&s->walk_tot, sizeof(unsigned long long) * 2));
     TRY(cudaMemsetAsync(s->walk_tot, 0, sizeof(unsigned long long) * 2, s->stream));
     TRY(cudaMallocHost(&s->h_step, sizeof(uint32_t)));
+    TRY(cudaMallocHost(&s->h_step_in, sizeof(uint32_t)));
     TRY(cudaMallocHost(&s->h_sums, sizeof(double) * 16));
     TRY(cudaMallocHost(&s->h_status, sizeof(uint32_t)));
     if (p->solver == SFGPU_SOLVER_TREE) {
@@ -560,6 +563,28 @@ extern "C" int sfgpu_synchronize(sfgpu_sim* s) {
     return SFGPU_OK;
 }
 
+__global__ static void k_set_step_host(uint32_t* d_step, const volatile uint32_t* h_step) { *d_step = *h_step; }
+
+// Everything of one drop-in call, queued on the simulation's stream: the
+// arrays a solve or a step reads (pos, vel, acc, mas, 0..9, and with SPH the
+// smoothing lengths, 13) in, the step number from page-locked memory, the
+// solve or the step, the whole slab and the status word out.
+static int host_step_body(sfgpu_sim* s, float* slab, int solve_only) {
+    const size_t n = s->n;
+    SF_CUDA(cudaMemcpyAsync(s->slab, slab, sizeof(float) * 10 * n, cudaMemcpyHostToDevice, s->stream));
+    if (s->dof > 13)
+        SF_CUDA(cudaMemcpyAsync(s->slab + 13 * n, slab + 13 * n, sizeof(float) * n, cudaMemcpyHostToDevice,
+                                s->stream));
+    k_set_step_host<<<1, 1, 0, s->stream>>>(s->d_step, s->h_step_in);
+    SF_CHECK_LAUNCH();
+    if (refresh_fp64(s) != SFGPU_OK) return SFGPU_FAILURE;
+    if ((solve_only ? solve_body(s, false) : step_body(s)) != SFGPU_OK) return SFGPU_FAILURE;
+    SF_CUDA(cudaMemcpyAsync(slab, s->slab, sizeof(float) * s->dof * n, cudaMemcpyDeviceToHost, s->stream));
+    SF_CUDA(cudaMemcpyAsync(s->h_status, s->d_status, sizeof(uint32_t), cudaMemcpyDeviceToHost, s->stream));
+    SF_CUDA(cudaMemsetAsync(s->d_status, 0, sizeof(uint32_t), s->stream));
+    return SFGPU_OK;
+}
+
 extern "C" int sfgpu_host_step(sfgpu_sim* s, float* slab, uint32_t step_number, int solve_only,
                                uint32_t* status) {
     sf_clear_error();
@@ -567,19 +592,41 @@ extern "C" int sfgpu_host_step(sfgpu_sim* s, float* slab, uint32_t step_number, 
         sf_set_error("sfgpu_host_step: NULL argument");
         return SFGPU_FAILURE;
     }
-    // the arrays a solve or a step reads: pos, vel, acc, mas (0..9) and,
-    // with SPH, the smoothing lengths (13); everything comes back
-    const size_t n = s->n;
-    SF_CUDA(cudaMemcpyAsync(s->slab, slab, sizeof(float) * 10 * n, cudaMemcpyHostToDevice, s->stream));
-    if (s->dof > 13)
-        SF_CUDA(cudaMemcpyAsync(s->slab + 13 * n, slab + 13 * n, sizeof(float) * n, cudaMemcpyHostToDevice,
-                                s->stream));
-    if (refresh_fp64(s) != SFGPU_OK) return SFGPU_FAILURE;
-    const int rc = solve_only ? sfgpu_solve(s, step_number) : sfgpu_run(s, step_number, 1);
-    if (rc != SFGPU_OK) return rc;
-    SF_CUDA(cudaMemcpyAsync(slab, s->slab, sizeof(float) * s->dof * n, cudaMemcpyDeviceToHost, s->stream));
-    SF_CUDA(cudaMemcpyAsync(s->h_status, s->d_status, sizeof(uint32_t), cudaMemcpyDeviceToHost, s->stream));
-    SF_CUDA(cudaMemsetAsync(s->d_status, 0, sizeof(uint32_t), s->stream));
+    *s->h_step_in = step_number;  // the previous call has synchronised: nothing reads it now
+    // a page-locked slab lets the copies live in one captured graph with the
+    // step, replayed by a single launch per call
+    bool use_graph = !(s->p.flags & SFGPU_FLAG_NOGRAPH) && !s->timer.enabled && s->host_graph_ok;
+    if (use_graph && (s->host_graph_slab != slab || s->host_graph_solve != (solve_only ? 1 : 0))) {
+        cudaPointerAttributes pa;
+        const bool pinned = cudaPointerGetAttributes(&pa, slab) == cudaSuccess && pa.type == cudaMemoryTypeHost;
+        cudaGetLastError();
+        if (s->host_graph) {
+            cudaGraphExecDestroy(s->host_graph);
+            s->host_graph = nullptr;
+        }
+        if (pinned) {
+            cudaGraph_t g = nullptr;
+            SF_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+            const int rc = host_step_body(s, slab, solve_only);
+            const cudaError_t ce = cudaStreamEndCapture(s->stream, &g);
+            if (rc == SFGPU_OK && ce == cudaSuccess && cudaGraphInstantiate(&s->host_graph, g, 0) == cudaSuccess) {
+                s->host_graph_slab = slab;
+                s->host_graph_solve = solve_only ? 1 : 0;
+            } else {
+                s->host_graph = nullptr;
+                s->host_graph_ok = false;
+            }
+            if (g) cudaGraphDestroy(g);
+            cudaGetLastError();
+            sf_clear_error();
+        }
+        use_graph = s->host_graph != nullptr;
+    }
+    if (use_graph) {
+        SF_CUDA(cudaGraphLaunch(s->host_graph, s->stream));
+    } else if (host_step_body(s, slab, solve_only) != SFGPU_OK) {
+        return SFGPU_FAILURE;
+    }
     SF_CUDA(cudaStreamSynchronize(s->stream));
     if (status) *status = *s->h_status;
     return SFGPU_OK;

@@ -304,6 +304,11 @@ struct sfgpu_sim {
     unsigned long long* walk_tot = nullptr;  // [2]
     StageTimer timer;
     cudaGraphExec_t graph = nullptr;
+    cudaGraphExec_t host_graph = nullptr;  // sfgpu_host_step: copies in, step, copies out
+    const float* host_graph_slab = nullptr;
+    int host_graph_solve = -1;
+    bool host_graph_ok = true;
+    uint32_t* h_step_in = nullptr;     // page-locked: the step number the host-step graph reads
     bool graph_ok = true;
     bool fuse_kick = false;        // set by a step: the walk may do kick_1 and the energies
     bool kicked = false;           // ... and did
