@@ -125,3 +125,38 @@ def test_compat_sph_reference(sf, oracle32):
     assert rel(v["acc"], d["solv_acc"]) < 1e-5
     L.sim_free(C.byref(sim))
     L.tree_free(C.byref(sim.tree))
+
+
+def test_host_step_graph_matches_eager(sf):
+    """sfgpu_host_step on a page-locked slab (one captured graph with the
+    copies) and on a pageable slab (queued calls) give identical slabs, for
+    steps and solve-only calls, and a changed slab pointer is followed."""
+    from starflood_gb300.ics import uniform_ball
+    L = sf.lib()
+    n = 4096
+    pos, vel, mas = uniform_ball(n, seed=31)
+    p = sf.default_params(solver=sf.SOLVER_TREE, eps=0.01, dt=1e-3, theta=0.5)
+    outs = []
+    for pinned in (True, False):
+        dof = sf.dof(p)
+        slabs = [np.zeros(n * dof, np.float32) for _ in range(2)]
+        for slab in slabs:
+            v = sf.slab_views(slab, n, dof)
+            v["pos"][:] = pos
+            v["vel"][:] = vel
+            v["mas"][:] = mas
+            if pinned:
+                sf.check(L.sfgpu_host_register(slab.ctypes.data, slab.nbytes), "register")
+        st = (C.c_uint32 * 1)()
+        with sf.Sim(n, p) as s:
+            for k in range(4):
+                slab = slabs[k // 2]  # the second pair of calls moves to another slab
+                if k == 2:
+                    slab[:] = slabs[0]
+                sf.check(L.sfgpu_host_step(s.h, slab.ctypes.data, k, 1 if k == 0 else 0, st), "host_step")
+                assert st[0] == 0
+            outs.append(slabs[1].copy())
+        if pinned:
+            for slab in slabs:
+                L.sfgpu_host_unregister(slab.ctypes.data)
+    np.testing.assert_array_equal(outs[0], outs[1])
