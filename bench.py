@@ -790,7 +790,7 @@ def main():
     ap.add_argument("--no-pm", action="store_true", help="skip the particle-mesh grid sub-benchmark")
     ap.add_argument("--walk-split", type=int, default=0, help="Barnes-Hut walk variant (sfgpu_params.walk_split)")
     ap.add_argument("--walk-group", type=int, default=0, help="bodies per warp of the group walk (sfgpu_params.walk_group)")
-    ap.add_argument("--only", choices=["pp", "sph", "pm"], default=None,
+    ap.add_argument("--only", choices=["pp", "sph", "pm", "batch"], default=None,
                     help="run one sub-benchmark alone and print its object (profiling runs)")
     ap.add_argument("--pp-n", type=int, default=N_PP, help="bodies of the PP sub-benchmark with --only pp")
     ap.add_argument("--sph-path", type=int, default=0, help="SPH pass variant with --only sph (sfgpu_params.sph_path)")
@@ -833,6 +833,9 @@ def main():
         return
     if args.only == "pm":
         print(json.dumps({"only": "pm", "pm": gpu_pm(sf)}))
+        return
+    if args.only == "batch":
+        print(json.dumps({"only": "batch", "batch": gpu_batch(sf)}))
         return
     if args.only == "sph":
         print(json.dumps({"only": "sph", "sph": gpu_sph(sf, max(3, args.steps), args.warmup, args.sph_path)}))

@@ -121,6 +121,12 @@ __global__ void __launch_bounds__(BS) k_batch_pp(const BatchItem* __restrict__ i
             sj[0][threadIdx.x] = make_float4(x, x, y, y);
             sj[1][threadIdx.x] = make_float4(z, z, m, m);
             __syncthreads();
+            // each tile's BS terms in their own sums, added to the running
+            // ones once per tile: two-level summation keeps the FP32
+            // rounding of a j-chunk near that of one tile
+            float2 tx[PAIRS], ty[PAIRS], tz[PAIRS], tp[PAIRS];
+#pragma unroll
+            for (int q = 0; q < PAIRS; q++) tx[q] = ty[q] = tz[q] = tp[q] = make_float2(0.f, 0.f);
 #pragma unroll 4
             for (int jj = 0; jj < BS; jj++) {
                 const float4 A = sj[0][jj], B = sj[1][jj];
@@ -128,7 +134,14 @@ __global__ void __launch_bounds__(BS) k_batch_pp(const BatchItem* __restrict__ i
                 const float2 sz = make_float2(B.x, B.y), sw = make_float2(B.z, B.w);
 #pragma unroll
                 for (int q = 0; q < PAIRS; q++)
-                    pp_pair_step<2>(sx, sy, sz, sw, nx[q], ny[q], nz[q], e2, ax[q], ay[q], az[q], ph[q]);
+                    pp_pair_step<2>(sx, sy, sz, sw, nx[q], ny[q], nz[q], e2, tx[q], ty[q], tz[q], tp[q]);
+            }
+#pragma unroll
+            for (int q = 0; q < PAIRS; q++) {
+                ax[q] = __fadd2_rn(ax[q], tx[q]);
+                ay[q] = __fadd2_rn(ay[q], ty[q]);
+                az[q] = __fadd2_rn(az[q], tz[q]);
+                ph[q] = __fadd2_rn(ph[q], tp[q]);
             }
         }
         float4* out = part + part_off[w.sys] + (size_t)w.chunk * nb;
@@ -168,60 +181,117 @@ __global__ void k_batch_reduce(const float4* __restrict__ part, const uint32_t* 
 }
 
 // xbar_k += sum_j K_kj (m_k b_j - m_j b_k), b = coef c abar (see file
-// comment).  Block r covers bodies [i0, i0+VJP_BS) of system blk[r].x, with
-// j-tiles of the same system in shared memory.
+// comment), with j-tiles of the same system in shared memory, on the paired
+// FP32 instructions: each thread owns VJP_IPT
+// bodies k (as VJP_IPT/2 pairs, one body per half of a float2), every j of
+// a tile is staged duplicated ((x,x,y,y), (z,z,m,m), (bx,bx,by,by),
+// (bz,bz,-,-)) so one 128-bit shared load feeds both halves, and every
+// arithmetic step of a (k, j) term is one instruction for two bodies.
+// Block r covers bodies [i0, i0 + VJP_BS * VJP_IPT) of system blk[r].x.
 constexpr int VJP_BS = 128;
-__global__ void __launch_bounds__(VJP_BS) k_batch_vjp(const uint2* __restrict__ blk, const uint32_t* __restrict__ off,
-                                                      const float* __restrict__ pos, const float* __restrict__ mas,
-                                                      const float* __restrict__ abar, float coef, ForceConsts fc,
-                                                      float* __restrict__ xbar) {
-    __shared__ float4 sx[VJP_BS];
-    __shared__ float4 sb[VJP_BS];
+constexpr int VJP_IPT = 4;
+__global__ void __launch_bounds__(VJP_BS) k_batch_vjp2(const uint2* __restrict__ blk, const uint32_t* __restrict__ off,
+                                                       const float* __restrict__ pos, const float* __restrict__ mas,
+                                                       const float* __restrict__ abar, float coef, ForceConsts fc,
+                                                       float* __restrict__ xbar) {
+    __shared__ float4 sj[4][VJP_BS];
+    constexpr int PAIRS = VJP_IPT / 2;
     const uint2 w = blk[blockIdx.x];
     const uint32_t base = off[w.x], nb = off[w.x + 1] - base;
-    const uint32_t i = w.y + threadIdx.x;
-    const bool live = i < nb;
-    const uint32_t g = base + (live ? i : 0u);
     const float cg = -fc.neg_g;
-    const float xk = pos[3u * g], yk = pos[3u * g + 1u], zk = pos[3u * g + 2u], mk = mas[g];
-    const float ck = coef * (fc.physical ? cg : cg * mk);
-    const float bkx = ck * abar[3u * g], bky = ck * abar[3u * g + 1u], bkz = ck * abar[3u * g + 2u];
-    float gx = 0.f, gy = 0.f, gz = 0.f;
+    float2 nx[PAIRS], ny[PAIRS], nz[PAIRS], mk[PAIRS], bkx[PAIRS], bky[PAIRS], bkz[PAIRS], gx[PAIRS], gy[PAIRS],
+        gz[PAIRS];
+#pragma unroll
+    for (int q = 0; q < PAIRS; q++) {
+        float v[2][7];
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const uint32_t i = w.y + (uint32_t)(2 * q + h) * VJP_BS + threadIdx.x;
+            const bool live = i < nb;
+            const uint32_t g = base + (live ? i : 0u);
+            const float m = live ? mas[g] : 0.f;
+            const float ck = coef * (fc.physical ? cg : cg * m);
+            v[h][0] = live ? -pos[3u * g] : 0.f;
+            v[h][1] = live ? -pos[3u * g + 1u] : 0.f;
+            v[h][2] = live ? -pos[3u * g + 2u] : 0.f;
+            v[h][3] = m;
+            v[h][4] = live ? ck * abar[3u * g] : 0.f;
+            v[h][5] = live ? ck * abar[3u * g + 1u] : 0.f;
+            v[h][6] = live ? ck * abar[3u * g + 2u] : 0.f;
+        }
+        nx[q] = make_float2(v[0][0], v[1][0]);
+        ny[q] = make_float2(v[0][1], v[1][1]);
+        nz[q] = make_float2(v[0][2], v[1][2]);
+        mk[q] = make_float2(v[0][3], v[1][3]);
+        bkx[q] = make_float2(v[0][4], v[1][4]);
+        bky[q] = make_float2(v[0][5], v[1][5]);
+        bkz[q] = make_float2(v[0][6], v[1][6]);
+        gx[q] = gy[q] = gz[q] = make_float2(0.f, 0.f);
+    }
+    const float2 e2 = make_float2(fc.eps2, fc.eps2);
+    const float2 m3 = make_float2(-3.0f, -3.0f);
     for (uint32_t jt = 0; jt < nb; jt += VJP_BS) {
-        float4 a = make_float4(0.f, 0.f, 0.f, 0.f), bv = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (jt + threadIdx.x < nb) {
-            const uint32_t j = base + jt + threadIdx.x;
-            const float mj = mas[j];
-            const float cj = coef * (fc.physical ? cg : cg * mj);
-            a = make_float4(pos[3u * j], pos[3u * j + 1u], pos[3u * j + 2u], mj);
-            bv = make_float4(cj * abar[3u * j], cj * abar[3u * j + 1u], cj * abar[3u * j + 2u], 0.f);
+        const uint32_t j = jt + threadIdx.x;
+        float x = 0.f, y = 0.f, z = 0.f, m = 0.f, bx = 0.f, by = 0.f, bz = 0.f;  // padding: zero mass, zero cotangent
+        if (j < nb) {
+            const uint32_t g = base + j;
+            m = mas[g];
+            const float cj = coef * (fc.physical ? cg : cg * m);
+            x = pos[3u * g];
+            y = pos[3u * g + 1u];
+            z = pos[3u * g + 2u];
+            bx = cj * abar[3u * g];
+            by = cj * abar[3u * g + 1u];
+            bz = cj * abar[3u * g + 2u];
         }
         __syncthreads();
-        sx[threadIdx.x] = a;
-        sb[threadIdx.x] = bv;
+        sj[0][threadIdx.x] = make_float4(x, x, y, y);
+        sj[1][threadIdx.x] = make_float4(z, z, m, m);
+        sj[2][threadIdx.x] = make_float4(bx, bx, by, by);
+        sj[3][threadIdx.x] = make_float4(bz, bz, 0.f, 0.f);
         __syncthreads();
         const uint32_t cnt = min((uint32_t)VJP_BS, nb - jt);
+#pragma unroll 2
         for (uint32_t jj = 0; jj < cnt; jj++) {
-            const float4 q = sx[jj];
-            const float4 bj = sb[jj];
-            const float dx = q.x - xk, dy = q.y - yk, dz = q.z - zk;
-            const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, fc.eps2)));
-            const float inv = rsqrtf(r2);
-            const float inv2 = inv * inv;
-            const float phi = inv * inv2;
-            const float psi3 = 3.0f * phi * inv2;
-            const float wx = mk * bj.x - q.w * bkx, wy = mk * bj.y - q.w * bky, wz = mk * bj.z - q.w * bkz;
-            const float dw = dx * wx + dy * wy + dz * wz;
-            gx += phi * wx - psi3 * dx * dw;
-            gy += phi * wy - psi3 * dy * dw;
-            gz += phi * wz - psi3 * dz * dw;
+            const float4 A = sj[0][jj], B = sj[1][jj], Cb = sj[2][jj], D = sj[3][jj];
+            const float2 xj = make_float2(A.x, A.y), yj = make_float2(A.z, A.w);
+            const float2 zj = make_float2(B.x, B.y), mj = make_float2(B.z, B.w);
+            const float2 bjx = make_float2(Cb.x, Cb.y), bjy = make_float2(Cb.z, Cb.w), bjz = make_float2(D.x, D.y);
+#pragma unroll
+            for (int q = 0; q < PAIRS; q++) {
+                const float2 dx = __fadd2_rn(xj, nx[q]), dy = __fadd2_rn(yj, ny[q]), dz = __fadd2_rn(zj, nz[q]);
+                float2 r2 = __ffma2_rn(dz, dz, e2);
+                r2 = __ffma2_rn(dy, dy, r2);
+                r2 = __ffma2_rn(dx, dx, r2);
+                const float2 inv = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
+                const float2 inv2 = __fmul2_rn(inv, inv);
+                const float2 phi = __fmul2_rn(inv, inv2);
+                // w = m_k b_j - m_j b_k; the gradient term phi w - 3 phi inv^2 d (d . w)
+                const float2 wx = __ffma2_rn(mk[q], bjx, __fmul2_rn(mj, make_float2(-bkx[q].x, -bkx[q].y)));
+                const float2 wy = __ffma2_rn(mk[q], bjy, __fmul2_rn(mj, make_float2(-bky[q].x, -bky[q].y)));
+                const float2 wz = __ffma2_rn(mk[q], bjz, __fmul2_rn(mj, make_float2(-bkz[q].x, -bkz[q].y)));
+                float2 dw = __fmul2_rn(dz, wz);
+                dw = __ffma2_rn(dy, wy, dw);
+                dw = __ffma2_rn(dx, wx, dw);
+                const float2 t = __fmul2_rn(__fmul2_rn(m3, __fmul2_rn(phi, inv2)), dw);  // -3 phi inv^2 (d . w)
+                gx[q] = __ffma2_rn(t, dx, __ffma2_rn(phi, wx, gx[q]));
+                gy[q] = __ffma2_rn(t, dy, __ffma2_rn(phi, wy, gy[q]));
+                gz[q] = __ffma2_rn(t, dz, __ffma2_rn(phi, wz, gz[q]));
+            }
         }
     }
-    if (live) {
-        xbar[3u * g] += gx;
-        xbar[3u * g + 1u] += gy;
-        xbar[3u * g + 2u] += gz;
-    }
+#pragma unroll
+    for (int q = 0; q < PAIRS; q++)
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const uint32_t i = w.y + (uint32_t)(2 * q + h) * VJP_BS + threadIdx.x;
+            if (i < nb) {
+                const uint32_t g = base + i;
+                xbar[3u * g] += h ? gx[q].y : gx[q].x;
+                xbar[3u * g + 1u] += h ? gy[q].y : gy[q].x;
+                xbar[3u * g + 2u] += h ? gz[q].y : gz[q].x;
+            }
+        }
 }
 
 __global__ void k_axpy(float* __restrict__ y, const float* __restrict__ x, float a, size_t m) {
@@ -439,7 +509,8 @@ extern "C" int sfgpu_batch_create(sfgpu_batch** out, uint32_t nsys, const uint32
     {
         std::vector<uint2> blk;
         for (uint32_t sy = 0; sy < nsys; sy++)
-            for (uint32_t i0 = 0; i0 < offsets[sy + 1] - offsets[sy]; i0 += VJP_BS) blk.push_back(make_uint2(sy, i0));
+            for (uint32_t i0 = 0; i0 < offsets[sy + 1] - offsets[sy]; i0 += VJP_BS * VJP_IPT)
+                blk.push_back(make_uint2(sy, i0));
         b->vjp_nblk = (uint32_t)blk.size();
         BTRY(cudaMalloc(&b->vjp_blk, sizeof(uint2) * blk.size()));
         BTRY(cudaMemcpy(b->vjp_blk, blk.data(), sizeof(uint2) * blk.size(), cudaMemcpyHostToDevice));
@@ -569,8 +640,8 @@ static int ensure(float** p, size_t* cap, size_t need) {
 
 static int vjp(sfgpu_batch* b, const float* pos, const float* abar, float coef, float* xbar) {
     const ForceConsts fc = sf_force_consts(b->sim->p);
-    k_batch_vjp<<<b->vjp_nblk, VJP_BS, 0, b->sim->stream>>>(b->vjp_blk, b->off, pos,
-                                                             b->sim->slab + (size_t)9 * b->total, abar, coef, fc, xbar);
+    k_batch_vjp2<<<b->vjp_nblk, VJP_BS, 0, b->sim->stream>>>(b->vjp_blk, b->off, pos,
+                                                              b->sim->slab + (size_t)9 * b->total, abar, coef, fc, xbar);
     SF_CHECK_LAUNCH();
     return SFGPU_OK;
 }
