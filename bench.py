@@ -282,10 +282,13 @@ def gpu_bh_e2e(steps, warmup, sf, pos, vel, mas):
         sim.step_number = warmup + k
         sf.check(L.sim_step(C.byref(sim)), "sim_step")
     dt = time.perf_counter() - t0
-    bytes_ = 4 * n * dof
+    # sfgpu_host_step uploads the arrays a step reads (pos, vel, acc, mas: 10
+    # floats per body; 11 with SPH's rad) and downloads the whole slab
+    h2d = 4 * n * (10 + (1 if dof > 13 else 0))
+    d2h = 4 * n * dof
     L.sim_free(C.byref(sim))
-    return {"value": n * steps / dt, "unit": "particle-steps/s", "h2d_bytes_per_step": bytes_,
-            "d2h_bytes_per_step": bytes_, "api": "sim_step() of include/starflood_compat.h, host slab"}
+    return {"value": n * steps / dt, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": d2h, "api": "sim_step() of include/starflood_compat.h, host slab"}
 
 
 def gpu_pp(sf, reps=2, n=N_PP):
