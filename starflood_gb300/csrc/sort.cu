@@ -217,6 +217,11 @@ __global__ void __launch_bounds__(SORT_THREADS) k_onesweep_all(uint64_t* k0, uin
     if (*enable == 0u) return;
     cooperative_groups::grid_group grid = cooperative_groups::this_grid();
     const uint32_t tiles = gridDim.x;
+    // the look-back words of every pass start clear (only this launch uses them)
+    for (size_t i = (size_t)blockIdx.x * SORT_THREADS + threadIdx.x; i < (size_t)passes * tiles * RADIX;
+         i += (size_t)tiles * SORT_THREADS)
+        status[i] = 0u;
+    grid.sync();
     uint64_t *ka = k0, *kb = k1;
     uint32_t *va = v0, *vb = v1;
     for (int p = 0; p < passes; p++) {
@@ -405,6 +410,19 @@ __global__ void __launch_bounds__(BK_THREADS, 1) k_bucket_sort(uint64_t* Kb, uin
 
 size_t bucket_sort_smem() { return (size_t)BK_CAP * 24; }  // + 21 KB of static scratch
 
+// The bucket path's work words cleared in one launch: the histograms of
+// every pass, the tile tickets and overflow flag, the top pass's look-back
+// words.
+__global__ void k_sort_clear(uint32_t* __restrict__ hist, uint32_t nhist, uint32_t* __restrict__ counters,
+                             uint32_t ncounters, uint32_t* __restrict__ status, uint32_t nstatus) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nhist + ncounters + nstatus;
+         i += gridDim.x * blockDim.x) {
+        if (i < nhist) hist[i] = 0u;
+        else if (i < nhist + ncounters) counters[i - nhist] = 0u;
+        else status[i - nhist - ncounters] = 0u;
+    }
+}
+
 __global__ void k_copy_pairs(const uint64_t* __restrict__ ks, const uint32_t* __restrict__ vs,
                              uint64_t* __restrict__ kd, uint32_t* __restrict__ vd, uint32_t n,
                              const uint32_t* enable) {
@@ -466,10 +484,14 @@ int sf_sort_pairs_keep(uint64_t* keys, uint32_t* vals, uint32_t n, int bits, Sor
         const int items = 4;
         const uint32_t tiles = sf_ceil_div(n, SORT_THREADS * items);
         uint32_t* big = w.counters + MAX_PASSES;
-        // pass slot 0: the top digit; slots 1..passes: the gated fallback
-        SF_CUDA(cudaMemsetAsync(w.hist, 0, sizeof(uint32_t) * passes * RADIX, st));
-        SF_CUDA(cudaMemsetAsync(w.counters, 0, sizeof(uint32_t) * (MAX_PASSES + 1), st));
-        SF_CUDA(cudaMemsetAsync(w.status, 0, sizeof(uint32_t) * (size_t)(passes + 1) * tiles * RADIX, st));
+        // pass slot 0: the top digit; slots 1..passes: the gated fallback,
+        // which clears its own
+        {
+            const uint32_t words = passes * RADIX + MAX_PASSES + 1 + tiles * RADIX;
+            k_sort_clear<<<std::min<uint32_t>(sf_ceil_div(words, 256), 64u), 256, 0, st>>>(
+                w.hist, passes * RADIX, w.counters, MAX_PASSES + 1, w.status, tiles * RADIX);
+            SF_CHECK_LAUNCH();
+        }
         const uint32_t hb = std::min<uint32_t>(sf_ceil_div(n, 256 * 8), (uint32_t)sf_num_sms() * 4);
         k_hist<<<hb, 256, 0, st>>>(keys, n, passes, w.hist, enable);
         SF_CHECK_LAUNCH();

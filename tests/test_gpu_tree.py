@@ -303,3 +303,30 @@ def test_tree_clustered_bucket_overflow(sf, oracle32):
         ni, no = s.walk_stats()
         np.testing.assert_array_equal(ni, stats[:, 0])
         assert rel_l2(v["acc"], a) < 1e-5
+
+
+@pytest.mark.parametrize("math", ["exact", "fast"])
+def test_tree_step_energies(sf, oracle32, math):
+    """The step's energy totals (computed in the walk's epilogue with FAST
+    arithmetic, by the separate kick kernel with EXACT) against the
+    reference's FP64 Kahan sums of ken and pen."""
+    d = golden("tree_uniform_n4096_theta0.5_3steps.npz")
+    n = len(d["pos"])
+    p = sf.default_params(solver=sf.SOLVER_TREE, eps=0.01, dt=1e-3, theta=0.5,
+                          math=sf.MATH_EXACT if math == "exact" else sf.MATH_FAST)
+    op = make_params(eps=0.01, theta=0.5, dt=1e-3, use_tree=1)
+    osim, oslab, _ = oracle32.new_sim(n, op)
+    ov = slab_views(oslab, n, 13)
+    ov["pos"][:] = d["pos"]
+    ov["vel"][:] = d["vel"]
+    ov["mas"][:] = d["mas"]
+    oracle32.sim_solv(op, osim, 0)
+    with sf.Sim(n, p) as s:
+        s.set_state(d["pos"], d["vel"], d["mas"])
+        s.solve(0)
+        for k in range(3):
+            _, T, V = oracle32.sim_step(op, osim, k)
+            s.step(k)
+            Tg, Vg = s.energies()
+            tol = 1e-13 if math == "exact" else 1e-5
+            assert abs(Tg - T) <= tol * abs(T) and abs(Vg - V) <= tol * abs(V), (k, Tg, T, Vg, V)
