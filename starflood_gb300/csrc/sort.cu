@@ -2,9 +2,11 @@
 //
 // One global histogram pass computes the digit counts of every pass at once;
 // each 7-bit digit pass is then a single kernel: tiles take tickets in launch
-// order, rank their keys with warp match/ballot, and chain their per-digit
-// offsets through a decoupled look-back over the preceding tiles.  All waits
-// are bounded and report SFGPU_STATUS_SPIN instead of hanging.
+// order, rank their keys with per-bit warp ballots, and chain their
+// per-digit offsets through a decoupled look-back over the preceding tiles.
+// Up to 2^17 pairs only the top digit takes a tile pass; each bucket of it
+// is then sorted by one CTA in shared memory (below).  All waits are bounded
+// and report SFGPU_STATUS_SPIN instead of hanging.
 #include <cooperative_groups.h>
 
 #include "internal.cuh"
@@ -246,11 +248,11 @@ __global__ void __launch_bounds__(SORT_THREADS) k_onesweep_all(uint64_t* k0, uin
 // After a tile pass on the most significant digit, the pairs of bucket b
 // (keys whose top digit is b) are contiguous.  One CTA per bucket finishes
 // the low digits with stable LSD passes in its own shared memory: per pass,
-// warps rank consecutive 32-key rounds (warp match), counts are prefixed
-// over warps and digits, and every pair moves to its place in the other
-// buffer; __syncthreads separate the steps, so no pass needs a grid-wide
-// wait.  A bucket larger than BK_CAP runs the same passes through global
-// memory in BK_CAP-pair chunks (slower, still exact).
+// warps rank consecutive 32-key rounds (per-bit ballots), counts are
+// prefixed over warps and digits, and every pair moves to its place in the
+// other buffer; __syncthreads separate the steps, so no pass needs a
+// grid-wide wait.  A bucket larger than BK_CAP (strongly clustered keys)
+// raises a flag on which every tile pass runs in one cooperative launch.
 constexpr int BK_THREADS = 1024;
 constexpr int BK_WARPS = BK_THREADS / 32;
 constexpr int BK_ITEMS = 8;
