@@ -26,8 +26,10 @@
 // owns nodes 1+8s .. 8+8s for its octants; (5) monopoles come from exact
 // fixed-point prefix sums of (m x, m y, m z, m) over the sorted bodies.
 //
-// Work per body: key pass reads 12 B and writes 12 B; 7 sort passes move
-// 12 B each way; the gather reads 16 B (random) and writes 16 B + 32 B of fixed-point sums.
+// Work per body: key pass reads 12 B and writes 12 B; each sort pass moves
+// 12 B each way (one tile pass plus a shared-memory bucket sort up to 2^17
+// bodies, seven tile passes above); the gather reads 16 B (random) and
+// writes 16 B + 32 B of fixed-point sums.
 #include <algorithm>
 
 #include "internal.cuh"

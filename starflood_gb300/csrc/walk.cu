@@ -455,8 +455,9 @@ int launch_body(sfgpu_sim* s, bool stats) {
 }
 
 // ---- group walk (FAST / COMPENSATED, the default) -----------------------------
-// A warp walks the tree for its 32 bodies (consecutive in key order), but the
-// lanes work on up to 32 stack entries (cell, mask of bodies still walking it)
+// A warp walks the tree for its group of bodies (16 by default, consecutive
+// in key order), but the lanes work on up to 32 stack entries (cell, mask of
+// bodies still walking it)
 // at once, so the loads of many cells are in flight together.  Each entry is
 // classified against the bounding box of the group: with margins of 2^-12 on
 // theta, far larger than the FP32 rounding of the reference's ratio, "every
@@ -465,7 +466,8 @@ int launch_body(sfgpu_sim* s, bool stats) {
 // decision; only the remaining "mixed" cells are tested body by body with the
 // reference's arithmetic.  Accepted (cell, mask) pairs go to a list in shared
 // memory that all 32 lanes then run through with dense monopole
-// interactions.  Every body ends up with exactly the cells the reference
+// interactions (one body per lane; with 16- or 8-body groups the sub-warps
+// share the entries).  Every body ends up with exactly the cells the reference
 // gives it (the per-body interaction counts are checked in the tests).
 // Bodies per group of the group walk unless sfgpu_params.walk_group says
 // otherwise.  On the 65,536-body uniform sphere (one GB300): 32 bodies
