@@ -244,6 +244,19 @@ struct SortWork {
     uint32_t flags = 0;            // SORT_NO_BUCKETS: always the tile passes
 };
 constexpr uint32_t SORT_NO_BUCKETS = 1u;
+constexpr uint32_t SORT_PRECLEARED = 2u;  // one-shot: the caller's kernel cleared the words of sf_sort_clear_words
+// The work words the small-array sort path needs cleared before a call,
+// for a kernel the caller launches anyway (empty when n takes the tile
+// passes); sets SORT_PRECLEARED for the next sort call.
+struct SortClear {
+    uint32_t* hist = nullptr;
+    uint32_t nhist = 0;
+    uint32_t* counters = nullptr;
+    uint32_t ncounters = 0;
+    uint32_t* status = nullptr;
+    uint32_t nstatus = 0;
+};
+SortClear sf_sort_clear_words(SortWork& w, uint32_t n, int bits);
 constexpr uint32_t BUCKET_SORT_MAX = 1u << 17;  // sf_sort_pairs* use one pass + per-bucket CTAs up to here
 int sf_sort_alloc(SortWork& w, size_t n);
 void sf_sort_free(SortWork& w);

@@ -253,14 +253,19 @@ __global__ void __launch_bounds__(SORT_THREADS) k_onesweep_all(uint64_t* k0, uin
 // other buffer; __syncthreads separate the steps, so no pass needs a
 // grid-wide wait.  A bucket larger than BK_CAP (strongly clustered keys)
 // raises a flag on which every tile pass runs in one cooperative launch.
-constexpr int BK_THREADS = 1024;
+#ifndef SF_BK_THREADS
+#define SF_BK_THREADS 512  // measured: 512 threads sort 2,000-key buckets slightly faster than 256 or 1024
+#endif
+constexpr int BK_THREADS = SF_BK_THREADS;
 constexpr int BK_WARPS = BK_THREADS / 32;
-constexpr int BK_ITEMS = 8;
-constexpr uint32_t BK_CAP = BK_THREADS * BK_ITEMS;  // 8192 pairs, 12 B each, two buffers
+constexpr int BK_GROUPS = BK_WARPS / 4;  // warp groups of the per-digit prefix
+constexpr uint32_t BK_CAP = 8192;        // pairs per bucket, 12 B each, two buffers
+constexpr int BK_ITEMS = BK_CAP / BK_THREADS;
+static_assert(BK_THREADS >= RADIX && BK_WARPS % 4 == 0 && BK_CAP % BK_THREADS == 0, "bucket sort shape");
 
 struct BucketScratch {
     uint32_t* wcnt;   // [BK_WARPS][RADIX] per-warp counts, then their exclusive prefix
-    uint32_t* gsum;   // [8][RADIX] warp-group totals
+    uint32_t* gsum;   // [BK_GROUPS][RADIX] warp-group totals
     uint32_t* run;    // [RADIX] start of each digit in the destination
     uint32_t* wtot;   // [4] digit-scan warp totals
 };
@@ -298,14 +303,16 @@ __device__ __forceinline__ void bucket_pass(const uint64_t* src_k, const uint32_
         }
     }
     __syncthreads();
-    // per digit: exclusive prefix over the 32 warps (8 groups of 4)
+    // per digit: exclusive prefix over the warps (BK_GROUPS groups of 4;
+    // thread (d, q) owns digit d of group q)
     const int d = threadIdx.x & (RADIX - 1), q = threadIdx.x >> 7;
+    constexpr int WPQ = BK_WARPS / (BK_THREADS / RADIX);  // warps per (d, q) thread
     {
         uint32_t r = 0;
 #pragma unroll
-        for (int j = 0; j < 4; j++) {
-            const uint32_t c = sc.wcnt[(4 * q + j) * RADIX + d];
-            sc.wcnt[(4 * q + j) * RADIX + d] = r;
+        for (int j = 0; j < WPQ; j++) {
+            const uint32_t c = sc.wcnt[(WPQ * q + j) * RADIX + d];
+            sc.wcnt[(WPQ * q + j) * RADIX + d] = r;
             r += c;
         }
         sc.gsum[q * RADIX + d] = r;
@@ -314,13 +321,13 @@ __device__ __forceinline__ void bucket_pass(const uint64_t* src_k, const uint32_
     {
         uint32_t add = 0, tot = 0;
 #pragma unroll
-        for (int j = 0; j < 8; j++) {
+        for (int j = 0; j < BK_THREADS / RADIX; j++) {
             const uint32_t g = sc.gsum[j * RADIX + d];
             add += j < q ? g : 0u;
             tot += g;
         }
 #pragma unroll
-        for (int j = 0; j < 4; j++) sc.wcnt[(4 * q + j) * RADIX + d] += add;
+        for (int j = 0; j < WPQ; j++) sc.wcnt[(WPQ * q + j) * RADIX + d] += add;
         if (q == 0) {  // digit totals -> exclusive digit starts (warps 0-3, one digit per thread)
             uint32_t x = tot;
 #pragma unroll
@@ -359,7 +366,7 @@ __global__ void __launch_bounds__(BK_THREADS, 1) k_bucket_sort(uint64_t* Kb, uin
                                                                int low_passes, uint32_t* big, const uint32_t* enable) {
     if (enable && *enable == 0u) return;
     extern __shared__ __align__(16) unsigned char bk_smem[];
-    __shared__ uint32_t s_wcnt[BK_WARPS * RADIX], s_gsum[8 * RADIX], s_run[RADIX], s_wtot[4];
+    __shared__ uint32_t s_wcnt[BK_WARPS * RADIX], s_gsum[(BK_THREADS / RADIX) * RADIX], s_run[RADIX], s_wtot[4];
     uint64_t* k0 = reinterpret_cast<uint64_t*>(bk_smem);
     uint64_t* k1 = k0 + BK_CAP;
     uint32_t* v0 = reinterpret_cast<uint32_t*>(k1 + BK_CAP);
@@ -459,6 +466,22 @@ void sf_sort_free(SortWork& w) {
     w = SortWork{};
 }
 
+SortClear sf_sort_clear_words(SortWork& w, uint32_t n, int bits) {
+    SortClear c;
+    const int passes = (bits + RADIX_BITS - 1) / RADIX_BITS;
+    if (n <= 1 || n > BUCKET_SORT_MAX || n > w.cap || passes < 2 || passes >= MAX_PASSES ||
+        (w.flags & SORT_NO_BUCKETS))
+        return c;
+    c.hist = w.hist;
+    c.nhist = (uint32_t)passes * RADIX;
+    c.counters = w.counters;
+    c.ncounters = MAX_PASSES + 1;
+    c.status = w.status;
+    c.nstatus = sf_ceil_div(n, SORT_THREADS * 4) * RADIX;
+    w.flags |= SORT_PRECLEARED;
+    return c;
+}
+
 int sf_sort_pairs_keep(uint64_t* keys, uint32_t* vals, uint32_t n, int bits, SortWork& w, cudaStream_t st,
                        uint32_t* d_status, uint64_t** out_keys, uint32_t** out_vals, const uint32_t* enable) {
     *out_keys = keys;
@@ -488,12 +511,13 @@ int sf_sort_pairs_keep(uint64_t* keys, uint32_t* vals, uint32_t n, int bits, Sor
         uint32_t* big = w.counters + MAX_PASSES;
         // pass slot 0: the top digit; slots 1..passes: the gated fallback,
         // which clears its own
-        {
+        if (!(w.flags & SORT_PRECLEARED)) {
             const uint32_t words = passes * RADIX + MAX_PASSES + 1 + tiles * RADIX;
             k_sort_clear<<<std::min<uint32_t>(sf_ceil_div(words, 256), 64u), 256, 0, st>>>(
                 w.hist, passes * RADIX, w.counters, MAX_PASSES + 1, w.status, tiles * RADIX);
             SF_CHECK_LAUNCH();
         }
+        w.flags &= ~SORT_PRECLEARED;
         const uint32_t hb = std::min<uint32_t>(sf_ceil_div(n, 256 * 8), (uint32_t)sf_num_sms() * 4);
         k_hist<<<hb, 256, 0, st>>>(keys, n, passes, w.hist, enable);
         SF_CHECK_LAUNCH();

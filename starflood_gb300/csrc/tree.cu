@@ -90,11 +90,18 @@ __device__ uint64_t descend(const float x[3], Cube c, uint64_t key, int from, ui
     return key;
 }
 
+// Besides the keys: clears the sort's work words (SortClear), which saves
+// the sort a launch.
 __global__ void k_keys(const float* __restrict__ pos, const float* __restrict__ mas, uint32_t n,
                        const float* __restrict__ bounds, uint64_t* __restrict__ keys, uint32_t* __restrict__ vals,
                        uint32_t* __restrict__ nin, uint2* __restrict__ ties, uint32_t* __restrict__ tie_count,
-                       uint32_t* __restrict__ mmax, uint32_t* d_status) {
+                       uint32_t* __restrict__ mmax, uint32_t* d_status, SortClear sc) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    for (uint32_t j = i; j < sc.nhist + sc.ncounters + sc.nstatus; j += gridDim.x * blockDim.x) {
+        if (j < sc.nhist) sc.hist[j] = 0u;
+        else if (j < sc.nhist + sc.ncounters) sc.counters[j - sc.nhist] = 0u;
+        else sc.status[j - sc.nhist - sc.ncounters] = 0u;
+    }
     bool inside = false;
     // largest |mass| (its bits: non-negative floats order as integers), the
     // scale of the monopoles' fixed-point sums
@@ -1033,8 +1040,9 @@ int sf_tree_build(sfgpu_sim* s) {
     SF_CUDA(cudaMemsetAsync(t->counters, 0, sizeof(uint32_t) * (8 + sf_ceil_div(n, SS_TILE)), st));
     const uint32_t nb = sf_ceil_div(n, 256);
     int tk = s->timer.begin(st, "tree_keys");
+    const SortClear sclr = sf_sort_clear_words(t->sort, n, KEY_BITS);
     k_keys<<<nb, 256, 0, st>>>(pos, mas, n, s->d_bounds, t->keys, t->vals, nin, t->ties, tie_count, t->counters + 4,
-                               s->d_status);
+                               s->d_status, sclr);
     SF_CHECK_LAUNCH();
     s->timer.end(st, tk);
     tk = s->timer.begin(st, "tree_sort");
