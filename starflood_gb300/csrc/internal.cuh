@@ -268,8 +268,8 @@ int sf_sort_pairs(uint64_t* keys, uint32_t* vals, uint32_t n, int bits, SortWork
                   cudaStream_t st, uint32_t* d_status, const uint32_t* d_n = nullptr,
                   const uint32_t* enable = nullptr);
 // The same without the final copy: the result is left in (*out_keys,
-// *out_vals), which is (w.keys_b, w.vals_b) for up to BUCKET_SORT_MAX pairs,
-// else (keys, vals) after an even number of passes and (w.keys_b, w.vals_b)
+// *out_vals), which is (keys, vals) for up to BUCKET_SORT_MAX pairs, else
+// (keys, vals) after an even number of passes and (w.keys_b, w.vals_b)
 // after an odd one.
 int sf_sort_pairs_keep(uint64_t* keys, uint32_t* vals, uint32_t n, int bits, SortWork& w, cudaStream_t st,
                        uint32_t* d_status, uint64_t** out_keys, uint32_t** out_vals,

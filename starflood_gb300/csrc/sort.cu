@@ -209,7 +209,7 @@ __global__ void __launch_bounds__(SORT_THREADS) k_onesweep(
 
 // Every pass of the tile sort in one cooperative launch (all tiles resident,
 // a grid barrier between passes), from (k0, v0) ping-ponging with (k1, v1);
-// the result ends in (k0, v0) (copied back when the pass count is odd).
+// the result ends in (k1, v1) (copied there when the pass count is even).
 // Returns at once (the whole grid, before any barrier) unless *enable.
 template <int SORT_ITEMS>
 __global__ void __launch_bounds__(SORT_THREADS) k_onesweep_all(uint64_t* k0, uint32_t* v0, uint64_t* k1,
@@ -237,10 +237,10 @@ __global__ void __launch_bounds__(SORT_THREADS) k_onesweep_all(uint64_t* k0, uin
         va = vb;
         vb = tv;
     }
-    if (ka != k0)
+    if (ka != k1)
         for (uint32_t i = blockIdx.x * SORT_THREADS + threadIdx.x; i < n; i += tiles * SORT_THREADS) {
-            k0[i] = ka[i];
-            v0[i] = va[i];
+            k1[i] = ka[i];
+            v1[i] = va[i];
         }
 }
 
@@ -359,9 +359,10 @@ __device__ __forceinline__ void bucket_pass(const uint64_t* src_k, const uint32_
 
 // A bucket larger than BK_CAP is left alone and raises *big, which enables
 // the full tile passes queued after this kernel.
-// In place: each CTA reads its whole bucket into shared memory before
-// writing it back sorted, and buckets are disjoint.
-__global__ void __launch_bounds__(BK_THREADS, 1) k_bucket_sort(uint64_t* Kb, uint32_t* Vb,
+// Bucket blockIdx.x of (Kb, Vb), sorted on its low digits, into (K, V).
+__global__ void __launch_bounds__(BK_THREADS, 1) k_bucket_sort(const uint64_t* __restrict__ Kb,
+                                                               const uint32_t* __restrict__ Vb,
+                                                               uint64_t* __restrict__ K, uint32_t* __restrict__ V,
                                                                const uint32_t* __restrict__ hist_top,
                                                                int low_passes, uint32_t* big, const uint32_t* enable) {
     if (enable && *enable == 0u) return;
@@ -412,8 +413,8 @@ __global__ void __launch_bounds__(BK_THREADS, 1) k_bucket_sort(uint64_t* Kb, uin
         vb = tv;
     }
     for (uint32_t e = threadIdx.x; e < size; e += BK_THREADS) {
-        Kb[start + e] = ka[e];
-        Vb[start + e] = va[e];
+        K[start + e] = ka[e];
+        V[start + e] = va[e];
     }
 }
 
@@ -498,7 +499,7 @@ int sf_sort_pairs_keep(uint64_t* keys, uint32_t* vals, uint32_t n, int bits, Sor
     }
     // small arrays (where the per-pass tile look-back chains cost more than
     // the data movement): one tile pass on the top digit, then one CTA per
-    // bucket for the rest; the result is left in (w.keys_b, w.vals_b)
+    // bucket for the rest; the result is left in (keys, vals)
     if (n <= BUCKET_SORT_MAX && passes >= 2 && passes < MAX_PASSES && !(w.flags & SORT_NO_BUCKETS)) {
         static bool smem_set = false;
         if (!smem_set) {
@@ -525,8 +526,8 @@ int sf_sort_pairs_keep(uint64_t* keys, uint32_t* vals, uint32_t n, int bits, Sor
         k_onesweep<4><<<tiles, SORT_THREADS, 0, st>>>(keys, vals, w.keys_b, w.vals_b, n, top * RADIX_BITS,
                                                       w.hist + top * RADIX, w.status, w.counters, d_status, enable);
         SF_CHECK_LAUNCH();
-        k_bucket_sort<<<RADIX, BK_THREADS, bucket_sort_smem(), st>>>(w.keys_b, w.vals_b, w.hist + top * RADIX,
-                                                                     top, big, enable);
+        k_bucket_sort<<<RADIX, BK_THREADS, bucket_sort_smem(), st>>>(w.keys_b, w.vals_b, keys, vals,
+                                                                     w.hist + top * RADIX, top, big, enable);
         SF_CHECK_LAUNCH();
         // fallback (only if a bucket overflowed): every pass from the top
         // pass's output, which holds all pairs, in one cooperative launch
@@ -547,9 +548,7 @@ int sf_sort_pairs_keep(uint64_t* keys, uint32_t* vals, uint32_t n, int bits, Sor
                                                 st));
             SF_CHECK_LAUNCH();
         }
-        *out_keys = w.keys_b;  // the result stays in the other buffer
-        *out_vals = w.vals_b;
-        return SFGPU_OK;
+        return SFGPU_OK;  // the result is back in (keys, vals)
     }
     // keys per thread, measured on GB300 (7 passes of 49-bit keys): 4 up to
     // 2^17 keys (0.087 ms at 65,536, against 0.101 with 2 or 8), 8 above

@@ -244,7 +244,8 @@ __global__ void __launch_bounds__(FIX_THREADS) k_tie_fix(const float* __restrict
                                                          const uint32_t* __restrict__ tie_count, uint32_t leaf_cap,
                                                          uint32_t depth_max, uint32_t* __restrict__ moved_out,
                                                          uint32_t* __restrict__ gpos, uint64_t* __restrict__ gkey,
-                                                         uint32_t* __restrict__ gbody) {
+                                                         uint32_t* __restrict__ gbody, uint32_t n,
+                                                         uint64_t* __restrict__ copyK, uint32_t* __restrict__ copyV) {
     __shared__ uint64_t prov[TIE_CAP];
     __shared__ uint64_t cur[TIE_CAP];
     __shared__ uint32_t body[TIE_CAP];
@@ -422,11 +423,19 @@ __global__ void __launch_bounds__(FIX_THREADS) k_tie_fix(const float* __restrict
             if (mask[moved[q]] < mask[t]) r++;
         gpos[r] = mask[t];
     }
+    // when the sort left the provisional order in the tree's own arrays, the
+    // merge needs it as a separate source (rare: only when a body moved)
+    if (M > 0 && copyK)
+        for (uint32_t k = threadIdx.x; k < n; k += FIX_THREADS) {
+            copyK[k] = K[k];
+            copyV[k] = V[k];
+        }
 }
 
 // (K, V) = the sorted provisional (Ks, Vs) with the moved bodies taken out
-// of their old slots and merged back at their new keys; a plain copy when
-// nothing moved.  Replaces a second sort.
+// of their old slots and merged back at their new keys.  When nothing moved:
+// a plain copy, or nothing at all when the provisional order already sits
+// in (K, V) (copy_unmoved = 0).  Replaces a second sort.
 constexpr int MERGE_THREADS = 256;
 
 __global__ void __launch_bounds__(MERGE_THREADS) k_tie_merge(const uint64_t* __restrict__ Ks,
@@ -436,15 +445,16 @@ __global__ void __launch_bounds__(MERGE_THREADS) k_tie_merge(const uint64_t* __r
                                                              const uint32_t* __restrict__ moved,
                                                              const uint32_t* __restrict__ gpos,
                                                              const uint64_t* __restrict__ gkey,
-                                                             const uint32_t* __restrict__ gbody) {
+                                                             const uint32_t* __restrict__ gbody, int copy_unmoved) {
     const uint32_t M = min(*moved, TIE_CAP);
     const uint32_t stride = gridDim.x * MERGE_THREADS;
     const uint32_t g = blockIdx.x * MERGE_THREADS + threadIdx.x;
     if (M == 0) {
-        for (uint32_t k = g; k < n; k += stride) {
-            K[k] = Ks[k];
-            V[k] = Vs[k];
-        }
+        if (copy_unmoved)
+            for (uint32_t k = g; k < n; k += stride) {
+                K[k] = Ks[k];
+                V[k] = Vs[k];
+            }
         return;
     }
     __shared__ uint32_t mpos[TIE_CAP];
@@ -1052,21 +1062,20 @@ int sf_tree_build(sfgpu_sim* s) {
     uint32_t* vs = t->vals;
     if (sf_sort_pairs_keep(t->keys, t->vals, n, KEY_BITS, t->sort, st, s->d_status, &ks, &vs) != SFGPU_OK)
         return SFGPU_FAILURE;
-    if (ks == t->keys) {  // n <= 1: nothing was sorted; merge from a copy
-        SF_CUDA(cudaMemcpyAsync(t->sort.keys_b, t->keys, sizeof(uint64_t) * n, cudaMemcpyDeviceToDevice, st));
-        SF_CUDA(cudaMemcpyAsync(t->sort.vals_b, t->vals, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st));
-        ks = t->sort.keys_b;
-        vs = t->sort.vals_b;
-    }
+    // the sorted provisional order is in the tree's own arrays (small N, and
+    // N <= 1) or in the sort's other buffer (the tile passes)
+    const bool in_place = ks == t->keys;
     s->timer.end(st, tk);
     tk = s->timer.begin(st, "tree_ties");
     k_tie_fix<<<1, FIX_THREADS, 0, st>>>(pos, s->d_bounds, ks, vs, nin, t->ties, tie_count, s->p.leaf_cap,
-                                         s->p.depth_max, resort, t->tie_pos, t->tie_key, t->tie_body);
+                                         s->p.depth_max, resort, t->tie_pos, t->tie_key, t->tie_body, n,
+                                         in_place ? t->sort.keys_b : nullptr, in_place ? t->sort.vals_b : nullptr);
     SF_CHECK_LAUNCH();
     const uint32_t mgb = std::max<uint32_t>(1u, std::min<uint32_t>(sf_ceil_div(n, MERGE_THREADS),
                                                                    (uint32_t)sf_num_sms() * 8u));
-    k_tie_merge<<<mgb, MERGE_THREADS, 0, st>>>(ks, vs, t->keys, t->vals, n, nin, resort, t->tie_pos, t->tie_key,
-                                                t->tie_body);
+    k_tie_merge<<<mgb, MERGE_THREADS, 0, st>>>(in_place ? t->sort.keys_b : ks, in_place ? t->sort.vals_b : vs,
+                                                t->keys, t->vals, n, nin, resort, t->tie_pos, t->tie_key,
+                                                t->tie_body, in_place ? 0 : 1);
     SF_CHECK_LAUNCH();
     s->timer.end(st, tk);
     const bool exact = s->p.math == SFGPU_MATH_EXACT && s->p.form == SFGPU_FORM_PLAIN;
