@@ -481,19 +481,19 @@ constexpr int GW_MIN_BLOCKS = 7;  // resident blocks per SM the register budget 
 constexpr int GW_SLOW = 48;   // accepted cells that may contain a body (self-exclusion test)
 
 // Per-warp lists in shared memory.  The fast list holds the monopole itself
-// (centre of mass and mass, as separate arrays so that two consecutive
-// entries are one 64-bit load) and the mask of the bodies taking it; the
-// slow list holds node ids for the few accepted cells whose closed bounds
-// meet the group's box, where the reference's self-exclusion test must run.
+// (centre of mass and mass) and the mask of the bodies taking it, entries
+// stored in pairs so that one 128-bit load brings (x0, x1, y0, y1) and
+// another (z0, z1, m0, m1) of two consecutive entries; the slow list holds
+// node ids for the few accepted cells whose closed bounds meet the group's
+// box, where the reference's self-exclusion test must run.
 struct GroupLists {
-    float* x;
-    float* y;
-    float* z;
-    float* m;
+    float* xy;  // entry e: x at 4 (e/2) + e%2, y at 4 (e/2) + 2 + e%2
+    float* zm;  // entry e: z at 4 (e/2) + e%2, m at 4 (e/2) + 2 + e%2
     uint32_t* msk;
     uint32_t* qn;
     uint32_t* qm;
 };
+__device__ __forceinline__ int lx_of(int e) { return 4 * (e >> 1) + (e & 1); }
 
 // Fast list: every lane runs every entry, its mask bit selecting the result,
 // so the inner loop has no per-lane branch.  FAST kind evaluates two entries
@@ -513,10 +513,11 @@ __device__ __forceinline__ void flush_fast(const GroupLists& L, int count, int l
         for (int e = half; e < count; e += H) {
             const uint32_t M = L.msk[e];
             if ((M >> lane) & 1u) {
-                const float dx = L.x[e] - rx, dy = L.y[e] - ry, dz = L.z[e] - rz;
+                const int ix = lx_of(e);
+                const float dx = L.xy[ix] - rx, dy = L.xy[ix + 2] - ry, dz = L.zm[ix] - rz;
                 const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
                 const float inv = rsqrtf(r2);
-                const float mphi = L.m[e] * inv;
+                const float mphi = L.zm[ix + 2] * inv;
                 const float f = mphi * (inv * inv);
                 ax.add(f * dx);
                 ay.add(f * dy);
@@ -531,10 +532,10 @@ __device__ __forceinline__ void flush_fast(const GroupLists& L, int count, int l
     const float2 e2 = make_float2(eps2, eps2);
 #pragma unroll 2
     for (int e = 2 * half; e < count; e += 2 * H) {  // count is a multiple of 2H (padded by the caller)
-        const float2 X = *reinterpret_cast<const float2*>(&L.x[e]);
-        const float2 Y = *reinterpret_cast<const float2*>(&L.y[e]);
-        const float2 Z = *reinterpret_cast<const float2*>(&L.z[e]);
-        const float2 M2 = *reinterpret_cast<const float2*>(&L.m[e]);
+        const float4 A = reinterpret_cast<const float4*>(L.xy)[e >> 1];
+        const float4 B = reinterpret_cast<const float4*>(L.zm)[e >> 1];
+        const float2 X = make_float2(A.x, A.y), Y = make_float2(A.z, A.w);
+        const float2 Z = make_float2(B.x, B.y), M2 = make_float2(B.z, B.w);
         const uint2 MK = *reinterpret_cast<const uint2*>(&L.msk[e]);
         const bool t0 = (MK.x >> lane) & 1u, t1 = (MK.y >> lane) & 1u;
         // a body not taking an entry sees it massless: its terms are +0
@@ -592,10 +593,11 @@ __device__ __forceinline__ void append_cells(const GroupLists& L, uint32_t am, u
         L.qm[q] = am;
     } else if (am) {
         const int q = count + __popc(fb & lt);
-        L.x[q] = C.x;
-        L.y[q] = C.y;
-        L.z[q] = C.z;
-        L.m[q] = C.w;
+        const int ix = lx_of(q);
+        L.xy[ix] = C.x;
+        L.xy[ix + 2] = C.y;
+        L.zm[ix] = C.z;
+        L.zm[ix + 2] = C.w;
         L.msk[q] = am;
     }
     count += __popc(fb);
@@ -718,10 +720,8 @@ __global__ void __launch_bounds__(GW_THREADS, GW_MIN_BLOCKS) k_walk_group(const 
                                                            WalkKick wk) {
     __shared__ uint32_t s_node[GW_WARPS][GW_STACK];
     __shared__ uint32_t s_mask[GW_WARPS][GW_STACK];
-    __shared__ __align__(16) float l_x[GW_WARPS][GW_LIST];
-    __shared__ __align__(16) float l_y[GW_WARPS][GW_LIST];
-    __shared__ __align__(16) float l_z[GW_WARPS][GW_LIST];
-    __shared__ __align__(16) float l_m[GW_WARPS][GW_LIST];
+    __shared__ __align__(16) float l_xy[GW_WARPS][2 * GW_LIST];
+    __shared__ __align__(16) float l_zm[GW_WARPS][2 * GW_LIST];
     __shared__ __align__(16) uint32_t l_k[GW_WARPS][GW_LIST];
     __shared__ uint32_t q_node[GW_WARPS][GW_SLOW];
     __shared__ uint32_t q_mask[GW_WARPS][GW_SLOW];
@@ -737,7 +737,7 @@ __global__ void __launch_bounds__(GW_THREADS, GW_MIN_BLOCKS) k_walk_group(const 
     float4* sbd = s_body[w];
     uint32_t* stn = s_node[w];
     uint32_t* stm = s_mask[w];
-    const GroupLists L{l_x[w], l_y[w], l_z[w], l_m[w], l_k[w], q_node[w], q_mask[w]};
+    const GroupLists L{l_xy[w], l_zm[w], l_k[w], q_node[w], q_mask[w]};
     static_assert(GB == 32 || ((GB == 16 || GB == 8) && GSPLIT == 1), "8- and 16-body groups walk unsplit");
     const uint32_t gw = blockIdx.x * GW_WARPS + w;
     const uint32_t group = gw / GSPLIT;
@@ -777,8 +777,8 @@ __global__ void __launch_bounds__(GW_THREADS, GW_MIN_BLOCKS) k_walk_group(const 
             constexpr int PAD = KIND == WALK_COMP ? 1 : 2 * (32 / GB);
             const int padded = (count + PAD - 1) / PAD * PAD;
             if (lane < padded - count) {
-                L.x[count + lane] = L.y[count + lane] = L.z[count + lane] = 0.f;
-                L.m[count + lane] = 0.f;
+                const int ix = lx_of(count + lane);
+                L.xy[ix] = L.xy[ix + 2] = L.zm[ix] = L.zm[ix + 2] = 0.f;
                 L.msk[count + lane] = 0u;
             }
             count = padded;
