@@ -210,6 +210,8 @@ extern "C" int sfgpu_destroy(sfgpu_sim* s) {
     cudaFreeHost(s->h_status);
     if (s->ev_fork) cudaEventDestroy(s->ev_fork);
     if (s->ev_join) cudaEventDestroy(s->ev_join);
+    if (s->ev_pos) cudaEventDestroy(s->ev_pos);
+    if (s->ev_pos_done) cudaEventDestroy(s->ev_pos_done);
     if (s->aux) cudaStreamDestroy(s->aux);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
@@ -250,6 +252,8 @@ extern "C" int sfgpu_create(sfgpu_sim** out, uint32_t n, const sfgpu_params* p) 
     TRY(cudaStreamCreateWithFlags(&s->aux, cudaStreamNonBlocking));
     TRY(cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming));
     TRY(cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming));
+    TRY(cudaEventCreateWithFlags(&s->ev_pos, cudaEventDisableTiming));
+    TRY(cudaEventCreateWithFlags(&s->ev_pos_done, cudaEventDisableTiming));
     const size_t slab_bytes = sizeof(float) * (size_t)n * s->dof;
     TRY(cudaMalloc(&s->slab, slab_bytes));
     TRY(cudaMemsetAsync(s->slab, 0, slab_bytes, s->stream));  // simulation.c:118
@@ -384,6 +388,15 @@ static int step_body(sfgpu_sim* s) {
     int tk = s->timer.begin(s->stream, "kick_drift");
     if (sf_stage_kick_drift(s, tree) != SFGPU_OK) return SFGPU_FAILURE;
     s->timer.end(s->stream, tk);
+    if (s->host_pos_out) {
+        // the positions are final after the drift: their download runs on
+        // the second stream beside the force solve
+        SF_CUDA(cudaEventRecord(s->ev_pos, s->stream));
+        SF_CUDA(cudaStreamWaitEvent(s->aux, s->ev_pos, 0));
+        SF_CUDA(cudaMemcpyAsync(s->host_pos_out, s->slab, sizeof(float) * 3 * (size_t)s->n,
+                                cudaMemcpyDeviceToHost, s->aux));
+        SF_CUDA(cudaEventRecord(s->ev_pos_done, s->aux));
+    }
     // without SPH the walk's epilogue may apply kick_1 and the energies
     // itself (sets kicked); SPH forces come after the walk, so not then
     s->fuse_kick = tree && s->p.sph == SFGPU_SPH_OFF;
@@ -564,12 +577,19 @@ extern "C" int sfgpu_synchronize(sfgpu_sim* s) {
 }
 
 __global__ static void k_set_step_host(uint32_t* d_step, const volatile uint32_t* h_step) { *d_step = *h_step; }
+// the status word to page-locked memory, cleared for the next call
+__global__ static void k_status_host(uint32_t* d_status, volatile uint32_t* h_status) {
+    *h_status = *d_status;
+    *d_status = 0u;
+}
 
 // Everything of one drop-in call, queued on the simulation's stream: the
 // arrays a solve or a step reads (pos, vel, acc, mas, 0..9, and with SPH the
 // smoothing lengths, 13) in, the step number from page-locked memory, the
 // solve or the step, the whole slab and the status word out.
-static int host_step_body(sfgpu_sim* s, float* slab, int solve_only) {
+// early_pos: the slab is page-locked and the body is being captured, so the
+// positions may be downloaded on the second stream while the forces run
+static int host_step_body(sfgpu_sim* s, float* slab, int solve_only, bool early_pos) {
     const size_t n = s->n;
     SF_CUDA(cudaMemcpyAsync(s->slab, slab, sizeof(float) * 10 * n, cudaMemcpyHostToDevice, s->stream));
     if (s->dof > 13)
@@ -578,10 +598,20 @@ static int host_step_body(sfgpu_sim* s, float* slab, int solve_only) {
     k_set_step_host<<<1, 1, 0, s->stream>>>(s->d_step, s->h_step_in);
     SF_CHECK_LAUNCH();
     if (refresh_fp64(s) != SFGPU_OK) return SFGPU_FAILURE;
-    if ((solve_only ? solve_body(s, false) : step_body(s)) != SFGPU_OK) return SFGPU_FAILURE;
-    SF_CUDA(cudaMemcpyAsync(slab, s->slab, sizeof(float) * s->dof * n, cudaMemcpyDeviceToHost, s->stream));
-    SF_CUDA(cudaMemcpyAsync(s->h_status, s->d_status, sizeof(uint32_t), cudaMemcpyDeviceToHost, s->stream));
-    SF_CUDA(cudaMemsetAsync(s->d_status, 0, sizeof(uint32_t), s->stream));
+    const bool split = early_pos && !solve_only;
+    s->host_pos_out = split ? slab : nullptr;
+    const int rc = solve_only ? solve_body(s, false) : step_body(s);
+    s->host_pos_out = nullptr;
+    if (rc != SFGPU_OK) return SFGPU_FAILURE;
+    if (split) {
+        SF_CUDA(cudaStreamWaitEvent(s->stream, s->ev_pos_done, 0));
+        SF_CUDA(cudaMemcpyAsync(slab + 3 * n, s->slab + 3 * n, sizeof(float) * (s->dof - 3) * n,
+                                cudaMemcpyDeviceToHost, s->stream));
+    } else {
+        SF_CUDA(cudaMemcpyAsync(slab, s->slab, sizeof(float) * s->dof * n, cudaMemcpyDeviceToHost, s->stream));
+    }
+    k_status_host<<<1, 1, 0, s->stream>>>(s->d_status, s->h_status);
+    SF_CHECK_LAUNCH();
     return SFGPU_OK;
 }
 
@@ -607,7 +637,7 @@ extern "C" int sfgpu_host_step(sfgpu_sim* s, float* slab, uint32_t step_number, 
         if (pinned) {
             cudaGraph_t g = nullptr;
             SF_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
-            const int rc = host_step_body(s, slab, solve_only);
+            const int rc = host_step_body(s, slab, solve_only, true);
             const cudaError_t ce = cudaStreamEndCapture(s->stream, &g);
             if (rc == SFGPU_OK && ce == cudaSuccess && cudaGraphInstantiate(&s->host_graph, g, 0) == cudaSuccess) {
                 s->host_graph_slab = slab;
@@ -624,7 +654,7 @@ extern "C" int sfgpu_host_step(sfgpu_sim* s, float* slab, uint32_t step_number, 
     }
     if (use_graph) {
         SF_CUDA(cudaGraphLaunch(s->host_graph, s->stream));
-    } else if (host_step_body(s, slab, solve_only) != SFGPU_OK) {
+    } else if (host_step_body(s, slab, solve_only, false) != SFGPU_OK) {
         return SFGPU_FAILURE;
     }
     SF_CUDA(cudaStreamSynchronize(s->stream));

@@ -289,6 +289,8 @@ struct sfgpu_sim {
     cudaStream_t stream = nullptr;
     cudaStream_t aux = nullptr;        // a second stream for independent stages of a step
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaEvent_t ev_pos = nullptr, ev_pos_done = nullptr;  // early position copy of the host-step graph
+    float* host_pos_out = nullptr;  // set while a step is captured for sfgpu_host_step
     float* slab = nullptr;         // N*dof, reference layout
     double* pos64 = nullptr;       // COMPENSATED: FP64 positions (3N)
     double* vel64 = nullptr;       // COMPENSATED: FP64 velocities (3N)
