@@ -111,3 +111,17 @@ def test_fails_loudly_without_gpu(built_lib):
         pytest.skip("a GPU is present")
     with pytest.raises(sf.SfgpuError):
         sf.Sim(16, sf.default_params(solver=sf.SOLVER_PP))
+
+
+def test_rejects_empty_and_bad_parameters_before_the_device(built_lib):
+    """N = 0 and out-of-range parameters fail in the host checks, with the
+    library's message, before any CUDA call (so also on a machine without a
+    GPU).  The reference's sim_init accepts N = 0 (malloc(0)) and its loops
+    then do nothing; here an empty simulation is an error."""
+    import starflood_gb300 as sf
+    with pytest.raises(sf.SfgpuError, match="N must be > 0"):
+        sf.Sim(0, sf.default_params(solver=sf.SOLVER_PP))
+    with pytest.raises(sf.SfgpuError, match="eps must be > 0"):
+        sf.Sim(16, sf.default_params(solver=sf.SOLVER_PP, eps=0.0))
+    with pytest.raises(sf.SfgpuError, match="leaf_cap must be in"):
+        sf.Sim(16, sf.default_params(solver=sf.SOLVER_TREE, leaf_cap=0))
