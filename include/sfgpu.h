@@ -146,6 +146,12 @@ int sfgpu_energies(sfgpu_sim* s, double* T, double* V);
 /* Energy with the double counting and self terms removed:
  * E = T + V/2 - (1/2) sum_i G m_i^2 / eps  (REFERENCE acc) . Synchronises. */
 int sfgpu_energies_corrected(sfgpu_sim* s, double* T, double* V, double* E);
+/* Momentum diagnostics of the current state (no reference counterpart):
+ * P = sum_i m_i v_i and L = sum_i m_i (x_i cross v_i), per body in FP64
+ * (from the FP64 state in the precision form), summed in a fixed order.
+ * Either pointer may be NULL.  Queued after the work on the simulation's
+ * stream; synchronises. */
+int sfgpu_momentum(sfgpu_sim* s, double P[3], double L[3]);
 /* Device status word (SFGPU_STATUS_* bits) accumulated since the last call;
  * reading it clears it.  Synchronises. */
 int sfgpu_status(sfgpu_sim* s, uint32_t* status);

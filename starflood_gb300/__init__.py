@@ -70,6 +70,7 @@ def lib():
             "sfgpu_energies": (i32, [vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
             "sfgpu_energies_corrected": (i32, [vp, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                                C.POINTER(C.c_double)]),
+            "sfgpu_momentum": (i32, [vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
             "sfgpu_status": (i32, [vp, u32p]),
             "sfgpu_stream": (vp, [vp]),
             "sfgpu_device_slab": (vp, [vp]),
@@ -236,6 +237,12 @@ class Sim:
         T, V, E = C.c_double(), C.c_double(), C.c_double()
         check(lib().sfgpu_energies_corrected(self.h, C.byref(T), C.byref(V), C.byref(E)), "energies")
         return T.value, V.value, E.value
+
+    def momentum(self):
+        """(P, L): total linear and angular momentum of the current state, FP64."""
+        P, L = (C.c_double * 3)(), (C.c_double * 3)()
+        check(lib().sfgpu_momentum(self.h, P, L), "sfgpu_momentum")
+        return np.array(P[:]), np.array(L[:])
 
     def status(self) -> int:
         s = C.c_uint32()

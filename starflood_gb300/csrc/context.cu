@@ -685,6 +685,22 @@ extern "C" int sfgpu_energies_corrected(sfgpu_sim* s, double* T, double* V, doub
     return SFGPU_OK;
 }
 
+extern "C" int sfgpu_momentum(sfgpu_sim* s, double P[3], double L[3]) {
+    sf_clear_error();
+    if (!s) {
+        sf_set_error("sim is NULL");
+        return SFGPU_FAILURE;
+    }
+    if (sf_stage_momentum(s) != SFGPU_OK) return SFGPU_FAILURE;
+    SF_CUDA(cudaMemcpyAsync(s->h_sums + 8, s->sums + 8, sizeof(double) * 6, cudaMemcpyDeviceToHost, s->stream));
+    SF_CUDA(cudaStreamSynchronize(s->stream));
+    for (int c = 0; c < 3; c++) {
+        if (P) P[c] = s->h_sums[8 + c];
+        if (L) L[c] = s->h_sums[11 + c];
+    }
+    return SFGPU_OK;
+}
+
 extern "C" int sfgpu_status(sfgpu_sim* s, uint32_t* status) {
     sf_clear_error();
     if (!s) return SFGPU_FAILURE;

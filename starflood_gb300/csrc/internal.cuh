@@ -342,6 +342,7 @@ int sf_stage_sph(sfgpu_sim* s);
 int sf_stage_kick_drift(sfgpu_sim* s, bool want_radius);
 int sf_stage_radius(sfgpu_sim* s);
 int sf_stage_kick_energy(sfgpu_sim* s);
+int sf_stage_momentum(sfgpu_sim* s);
 int sf_sph_alloc(sfgpu_sim* s);
 void sf_sph_free(sfgpu_sim* s);
 

@@ -223,6 +223,42 @@ __global__ void __launch_bounds__(SF_RED_BLOCK) k_kick_energy(float* __restrict_
     }
 }
 
+// Momentum diagnostics of the current state: P = sum m v and
+// L = sum m (x cross v), per body in FP64 (from the FP64 state in the
+// precision form), summed in float-float within warps and FP64 across
+// warps and blocks in a fixed order (last-block pattern), into out[0..5].
+__global__ void __launch_bounds__(SF_RED_BLOCK) k_momentum(const float* __restrict__ slab, uint32_t n,
+                                                           const double* __restrict__ pos64,
+                                                           const double* __restrict__ vel64,
+                                                           double* __restrict__ part, uint32_t* done,
+                                                           double* __restrict__ out) {
+    const uint32_t i = blockIdx.x * SF_RED_BLOCK + threadIdx.x;
+    ff r[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) r[k] = ff{0.0f, 0.0f};
+    if (i < n) {
+        double x[3], v[3];
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            const size_t q = 3u * (size_t)i + c;
+            x[c] = pos64 ? pos64[q] : (double)slab[q];
+            v[c] = vel64 ? vel64[q] : (double)slab[(size_t)3 * n + q];
+        }
+        const double m = (double)slab[(size_t)9 * n + i];
+#pragma unroll
+        for (int c = 0; c < 3; c++) r[c] = ff_from_double(m * v[c]);
+        r[3] = ff_from_double(m * (x[1] * v[2] - x[2] * v[1]));
+        r[4] = ff_from_double(m * (x[2] * v[0] - x[0] * v[2]));
+        r[5] = ff_from_double(m * (x[0] * v[1] - x[1] * v[0]));
+    }
+    block_sum<6>(r, part);
+    if (!last_block(done)) return;
+    __shared__ double tot[6];
+    sum_partials<6>(part, gridDim.x, tot);
+    __syncthreads();
+    if (threadIdx.x < 6) out[threadIdx.x] = tot[threadIdx.x];
+}
+
 }  // namespace
 
 static int ensure_red(sfgpu_sim* s, uint32_t entries) {
@@ -261,6 +297,16 @@ int sf_stage_kick_energy(sfgpu_sim* s) {
     k_kick_energy<<<nb, SF_RED_BLOCK, 0, s->stream>>>(s->slab, s->n, 0.5f * dt, s->vel64, s->p.dt, g_over_eps,
                                                       s->p.acc_mode == SFGPU_ACC_PHYSICAL, (double*)s->red, s->d_done + 1,
                                                       s->sums, s->d_step, s->u, s->dudt);
+    SF_CHECK_LAUNCH();
+    return SFGPU_OK;
+}
+
+// sums[8..10] = P, sums[11..13] = L; ticket d_done[2]
+int sf_stage_momentum(sfgpu_sim* s) {
+    const uint32_t nb = sf_ceil_div(s->n, SF_RED_BLOCK);
+    if (ensure_red(s, nb * 6) != SFGPU_OK) return SFGPU_FAILURE;
+    k_momentum<<<nb, SF_RED_BLOCK, 0, s->stream>>>(s->slab, s->n, s->pos64, s->vel64, (double*)s->red,
+                                                   s->d_done + 2, s->sums + 8);
     SF_CHECK_LAUNCH();
     return SFGPU_OK;
 }

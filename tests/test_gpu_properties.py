@@ -75,3 +75,30 @@ def test_bh_full_size_steps_keep_bodies(sf):
     assert np.array_equal(v["mas"], mas)
     for k in ("pos", "vel", "acc", "pot", "ken", "pen"):
         assert np.all(np.isfinite(v[k])), k
+
+
+@pytest.mark.parametrize("form", ["plain", "compensated"])
+def test_momentum_diagnostics_vs_fp64_and_conserved_by_pp(sf, form):
+    """sfgpu_momentum against numpy FP64 sums of the same state, then
+    conserved over 20 PP steps (pairwise antisymmetric forces)."""
+    from starflood_gb300.ics import plummer
+    n = 16384
+    pos, vel, mas = plummer(n, seed=11)
+    m = mas.astype(np.float64)[:, None]
+    x, v = pos.astype(np.float64), vel.astype(np.float64)
+    P_ref = (m * v).sum(axis=0)
+    L_ref = (m * np.cross(x, v)).sum(axis=0)
+    scale_p = float((np.abs(m * v)).sum())
+    scale_l = float((np.abs(m * np.cross(x, v))).sum())
+    f = sf.FORM_PLAIN if form == "plain" else sf.FORM_COMPENSATED
+    p = sf.default_params(solver=sf.SOLVER_PP, eps=0.01, dt=1e-3, form=f)
+    with sf.Sim(n, p) as s:
+        s.set_state(pos, vel, mas)
+        P0, L0 = s.momentum()
+        assert np.abs(P0 - P_ref).max() <= 1e-12 * scale_p, (P0, P_ref)
+        assert np.abs(L0 - L_ref).max() <= 1e-12 * scale_l, (L0, L_ref)
+        s.solve(0)
+        s.run(0, 20)
+        P1, L1 = s.momentum()
+    assert np.abs(P1 - P0).max() <= 1e-6 * scale_p, (P0, P1)
+    assert np.abs(L1 - L0).max() <= 1e-5 * scale_l, (L0, L1)
