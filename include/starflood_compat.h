@@ -71,6 +71,9 @@ int sfgpu_compat_configure(const sfgpu_params* p);
 void sfgpu_compat_params(sfgpu_params* out);
 /* The device simulation behind a sim_t (NULL if none). */
 sfgpu_sim* sfgpu_compat_handle(const sim_t* sim);
+/* Copy the device state behind sim (ahead of sim->mem after resident calls
+ * such as sfgpu_run on sfgpu_compat_handle(sim)) into sim->mem; 0 or -1. */
+int sfgpu_sync_host(sim_t* sim);
 
 /* src/simulation.c:33-53 */
 real* sim_find(const sim_t* sim, enum sim_conf parameter);

@@ -497,6 +497,10 @@ def compat_functions():
         fn.argtypes = args
     L.sim_find.restype = C.c_void_p
     L.sim_find.argtypes = [S, C.c_int]
+    L.sfgpu_sync_host.restype = C.c_int
+    L.sfgpu_sync_host.argtypes = [S]
+    L.sfgpu_compat_handle.restype = C.c_void_p
+    L.sfgpu_compat_handle.argtypes = [S]
     return L
 
 

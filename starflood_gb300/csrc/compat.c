@@ -94,7 +94,24 @@ static sfgpu_sim* take_slot(const void* key) {
     return r;
 }
 
+static void fail_msg(const char* fn);
 sfgpu_sim* sfgpu_compat_handle(const sim_t* sim) { return sim ? find_slot(sim->mem, NULL) : NULL; }
+
+/* Resident work queued on the handle (sfgpu_run, sfgpu_step) leaves the
+ * device state ahead of sim->mem; this copies it back (one synchronisation).
+ * 0, or -1 with a message on stderr as the reference's calls do. */
+int sfgpu_sync_host(sim_t* sim) {
+    sfgpu_sim* s = sfgpu_compat_handle(sim);
+    if (!s) {
+        fprintf(stderr, "sfgpu_sync_host() error: no device simulation behind this sim_t\n");
+        return SFGPU_FAILURE;
+    }
+    if (sfgpu_download(s, (float*)sim->mem) != SFGPU_OK) {
+        fail_msg("sfgpu_sync_host()");
+        return SFGPU_FAILURE;
+    }
+    return SFGPU_OK;
+}
 
 static uint32_t dof_now(void) {
     sfgpu_params p;

@@ -160,3 +160,34 @@ def test_host_step_graph_matches_eager(sf):
             for slab in slabs:
                 L.sfgpu_host_unregister(slab.ctypes.data)
     np.testing.assert_array_equal(outs[0], outs[1])
+
+
+def test_sync_host_after_resident_steps(sf):
+    """Steps queued on the handle behind a sim_t (sfgpu_run, one graph per
+    step, no host copies) and then sfgpu_sync_host give the same slab as the
+    same steps made by drop-in sim_step calls."""
+    d = golden("tree_uniform_n4096_theta0.5_3steps.npz")
+    L = sf.compat_functions()
+    sf.compat_configure(sf.default_params(solver=sf.SOLVER_TREE, eps=0.01, dt=1e-3, theta=0.5,
+                                          math=sf.MATH_EXACT))
+    slabs = []
+    for resident in (False, True):
+        sim = sf.SimT()
+        assert L.sim_init(C.byref(sim), len(d["pos"])) == 0
+        slab = _fill(L, sf, sim, d, 13)
+        assert L.sim_solv(C.byref(sim)) == 0
+        steps = int(d["steps"])
+        if resident:
+            h = L.sfgpu_compat_handle(C.byref(sim))
+            assert h
+            sf.check(sf.lib().sfgpu_run(h, 0, steps), "sfgpu_run")
+            assert L.sfgpu_sync_host(C.byref(sim)) == 0
+        else:
+            for k in range(steps):
+                sim.step_number = k
+                assert L.sim_step(C.byref(sim)) == 0
+        slabs.append(slab.copy())
+        L.sim_free(C.byref(sim))
+        L.tree_free(C.byref(sim.tree))
+    np.testing.assert_array_equal(slabs[1], slabs[0])
+    np.testing.assert_array_equal(slabs[0], d["final_slab"])
