@@ -55,51 +55,59 @@ def env_rank():
             int(os.environ.get("LOCAL_RANK", "0")))
 
 
-class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+def nvml_index(local):
+    """NVML numbers every GPU of the machine: the first CUDA_VISIBLE_DEVICES
+    entry when it is an index, else the local rank."""
+    first = os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0].strip()
+    return int(first) if first.isdigit() else local
+
+
+class NvmlClocks:
+    """SM clock, maximum clock, power and throttle reasons read through NVML
+    (libnvidia-ml, ctypes: read-only queries), sampled by the caller inside
+    the timed loop (once per step); nvidia-smi polling as the fallback."""
+    # nvmlClocksEventReasons bits
+    REASONS = {0x8: "hw_slowdown", 0x40: "hw_thermal_slowdown", 0x20: "sw_thermal_slowdown",
+               0x4: "sw_power_cap"}
 
     def __init__(self, index: int):
-        self.index = index
+        import ctypes as C
         self.samples = []
-        self.proc = None
-
-    def __enter__(self):
+        self.h = None
         try:
-            self.proc = subprocess.Popen(
-                ["nvidia-smi", "-i", str(self.index), "--query-gpu=clocks.sm,clocks.max.sm,power.draw,"
-                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
-                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.thread = threading.Thread(target=self._read, daemon=True)
-            self.thread.start()
-        except Exception:
-            self.proc = None
-        return self
+            self.nv = C.CDLL("libnvidia-ml.so.1")
+            if self.nv.nvmlInit_v2() != 0:
+                raise OSError("nvmlInit")
+            h = C.c_void_p()
+            if self.nv.nvmlDeviceGetHandleByIndex_v2(index, C.byref(h)) != 0 and \
+                    self.nv.nvmlDeviceGetHandleByIndex_v2(0, C.byref(h)) != 0:
+                raise OSError("handle")
+            self.h = h
+            mx = C.c_uint()
+            self.max_mhz = float(mx.value) if self.nv.nvmlDeviceGetMaxClockInfo(h, 1, C.byref(mx)) == 0 else None
+        except OSError:
+            self.h = None
 
-    def _read(self):
-        for line in self.proc.stdout:
-            parts = [x.strip() for x in line.split(",")]
-            if len(parts) >= 7:
-                self.samples.append(parts)
-
-    def __exit__(self, *a):
-        if self.proc:
-            self.proc.terminate()
-            try:
-                self.proc.wait(timeout=5)
-            except Exception:
-                self.proc.kill()
+    def sample(self):
+        if self.h is None:
+            return
+        import ctypes as C
+        clk, pw, rs = C.c_uint(), C.c_uint(), C.c_ulonglong()
+        if self.nv.nvmlDeviceGetClockInfo(self.h, 1, C.byref(clk)) != 0:
+            return
+        self.nv.nvmlDeviceGetPowerUsage(self.h, C.byref(pw))
+        fn = getattr(self.nv, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            self.nv.nvmlDeviceGetCurrentClocksThrottleReasons
+        fn(self.h, C.byref(rs))
+        self.samples.append((float(clk.value), pw.value / 1000.0, int(rs.value)))
 
     def summary(self):
         if not self.samples:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
-        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
-        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[k] for s in self.samples for k in range(4) if s[3 + k].lower() == "active"})
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.samples)}
+        reasons = sorted({name for _, _, r in self.samples for bit, name in self.REASONS.items() if r & bit})
+        return {"sm_mhz": statistics.median(s[0] for s in self.samples), "sm_max_mhz": self.max_mhz,
+                "power_w_max": max(s[1] for s in self.samples), "reasons": reasons,
+                "samples": len(self.samples), "source": "NVML, one sample per timed step"}
 
 
 def fp32_peak_tflops():
@@ -208,20 +216,21 @@ def gpu_bh(steps, warmup, sf):
     s.sync()
     events = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
     rank, world, local = env_rank()
-    with ClockSampler(local) as clk:
-        if world > 1:
-            import torch.distributed as dist
-            dist.barrier()
-        torch.cuda.synchronize()
-        for k in range(steps):
-            sf.check(L.sfgpu_flush_l2(C.c_void_p(stream)), "flush")
-            with torch.cuda.stream(ext):
-                events[k][0].record(ext)
-            s.run(warmup + 1 + k, 1)
-            with torch.cuda.stream(ext):
-                events[k][1].record(ext)
-        s.sync()
-        torch.cuda.synchronize()
+    clk = NvmlClocks(nvml_index(local))
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    for k in range(steps):
+        sf.check(L.sfgpu_flush_l2(C.c_void_p(stream)), "flush")
+        with torch.cuda.stream(ext):
+            events[k][0].record(ext)
+        s.run(warmup + 1 + k, 1)
+        with torch.cuda.stream(ext):
+            events[k][1].record(ext)
+        clk.sample()  # host-side query while the GPU works through the queued steps
+    s.sync()
+    torch.cuda.synchronize()
     step_ms = [a.elapsed_time(b) for a, b in events]
     total_ms = float(sum(step_ms))
     status = s.status()
@@ -259,6 +268,104 @@ def gpu_bh(steps, warmup, sf):
                 per_step=per_step, clocks=clk.summary(), e2e=e2e)
 
 
+def bh_per_particle_err(sf, oracle_threads_ok=True):
+    """Per-particle relative L2 error |a_i - a_ref,i| / |a_ref,i| of one FAST
+    solve of the headline's initial state against the FP32 restatement of the
+    reference's tree build and walk (bit-identical to the compiled reference),
+    all 65,536 bodies: median, p99, max."""
+    from oracle import build as ob
+    ob.build_oracle()
+    from oracle.pyoracle import Oracle, make_params
+    pos, vel, mas = bh_inputs()
+    n = N_BH
+    orc = Oracle("f32")
+    op = make_params(eps=0.01, theta=0.5, use_tree=1)
+    st, nodes = orc.tree_build(pos, mas, orc.root_bounds(pos, 0), op)
+    a_ref, p_ref, _, mag = orc.walk(pos, mas, nodes, op, with_mag=True)
+    p = sf.default_params(solver=sf.SOLVER_TREE, eps=0.01, dt=1e-3, theta=0.5, **BH_EXTRA)
+    with sf.Sim(n, p) as s:
+        s.set_state(pos, vel, mas)
+        s.solve(0)
+        v = sf.slab_views(s.download(), n, 13)
+    a = v["acc"].astype(np.float64)
+    r = a_ref.astype(np.float64)
+    e = np.linalg.norm(a - r, axis=1) / np.linalg.norm(r, axis=1)
+    em = np.linalg.norm(a - r, axis=1) / mag.astype(np.float64)
+    return {"median": float(np.median(e)), "p99": float(np.quantile(e, 0.99)), "max": float(e.max()),
+            "max_over_term_magnitudes": float(em.max()),
+            "global_l2": float(np.linalg.norm(a - r) / np.linalg.norm(r)),
+            "against": "FP32 restatement of tree.c + gravity.c (bit-identical to the reference), N=65536, step 0"}
+
+
+def bh_variant_rates(sf, steps=20, warmup=3):
+    """Particle-steps/s of the headline workload with leaf 16 (the leaf size
+    BASELINE's Barnes-Hut config names) and with EXACT arithmetic (the
+    reference's FP32 expressions, bit-identical results), each K graph
+    replays with the L2 flushed between steps (CUDA events)."""
+    import ctypes as C
+    import torch
+    pos, vel, mas = bh_inputs()
+    n = N_BH
+    L = sf.lib()
+    out = {}
+    for name, kw in (("leaf16", dict(leaf_cap=16)), ("exact", dict(math=sf.MATH_EXACT))):
+        p = sf.default_params(solver=sf.SOLVER_TREE, eps=0.01, dt=1e-3, theta=0.5, **kw)
+        with sf.Sim(n, p) as s:
+            s.set_state(pos, vel, mas)
+            s.solve(0)
+            s.run(0, warmup)
+            s.sync()
+            ext = torch.cuda.ExternalStream(s.stream())
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+            for k in range(steps):
+                sf.check(L.sfgpu_flush_l2(C.c_void_p(s.stream())), "flush")
+                with torch.cuda.stream(ext):
+                    ev[k][0].record(ext)
+                s.run(warmup + k, 1)
+                with torch.cuda.stream(ext):
+                    ev[k][1].record(ext)
+            s.sync()
+            ms = sum(a.elapsed_time(b) for a, b in ev) / steps
+            out[name] = {"value": n / (ms * 1e-3), "unit": "particle-steps/s", "ms_per_step": ms,
+                         "device_status": s.status()}
+    return out
+
+
+def walk_vs_n(sf, sizes=(262144, 1048576), steps=5, warmup=2):
+    """The walk's roofline fraction at larger N (uniform sphere, theta 0.5,
+    leaf 8): stage times from CUDA events of the instrumented step, device
+    counts of interactions and opening tests."""
+    import ctypes as C
+    from starflood_gb300.ics import uniform_ball
+    peak, _ = fp32_peak_tflops()
+    L = sf.lib()
+    out = {}
+    for n in sizes:
+        pos, vel, mas = uniform_ball(n, seed=2024)
+        p = sf.default_params(solver=sf.SOLVER_TREE, eps=0.01, dt=1e-3, theta=0.5, flags=sf.FLAG_TIMING)
+        with sf.Sim(n, p) as s:
+            s.set_state(pos, vel, mas)
+            s.solve(0)
+            s.run(0, warmup)
+            s.sync()
+            s.stage_times()
+            s.walk_totals()
+            for k in range(steps):
+                sf.check(L.sfgpu_flush_l2(C.c_void_p(s.stream())), "flush")
+                s.step(warmup + k)
+            s.sync()
+            st = s.stage_times()
+            ni, no = s.walk_totals()
+        wms = st["walk"][0] / max(1, st["walk"][1])
+        step_ms = sum(v[0] for v in st.values()) / steps
+        flops = (FLOP_INTERACTION * ni + FLOP_OPEN * no) / max(1, st["walk"][1])
+        ach = flops / (wms * 1e-3) / 1e12
+        out[str(n)] = {"walk_ms": wms, "walk_tflops": ach, "walk_frac": ach / peak,
+                       "interactions_per_step": ni / max(1, st["walk"][1]),
+                       "eager_step_ms": step_ms, "particle_steps_per_s_eager": n / (step_ms * 1e-3)}
+    return out
+
+
 def gpu_bh_e2e(steps, warmup, sf, pos, vel, mas):
     import ctypes as C
     n = N_BH
@@ -291,21 +398,27 @@ def gpu_bh_e2e(steps, warmup, sf, pos, vel, mas):
             "d2h_bytes_per_step": d2h, "api": "sim_step() of include/starflood_compat.h, host slab"}
 
 
-def gpu_pp(sf, reps=2, n=N_PP):
+def gpu_pp(sf, reps=2, n=N_PP, exact=True):
+    """PP solves at N = 1,048,576 (CUDA events around the force stage): the
+    plain form (FP32, FAST), the compensated form, and the plain form with
+    EXACT arithmetic (the reference's expression and Kahan sums, one rep)."""
     from starflood_gb300.ics import plummer
     pos, vel, mas = plummer(n, seed=5)
     out = {}
-    for name, form in (("plain", sf.FORM_PLAIN), ("compensated", sf.FORM_COMPENSATED)):
-        p = sf.default_params(solver=sf.SOLVER_PP, eps=0.005, dt=1e-3, form=form, flags=sf.FLAG_TIMING)
+    forms = [("plain", sf.FORM_PLAIN, sf.MATH_FAST, reps), ("compensated", sf.FORM_COMPENSATED, sf.MATH_FAST, reps)]
+    if exact:
+        forms.append(("plain_exact", sf.FORM_PLAIN, sf.MATH_EXACT, 1))
+    for name, form, math, r in forms:
+        p = sf.default_params(solver=sf.SOLVER_PP, eps=0.005, dt=1e-3, form=form, math=math, flags=sf.FLAG_TIMING)
         with sf.Sim(n, p) as s:
             s.set_state(pos, vel, mas)
             s.solve(0)
             s.sync()
             s.stage_times()
-            for _ in range(reps):
+            for _ in range(r):
                 s.solve(0)
             s.sync()
-            ms = s.stage_times()["pp"][0] / reps
+            ms = s.stage_times()["pp"][0] / r
         out[name] = {"interactions_per_s": float(n) * n / (ms * 1e-3), "ms_per_eval": ms}
     return out
 
@@ -334,40 +447,28 @@ def pp_energy_drift(sf, steps=20):
 def pp_accuracy(sf):
     """Force error of plain vs compensated against the FP64 oracle on a seeded
     8192-body subsample of the N=1,048,576 Plummer sphere (i in the sample,
-    all j)."""
+    all j): the global relative L2 and the per-particle distribution."""
+    from oracle import build as ob
+    ob.build_oracle()
     from oracle.pyoracle import Oracle, make_params
     from starflood_gb300.ics import plummer
-    import ctypes as C
     n = N_PP
     pos, vel, mas = plummer(n, seed=5)
-    rng = np.random.default_rng(8192)
-    sub = np.sort(rng.choice(n, 8192, replace=False))
-    o64 = Oracle("f64")
-    # FP64 reference forces on the subsample: sum over all j, done in chunks
-    a64 = np.zeros((len(sub), 3))
-    p64 = make_params(eps=0.005)
-    # the oracle computes all-pairs; restrict i by evaluating a reduced system
-    # per chunk of j (superposition of partial sums)
-    pos64 = pos.astype(np.float64)
-    for j0 in range(0, n, 65536):
-        j1 = min(n, j0 + 65536)
-        xi = pos64[sub][:, None, :]
-        xj = pos64[j0:j1][None, :, :]
-        d = xi - xj
-        r2 = (d * d).sum(-1) + 0.005 ** 2
-        w = mas[j0:j1].astype(np.float64)[None, :] / (r2 * np.sqrt(r2))
-        a64 -= (d * w[..., None]).sum(1)
-    a64 *= mas[sub].astype(np.float64)[:, None]
-    del o64, p64
+    sub = np.sort(np.random.default_rng(8192).choice(n, 8192, replace=False)).astype(np.uint32)
+    a64, _ = Oracle("f64").pp_subset(pos.astype(np.float64), mas.astype(np.float64), sub, make_params(eps=0.005))
     errs = {}
-    for name, form in (("plain", sf.FORM_PLAIN), ("compensated", sf.FORM_COMPENSATED)):
-        p = sf.default_params(solver=sf.SOLVER_PP, eps=0.005, form=form)
+    for name, form, math in (("plain", sf.FORM_PLAIN, sf.MATH_FAST), ("compensated", sf.FORM_COMPENSATED, sf.MATH_FAST),
+                             ("plain_exact", sf.FORM_PLAIN, sf.MATH_EXACT)):
+        p = sf.default_params(solver=sf.SOLVER_PP, eps=0.005, form=form, math=math)
         with sf.Sim(n, p) as s:
             s.set_state(pos, vel, mas)
             s.solve(0)
             v = sf.slab_views(s.download(), n, 13)
         a = v["acc"][sub].astype(np.float64)
+        e = np.linalg.norm(a - a64, axis=1) / np.linalg.norm(a64, axis=1)
         errs[name] = float(np.linalg.norm(a - a64) / np.linalg.norm(a64))
+        errs[name + "_per_particle"] = {"median": float(np.median(e)), "p99": float(np.quantile(e, 0.99)),
+                                        "max": float(e.max())}
     return errs
 
 
@@ -398,20 +499,29 @@ def sph_cell_tile_records(pos, h):
     return total
 
 
-def gpu_sph(sf, steps, warmup, sph_path=0):
+def gpu_sph(sf, steps, warmup, sph_path=0, mode="cubic"):
+    """Barnes-Hut + SPH steps of the 262,144-body Plummer gas: mode "cubic"
+    (cubic spline, ideal gas, Monaghan viscosity) or "reference" (the
+    reference's Gaussian SPH of sph.c, FAST arithmetic: cell-grid search)."""
     import ctypes as C
     import torch
     n = N_SPH
     pos, vel, mas, rad, u = sph_inputs()
     L = sf.lib()
+    cubic = mode == "cubic"
 
     def new_sim(flags):
-        p = sf.default_params(solver=sf.SOLVER_TREE, sph=sf.SPH_CUBIC, eps=0.01, dt=5e-4, theta=0.5,
-                              acc_mode=sf.ACC_PHYSICAL, sph_gamma=5.0 / 3.0, sph_alpha=1.0, sph_beta=2.0,
-                              flags=flags, sph_path=sph_path)
+        if cubic:
+            p = sf.default_params(solver=sf.SOLVER_TREE, sph=sf.SPH_CUBIC, eps=0.01, dt=5e-4, theta=0.5,
+                                  acc_mode=sf.ACC_PHYSICAL, sph_gamma=5.0 / 3.0, sph_alpha=1.0, sph_beta=2.0,
+                                  flags=flags, sph_path=sph_path)
+        else:
+            p = sf.default_params(solver=sf.SOLVER_TREE, sph=sf.SPH_REFERENCE, eps=0.01, dt=5e-4, theta=0.5,
+                                  flags=flags)
         s = sf.Sim(n, p)
         s.set_state(pos, vel, mas, rad)
-        s.sph_set_u(u)
+        if cubic:
+            s.sph_set_u(u)
         s.solve(0)
         return s
 
@@ -448,32 +558,46 @@ def gpu_sph(sf, steps, warmup, sph_path=0):
     stages = st.stage_times()
     pairs = float(st.sph_neighbours().astype(np.float64).sum())
     st.close()
-
-    records = 0.5 * (sph_cell_tile_records(pos, 0.05) + sph_cell_tile_records(mid, 0.05))
-    dens_bytes = records * 16 + n * 32    # x, y, z, m per tile record; 16 B in + 16 B out per body
-    force_bytes = records * 48 + n * 32   # + vx, vy, vz, u and rho, P/rho^2, c, h per tile record
     d_ms = stages["sph_density"][0] / max(1, stages["sph_density"][1])
     f_ms = stages["sph_force"][0] / max(1, stages["sph_force"][1])
-    peak = hbm_peak()
-    dens_gbs = dens_bytes / (d_ms * 1e-3) / 1e9
-    force_gbs = force_bytes / (f_ms * 1e-3) / 1e9
-    dom = ("sph_force", force_gbs, force_bytes, f_ms) if f_ms >= d_ms else ("sph_density", dens_gbs, dens_bytes, d_ms)
-    return {
-        "workload": "Barnes-Hut (theta=0.5, leaf 8, eps=0.01) + cubic-spline SPH (h=0.05, gamma=5/3, u0=0.05, "
-                    "alpha=1, beta=2), N=262144 Plummer a=1 M=1 with isotropic velocities, dt=5e-4",
+    out = {
         "value": n * steps / (total_ms * 1e-3), "unit": "particle-steps/s", "steps": steps,
         "ms_per_step": total_ms / steps, "device_status": status,
         "l2": "flushed between timed steps (256 MiB memset, untimed)",
         "stage_ms_per_step": {k: round(v[0] / max(1, v[1]), 4) for k, v in stages.items()},
+    }
+    if not cubic:
+        out["workload"] = ("Barnes-Hut (theta=0.5, leaf 8, eps=0.01) + the reference's SPH (sph.c: Gaussian kernel, "
+                           "P=(0.1 rho)^2, momentum over r<=1; FAST arithmetic, cell-grid neighbour search), "
+                           "h=0.05, N=262144 Plummer a=1 M=1, dt=5e-4")
+        out["momentum_set_pairs_per_pass"] = pairs
+        out["set_pairs_per_s"] = pairs / (f_ms * 1e-3)
+        return out
+    records = 0.5 * (sph_cell_tile_records(pos, 0.05) + sph_cell_tile_records(mid, 0.05))
+    dens_bytes = records * 16 + n * 32    # x, y, z, m per tile record; 16 B in + 16 B out per body
+    force_bytes = records * 48 + n * 32   # + vx, vy, vz, u and rho, P/rho^2, c, h per tile record
+    peak = hbm_peak()
+    dens_gbs = dens_bytes / (d_ms * 1e-3) / 1e9
+    force_gbs = force_bytes / (f_ms * 1e-3) / 1e9
+    dom = ("sph_force", force_gbs, force_bytes, f_ms) if f_ms >= d_ms else ("sph_density", dens_gbs, dens_bytes, d_ms)
+    out.update({
+        "workload": "Barnes-Hut (theta=0.5, leaf 8, eps=0.01) + cubic-spline SPH (h=0.05, gamma=5/3, u0=0.05, "
+                    "alpha=1, beta=2), N=262144 Plummer a=1 M=1 with isotropic velocities, dt=5e-4",
         "neighbour_pairs_per_pass": pairs,
         "pairs_per_s": {"density": pairs / (d_ms * 1e-3), "force": pairs / (f_ms * 1e-3)},
-        "roofline": {"kernel": "k_cubic_pass<%s>" % ("true" if dom[0] == "sph_force" else "false"),
+        "roofline": {"kernel": "k_cubic_body<2, %s>" % ("true" if dom[0] == "sph_force" else "false"),
                      "bound": "hbm", "achieved": dom[1], "peak": peak[0], "unit": "GB/s", "frac": dom[1] / peak[0],
-                     "traffic": None, "peak_source": peak[1],
+                     "traffic": profiled_traffic("sph_cubic_body_plummer262144.md"),
+                     "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum per launch of the force pass, "
+                                       "profiles/sph_cubic_body_plummer262144.md (ncu)",
+                     "peak_source": peak[1],
                      "algorithmic_bytes_per_launch": dom[2], "avg_launch_ms": dom[3],
                      "density_pass_gbs": dens_gbs, "force_pass_gbs": force_gbs,
-                     "cell_tile_records_per_pass": records},
-    }
+                     "cell_tile_records_per_pass": records,
+                     "bytes_model": "the 27-cell tile stream of side-2h cells (sum over cells of the records of their "
+                                    "27 neighbours) + 32 B per body"},
+    })
+    return out
 
 
 def cpu_sph_rate(max_seconds=20.0):
@@ -779,6 +903,89 @@ def job_value(world, n, steps, t_ms):
     return world * n * steps / (t_ms * 1e-3)
 
 
+def bh_config(world):
+    """The `config` object of both arms (same keys, so the two lines name the
+    same workload)."""
+    return {"workload": WORKLOAD, "N": N_BH, "leaf": 8, "theta": 0.5, "eps": 0.01, "dt": 1e-3,
+            "parallelism": "replicas" if world > 1 else "single GPU",
+            "l2": "flushed between timed steps (256 MiB memset, untimed)",
+            "step": "one sim_step (kick, drift, bounds, tree build, walk, kick, energies)"}
+
+
+def reference_line(args):
+    """--impl reference: the reference path on the host cores (the FP32
+    restatement, bit-identical to the compiled reference; OpenMP, all host
+    threads).  `warmup` untimed steps, then `steps` timed steps."""
+    from oracle import build as ob
+    ob.build_oracle()
+    from oracle.pyoracle import Oracle, make_params, slab_views
+    pos, vel, mas = bh_inputs()
+    n = N_BH
+    orc = Oracle("f32")
+    p = make_params(dt=1e-3, eps=0.01, theta=0.5, use_tree=1)
+    sim, slab, _ = orc.new_sim(n, p)
+    v = slab_views(slab, n, 13)
+    v["pos"][:] = pos
+    v["vel"][:] = vel
+    v["mas"][:] = mas
+    orc.sim_solv(p, sim, 0)
+    for k in range(args.warmup):
+        orc.sim_step(p, sim, k)
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        orc.sim_step(p, sim, args.warmup + k)
+    dt = time.perf_counter() - t0
+    value = n * args.steps / dt
+    cb = {"value": value, "unit": "particle-steps/s", "cores": orc.threads(), "kind": "port",
+          "sample": "%d timed sim_step calls of the N=%d Barnes-Hut workload after %d untimed (%.2f s)" % (
+              args.steps, n, args.warmup, dt)}
+    config = bh_config(1)
+    config["parallelism"] = "host OpenMP, %d threads" % orc.threads()
+    return {"impl": "reference", "metric": METRIC, "value": value, "unit": "particle-steps/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded uniform unit sphere, pcg4d)", "config": config, "cpu_baseline": cb,
+            "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def compact_summary(line):
+    """The sub-benchmarks' key figures, short enough to sit in the last
+    ~1.4 kB of the line (what a log tail keeps)."""
+    def g(d, *ks):
+        for k in ks:
+            if not isinstance(d, dict) or k not in d:
+                return None
+            d = d[k]
+        return float("%.4g" % d) if isinstance(d, float) else d
+    out = {"headline_roofline_frac": g(line, "roofline", "frac"),
+           "per_particle_err": {k: g(line, "per_particle_err", k)
+                                for k in ("median", "p99", "max", "max_over_term_magnitudes")}}
+    pp = line.get("pp")
+    if isinstance(pp, dict):
+        out["pp"] = {"plain_ips": g(pp, "plain", "interactions_per_s"),
+                     "comp_ips": g(pp, "compensated", "interactions_per_s"),
+                     "comp_over_plain": g(pp, "compensated_over_plain"),
+                     "exact_ips": g(pp, "plain_exact", "interactions_per_s"),
+                     "comp_over_plain_at_1e-6": g(pp, "compensated_over_plain_at_1e-6"),
+                     "plain_frac": g(pp, "plain", "roofline_frac"), "comp_frac": g(pp, "compensated", "roofline_frac"),
+                     "err_fp64": {k: g(pp, "force_error_vs_fp64", k) for k in ("plain", "compensated", "plain_exact")},
+                     "err_fp64_per_particle_max": {k: g(pp, "force_error_vs_fp64", k + "_per_particle", "max")
+                                                   for k in ("plain", "compensated", "plain_exact")},
+                     "drift": {k: g(pp, "energy_drift_20_steps", k, "relative_drift") for k in ("plain", "compensated")}}
+    for key in ("sph", "sph_reference"):
+        sp = line.get(key)
+        if isinstance(sp, dict):
+            out[key] = {"value": g(sp, "value"), "ms": g(sp, "ms_per_step"), "frac": g(sp, "roofline", "frac"),
+                        "vs_cpu_mode_a": g(sp, "vs_cpu_mode_a")}
+    bt = line.get("batch")
+    if isinstance(bt, dict):
+        out["batch"] = {"ips": g(bt, "batched", "value"), "over_plain": g(bt, "batched_over_plain"),
+                        "err_fp64": g(bt, "batched", "force_error_vs_fp64"), "adjoint_s": g(bt, "adjoint", "seconds")}
+    out["bh_variants"] = {k: g(line, "bh_variants", k, "value") for k in ("leaf16", "exact")}
+    out["walk_frac_vs_n"] = {k: g(v, "walk_frac") for k, v in (line.get("walk_vs_n") or {}).items()}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -787,13 +994,15 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-pp", action="store_true", help="skip the N=1M PP sub-benchmark")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
-    ap.add_argument("--no-sph", action="store_true", help="skip the N=262144 Barnes-Hut + SPH sub-benchmark")
+    ap.add_argument("--no-sph", action="store_true", help="skip the N=262144 Barnes-Hut + SPH sub-benchmarks")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched + adjoint sub-benchmark")
     ap.add_argument("--no-vis", action="store_true", help="skip the vis_draw splat sub-benchmark")
     ap.add_argument("--no-pm", action="store_true", help="skip the particle-mesh grid sub-benchmark")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the leaf-16 / EXACT lines, the walk at larger N and the per-particle error")
     ap.add_argument("--walk-split", type=int, default=0, help="Barnes-Hut walk variant (sfgpu_params.walk_split)")
     ap.add_argument("--walk-group", type=int, default=0, help="bodies per warp of the group walk (sfgpu_params.walk_group)")
-    ap.add_argument("--only", choices=["pp", "sph", "pm", "batch"], default=None,
+    ap.add_argument("--only", choices=["pp", "sph", "sph_reference", "pm", "batch"], default=None,
                     help="run one sub-benchmark alone and print its object (profiling runs)")
     ap.add_argument("--pp-n", type=int, default=N_PP, help="bodies of the PP sub-benchmark with --only pp")
     ap.add_argument("--sph-path", type=int, default=0, help="SPH pass variant with --only sph (sfgpu_params.sph_path)")
@@ -807,15 +1016,7 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        cb = cpu_bh_rate(max_seconds=min(60.0, 3.0 + 1.0 * args.steps), max_steps=args.steps + args.warmup)
-        line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "particle-steps/s",
-                "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-                "ms_per_step": N_BH / cb["value"] * 1e3, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded uniform sphere)",
-                "config": {"workload": WORKLOAD, "N": N_BH, "parallelism": "host OpenMP"},
-                "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": "particle-steps/s",
-                                            "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        print(json.dumps(line))
+        print(json.dumps(reference_line(args)))
         return
 
     if world > 1:
@@ -840,8 +1041,10 @@ def main():
     if args.only == "batch":
         print(json.dumps({"only": "batch", "batch": gpu_batch(sf)}))
         return
-    if args.only == "sph":
-        print(json.dumps({"only": "sph", "sph": gpu_sph(sf, max(3, args.steps), args.warmup, args.sph_path)}))
+    if args.only in ("sph", "sph_reference"):
+        mode = "cubic" if args.only == "sph" else "reference"
+        print(json.dumps({"only": args.only, args.only: gpu_sph(sf, max(3, args.steps), args.warmup, args.sph_path,
+                                                              mode=mode)}))
         return
 
     r = gpu_bh(args.steps, args.warmup, sf)
@@ -859,10 +1062,7 @@ def main():
     line = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded uniform unit sphere, pcg4d)",
-            "config": {"workload": WORKLOAD, "N": N_BH, "leaf": 8,
-                       "parallelism": "replicas" if world > 1 else "single GPU",
-                       "l2": "flushed between timed steps (256 MiB memset, untimed)",
-                       "step": "one CUDA-graph replay of sim_step (kick, drift, bounds, tree build, walk, kick, energies)"},
+            "config": bh_config(world),
             "clocks": r["clocks"], "e2e": r["e2e"], "gpu_launches": r["per_step"] * args.steps,
             "roofline": {"kernel": "k_walk_group (Barnes-Hut group walk; its epilogue also applies the second "
                                    "kick and the energy sums, included in its duration)",
@@ -882,6 +1082,13 @@ def main():
             line["cpu_baseline"] = {"skipped": "--no-cpu"} if args.no_cpu else cpu_bh_rate(max_seconds=10.0)
         except Exception as e:  # the baseline must not hide the GPU line
             line["cpu_baseline"] = {"error": str(e)}
+        if not args.no_extra:
+            for key, fn in (("per_particle_err", lambda: bh_per_particle_err(sf)),
+                            ("bh_variants", lambda: bh_variant_rates(sf)), ("walk_vs_n", lambda: walk_vs_n(sf))):
+                try:
+                    line[key] = fn()
+                except Exception as e:
+                    line[key] = {"error": str(e)}
         if not args.no_pp:
             pp = gpu_pp(sf)
             try:
@@ -892,9 +1099,14 @@ def main():
                 pp["energy_drift_20_steps"] = pp_energy_drift(sf)
             except Exception as e:
                 pp["energy_drift_20_steps"] = {"error": str(e)}
-            for k in ("plain", "compensated"):
-                ips = pp[k]["interactions_per_s"]
-                pp[k]["roofline_frac"] = ips * FLOP_INTERACTION / (peak * 1e12)
+            for k in ("plain", "compensated", "plain_exact"):
+                if k in pp:
+                    pp[k]["roofline_frac"] = pp[k]["interactions_per_s"] * FLOP_INTERACTION / (peak * 1e12)
+            pp["compensated_over_plain"] = pp["compensated"]["interactions_per_s"] / pp["plain"]["interactions_per_s"]
+            if "plain_exact" in pp:
+                # at force error <= 1e-6 of FP64 the plain form needs EXACT arithmetic (FAST: about 3e-6)
+                pp["compensated_over_plain_at_1e-6"] = (pp["compensated"]["interactions_per_s"] /
+                                                        pp["plain_exact"]["interactions_per_s"])
             try:
                 pp["cpu_baseline"] = {"skipped": "--no-cpu"} if args.no_cpu else cpu_pp_rate()
             except Exception as e:
@@ -902,12 +1114,20 @@ def main():
             pp["workload"] = "PP gravity N=1048576 Plummer a=1 M=1 eps=0.005, %d flop/interaction" % FLOP_INTERACTION
             line["pp"] = pp
         if not args.no_sph:
-            sph = gpu_sph(sf, max(10, min(args.steps, 50)), args.warmup)
+            nsteps = max(10, min(args.steps, 50))
             try:
-                sph["cpu_baseline"] = {"skipped": "--no-cpu"} if args.no_cpu else cpu_sph_rate()
+                cpu_a = None if args.no_cpu else cpu_sph_rate()
             except Exception as e:
-                sph["cpu_baseline"] = {"error": str(e)}
-            line["sph"] = sph
+                cpu_a = {"error": str(e)}
+            for key, mode in (("sph", "cubic"), ("sph_reference", "reference")):
+                sp = gpu_sph(sf, nsteps if mode == "cubic" else max(3, nsteps // 5), args.warmup, mode=mode)
+                sp["cpu_baseline"] = cpu_a if cpu_a is not None else {"skipped": "--no-cpu"}
+                if isinstance(cpu_a, dict) and "value" in cpu_a:
+                    sp["vs_cpu_mode_a"] = sp["value"] / cpu_a["value"]
+                    sp["vs_cpu_mode_a_kind"] = ("like for like: the reference's SPH on both sides" if mode != "cubic"
+                                                else "cross-algorithm: cubic-spline SPH on the GPU against the "
+                                                     "reference's Gaussian all-pairs SPH on the CPU")
+                line[key] = sp
         if not args.no_batch:
             bt = gpu_batch(sf)
             if not args.no_cpu and isinstance(line.get("pp", {}).get("cpu_baseline"), dict) \
@@ -925,6 +1145,7 @@ def main():
                 line["pm"] = gpu_pm(sf)
             except Exception as e:
                 line["pm"] = {"error": str(e)}
+        line["summary"] = compact_summary(line)
         print(json.dumps(line))
     if world > 1:
         dist.barrier()

@@ -78,25 +78,32 @@ typedef struct {
     double   sph_beta;    /* CUBIC: Monaghan viscosity beta                 */
     uint32_t flags;       /* SFGPU_FLAG_*                                   */
     uint32_t walk_split;  /* walk variant: 0 group walk (default), 1 thread per body, 8 thread per body and root octant, 64 32-body group walk over 8 warps */
-    uint32_t sph_path;    /* CUBIC SPH passes: 0 one thread per body (default), 1 one warp per 32-body slice of a cell */
+    uint32_t sph_path;    /* CUBIC SPH neighbour search: 0 cells of side h, rows culled to the 2h sphere
+                             (default); 1 the 27 cells of side 2h around the body */
     uint32_t walk_group;  /* bodies per warp of the group walk: 0 the default (16), 8, 16 or 32 */
-    uint32_t reserved[4];
+    uint32_t spin_limit;  /* rounds a bounded device wait (the look-backs of the sort and of the
+                             node scan) spins on an unpublished word before it gives up and sets
+                             SFGPU_STATUS_SPIN; 0: the default, 2^24 */
+    uint32_t walk_limit;  /* rounds of a warp's tree-walk loop before it stops and sets
+                             SFGPU_STATUS_WALK; 0: the default, 2^24 */
+    uint32_t reserved[2];
 } sfgpu_params;
 
 /* flags */
-#define SFGPU_FLAG_STATS   0x1u  /* count walk interactions / opening tests per particle */
+#define SFGPU_FLAG_STATS   0x1u  /* per-particle statistics: walk interactions and opening tests,
+                                    SPH neighbour-set hashes */
 #define SFGPU_FLAG_TIMING  0x2u  /* record CUDA-event times per stage            */
 #define SFGPU_FLAG_NOGRAPH 0x4u  /* sfgpu_run launches kernels one by one         */
 #define SFGPU_FLAG_EXPORT_TREE 0x8u /* compat sim_solv/sim_step also fill sim_t.tree.node */
 #define SFGPU_FLAG_VERBOSE 0x10u /* compat sim_step prints the energies like the reference */
 
 /* Device status word bits (sfgpu_status). */
-#define SFGPU_STATUS_TREE_NODES   0x01u /* node capacity exceeded (tree.c:224)   */
-#define SFGPU_STATUS_TREE_DEPTH   0x02u /* depth limit exceeded  (tree.c:230)    */
+#define SFGPU_STATUS_TREE_NODES   0x01u /* node capacity exceeded (tree.c:180)   */
+#define SFGPU_STATUS_TREE_DEPTH   0x02u /* depth limit exceeded  (tree.c:186)    */
 #define SFGPU_STATUS_TIES         0x04u /* too many bodies exactly on cell midplanes */
 #define SFGPU_STATUS_SPIN         0x08u /* a bounded device wait gave up         */
 #define SFGPU_STATUS_WALK         0x10u /* walk stack or iteration bound hit     */
-#define SFGPU_STATUS_SPH_CELLS    0x20u /* SPH cell grid capacity exceeded       */
+#define SFGPU_STATUS_SPH_CELLS    0x20u /* a body beyond the SPH cell grid's 2^20 cells per axis */
 
 /* The reference's compiled-in defaults (src/config.h): dt=1, eps=1e-3, G=1,
  * theta=0.5, tree on, SPH off, leaf 8, depth 16, 262144 nodes; FAST math,
@@ -173,7 +180,7 @@ int sfgpu_walk_totals(sfgpu_sim* s, uint64_t* interactions, uint64_t* opening_te
 
 /* Replaces tree_build (src/tree.c:74-318) for the positions and masses
  * already on the device: builds in the given root cube (min xyz, max xyz).
- * The status word reports node or depth overflow (tree.c:224-233). */
+ * The status word reports node or depth overflow (tree.c:179-189). */
 int sfgpu_tree_build(sfgpu_sim* s, const float bounds[6]);
 /* Replaces solve_gravity_part_tree (src/gravity.c:242-663): walks the last
  * built tree for the current positions. */
@@ -187,6 +194,11 @@ int sfgpu_solve_sph(sfgpu_sim* s);
  * with fl(r^2) <= 1 in the momentum pass (src/sph.c:231, j = i included);
  * CUBIC, the bodies with fl(r^2) < fl((2h)^2). */
 int sfgpu_sph_neighbours(sfgpu_sim* s, uint32_t* counts);
+/* The same neighbour sets as order-independent hashes (no reference
+ * counterpart; for comparing two searches set for set): per body, the sum
+ * modulo 2^64 of splitmix64's output function applied to each member's body
+ * index.  Needs a simulation created with SFGPU_FLAG_STATS. */
+int sfgpu_sph_neighbour_hashes(sfgpu_sim* s, uint64_t* hashes);
 /* CUBIC SPH: specific internal energy u per body (kicked with du/dt in the
  * leapfrog, like the velocities).  Set it after sfgpu_create; read it and the
  * last du/dt back (either pointer may be NULL). */
@@ -207,6 +219,20 @@ int sfgpu_tree_num_nodes(sfgpu_sim* s, uint32_t* num_nodes);
  * {COM x, y, z, mass}.  Arrays hold num_nodes entries. */
 int sfgpu_tree_export(sfgpu_sim* s, uint32_t* parent, uint32_t* bodies, uint32_t* branch8,
                       float* bounds6, float* params4);
+
+/* ---- failure detection ------------------------------------------------- */
+/* Checks the bounded device wait of the radix sort's decoupled look-back
+ * without a GPU fault (no reference counterpart): sorts the n host keys on
+ * their low 7 bits in one tile pass of 256-thread tiles (4 keys per thread
+ * up to 2^17 keys, 8 above) in which tile `withheld_tile` never publishes
+ * its look-back words (0xFFFFFFFF: every tile publishes).  The tiles after
+ * it wait `spin_limit` rounds (0: the default 2^24) on a word that nothing
+ * sets, then give up, set SFGPU_STATUS_SPIN and finish, so the call
+ * returns.  Writes the sorted keys, the original index of each sorted slot
+ * and the device status word (all host arrays); the order is right only if
+ * no tile was withheld. */
+int sfgpu_sort_withheld_check(const uint64_t* keys, uint32_t n, uint32_t withheld_tile, uint32_t spin_limit,
+                              uint64_t* sorted, uint32_t* index, uint32_t* status);
 
 /* ---- process utilities ------------------------------------------------- */
 /* Kernel launches the host has issued through this library in this process.

@@ -27,7 +27,9 @@ import sys
 from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REFERENCE_SRC = "/root/reference/src"
+# The reference sources: STARFLOOD_REFERENCE_SRC if set, else where this
+# recipe expects the read-only Starflood tree.
+REFERENCE_SRC = os.environ.get("STARFLOOD_REFERENCE_SRC", "/root/reference/src")
 REF_OUT = os.path.join(HERE, "_ref")
 
 CFLAGS = ["-O2", "-std=c99", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-fopenmp",

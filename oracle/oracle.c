@@ -106,7 +106,7 @@ void orc_root_bounds(uint32_t n, const R* pos, uint32_t step_number, R bounds[6]
     }
 }
 
-/* ---- tree.c:118-362: build by inserting particles one at a time. */
+/* ---- tree.c:74-318: build by inserting particles one at a time. */
 static void node_clear(orc_node* nd, uint32_t parent) {
     memset(nd, 0, sizeof(*nd));
     nd->parent = parent;
@@ -119,7 +119,7 @@ int orc_tree_build(const orc_params* p, uint32_t n, const R* pos, const R* mas,
     const int depth_max = (int)p->depth_max;
     uint32_t count = 1u;
 
-    /* tree.c:129-151 purge, 156-159 root bounds */
+    /* tree.c:85-107 purge, 112-115 root bounds */
     for (uint32_t i = 0; i < max_nodes; i++) node_clear(&nodes[i], 0u);
     for (int a = 0; a < 6; a++) nodes[0].bounds[a] = bounds[a];
 
@@ -130,7 +130,7 @@ int orc_tree_build(const orc_params* p, uint32_t n, const R* pos, const R* mas,
         R lo[3] = {bounds[0], bounds[1], bounds[2]};
         R hi[3] = {bounds[3], bounds[4], bounds[5]};
 
-        /* tree.c:186-190: particles outside the closed root cube are skipped */
+        /* tree.c:141-146: particles outside the closed root cube are skipped */
         int outside = 0;
         for (int a = 0; a < 3; a++) outside |= (lo[a] > x[a]) | (x[a] > hi[a]);
         if (outside) continue;
@@ -138,7 +138,7 @@ int orc_tree_build(const orc_params* p, uint32_t n, const R* pos, const R* mas,
         uint32_t cur = 0u;
         for (int depth = 0; depth <= depth_max; depth++) {
             orc_node* nd = &nodes[cur];
-            const uint32_t before = nd->bodies;           /* tree.c:198-200 */
+            const uint32_t before = nd->bodies;           /* tree.c:154-156 */
             nd->bodies = before + 1u;
             R mid[3];
             for (int a = 0; a < 3; a++) mid[a] = (R)0.5 * (lo[a] + hi[a]);  /* 203-207 */
@@ -197,9 +197,9 @@ int orc_tree_build(const orc_params* p, uint32_t n, const R* pos, const R* mas,
         }
     }
     *num_nodes = count;
-    if (status != 0) return -1;   /* tree.c:224-233 leave COMs unnormalised */
+    if (status != 0) return -1;   /* tree.c:179-189 leave COMs unnormalised */
 
-    for (uint32_t i = 0; i < count; i++) {                /* tree.c:346-354 */
+    for (uint32_t i = 0; i < count; i++) {                /* tree.c:302-310 */
         const R w = nodes[i].params[3];
         const R inv = (R)0.0 < w ? (R)1.0 / w : (R)1.0;
         nodes[i].params[0] *= inv;
@@ -211,8 +211,8 @@ int orc_tree_build(const orc_params* p, uint32_t n, const R* pos, const R* mas,
 
 /* ---- gravity.c:242-663: per-particle depth-first walk without a stack of
  * node ids: parent links plus the octant being visited at every depth. */
-void orc_gravity_tree(const orc_params* p, uint32_t n, const R* pos, const R* mas,
-                      const orc_node* nodes, R* acc, R* pot, orc_walk_stats* stats) {
+static void gravity_tree_impl(const orc_params* p, uint32_t n, const R* pos, const R* mas,
+                              const orc_node* nodes, R* acc, R* pot, orc_walk_stats* stats, R* mag) {
     const uint32_t cap = p->leaf_cap;
     const R eps2 = (R)(p->eps * p->eps);
     const R theta = (R)p->theta;
@@ -229,6 +229,7 @@ void orc_gravity_tree(const orc_params* p, uint32_t n, const R* pos, const R* ma
         const R ri[3] = {pos[3u * i], pos[3u * i + 1u], pos[3u * i + 2u]};
         const R mi = mas[i];
         ksum ax = {0, 0}, ay = {0, 0}, az = {0, 0}, ph = {0, 0};
+        double tmag = 0.0;  /* sum of |term| (FP64), the scale of the sum's rounding */
         uint32_t n_int = 0u, n_open = 0u;
 
         int path[64];
@@ -303,6 +304,7 @@ void orc_gravity_tree(const orc_params* p, uint32_t n, const R* pos, const R* ma
                 az.s += phi * inv2 * dz;
                 ph.s += phi;
             }
+            if (mag) tmag += (double)(phi * inv2) * sqrt((double)r2);
             n_int++;
             at = nd->parent;                              /* 577-578 */
             depth--;
@@ -315,7 +317,22 @@ void orc_gravity_tree(const orc_params* p, uint32_t n, const R* pos, const R* ma
             stats[i].interactions = n_int;
             stats[i].opening_tests = n_open;
         }
+        if (mag) mag[i] = (R)(fabs((double)neg_g) * fabs((double)mi) * tmag);
     }
+}
+
+void orc_gravity_tree(const orc_params* p, uint32_t n, const R* pos, const R* mas,
+                      const orc_node* nodes, R* acc, R* pot, orc_walk_stats* stats) {
+    gravity_tree_impl(p, n, pos, mas, nodes, acc, pot, stats, NULL);
+}
+
+/* The same walk, also returning per body G m_i sum_k |F_k|: the sum of the
+ * magnitudes of the terms whose vector sum is acc_i (test infrastructure:
+ * the scale against which a body's rounding error is judged when its terms
+ * cancel). */
+void orc_gravity_tree_mag(const orc_params* p, uint32_t n, const R* pos, const R* mas,
+                          const orc_node* nodes, R* acc, R* pot, orc_walk_stats* stats, R* mag) {
+    gravity_tree_impl(p, n, pos, mas, nodes, acc, pot, stats, mag);
 }
 
 /* ---- gravity.c:666-819: every j, including j == i. */
@@ -355,6 +372,44 @@ void orc_gravity_pp(const orc_params* p, uint32_t n, const R* pos, const R* mas,
         acc[3u * i + 1u] = neg_g * mi * ay.s;
         acc[3u * i + 2u] = neg_g * mi * az.s;
         pot[i] = neg_g * ph.s;
+    }
+}
+
+/* The same sums for the bodies idx[0..ni) only, over all n bodies j (a
+ * seeded subsample of a workload too large for all pairs); outputs are
+ * indexed like idx. */
+void orc_gravity_pp_subset(const orc_params* p, uint32_t n, const R* pos, const R* mas, uint32_t ni,
+                           const uint32_t* idx, R* acc, R* pot, R* mag) {
+    const R eps2 = (R)(p->eps * p->eps);
+    const R neg_g = (R)(-p->G);
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 4)
+#endif
+    for (int64_t kk = 0; kk < (int64_t)ni; kk++) {
+        const uint32_t i = idx[kk];
+        const R mi = mas[i];
+        const R xi = pos[3u * i], yi = pos[3u * i + 1u], zi = pos[3u * i + 2u];
+        ksum ax = {0, 0}, ay = {0, 0}, az = {0, 0}, ph = {0, 0};
+        double tmag = 0.0;
+        for (uint32_t j = 0; j < n; j++) {
+            const R dx = xi - pos[3u * j];
+            const R dy = yi - pos[3u * j + 1u];
+            const R dz = zi - pos[3u * j + 2u];
+            const R r2 = (dx * dx) + (dy * dy) + (dz * dz);
+            const R inv2 = (R)1.0 / (r2 + eps2);
+            const R inv1 = (R)1.0 / R_SQRT(r2 + eps2);
+            const R phi = mas[j] * inv1;
+            ksum_add(&ax, phi * inv2 * dx);
+            ksum_add(&ay, phi * inv2 * dy);
+            ksum_add(&az, phi * inv2 * dz);
+            ksum_add(&ph, phi);
+            if (mag) tmag += (double)(phi * inv2) * sqrt((double)r2);
+        }
+        acc[3u * kk + 0u] = neg_g * mi * ax.s;
+        acc[3u * kk + 1u] = neg_g * mi * ay.s;
+        acc[3u * kk + 2u] = neg_g * mi * az.s;
+        pot[kk] = neg_g * ph.s;
+        if (mag) mag[kk] = (R)(fabs((double)neg_g) * fabs((double)mi) * tmag);
     }
 }
 

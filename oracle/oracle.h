@@ -72,9 +72,9 @@ double orc_mean_radius(uint32_t n, const orc_real* pos);
 void orc_root_bounds(uint32_t n, const orc_real* pos, uint32_t step_number,
                      orc_real bounds[6]);
 
-/* tree.c:118-362: serial insertion build.  Returns 0, or -1 on node or depth
+/* tree.c:74-318: serial insertion build.  Returns 0, or -1 on node or depth
  * overflow (the tree is left partial, as in the reference).  *num_nodes gets
- * the node count (the reference forgets to store it, tree.c:121,359). */
+ * the node count (the reference forgets to store it, tree.c:77-79,315). */
 int orc_tree_build(const orc_params* p, uint32_t n, const orc_real* pos,
                    const orc_real* mas, const orc_real bounds[6],
                    orc_node* nodes, uint32_t* num_nodes);
@@ -87,6 +87,15 @@ void orc_gravity_tree(const orc_params* p, uint32_t n, const orc_real* pos,
 /* gravity.c:666-819: all-pairs softened gravity with Kahan sums. */
 void orc_gravity_pp(const orc_params* p, uint32_t n, const orc_real* pos,
                     const orc_real* mas, orc_real* acc, orc_real* pot);
+
+/* orc_gravity_pp for the bodies idx[0..ni) only (outputs indexed like idx);
+ * mag (may be NULL) receives G m_i sum_j |F_ij|. */
+void orc_gravity_pp_subset(const orc_params* p, uint32_t n, const orc_real* pos, const orc_real* mas,
+                           uint32_t ni, const uint32_t* idx, orc_real* acc, orc_real* pot, orc_real* mag);
+/* orc_gravity_tree, also writing per body G m_i sum_k |F_k| into mag. */
+void orc_gravity_tree_mag(const orc_params* p, uint32_t n, const orc_real* pos, const orc_real* mas,
+                          const orc_node* nodes, orc_real* acc, orc_real* pot, orc_walk_stats* stats,
+                          orc_real* mag);
 
 /* sph.c:14-282: reference SPH (Gaussian, all pairs).  Adds the pressure
  * force into acc, writes rho and prs.  nbr (may be NULL) receives, per

@@ -123,7 +123,9 @@ class Oracle:
                                      nodes.ctypes.data_as(C.c_void_p), C.byref(nn))
         return st, nodes[: nn.value].copy() if st == 0 else nodes[: nn.value].copy()
 
-    def walk(self, pos, mas, nodes, params: Params | None = None):
+    def walk(self, pos, mas, nodes, params: Params | None = None, with_mag=False):
+        """(acc, pot, stats), and with with_mag the per-body sum of the
+        terms' magnitudes G m_i sum |F|."""
         p = params or make_params(use_tree=1)
         pos, pp = self._arr(pos)
         mas, mp = self._arr(mas)
@@ -133,6 +135,12 @@ class Oracle:
         acc = np.zeros((n, 3), self.real)
         pot = np.zeros(n, self.real)
         stats = np.zeros((n, 2), np.uint32)
+        if with_mag:
+            mag = np.zeros(n, self.real)
+            self.lib.orc_gravity_tree_mag(C.byref(p), n, pp, mp, full.ctypes.data_as(C.c_void_p),
+                                          acc.ctypes.data_as(self._rp), pot.ctypes.data_as(self._rp),
+                                          stats.ctypes.data_as(u32p), mag.ctypes.data_as(self._rp))
+            return acc, pot, stats, mag
         self.lib.orc_gravity_tree(C.byref(p), n, pp, mp, full.ctypes.data_as(C.c_void_p),
                                   acc.ctypes.data_as(self._rp), pot.ctypes.data_as(self._rp),
                                   stats.ctypes.data_as(u32p))
@@ -148,6 +156,21 @@ class Oracle:
         self.lib.orc_gravity_pp(C.byref(p), n, pp, mp, acc.ctypes.data_as(self._rp),
                                 pot.ctypes.data_as(self._rp))
         return acc, pot
+
+    def pp_subset(self, pos, mas, idx, params: Params | None = None, with_mag=False):
+        """orc_gravity_pp for the bodies idx only, over all bodies: (acc,
+        pot), and with with_mag the per-body G m_i sum_j |F_ij|."""
+        p = params or make_params()
+        pos, pp = self._arr(pos)
+        mas, mp = self._arr(mas)
+        idx = np.ascontiguousarray(idx, np.uint32)
+        acc = np.zeros((len(idx), 3), self.real)
+        pot = np.zeros(len(idx), self.real)
+        mag = np.zeros(len(idx), self.real)
+        self.lib.orc_gravity_pp_subset(C.byref(p), len(pos), pp, mp, len(idx), idx.ctypes.data_as(u32p),
+                                       acc.ctypes.data_as(self._rp), pot.ctypes.data_as(self._rp),
+                                       mag.ctypes.data_as(self._rp) if with_mag else None)
+        return (acc, pot, mag) if with_mag else (acc, pot)
 
     def sph_reference(self, pos, mas, rad, acc_in=None, params: Params | None = None):
         p = params or make_params(use_sph=1)

@@ -89,7 +89,7 @@ int refh_sph(void) { return solve_sph(&g_sim); }
 #endif
 
 #ifdef ENABLE_TREE
-/* tree_build() keeps its node count local (tree.c:121), so count the nodes
+/* tree_build() keeps its node count local (tree.c:77-79), so count the nodes
  * reachable from the root.  Returns -1 if the count exceeds max. */
 static unsigned int count_nodes(const node_t* node, unsigned int at, unsigned int max, unsigned int depth) {
     unsigned int total = 1u;

@@ -37,8 +37,8 @@ class Params(C.Structure):
                 ("acc_mode", C.c_int32), ("leaf_cap", C.c_uint32), ("depth_max", C.c_uint32),
                 ("nodes_max", C.c_uint32), ("sph_gamma", C.c_double), ("sph_alpha", C.c_double),
                 ("sph_beta", C.c_double), ("flags", C.c_uint32), ("walk_split", C.c_uint32),
-                ("sph_path", C.c_uint32), ("walk_group", C.c_uint32),
-                ("reserved", C.c_uint32 * 4)]
+                ("sph_path", C.c_uint32), ("walk_group", C.c_uint32), ("spin_limit", C.c_uint32),
+                ("walk_limit", C.c_uint32), ("reserved", C.c_uint32 * 2)]
 
 
 _lib = None
@@ -82,6 +82,8 @@ def lib():
             "sfgpu_gravity_part": (i32, [vp]),
             "sfgpu_solve_sph": (i32, [vp]),
             "sfgpu_sph_neighbours": (i32, [vp, u32p]),
+            "sfgpu_sph_neighbour_hashes": (i32, [vp, C.POINTER(C.c_uint64)]),
+            "sfgpu_sort_withheld_check": (i32, [vp, u32, u32, u32, vp, vp, u32p]),
             "sfgpu_sph_set_u": (i32, [vp, f32p]),
             "sfgpu_sph_get_u": (i32, [vp, f32p, f32p]),
             "sfgpu_tree_keys": (i32, [vp, C.POINTER(C.c_uint64), u32p, u32p, f32p]),
@@ -135,6 +137,28 @@ def lib():
             fn.argtypes = args
         _lib = L
     return _lib
+
+
+def mix64(idx):
+    """splitmix64's output function on body indices (uint64 array), the
+    per-member term of the neighbour-set hashes."""
+    with np.errstate(over="ignore"):
+        x = np.asarray(idx, np.uint64) + np.uint64(0x9E3779B97F4A7C15)
+        x = (x ^ (x >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        x = (x ^ (x >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        return x ^ (x >> np.uint64(31))
+
+
+def sort_withheld_check(keys, withheld_tile=0xFFFFFFFF, spin_limit=0):
+    """sfgpu_sort_withheld_check: (sorted keys, index, status word)."""
+    keys = np.ascontiguousarray(keys, np.uint64)
+    n = len(keys)
+    out = np.zeros(n, np.uint64)
+    idx = np.zeros(n, np.uint32)
+    st = C.c_uint32()
+    check(lib().sfgpu_sort_withheld_check(_ptr(keys), n, withheld_tile, spin_limit, _ptr(out), _ptr(idx),
+                                          C.byref(st)), "sfgpu_sort_withheld_check")
+    return out, idx, st.value
 
 
 def last_error() -> str:
@@ -323,6 +347,12 @@ class Sim:
     def sph_neighbours(self):
         a = np.zeros(self.n, np.uint32)
         check(lib().sfgpu_sph_neighbours(self.h, a.ctypes.data_as(C.POINTER(C.c_uint32))), "sfgpu_sph_neighbours")
+        return a
+
+    def sph_neighbour_hashes(self):
+        a = np.zeros(self.n, np.uint64)
+        check(lib().sfgpu_sph_neighbour_hashes(self.h, a.ctypes.data_as(C.POINTER(C.c_uint64))),
+              "sfgpu_sph_neighbour_hashes")
         return a
 
     def sph_set_u(self, u):

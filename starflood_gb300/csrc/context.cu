@@ -546,6 +546,20 @@ extern "C" int sfgpu_sph_neighbours(sfgpu_sim* s, uint32_t* counts) {
     return SFGPU_OK;
 }
 
+uint64_t* sf_sph_neighbour_hashes(sfgpu_sim* s);
+
+extern "C" int sfgpu_sph_neighbour_hashes(sfgpu_sim* s, uint64_t* hashes) {
+    sf_clear_error();
+    uint64_t* d = s ? sf_sph_neighbour_hashes(s) : nullptr;
+    if (!d || !hashes) {
+        sf_set_error("sfgpu_sph_neighbour_hashes needs a simulation with SPH created with SFGPU_FLAG_STATS");
+        return SFGPU_FAILURE;
+    }
+    SF_CUDA(cudaStreamSynchronize(s->stream));
+    SF_CUDA(cudaMemcpy(hashes, d, sizeof(uint64_t) * s->n, cudaMemcpyDeviceToHost));
+    return SFGPU_OK;
+}
+
 extern "C" int sfgpu_sph_set_u(sfgpu_sim* s, const float* u) {
     sf_clear_error();
     if (!s || !s->u || !u) {

@@ -2,7 +2,7 @@
 //
 // The reference numbers nodes in creation order: the root is 0 and a split
 // appends the 8 children of the split cell at num_nodes .. num_nodes+7
-// (tree.c:307-317).  A cell splits when its (leaf_cap+1)-th body arrives,
+// (tree.c:263-273).  A cell splits when its (leaf_cap+1)-th body arrives,
 // i.e. at the insertion of the (leaf_cap+1)-th smallest body index among its
 // members, and one insertion splits cells top-down.  So the reference id of
 // the children of split cell s is 1 + 8 r(s) + octant, with r(s) the rank of

@@ -187,6 +187,17 @@ __device__ __forceinline__ double2 dd_add(double2 a, double2 b) {
     return make_double2(hi, lo);
 }
 
+// The output function of splitmix64 (Steele, Lea and Flood, OOPSLA 2014): a
+// bijective 64-bit mix.  Summed (mod 2^64) over the body indices of a
+// neighbour set it identifies the set regardless of the order the bodies are
+// found in, so two searches can be compared set for set.
+__host__ __device__ __forceinline__ uint64_t sf_mix64(uint64_t x) {
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+
 // rng.h:13-40 (pcg4d), used for the root-cube jitter.
 __host__ __device__ __forceinline__ void pcg4d(uint32_t& a, uint32_t& b, uint32_t& c, uint32_t& d) {
     a = a * 1664525u + 1013904223u;
@@ -207,6 +218,7 @@ struct ForceConsts {
     float theta;   // (real)TREE_THETA                  gravity.c:448
     float third;   // (real)(1.0/3.0)                   gravity.c:370
     int physical;  // SFGPU_ACC_PHYSICAL
+    uint32_t walk_limit;  // rounds of a warp's walk loop before SFGPU_STATUS_WALK
 };
 ForceConsts sf_force_consts(const sfgpu_params& p);
 
@@ -242,6 +254,9 @@ struct SortWork {
     size_t cap = 0;
     size_t tiles_cap = 0;
     uint32_t flags = 0;            // SORT_NO_BUCKETS: always the tile passes
+    uint32_t spin_limit = 1u << 24;  // look-back rounds on an unpublished word before SFGPU_STATUS_SPIN
+    uint32_t withheld = 0xFFFFFFFFu; // failure-detection check only: this tile of the first tile pass
+                                     // never publishes its look-back words (0xFFFFFFFF: none)
 };
 constexpr uint32_t SORT_NO_BUCKETS = 1u;
 constexpr uint32_t SORT_PRECLEARED = 2u;  // one-shot: the caller's kernel cleared the words of sf_sort_clear_words

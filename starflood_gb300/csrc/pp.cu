@@ -10,9 +10,9 @@
 //               the j range is split over blockIdx.y so the grid covers the
 //               152 SMs several times, partial sums land in a scratch array
 //               and a second kernel adds them in a fixed order;
-//   compensated the same tiles, but each j-tile's partial sum is added to a
-//               (hi, lo) pair with two-sum (the precision form), and the
-//               split partials are added in FP64.
+//   compensated the same tiles, but the partial sum of every four j-tiles
+//               is added to a (hi, lo) pair with a paired two-sum (the
+//               precision form), and the split partials are added in FP64.
 #include <algorithm>
 
 #include "internal.cuh"
@@ -150,6 +150,20 @@ __global__ void __launch_bounds__(BS) k_pp_tile(const float* __restrict__ pos, c
 // in k_pp_tile (same operations, same order), so the results are identical.
 // Each j is staged pre-duplicated as (x,x,y,y) and (z,z,w,w) so the paired
 // operands come straight out of one 128-bit shared load.
+// Paired two-sum (Knuth) on both elements: (h, l) += a, error term into l.
+__device__ __forceinline__ void two_sum2(float2& h, float2 a, float2& l) {
+    const float2 s = __fadd2_rn(h, a);
+    const float2 bp = __fadd2_rn(s, make_float2(-h.x, -h.y));
+    const float2 ap = __fadd2_rn(s, make_float2(-bp.x, -bp.y));
+    const float2 e = __fadd2_rn(__fadd2_rn(h, make_float2(-ap.x, -ap.y)), __fadd2_rn(a, make_float2(-bp.x, -bp.y)));
+    h = s;
+    l = __fadd2_rn(l, e);
+}
+
+// j-tiles the compensated form sums plainly before each two-sum: 512
+// bodies, whose FP32 partial sum is far inside the 1e-6 bound.
+constexpr int COMP_TILES = 4;
+
 template <int BS, int PAIRS, bool COMP, int RSQ = 0>
 __global__ void __launch_bounds__(BS) k_pp_tile2(const float* __restrict__ pos, const float* __restrict__ mas,
                                                  uint32_t n, float eps2, uint32_t jchunk,
@@ -175,6 +189,7 @@ __global__ void __launch_bounds__(BS) k_pp_tile2(const float* __restrict__ pos, 
     const float2 e2 = make_float2(eps2, eps2);
     const uint32_t j0 = blockIdx.y * jchunk;
     const uint32_t j1 = min(n, j0 + jchunk);
+    int tiles = 0;
     for (uint32_t jt = j0; jt < j1; jt += BS) {
         const uint32_t j = jt + threadIdx.x;
         float x = 0.f, y = 0.f, z = 0.f, w = 0.f;  // padding: zero mass
@@ -198,18 +213,16 @@ __global__ void __launch_bounds__(BS) k_pp_tile2(const float* __restrict__ pos, 
             for (int q = 0; q < PAIRS; q++)
                 pp_pair_step<RSQ>(sx, sy, sz, sw, nx[q], ny[q], nz[q], e2, ax[q], ay[q], az[q], ph[q]);
         }
-        if (COMP) {
+        // every COMP_TILES tiles (and after the last) the running partial
+        // sums join the (hi, lo) totals through a paired two-sum
+        if (COMP && (++tiles == COMP_TILES || jt + BS >= j1)) {
+            tiles = 0;
 #pragma unroll
             for (int q = 0; q < PAIRS; q++) {
-                float e;
-                two_sumf(hx[q].x, ax[q].x, hx[q].x, e); lx[q].x += e;
-                two_sumf(hx[q].y, ax[q].y, hx[q].y, e); lx[q].y += e;
-                two_sumf(hy[q].x, ay[q].x, hy[q].x, e); ly[q].x += e;
-                two_sumf(hy[q].y, ay[q].y, hy[q].y, e); ly[q].y += e;
-                two_sumf(hz[q].x, az[q].x, hz[q].x, e); lz[q].x += e;
-                two_sumf(hz[q].y, az[q].y, hz[q].y, e); lz[q].y += e;
-                two_sumf(hp[q].x, ph[q].x, hp[q].x, e); lp[q].x += e;
-                two_sumf(hp[q].y, ph[q].y, hp[q].y, e); lp[q].y += e;
+                two_sum2(hx[q], ax[q], lx[q]);
+                two_sum2(hy[q], ay[q], ly[q]);
+                two_sum2(hz[q], az[q], lz[q]);
+                two_sum2(hp[q], ph[q], lp[q]);
                 ax[q] = ay[q] = az[q] = ph[q] = zero2;
             }
         }
@@ -297,6 +310,7 @@ ForceConsts sf_force_consts(const sfgpu_params& p) {
     c.theta = (float)p.theta;
     c.third = (float)(1.0 / 3.0);
     c.physical = p.acc_mode == SFGPU_ACC_PHYSICAL;
+    c.walk_limit = p.walk_limit ? p.walk_limit : (1u << 24);
     return c;
 }
 

@@ -22,7 +22,6 @@ constexpr int MAX_PASSES = 10;
 constexpr uint32_t FLAG_AGG = 1u << 30;
 constexpr uint32_t FLAG_INC = 2u << 30;
 constexpr uint32_t VALUE_MASK = (1u << 30) - 1u;
-constexpr uint32_t SPIN_LIMIT = 1u << 24;
 constexpr int LOOKBACK = 16;  // predecessor words read per look-back round
 
 // The lanes of the warp holding the same 7-bit digit as this one (only this
@@ -68,7 +67,8 @@ template <int SORT_ITEMS>
 __device__ __forceinline__ void onesweep_tile(const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin,
                                               uint64_t* __restrict__ kout, uint32_t* __restrict__ vout, uint32_t n,
                                               int shift, const uint32_t* __restrict__ hist, uint32_t* status,
-                                              uint32_t tile, uint32_t* d_status) {
+                                              uint32_t tile, uint32_t* d_status, uint32_t spin_limit,
+                                              uint32_t withheld) {
     __shared__ uint32_t wcnt[SORT_WARPS][RADIX];
     __shared__ uint32_t base[RADIX];
     __shared__ uint32_t toff[RADIX];
@@ -148,10 +148,11 @@ __device__ __forceinline__ void onesweep_tile(const uint64_t* __restrict__ kin, 
         const int d = threadIdx.x;
         volatile uint32_t* st = status;
         uint32_t prefix = 0;
+        const bool publish = tile != withheld;
         if (tile == 0) {
-            st[d] = FLAG_INC | tcount[d];
+            if (publish) st[d] = FLAG_INC | tcount[d];
         } else {
-            st[(size_t)tile * RADIX + d] = FLAG_AGG | tcount[d];
+            if (publish) st[(size_t)tile * RADIX + d] = FLAG_AGG | tcount[d];
             int64_t look = (int64_t)tile - 1;
             uint32_t spins = 0;
             bool done = false;
@@ -173,13 +174,15 @@ __device__ __forceinline__ void onesweep_tile(const uint64_t* __restrict__ kin, 
                     look--;
                     if (flag == FLAG_INC) done = true;
                 }
-                if (stalled && ++spins > SPIN_LIMIT) {
+                if (stalled && ++spins > spin_limit) {
+                    // a predecessor never published: give up (the offsets
+                    // stay within [0, n) but the order is wrong) and say so
                     atomicOr(d_status, SFGPU_STATUS_SPIN);
                     break;
                 }
             }
             __threadfence();
-            st[(size_t)tile * RADIX + d] = FLAG_INC | ((prefix + tcount[d]) & VALUE_MASK);
+            if (publish) st[(size_t)tile * RADIX + d] = FLAG_INC | ((prefix + tcount[d]) & VALUE_MASK);
         }
         toff[d] = base[d] + prefix;
     }
@@ -199,12 +202,13 @@ template <int SORT_ITEMS>
 __global__ void __launch_bounds__(SORT_THREADS) k_onesweep(
     const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint64_t* __restrict__ kout,
     uint32_t* __restrict__ vout, uint32_t n, int shift, const uint32_t* __restrict__ hist,
-    uint32_t* status, uint32_t* counter, uint32_t* d_status, const uint32_t* enable) {
+    uint32_t* status, uint32_t* counter, uint32_t* d_status, const uint32_t* enable, uint32_t spin_limit,
+    uint32_t withheld) {
     if (enable && *enable == 0u) return;
     __shared__ uint32_t s_tile;
     if (threadIdx.x == 0) s_tile = atomicAdd(counter, 1u);
     __syncthreads();
-    onesweep_tile<SORT_ITEMS>(kin, vin, kout, vout, n, shift, hist, status, s_tile, d_status);
+    onesweep_tile<SORT_ITEMS>(kin, vin, kout, vout, n, shift, hist, status, s_tile, d_status, spin_limit, withheld);
 }
 
 // Every pass of the tile sort in one cooperative launch (all tiles resident,
@@ -215,7 +219,8 @@ template <int SORT_ITEMS>
 __global__ void __launch_bounds__(SORT_THREADS) k_onesweep_all(uint64_t* k0, uint32_t* v0, uint64_t* k1,
                                                                uint32_t* v1, uint32_t n, int passes,
                                                                const uint32_t* __restrict__ hist, uint32_t* status,
-                                                               uint32_t* d_status, const uint32_t* enable) {
+                                                               uint32_t* d_status, const uint32_t* enable,
+                                                               uint32_t spin_limit) {
     if (*enable == 0u) return;
     cooperative_groups::grid_group grid = cooperative_groups::this_grid();
     const uint32_t tiles = gridDim.x;
@@ -228,7 +233,8 @@ __global__ void __launch_bounds__(SORT_THREADS) k_onesweep_all(uint64_t* k0, uin
     uint32_t *va = v0, *vb = v1;
     for (int p = 0; p < passes; p++) {
         onesweep_tile<SORT_ITEMS>(ka, va, kb, vb, n, p * RADIX_BITS, hist + p * RADIX,
-                                  status + (size_t)p * tiles * RADIX, blockIdx.x, d_status);
+                                  status + (size_t)p * tiles * RADIX, blockIdx.x, d_status, spin_limit,
+                                  0xFFFFFFFFu);
         grid.sync();
         uint64_t* tk = ka;
         ka = kb;
@@ -527,7 +533,8 @@ int sf_sort_pairs_keep(uint64_t* keys, uint32_t* vals, uint32_t n, int bits, Sor
         SF_CHECK_LAUNCH();
         const int top = passes - 1;
         k_onesweep<4><<<tiles, SORT_THREADS, 0, st>>>(keys, vals, w.keys_b, w.vals_b, n, top * RADIX_BITS,
-                                                      w.hist + top * RADIX, w.status, w.counters, d_status, enable);
+                                                      w.hist + top * RADIX, w.status, w.counters, d_status, enable,
+                                                      w.spin_limit, w.withheld);
         SF_CHECK_LAUNCH();
         k_bucket_sort<<<RADIX, BK_THREADS, bucket_sort_smem(), st>>>(w.keys_b, w.vals_b, keys, vals,
                                                                      w.hist + top * RADIX, top, big, enable);
@@ -546,7 +553,8 @@ int sf_sort_pairs_keep(uint64_t* keys, uint32_t* vals, uint32_t n, int bits, Sor
             uint32_t* ss = w.status + (size_t)tiles * RADIX;
             uint32_t* ds = d_status;
             const uint32_t* en = big;
-            void* args[] = {&k0, &v0, &k1, &v1, &nn, &np, &hh, &ss, &ds, &en};
+            uint32_t sl = w.spin_limit;
+            void* args[] = {&k0, &v0, &k1, &v1, &nn, &np, &hh, &ss, &ds, &en, &sl};
             SF_CUDA(cudaLaunchCooperativeKernel((const void*)k_onesweep_all<4>, dim3(tiles), dim3(SORT_THREADS), args, 0,
                                                 st));
             SF_CHECK_LAUNCH();
@@ -573,13 +581,16 @@ int sf_sort_pairs_keep(uint64_t* keys, uint32_t* vals, uint32_t n, int bits, Sor
         uint32_t* stp = w.status + (size_t)p * tiles * RADIX;
         if (items == 2)
             k_onesweep<2><<<tiles, SORT_THREADS, 0, st>>>(ka, va, kb, vb, n, p * RADIX_BITS, w.hist + p * RADIX, stp,
-                                                          w.counters + p, d_status, enable);
+                                                          w.counters + p, d_status, enable, w.spin_limit,
+                                                          p == 0 ? w.withheld : 0xFFFFFFFFu);
         else if (items == 4)
             k_onesweep<4><<<tiles, SORT_THREADS, 0, st>>>(ka, va, kb, vb, n, p * RADIX_BITS, w.hist + p * RADIX, stp,
-                                                          w.counters + p, d_status, enable);
+                                                          w.counters + p, d_status, enable, w.spin_limit,
+                                                          p == 0 ? w.withheld : 0xFFFFFFFFu);
         else
             k_onesweep<8><<<tiles, SORT_THREADS, 0, st>>>(ka, va, kb, vb, n, p * RADIX_BITS, w.hist + p * RADIX, stp,
-                                                          w.counters + p, d_status, enable);
+                                                          w.counters + p, d_status, enable, w.spin_limit,
+                                                          p == 0 ? w.withheld : 0xFFFFFFFFu);
         SF_CHECK_LAUNCH();
         std::swap(ka, kb);
         std::swap(va, vb);
@@ -600,4 +611,59 @@ int sf_sort_pairs(uint64_t* keys, uint32_t* vals, uint32_t n, int bits, SortWork
         SF_CHECK_LAUNCH();
     }
     return SFGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Failure detection of the bounded look-back wait, without a GPU fault: one
+// 7-bit tile pass over the given keys in which tile `withheld_tile` (0xFFFFFFFF:
+// none) never publishes its look-back words, so the tiles after it wait on a
+// word that nothing sets until `spin_limit` rounds have passed, then set
+// SFGPU_STATUS_SPIN and finish.  With a single pass every scatter offset
+// stays inside [0, n) whatever the wait gave (each tile's prefix can only
+// fall short), so the call completes and the context stays usable; the
+// order is then wrong for the keys after the withheld tile.
+// ---------------------------------------------------------------------------
+extern "C" int sfgpu_sort_withheld_check(const uint64_t* keys, uint32_t n, uint32_t withheld_tile,
+                                         uint32_t spin_limit, uint64_t* sorted, uint32_t* index,
+                                         uint32_t* status) {
+    sf_clear_error();
+    if (!keys || !sorted || !index || !status || n == 0) {
+        sf_set_error("sfgpu_sort_withheld_check: NULL argument or n = 0");
+        return SFGPU_FAILURE;
+    }
+    uint64_t* dk = nullptr;
+    uint32_t* dv = nullptr;
+    uint32_t* ds = nullptr;
+    cudaStream_t st = nullptr;
+    SortWork w;
+    int rc = SFGPU_FAILURE;
+    std::vector<uint32_t> iota(n);
+    for (uint32_t i = 0; i < n; i++) iota[i] = i;
+    do {
+        if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) break;
+        if (cudaMalloc(&dk, sizeof(uint64_t) * n) != cudaSuccess) break;
+        if (cudaMalloc(&dv, sizeof(uint32_t) * n) != cudaSuccess) break;
+        if (cudaMalloc(&ds, sizeof(uint32_t)) != cudaSuccess) break;
+        if (cudaMemcpy(dk, keys, sizeof(uint64_t) * n, cudaMemcpyHostToDevice) != cudaSuccess) break;
+        if (cudaMemcpy(dv, iota.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice) != cudaSuccess) break;
+        if (cudaMemset(ds, 0, sizeof(uint32_t)) != cudaSuccess) break;
+        if (sf_sort_alloc(w, n) != SFGPU_OK) break;
+        w.flags |= SORT_NO_BUCKETS;
+        if (spin_limit) w.spin_limit = spin_limit;
+        w.withheld = withheld_tile;
+        if (sf_sort_pairs(dk, dv, n, RADIX_BITS, w, st, ds) != SFGPU_OK) break;
+        if (cudaStreamSynchronize(st) != cudaSuccess) break;
+        if (cudaMemcpy(sorted, dk, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost) != cudaSuccess) break;
+        if (cudaMemcpy(index, dv, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost) != cudaSuccess) break;
+        if (cudaMemcpy(status, ds, sizeof(uint32_t), cudaMemcpyDeviceToHost) != cudaSuccess) break;
+        rc = SFGPU_OK;
+    } while (0);
+    if (rc != SFGPU_OK && !*sfgpu_last_error())
+        sf_set_error("sfgpu_sort_withheld_check: %s", cudaGetErrorString(cudaGetLastError()));
+    sf_sort_free(w);
+    cudaFree(dk);
+    cudaFree(dv);
+    cudaFree(ds);
+    if (st) cudaStreamDestroy(st);
+    return rc;
 }

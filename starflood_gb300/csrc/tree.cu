@@ -1,9 +1,9 @@
-// tree.cu -- the octree of tree_build (src/tree.c:118-362), built in parallel
+// tree.cu -- the octree of tree_build (src/tree.c:74-318), built in parallel
 // with the reference's exact topology.
 //
 // The reference inserts bodies one at a time; a node splits when its
 // (leaf_cap+1)-th body arrives, the resident bodies move down by "mid < x"
-// (tree.c:289-291) and every later arrival by "mid <= x" (tree.c:327-329),
+// (tree.c:244-247) and every later arrival by "mid <= x" (tree.c:282-285),
 // with mid = 0.5f*(min+max) recomputed per level in FP32.  Hence:
 //
 //  * the node set is {root} plus the 8 children of every cell holding more
@@ -54,7 +54,7 @@ struct Cube {
 __device__ __forceinline__ float midf(float lo, float hi) { return fmul(0.5f, fadd(lo, hi)); }
 
 // Descend `levels` levels of `key` (digits of levels 0..levels-1) from the
-// root cube, reproducing the bounds of the reference's nodes (tree.c:203-207,
+// root cube, reproducing the bounds of the reference's nodes (tree.c:159-163,
 // 263-270, 331-335).
 __device__ Cube cube_of(const float* __restrict__ root, uint64_t key, int levels) {
     Cube c;
@@ -95,7 +95,8 @@ __device__ uint64_t descend(const float x[3], Cube c, uint64_t key, int from, ui
 __global__ void k_keys(const float* __restrict__ pos, const float* __restrict__ mas, uint32_t n,
                        const float* __restrict__ bounds, uint64_t* __restrict__ keys, uint32_t* __restrict__ vals,
                        uint32_t* __restrict__ nin, uint2* __restrict__ ties, uint32_t* __restrict__ tie_count,
-                       uint32_t* __restrict__ mmax, uint32_t* d_status, SortClear sc) {
+                       uint32_t* __restrict__ mmax, uint32_t* __restrict__ nan_in, uint32_t* d_status,
+                       SortClear sc) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     for (uint32_t j = i; j < sc.nhist + sc.ncounters + sc.nstatus; j += gridDim.x * blockDim.x) {
         if (j < sc.nhist) sc.hist[j] = 0u;
@@ -115,11 +116,15 @@ __global__ void k_keys(const float* __restrict__ pos, const float* __restrict__ 
             c.lo[a] = bounds[a];
             c.hi[a] = bounds[3 + a];
         }
-        // tree.c:186-190: closed root cube (NaN coordinates fall outside)
-        inside = (c.lo[0] <= x[0] && x[0] <= c.hi[0]) && (c.lo[1] <= x[1] && x[1] <= c.hi[1]) &&
-                 (c.lo[2] <= x[2] && x[2] <= c.hi[2]);
+        // tree.c:141-146: skipped only when a comparison with the closed
+        // root cube says outside, so a NaN coordinate is inserted: every
+        // midpoint comparison is false and it takes octant 0 at every level
+        // (key 0, the first sorted slot)
+        inside = !(c.lo[0] > x[0] || x[0] > c.hi[0] || c.lo[1] > x[1] || x[1] > c.hi[1] || c.lo[2] > x[2] ||
+                   x[2] > c.hi[2]);
         uint64_t key = KEY_OUT;
         if (inside) {
+            if (isnan(x[0]) || isnan(x[1]) || isnan(x[2])) atomicOr(nan_in, 1u);
             uint32_t tb = 0;
             key = descend(x, c, 0ull, 0, tb);
             if (tb) {
@@ -528,7 +533,7 @@ __global__ void __launch_bounds__(SS_THREADS) k_split_scan(
     const uint64_t* __restrict__ K, uint32_t n, const uint32_t* __restrict__ nin_p, uint32_t leaf_cap,
     uint32_t depth_max, uint32_t* __restrict__ sbase, uint32_t* __restrict__ split_start,
     uint8_t* __restrict__ split_level, uint32_t split_cap, uint32_t* __restrict__ nsplit_p, uint32_t nodes_max,
-    uint32_t* tile_status, uint32_t* ticket, uint32_t* d_status) {
+    uint32_t* tile_status, uint32_t* ticket, uint32_t* d_status, uint32_t spin_limit) {
     __shared__ uint32_t s_tile, s_prefix;
     __shared__ uint32_t wsum[SS_THREADS / 32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -597,7 +602,7 @@ __global__ void __launch_bounds__(SS_THREADS) k_split_scan(
                 prefix += __reduce_add_sync(0xffffffffu, lane < take ? (w & SS_VAL) : 0u);
                 if (fi < fz) break;
                 look -= take;
-                if (fz < 32 && ++spins > (1u << 24)) {
+                if (fz < 32 && ++spins > spin_limit) {
                     if (lane == 0) atomicOr(d_status, SFGPU_STATUS_SPIN);
                     break;
                 }
@@ -621,7 +626,7 @@ __global__ void __launch_bounds__(SS_THREADS) k_split_scan(
         }
         run += c[i];
     }
-    if (tile == ntiles - 1 && threadIdx.x == 0) {  // the total, and tree.c:224's node limit
+    if (tile == ntiles - 1 && threadIdx.x == 0) {  // the total, and tree.c:180's node limit
         const uint32_t total = s_prefix + agg;
         *nsplit_p = total;
         if (1ull + 8ull * (uint64_t)total >= nodes_max || total > split_cap) atomicOr(d_status, SFGPU_STATUS_TREE_NODES);
@@ -782,16 +787,20 @@ __device__ __forceinline__ fix4 slot_prefix(const fix4* __restrict__ pre, const 
     return fix4{a.x + b.x, a.y + b.y, a.z + b.z, a.m + b.m};
 }
 
-// tree.c:346-354: centre of mass = sum(m x) / sum(m), from the exact sums
+// tree.c:302-310: centre of mass = sum(m x) / sum(m), from the exact sums
 // over the sorted slots [s, s + cnt)
 __device__ __forceinline__ float4 node_monopole(uint32_t s, uint32_t cnt, uint32_t n, const uint32_t* __restrict__ mmax,
                                                 const float* __restrict__ bounds, const fix4* __restrict__ msum,
-                                                const fix4* __restrict__ cpre) {
+                                                const fix4* __restrict__ cpre, bool nan_in) {
     if (!cnt) return make_float4(0.f, 0.f, 0.f, 0.f);
     const fix4 a = slot_prefix(msum, cpre, s, n), b = slot_prefix(msum, cpre, s + cnt, n);
     const long long sx = b.x - a.x, sy = b.y - a.y, sz = b.z - a.z, sm = b.m - a.m;
     const FixScale f = fix_scale(n, *mmax, bounds);
     const double m = ldexp((double)sm, -f.km);
+    // bodies with a NaN coordinate hold the first sorted slots (key 0): in
+    // the reference their m x makes every node on their path NaN
+    if (nan_in && s == 0u) return make_float4(__int_as_float(0x7fffffff), __int_as_float(0x7fffffff),
+                                              __int_as_float(0x7fffffff), (float)m);
     if (sm > 0) {
         const double inv = ldexp(1.0 / (double)sm, f.km - f.kx);  // 2^km / (sm 2^kx)
         return make_float4((float)((double)sx * inv), (float)((double)sy * inv), (float)((double)sz * inv),
@@ -816,21 +825,22 @@ __global__ void __launch_bounds__(FILL_THREADS) k_split_fill(const uint64_t* __r
                              const uint8_t* __restrict__ split_level, const float* __restrict__ bounds,
                              uint32_t leaf_cap, uint32_t depth_max, NodeArrays nd, float third,
                              uint32_t* __restrict__ split_node, uint32_t n, const uint32_t* __restrict__ mmax,
-                             const fix4* __restrict__ msum, const fix4* __restrict__ cpre) {
+                             const fix4* __restrict__ msum, const fix4* __restrict__ cpre,
+                             const uint32_t* __restrict__ nan_in_p) {
     __shared__ uint64_t samp[NSAMP];
     const uint32_t ns = min(*nsplit_p, split_cap);
     const uint32_t nin = *nin_p;
     const uint32_t g = blockIdx.x * FILL_THREADS + threadIdx.x;
     const uint32_t s = g >> 3;
     const uint32_t o = g & 7u;
-    if (g == 0) {  // the root record (tree.c:156-159: bounds = the root cube)
+    if (g == 0) {  // the root record (tree.c:112-115: bounds = the root cube)
         Cube r;
         for (int a = 0; a < 3; a++) {
             r.lo[a] = bounds[a];
             r.hi[a] = bounds[3 + a];
         }
         write_node(nd, 0, r, nin, (nin > leaf_cap && depth_max > 0) ? 1u : NODE_NONE, 0u, 0u, third);
-        if (msum) nd.com[0] = node_monopole(0u, nin, n, mmax, bounds, msum, cpre);
+        if (msum) nd.com[0] = node_monopole(0u, nin, n, mmax, bounds, msum, cpre, *nan_in_p != 0u);
     }
     if ((blockIdx.x * FILL_THREADS) / 8u >= ns) return;  // the whole block is past the split nodes
     const KeySamples ks = load_key_samples(K, nin, samp);
@@ -878,13 +888,15 @@ __global__ void __launch_bounds__(FILL_THREADS) k_split_fill(const uint64_t* __r
         fc = sid < split_cap ? 1u + 8u * sid : NODE_NONE;
     }
     write_node(nd, 1u + 8u * s + o, cc, cnt, fc, self, cstart, third);
-    if (msum) nd.com[NODE_REC * (1u + 8u * s + o)] = node_monopole(cstart, cnt, n, mmax, bounds, msum, cpre);
+    if (msum)
+        nd.com[NODE_REC * (1u + 8u * s + o)] = node_monopole(cstart, cnt, n, mmax, bounds, msum, cpre,
+                                                             *nan_in_p != 0u);
 }
 
 // ---- reference-order monopoles (EXACT arithmetic) ----------------------------
 // The reference accumulates each node's sum(m x) and sum(m) in FP32 as bodies
-// arrive (tree.c:210-213, 300-303), i.e. in body-index order over the node's
-// members, then scales by 1/sum(m) (tree.c:346-354).  Reproduced here: every
+// arrive (tree.c:166-169, 256-259), i.e. in body-index order over the node's
+// members, then scales by 1/sum(m) (tree.c:302-310).  Reproduced here: every
 // leaf sorts its members by index; going up one level at a time, every split
 // node merges its eight children's index-ordered lists (children's ranges are
 // adjacent) and adds up its members in that order.
@@ -978,9 +990,11 @@ int sf_tree_alloc(TreeWork** out, uint32_t n, const sfgpu_params& p) {
     SF_CUDA(cudaMalloc(&t->keys, sizeof(uint64_t) * nn));
     SF_CUDA(cudaMalloc(&t->vals, sizeof(uint32_t) * nn));
     if (sf_sort_alloc(t->sort, nn) != SFGPU_OK) return SFGPU_FAILURE;
+    if (p.spin_limit) t->sort.spin_limit = p.spin_limit;
     // counters: [0] bodies inside, [1] ties, [2] moved, [3] split nodes,
     // [4] largest mass bits, [5] gather ticket, [6] split-scan ticket, [7]
-    // unused, then one look-back word per split-scan tile
+    // a body inside the tree has a NaN coordinate, then one look-back word
+    // per split-scan tile
     const size_t ncount = 8 + (nn + SS_TILE - 1) / SS_TILE;
     SF_CUDA(cudaMalloc(&t->counters, sizeof(uint32_t) * ncount));
     SF_CUDA(cudaMemset(t->counters, 0, sizeof(uint32_t) * ncount));
@@ -1052,7 +1066,7 @@ int sf_tree_build(sfgpu_sim* s) {
     int tk = s->timer.begin(st, "tree_keys");
     const SortClear sclr = sf_sort_clear_words(t->sort, n, KEY_BITS);
     k_keys<<<nb, 256, 0, st>>>(pos, mas, n, s->d_bounds, t->keys, t->vals, nin, t->ties, tie_count, t->counters + 4,
-                               s->d_status, sclr);
+                               t->counters + 7, s->d_status, sclr);
     SF_CHECK_LAUNCH();
     s->timer.end(st, tk);
     tk = s->timer.begin(st, "tree_sort");
@@ -1101,14 +1115,15 @@ int sf_tree_build(sfgpu_sim* s) {
     k_split_scan<<<sf_ceil_div(n, SS_TILE), SS_THREADS, 0, st>>>(t->keys, n, nin, s->p.leaf_cap, s->p.depth_max,
                                                                   t->sbase, t->split_start, t->split_level,
                                                                   t->split_cap, nsplit, t->nodes_max,
-                                                                  t->counters + 8, t->counters + 6, s->d_status);
+                                                                  t->counters + 8, t->counters + 6, s->d_status,
+                                                                  t->sort.spin_limit);
     SF_CHECK_LAUNCH();
     if (fork) SF_CUDA(cudaStreamWaitEvent(st, s->ev_join, 0));
     const uint32_t sb = sf_ceil_div((uint64_t)std::max<uint32_t>(t->split_cap, 1) * 8u, FILL_THREADS);
     k_split_fill<<<sb, FILL_THREADS, 0, st>>>(t->keys, nin, t->sbase, nsplit, t->split_cap, t->split_start, t->split_level,
                                      s->d_bounds, s->p.leaf_cap, s->p.depth_max, t->nd, third, t->split_node, n,
                                      t->counters + 4, exact ? nullptr : (const fix4*)t->msum,
-                                     (const fix4*)t->cpre);
+                                     (const fix4*)t->cpre, t->counters + 7);
     SF_CHECK_LAUNCH();
     s->timer.end(st, tk);
     if (exact) {

@@ -9,7 +9,7 @@ constexpr uint32_t NODE_NONE = 0xFFFFFFFFu;
 //   geo    (mid x, mid y, mid z, w*w)       opening test, gravity.c:352-377
 //   lo     (min x, min y, min z, max x)     self test, gravity.c:473-476
 //   hi     (max y, max z, bodies, first child) as raw bits in .z/.w
-//   com    (COM x, COM y, COM z, mass)      monopole, tree.c:346-354
+//   com    (COM x, COM y, COM z, mass)      monopole, tree.c:302-310
 //   parent, start (first sorted body)       export and monopoles
 // Nodes are numbered: root 0; the children of the s-th split node in
 // depth-first preorder are 1+8s .. 8+8s, in octant order.

@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(WALK_THREADS) k_walk(const float4* __restrict_
         const uint32_t v = s_node[w][top];
         const uint32_t M = s_mask[w][top];
         __syncwarp();
-        if (++guard > (1u << 26)) {  // cannot happen for a well-formed tree
+        if (++guard > fc.walk_limit) {  // cannot happen for a well-formed tree under the default limit
             if (lane == 0) atomicOr(d_status, SFGPU_STATUS_WALK);
             break;
         }
@@ -303,7 +303,7 @@ __global__ void __launch_bounds__(WALK_THREADS) k_walk_body(const float4* __rest
             uint32_t v = SPLIT_ == 1 ? first : first + oct;
             uint32_t guard = 0;
             while (true) {
-                if (++guard > (1u << 26)) {
+                if (++guard > fc.walk_limit) {
                     atomicOr(d_status, SFGPU_STATUS_WALK);
                     break;
                 }
@@ -476,6 +476,7 @@ constexpr uint32_t WALK_GROUP_DEFAULT = 16;
 constexpr int GW_WARPS = 4;
 constexpr int GW_THREADS = GW_WARPS * 32;
 constexpr int GW_STACK = 512;
+constexpr int GW_GSTACK = 128;  // sibling-group entries per warp of k_walk_sib
 constexpr int GW_LIST = 112;  // accepted cells whose bounds miss the group box
 constexpr int GW_MIN_BLOCKS = 7;  // resident blocks per SM the register budget is cut for
 constexpr int GW_SLOW = 48;   // accepted cells that may contain a body (self-exclusion test)
@@ -875,7 +876,7 @@ __global__ void __launch_bounds__(GW_THREADS, GW_MIN_BLOCKS) k_walk_group(const 
     __syncwarp();
     uint32_t guard = 0;
     while (top > 0) {
-        if (++guard > (1u << 24)) {
+        if (++guard > fc.walk_limit) {
             if (lane == 0) atomicOr(d_status, SFGPU_STATUS_WALK);
             break;
         }
@@ -1064,6 +1065,276 @@ __global__ void __launch_bounds__(GW_THREADS, GW_MIN_BLOCKS) k_walk_group(const 
     if (KICK) walk_kick_reduce(wk, e);
 }
 
+// The default walk: the group walk above with a stack of sibling groups.
+template <int KIND, int GB, bool STATS, bool KICK = false>
+__global__ void __launch_bounds__(GW_THREADS, GW_MIN_BLOCKS) k_walk_sib(const float4* __restrict__ sp,
+                                                           const uint32_t* __restrict__ V, uint32_t n, NodeArrays nd,
+                                                           ForceConsts fc, float th_lo, float th_hi,
+                                                           float th_acc, float th_open, uint32_t leaf_cap,
+                                                           float4* __restrict__ part,
+                                                           float* __restrict__ acc, float* __restrict__ pot,
+                                                           uint32_t* __restrict__ st_int,
+                                                           uint32_t* __restrict__ st_open,
+                                                           unsigned long long* __restrict__ tot, uint32_t* d_status,
+                                                           WalkKick wk) {
+    __shared__ uint2 s_stk[GW_WARPS][GW_GSTACK];  // sibling groups: (first child, mask)
+    __shared__ __align__(16) float l_xy[GW_WARPS][2 * GW_LIST];
+    __shared__ __align__(16) float l_zm[GW_WARPS][2 * GW_LIST];
+    __shared__ __align__(16) uint32_t l_k[GW_WARPS][GW_LIST];
+    __shared__ uint32_t q_node[GW_WARPS][GW_SLOW];
+    __shared__ uint32_t q_mask[GW_WARPS][GW_SLOW];
+    __shared__ float4 s_body[GW_WARPS][32];
+    __shared__ float4 s_mg[GW_WARPS][32];     // a round's mixed cells: centre and w^2,
+    __shared__ uint32_t s_mm[GW_WARPS][32];   // the bodies walking them,
+    __shared__ uint32_t s_om[GW_WARPS][32];   // and the bodies that open them
+    const int lane = threadIdx.x & 31;
+    const int w = threadIdx.x >> 5;
+    float4* sbd = s_body[w];
+    uint2* stk = s_stk[w];
+    const GroupLists L{l_xy[w], l_zm[w], l_k[w], q_node[w], q_mask[w]};
+    static_assert(GB == 32 || GB == 16 || GB == 8, "8-, 16- or 32-body groups");
+    const uint32_t group = blockIdx.x * GW_WARPS + w;
+    // body slot of the lane (both half-warps hold the same 16 bodies when GB = 16)
+    const int bl = lane & (GB - 1), half = lane / GB;
+    const uint32_t body_bits = GB == 32 ? 0xffffffffu : (1u << GB) - 1u;
+    const uint32_t k = group * (uint32_t)GB + (uint32_t)bl;
+    const bool live = k < n;
+    const uint32_t live_mask = __ballot_sync(0xffffffffu, live) & body_bits;
+    // with the fused kick every warp reaches the block reduction; a warp
+    // past the last body walks nothing
+    if (!live_mask && !KICK) return;
+    const float4 b = sp[live ? k : min(group * (uint32_t)GB, n - 1u)];
+    const float rx = b.x, ry = b.y, rz = b.z, mi = b.w;
+    if (half == 0) sbd[bl] = b;
+    __syncwarp();
+    // bounding box of the group (dead lanes repeat the first body)
+    float bx0 = rx, by0 = ry, bz0 = rz, bx1 = rx, by1 = ry, bz1 = rz;
+    for (int o = 16; o > 0; o >>= 1) {
+        bx0 = fminf(bx0, __shfl_xor_sync(0xffffffffu, bx0, o));
+        by0 = fminf(by0, __shfl_xor_sync(0xffffffffu, by0, o));
+        bz0 = fminf(bz0, __shfl_xor_sync(0xffffffffu, bz0, o));
+        bx1 = fmaxf(bx1, __shfl_xor_sync(0xffffffffu, bx1, o));
+        by1 = fmaxf(by1, __shfl_xor_sync(0xffffffffu, by1, o));
+        bz1 = fmaxf(bz1, __shfl_xor_sync(0xffffffffu, bz1, o));
+    }
+    KSum ax{0.f, 0.f}, ay{0.f, 0.f}, az{0.f, 0.f}, ph{0.f, 0.f};
+    float2 a2x = make_float2(0.f, 0.f), a2y = a2x, a2z = a2x, p2 = a2x;
+    uint32_t n_int = 0, n_open = 0;
+    unsigned long long open_total = 0;
+    int top = 0, count = 0, qcount = 0;
+    auto flush = [&](bool all) {
+        if (all || count > GW_LIST - 36) {
+            // FAST: pad to a multiple of 2 (4 with two half-warps) with
+            // entries no lane takes
+            constexpr int PAD = KIND == WALK_COMP ? 1 : 2 * (32 / GB);
+            const int padded = (count + PAD - 1) / PAD * PAD;
+            if (lane < padded - count) {
+                const int ix = lx_of(count + lane);
+                L.xy[ix] = L.xy[ix + 2] = L.zm[ix] = L.zm[ix + 2] = 0.f;
+                L.msk[count + lane] = 0u;
+            }
+            count = padded;
+            __syncwarp();
+            flush_fast<KIND, GB, STATS>(L, count, bl, half, rx, ry, rz, fc.eps2, a2x, a2y, a2z, p2, ax, ay, az, ph,
+                                        n_int);
+            count = 0;
+            __syncwarp();
+        }
+        if (all || qcount > GW_SLOW - 32) {
+            flush_slow<KIND, GB, STATS>(L, qcount, nd, bl, half, rx, ry, rz, mi, fc.eps2, ax, ay, az, ph, n_int);
+            qcount = 0;
+            __syncwarp();
+        }
+    };
+    // The stack holds groups of 8 siblings (the children of an opened
+    // cell: first child id, mask of the bodies that opened it); a round pops
+    // up to 4 groups, lane l taking child l % 8 of group l / 8, so one push
+    // per opened cell replaces eight.  The root is the first round's only
+    // cell.  A round may push one group per lane: popping ng groups leaves
+    // room when top + 7 ng <= GW_GSTACK.
+    bool root_round = live_mask != 0u;
+    __syncwarp();
+    uint32_t guard = 0;
+    while (root_round || top > 0) {
+        if (++guard > fc.walk_limit) {
+            if (lane == 0) atomicOr(d_status, SFGPU_STATUS_WALK);
+            break;
+        }
+        uint32_t v = 0, M = 0;
+        bool valid = false;
+        if (root_round) {
+            valid = lane == 0;
+            M = live_mask;
+            root_round = false;
+        } else {
+            const int ng = min(4, min(top, (GW_GSTACK - top) / 7));
+            if (ng == 0) {  // no room for children: cannot happen with GW_GSTACK >> 7 x depth x 4
+                if (lane == 0) atomicOr(d_status, SFGPU_STATUS_WALK);
+                break;
+            }
+            if ((lane >> 3) < ng) {
+                const uint2 e = stk[top - 1 - (lane >> 3)];
+                v = e.x + (uint32_t)(lane & 7);
+                M = e.y;
+                valid = true;
+            }
+            top -= ng;
+            __syncwarp();
+        }
+        // 0 drop, 1 accept, 2 open, 3 mixed
+        int kind = 0;
+        bool internal = false;
+        float4 G = make_float4(0.f, 0.f, 0.f, 0.f), H = G, C = G, Lo = G;
+        uint32_t first = NODE_NONE;
+        if (valid) {
+            // the whole node record in one round trip (the monopole half is
+            // needed by every accepted or mixed cell, most of the entries)
+            H = __ldg(&nd.hi[NODE_REC * v]);
+            G = __ldg(&nd.geo[NODE_REC * v]);
+            C = __ldg(&nd.com[NODE_REC * v]);
+            Lo = __ldg(&nd.lo[NODE_REC * v]);
+            const uint32_t bodies = __float_as_uint(H.z);
+            first = __float_as_uint(H.w);
+            internal = bodies > leaf_cap;
+            if (bodies == 0u) {
+                kind = 0;
+            } else if (bodies <= leaf_cap) {
+                kind = 1;
+            } else {
+                open_total += __popc(M);
+                // distances from the cell centre to the group's box (nearest, farthest)
+                const float ex = fmaxf(0.f, fmaxf(bx0 - G.x, G.x - bx1));
+                const float ey = fmaxf(0.f, fmaxf(by0 - G.y, G.y - by1));
+                const float ez = fmaxf(0.f, fmaxf(bz0 - G.z, G.z - bz1));
+                const float fx = fmaxf(fabsf(G.x - bx0), fabsf(G.x - bx1));
+                const float fy = fmaxf(fabsf(G.y - by0), fabsf(G.y - by1));
+                const float fz = fmaxf(fabsf(G.z - bz0), fabsf(G.z - bz1));
+                const float dmin2 = (ex * ex + ey * ey + ez * ez) * (1.0f - 1.0f / 65536.0f);
+                const float dmax2 = (fx * fx + fy * fy + fz * fz) * (1.0f + 1.0f / 65536.0f);
+                if (dmin2 > 0.0f && G.w < th_acc * dmin2) kind = 1;
+                else if (G.w >= th_open * dmax2 && first != NODE_NONE) kind = 2;
+                else kind = 3;
+            }
+        }
+        const uint32_t lt = (1u << lane) - 1u;
+        // mixed cells: the reference's test for each (cell, body) pair of
+        // the masks.  Either one lane per cell loops over its bodies, or the
+        // warp goes through the cells one at a time with one lane per body,
+        // whichever takes fewer rounds.
+        const bool mixed = kind == 3 && first != NODE_NONE;
+        const uint32_t mix_b = __ballot_sync(0xffffffffu, mixed);
+        uint32_t om = 0u;
+        if (mix_b) {
+            constexpr int H = 32 / GB;  // sub-warps, each testing one cell per round
+            const int rounds_cell = (__popc(mix_b) + H - 1) / H;
+            const int rounds_body = __reduce_max_sync(0xffffffffu, mixed ? (uint32_t)__popc(M) : 0u);
+            if (rounds_body <= rounds_cell) {
+                if (mixed) {
+                    uint32_t mm = M;
+                    while (mm) {
+                        const int i = __ffs(mm) - 1;
+                        mm &= mm - 1u;
+                        const float4 bi = sbd[i];
+                        if (opens(G, bi.x, bi.y, bi.z, fc, th_lo, th_hi)) om |= 1u << i;
+                    }
+                }
+            } else {
+                // the mixed cells staged in shared memory in lane order;
+                // sub-warp h tests cell j H + h in round j, one lane per body
+                const int nmix = __popc(mix_b);
+                const int slot = __popc(mix_b & lt);
+                if (mixed) {
+                    s_mg[w][slot] = G;
+                    s_mm[w][slot] = M;
+                }
+                __syncwarp();
+                for (int j0 = 0; j0 < nmix; j0 += H) {  // the same trip count on every lane
+                    const int j = j0 + half;
+                    bool t = false;
+                    if (j < nmix) {
+                        const uint32_t Mj = s_mm[w][j];
+                        t = ((Mj >> bl) & 1u) && opens(s_mg[w][j], rx, ry, rz, fc, th_lo, th_hi);
+                    }
+                    const uint32_t ol = __ballot_sync(0xffffffffu, t);
+                    if (bl == 0 && j < nmix) s_om[w][j] = (ol >> (half * GB)) & body_bits;
+                }
+                __syncwarp();
+                if (mixed) om = s_om[w][slot];
+            }
+        }
+        // accepted cells (all of the mask, or the bodies of a mixed cell
+        // that do not open it) -> lists
+        const uint32_t am = (kind == 1) ? M : ((kind == 3) ? (M & ~om) : 0u);
+        append_cells(L, am, v, C, Lo, H, bx0, by0, bz0, bx1, by1, bz1, lane, count, qcount);
+        if (!STATS) n_int += __popc(am);
+        // children of the cells every body opens, and of the mixed cells
+        // for the bodies that open them: one sibling group each
+        const uint32_t pm = kind == 2 ? M : om;
+        const uint32_t ob = __ballot_sync(0xffffffffu, pm != 0u);
+        if (pm) stk[top + __popc(ob & lt)] = make_uint2(first, pm);
+        top += __popc(ob);
+        __syncwarp();
+        if (STATS) {  // opening tests (internal cells only) attributed to bodies
+            for (int l = 0; l < 32; l++) {
+                const bool il = __shfl_sync(0xffffffffu, internal, l);
+                const uint32_t ml = __shfl_sync(0xffffffffu, M, l);
+                if (il && half == 0 && ((ml >> bl) & 1u)) n_open++;
+            }
+        }
+        flush(false);
+    }
+    flush(true);
+    float sx = ax.s, sy = ay.s, sz = az.s, sw = ph.s;
+    if (KIND == WALK_COMP) {
+        sx -= ax.c;
+        sy -= ay.c;
+        sz -= az.c;
+        sw -= ph.c;
+    } else {
+        sx += a2x.x + a2x.y;
+        sy += a2y.x + a2y.y;
+        sz += a2z.x + a2z.y;
+        sw += p2.x + p2.y;
+    }
+    uint32_t n_int_body = n_int;
+#pragma unroll
+    for (int o = 16; o >= GB; o >>= 1) {  // the sub-warps' shares of the same bodies
+        sx += __shfl_xor_sync(0xffffffffu, sx, o);
+        sy += __shfl_xor_sync(0xffffffffu, sy, o);
+        sz += __shfl_xor_sync(0xffffffffu, sz, o);
+        sw += __shfl_xor_sync(0xffffffffu, sw, o);
+        n_int_body += __shfl_xor_sync(0xffffffffu, n_int_body, o);
+    }
+    ff e[4] = {ff{0.f, 0.f}, ff{0.f, 0.f}, ff{0.f, 0.f}, ff{0.f, 0.f}};
+    if (live && half == 0) {
+        const uint32_t p = V[k];
+        {
+            const float g = -fc.neg_g;
+            const float scale = fc.physical ? g : g * mi;
+            const float a[3] = {scale * sx, scale * sy, scale * sz};
+            acc[3u * p + 0u] = a[0];
+            acc[3u * p + 1u] = a[1];
+            acc[3u * p + 2u] = a[2];
+            pot[p] = fc.neg_g * sw;
+            if (KICK) walk_kick_body(wk, p, mi, a, fc.neg_g * sw, e);
+            if (STATS) {
+                st_int[p] = n_int_body;
+                st_open[p] = n_open;
+            }
+        }
+    }
+    unsigned long long ci = n_int;
+    for (int o = 16; o > 0; o >>= 1) {
+        ci += __shfl_xor_sync(0xffffffffu, ci, o);
+        open_total += __shfl_xor_sync(0xffffffffu, open_total, o);
+    }
+    if (lane == 0) {
+        atomicAdd(&tot[0], ci);
+        atomicAdd(&tot[1], open_total);
+    }
+    if (KICK) walk_kick_reduce(wk, e);
+}
+
 template <int KIND, int GSPLIT, int GB = 32>
 int launch_group(sfgpu_sim* s, bool stats) {
     TreeWork* t = s->tree;
@@ -1115,10 +1386,53 @@ int launch_group(sfgpu_sim* s, bool stats) {
     return SFGPU_OK;
 }
 
+template <int KIND, int GB>
+int launch_sib(sfgpu_sim* s, bool stats) {
+    TreeWork* t = s->tree;
+    const ForceConsts fc = sf_force_consts(s->p);
+    const float th_lo = fc.theta * (1.0f - 1.0f / 524288.0f);
+    const float th_hi = fc.theta * (1.0f + 1.0f / 524288.0f);
+    const float th_acc = fc.theta * (1.0f - 1.0f / 4096.0f);
+    const float th_open = fc.theta * (1.0f + 1.0f / 4096.0f);
+    const uint32_t grid = sf_ceil_div((uint64_t)sf_ceil_div(s->n, GB), GW_WARPS);
+    float* acc = s->slab + (size_t)6 * s->n;
+    float* pot = s->slab + (size_t)10 * s->n;
+    if (stats) {
+        k_walk_sib<KIND, GB, true><<<grid, GW_THREADS, 0, s->stream>>>(
+            t->sp, t->vals, s->n, t->nd, fc, th_lo, th_hi, th_acc, th_open, s->p.leaf_cap, t->walk_part, acc, pot,
+            s->stat_int, s->stat_open, s->walk_tot, s->d_status, WalkKick{});
+    } else if (s->fuse_kick && s->red_cap * 2u >= grid * 4u) {
+        WalkKick wk;
+        wk.vel = s->slab + (size_t)3 * s->n;
+        wk.ken = s->slab + (size_t)11 * s->n;
+        wk.pen = s->slab + (size_t)12 * s->n;
+        wk.vel64 = s->vel64;
+        wk.dt64 = s->p.dt;
+        wk.half_dt = 0.5f * (float)s->p.dt;
+        wk.g_over_eps = (float)(s->p.G / s->p.eps);
+        wk.physical = s->p.acc_mode == SFGPU_ACC_PHYSICAL;
+        wk.part = (double*)s->red;
+        wk.done = s->d_done + 1;
+        wk.sums = s->sums;
+        wk.d_step = s->d_step;
+        k_walk_sib<KIND, GB, false, true><<<grid, GW_THREADS, 0, s->stream>>>(
+            t->sp, t->vals, s->n, t->nd, fc, th_lo, th_hi, th_acc, th_open, s->p.leaf_cap, t->walk_part, acc, pot,
+            nullptr, nullptr, s->walk_tot, s->d_status, wk);
+        s->kicked = true;
+    } else {
+        k_walk_sib<KIND, GB, false><<<grid, GW_THREADS, 0, s->stream>>>(
+            t->sp, t->vals, s->n, t->nd, fc, th_lo, th_hi, th_acc, th_open, s->p.leaf_cap, t->walk_part, acc, pot,
+            nullptr, nullptr, s->walk_tot, s->d_status, WalkKick{});
+    }
+    SF_CHECK_LAUNCH();
+    return SFGPU_OK;
+}
+
 template <int KIND>
 int launch_fast(sfgpu_sim* s, bool stats) {
-    // walk_split: 0 or 32 (default) group walk of walk_group bodies per warp
-    // (0 = the default size, 8, 16 or 32); 1 one thread per body; 8 one
+    // walk_split: 0 (default) group walk of walk_group bodies per warp (0 =
+    // the default size, 8, 16 or 32) with a stack of sibling groups; 32 the
+    // same walk with a stack of single cells; 1 one thread per body; 8 one
     // thread per body and root octant; 64 32-body group walk with the
     // level-2 frontier dealt over 8 warps per group.  The split variants pay
     // for their redundant top levels and imbalance more than they gain.
@@ -1127,9 +1441,14 @@ int launch_fast(sfgpu_sim* s, bool stats) {
     if (split == 8) return launch_body<KIND, SPLIT>(s, stats);
     if (split == 64) return launch_group<KIND, SPLIT>(s, stats);
     const uint32_t gb = s->p.walk_group ? s->p.walk_group : WALK_GROUP_DEFAULT;
-    if (gb == 8) return launch_group<KIND, 1, 8>(s, stats);
-    if (gb == 16) return launch_group<KIND, 1, 16>(s, stats);
-    return launch_group<KIND, 1, 32>(s, stats);
+    if (split == 32) {  // the group walk with a stack of single cells
+        if (gb == 8) return launch_group<KIND, 1, 8>(s, stats);
+        if (gb == 16) return launch_group<KIND, 1, 16>(s, stats);
+        return launch_group<KIND, 1, 32>(s, stats);
+    }
+    if (gb == 8) return launch_sib<KIND, 8>(s, stats);
+    if (gb == 16) return launch_sib<KIND, 16>(s, stats);
+    return launch_sib<KIND, 32>(s, stats);
 }
 
 }  // namespace

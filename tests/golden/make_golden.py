@@ -88,7 +88,7 @@ def tree_uniform():
 
 def tree_ties():
     """Lattice points sitting exactly on cell midpoints, in shuffled order, so
-    that the strict/non-strict octant rule of tree.c:289 vs tree.c:327 and the
+    that the strict/non-strict octant rule of tree.c:244-247 vs tree.c:282-285 and the
     closed-interval self test of gravity.c:473 are exercised."""
     g = np.arange(-4, 4, dtype=np.float32) * np.float32(0.25)
     lat = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)

@@ -77,7 +77,7 @@ def test_defaults_are_reference_config(built_lib):
 
 def test_reference_abi_sizes_when_available():
     """node_t / tree_t / sim_t of the compiled reference have the same sizes."""
-    ref = "/root/reference/src"
+    from oracle.build import REFERENCE_SRC as ref
     if not os.path.isdir(ref):
         pytest.skip("reference sources not present")
     src = r"""
@@ -125,3 +125,34 @@ def test_rejects_empty_and_bad_parameters_before_the_device(built_lib):
         sf.Sim(16, sf.default_params(solver=sf.SOLVER_PP, eps=0.0))
     with pytest.raises(sf.SfgpuError, match="leaf_cap must be in"):
         sf.Sim(16, sf.default_params(solver=sf.SOLVER_TREE, leaf_cap=0))
+
+
+def test_reference_main_links_against_library():
+    """The drop-in at link time: the reference's
+    own main.c, initcond.c, simulation_io.c and log.c, compiled from its
+    sources with SOLVER_VIS off, link against libsfgpu.so in place of the
+    solver objects, and every sim_* / vis_* symbol main.c needs resolves to
+    the library."""
+    from oracle.build import REFERENCE_SRC as ref, REF_VARIANTS, reference_config
+    if not os.path.isfile(os.path.join(ref, "main.c")):
+        pytest.skip("reference sources not present")
+    import starflood_gb300 as sf
+    libdir = os.path.dirname(sf.LIB_PATH)
+    if not os.path.exists(sf.LIB_PATH):
+        pytest.skip("libsfgpu.so not built")
+    with tempfile.TemporaryDirectory() as d:
+        open(os.path.join(d, "config.h"), "w").write(reference_config(REF_VARIANTS["tree_e0.01"]))
+        objs = []
+        for unit in ("main", "initcond", "simulation_io", "log"):
+            o = os.path.join(d, unit + ".o")
+            subprocess.check_call(["gcc", "-std=c99", "-O1", "-fopenmp", "-iquote", d, "-I-", "-I" + ref, "-c",
+                                   os.path.join(ref, unit + ".c"), "-o", o], stderr=subprocess.DEVNULL)
+            objs.append(o)
+        exe = os.path.join(d, "starflood_gpu")
+        subprocess.check_call(["gcc", "-fopenmp", *objs, "-L" + libdir, "-lsfgpu", "-Wl,-rpath," + libdir, "-lm",
+                               "-o", exe])
+        undef = subprocess.check_output(["nm", "-D", "--undefined-only", exe], text=True).split()
+        exported = set(subprocess.check_output(["nm", "-D", "--defined-only", sf.LIB_PATH], text=True).split())
+    wanted = [s for s in undef if s.startswith(("sim_", "tree_", "solve_", "vis_", "grid_"))]
+    assert {"sim_init", "sim_free", "sim_solv", "sim_step", "sim_find"} <= set(wanted)
+    assert all(s in exported for s in wanted), [s for s in wanted if s not in exported]

@@ -190,3 +190,59 @@ def test_adjoint_vs_finite_differences(sf, checkpoint):
             assert abs(g[i, c] - fd) <= 1e-4 * gscale, (which, i, c, g[i, c], fd)
     # the batch is left at the final state
     assert np.all(np.isfinite(fpos))
+
+
+def test_adjoint_c5_ensemble_vs_finite_differences(sf, oracle64):
+    """The batched-adjoint benchmark ensemble itself: 256 uniform spheres
+    with N log-uniform in [1024, 32768], 200 KDK steps at dt = 1e-3,
+    checkpoints every 20 steps.  On its two smallest systems, the gradient of
+    one position and one velocity coordinate each is checked against central
+    finite differences (h = 1e-3) of an FP64 forward integration of that
+    system (the oracle's FP64 build; the systems are independent, so the
+    ensemble loss changes only through that system's mean r^2)."""
+    from starflood_gb300.ics import log_uniform_sizes, uniform_ball
+    sizes = [int(x) for x in log_uniform_sizes(256, 1024, 32768, seed=7)]
+    P, V, M = [], [], []
+    for k, n in enumerate(sizes):
+        a, b_, c = uniform_ball(n, seed=1000 + k)
+        P.append(a)
+        V.append(b_)
+        M.append(c)
+    pos, vel, mas = np.concatenate(P), np.concatenate(V), np.concatenate(M)
+    off = np.concatenate([[0], np.cumsum(sizes)])
+    K, ckpt, dt, eps, h = 200, 20, 1e-3, 0.01, 1e-3
+    p = sf.default_params(solver=sf.SOLVER_PP, eps=eps, dt=dt)
+    with sf.Batch(sizes, p) as b:
+        b.upload(pos, vel, mas)
+        loss, gp, gv = b.grad(K, ckpt)
+    assert np.isfinite(loss) and np.all(np.isfinite(gp)) and np.all(np.isfinite(gv))
+    op = make_params(dt=dt, eps=eps)
+
+    def loss64(x0, v0, m):
+        n = len(m)
+        sim, slab, _ = oracle64.new_sim(n, op)
+        sv = slab_views(slab, n, 13)
+        sv["pos"][:] = x0
+        sv["vel"][:] = v0
+        sv["mas"][:] = m
+        oracle64.sim_solv(op, sim, 0)
+        for t in range(K):
+            oracle64.sim_step(op, sim, t)
+        return float((sv["pos"] ** 2).sum() / n)
+
+    rng = np.random.default_rng(2)
+    for k in np.argsort(sizes)[:2]:
+        s = slice(off[k], off[k + 1])
+        x0, v0, m = pos[s].astype(np.float64), vel[s].astype(np.float64), mas[s].astype(np.float64)
+        gscale = max(np.abs(gp[s]).max(), np.abs(gv[s]).max())
+        i, c = int(rng.integers(sizes[k])), int(rng.integers(3))
+        for which, g in (("pos", gp[s]), ("vel", gv[s])):
+            xp, vp = x0.copy(), v0.copy()
+            arr = xp if which == "pos" else vp
+            arr[i, c] += h
+            lp = loss64(xp, vp, m)
+            arr[i, c] -= 2 * h
+            lm = loss64(xp, vp, m)
+            fd = (lp - lm) / (2 * h)
+            print("C5 adjoint system %d (N=%d) %s[%d,%d]: %.9g fd %.9g" % (k, sizes[k], which, i, c, g[i, c], fd))
+            assert abs(g[i, c] - fd) <= 1e-4 * gscale, (k, which, i, c, g[i, c], fd)

@@ -105,7 +105,7 @@ def test_compat_tree_build_depth_overflow(sf):
         tree.bounds[a] = float(d["bounds"][a])
     pos = np.ascontiguousarray(d["pos"], np.float32)
     mas = np.ascontiguousarray(d["mas"], np.float32)
-    assert L.tree_build(C.byref(tree), len(pos), pos.ctypes.data, mas.ctypes.data) == -1  # tree.c:230-233
+    assert L.tree_build(C.byref(tree), len(pos), pos.ctypes.data, mas.ctypes.data) == -1  # tree.c:186-189
     L.tree_free(C.byref(tree))
 
 

@@ -6,7 +6,7 @@ the COMPENSATED form within 1e-6 of the FP64 oracle."""
 import numpy as np
 import pytest
 
-from conftest import golden
+from conftest import err_summary, golden, per_body_rel
 from oracle.pyoracle import make_params, slab_views
 
 pytestmark = pytest.mark.gpu
@@ -63,6 +63,11 @@ def test_pp_fast_c1(sf, oracle32, oracle64):
     assert rel_l2(v["pot"], d["solv_pot"]) < 1e-6
     a64, p64 = oracle64.pp(d["pos"].astype(np.float64), d["mas"].astype(np.float64), make_params(eps=0.01))
     assert rel_l2(v["acc"], a64) < 1e-5
+    # per-particle relative L2 against the reference (FP32, Kahan) and FP64
+    e32 = per_body_rel(v["acc"], d["solv_acc"])
+    e64 = per_body_rel(v["acc"], a64)
+    print("PP FAST C1 per-body acc err vs FP32 ref", err_summary(e32), "vs FP64", err_summary(e64))
+    assert e32.max() < 1e-5 and e64.max() < 1e-5
     for k in range(int(d["steps"])):
         s.step(k)
     out = slab_views(s.download(), n, 13)
@@ -169,3 +174,104 @@ def test_energies_match_reference_sums(sf, oracle32):
         Tg, Vg = s.energies()
         assert abs(Tg - T) <= 1e-14 * abs(T) and abs(Vg - V) <= 1e-14 * abs(V)
     s.close()
+
+
+@pytest.mark.parametrize("form", ["plain", "compensated"])
+def test_pp_plummer1m_subsample_per_body(sf, oracle64, form):
+    """The N = 1,048,576 Plummer sphere (eps = 0.005) of the PP benchmark:
+    per-particle force error on a seeded 8192-body subsample against the
+    FP64 oracle over all j.  Plain (one FP32 sum over each j-split): every
+    body within 1e-5 of the sum of its terms' magnitudes, median and p99 of
+    |da|/|a| within 5e-6 and 1e-5; compensated: every body within 1e-6 of
+    |a|."""
+    from starflood_gb300.ics import plummer
+    n = 1 << 20
+    pos, vel, mas = plummer(n, seed=5)
+    sub = np.sort(np.random.default_rng(8192).choice(n, 8192, replace=False)).astype(np.uint32)
+    a64, _, mag = oracle64.pp_subset(pos.astype(np.float64), mas.astype(np.float64), sub, make_params(eps=0.005),
+                                     with_mag=True)
+    f = sf.FORM_PLAIN if form == "plain" else sf.FORM_COMPENSATED
+    p = sf.default_params(solver=sf.SOLVER_PP, eps=0.005, form=f)
+    with sf.Sim(n, p) as s:
+        s.set_state(pos, vel, mas)
+        s.solve(0)
+        v = slab_views(s.download(), n, 13)
+    e = per_body_rel(v["acc"][sub], a64)
+    e_mag = np.linalg.norm(v["acc"][sub].astype(np.float64) - a64, axis=1) / mag
+    print("PP N=1M %s per-body acc err vs FP64" % form, err_summary(e), "over sum|terms|", err_summary(e_mag),
+          "global", rel_l2(v["acc"][sub], a64))
+    if form == "plain":
+        # FP32 sums over 1M terms: within 1e-5 of the terms' magnitudes
+        assert e_mag.max() < 1e-5 and np.median(e) < 5e-6 and np.quantile(e, 0.99) < 1e-5
+    else:
+        assert e.max() < 1e-6
+
+
+@pytest.mark.parametrize("form", ["plain", "compensated"])
+def test_energies_corrected_vs_fp64(sf, form):
+    """sfgpu_energies_corrected after a step: T = sum v^2 / 2 (the kinetic
+    term of the reference's m_i-scaled dynamics) and V = (1/2) sum_{i != j}
+    -G m_i m_j / sqrt(r^2 + eps^2) (each pair once, no self term; the
+    reference's V, simulation.c:449-451, has neither), against FP64 sums of
+    the downloaded state."""
+    from starflood_gb300.ics import uniform_ball
+    n = 4096
+    pos, vel, mas = uniform_ball(n, seed=31)
+    f = sf.FORM_PLAIN if form == "plain" else sf.FORM_COMPENSATED
+    p = sf.default_params(solver=sf.SOLVER_PP, eps=0.01, dt=1e-3, form=f)
+    with sf.Sim(n, p) as s:
+        s.set_state(pos, vel, mas)
+        s.solve(0)
+        s.step(0)
+        T, V, E = s.energies_corrected()
+        v = slab_views(s.download(), n, 13)
+    x = v["pos"].astype(np.float64)
+    m = v["mas"].astype(np.float64)
+    T64 = 0.5 * (v["vel"].astype(np.float64) ** 2).sum()
+    d = x[:, None, :] - x[None, :, :]
+    inv = 1.0 / np.sqrt((d * d).sum(-1) + 0.01 ** 2)
+    np.fill_diagonal(inv, 0.0)
+    V64 = -0.5 * (m[:, None] * m[None, :] * inv).sum()
+    assert abs(T - T64) <= 1e-7 * abs(T64), (T, T64)
+    assert abs(V - V64) <= 1e-6 * abs(V64), (V, V64)
+    assert abs(E - (T + V)) <= 1e-15 * abs(T - V)
+
+
+@pytest.mark.parametrize("solver", ["pp", "tree"])
+def test_compensated_trajectory_vs_fp64_oracle(sf, oracle64, solver):
+    """20 KDK steps of the precision form (compensated forces, FP64
+    positions and velocities) against 20 steps of the FP64 oracle, beside
+    the plain FP32 form: per-body relative position and velocity errors."""
+    from starflood_gb300.ics import uniform_ball
+    n, steps = 4096, 20
+    pos, vel, mas = uniform_ball(n, seed=17)
+    tree = solver == "tree"
+    op = make_params(dt=1e-3, eps=0.01, theta=0.5, use_tree=1 if tree else 0)
+    osim, oslab, _ = oracle64.new_sim(n, op)
+    ov = slab_views(oslab, n, 13)
+    ov["pos"][:] = pos
+    ov["vel"][:] = vel
+    ov["mas"][:] = mas
+    oracle64.sim_solv(op, osim, 0)
+    for k in range(steps):
+        oracle64.sim_step(op, osim, k)
+    errs = {}
+    for form in (sf.FORM_PLAIN, sf.FORM_COMPENSATED):
+        p = sf.default_params(solver=sf.SOLVER_TREE if tree else sf.SOLVER_PP, eps=0.01, dt=1e-3, theta=0.5,
+                              form=form)
+        with sf.Sim(n, p) as s:
+            s.set_state(pos, vel, mas)
+            s.solve(0)
+            s.run(0, steps)
+            v = slab_views(s.download(), n, 13)
+        errs[form] = (per_body_rel(v["pos"], ov["pos"]), per_body_rel(v["vel"], ov["vel"]))
+        print(solver, "form", form, "pos", err_summary(errs[form][0]), "vel", err_summary(errs[form][1]))
+    ep, ev = errs[sf.FORM_COMPENSATED]
+    pp_, pv_ = errs[sf.FORM_PLAIN]
+    if not tree:
+        assert ep.max() < 1e-7 and ev.max() < 1e-6
+        assert np.median(ep) <= np.median(pp_) and np.median(ev) <= np.median(pv_)
+    else:
+        # the FP64 oracle builds its tree in FP64: opening decisions within
+        # rounding of theta may differ, so the bound is on the bulk
+        assert np.quantile(ep, 0.99) < 1e-6 and np.median(ev) < 1e-6

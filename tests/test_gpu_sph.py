@@ -1,15 +1,22 @@
 """SPH on the GPU against the oracle (GPU only).
 
-Reference SPH (sph.c): neighbour sets of the momentum pass bit-identical
-(per-body counts); densities, pressures and accelerations within 1e-5 global
-relative L2 (the exponentials are CUDA's expf, not the host libm's)."""
+Reference SPH (sph.c, mode A): the momentum pass's neighbour sets are the
+reference's bit for bit, compared as per-body counts and order-independent
+set hashes against the brute-force FP32 enumeration; densities, pressures and
+accelerations within 1e-5 (the exponentials are CUDA's expf, not the host
+libm's).  Cubic-spline SPH (mode B): neighbour sets (counts and hashes)
+bit-identical to the brute-force FP32 enumeration, physics against the FP64
+restatement.  Both at the 262,144-body Plummer configuration on an
+i-subsample with all j."""
 import numpy as np
 import pytest
 
-from conftest import golden
+from conftest import err_summary, golden, neighbour_sets_fp32, per_body_rel
 from oracle.pyoracle import make_params, slab_views
 
 pytestmark = pytest.mark.gpu
+
+PI15 = np.pi ** 1.5
 
 
 @pytest.fixture(scope="module")
@@ -29,17 +36,22 @@ def test_sph_reference_golden(sf, oracle32, math):
     d = golden("tree_sph_plummer_n1024_h0.05_2steps.npz")
     n = len(d["pos"])
     p = sf.default_params(solver=sf.SOLVER_TREE, sph=sf.SPH_REFERENCE, eps=0.01, dt=5e-4, theta=0.5,
-                          math=sf.MATH_EXACT if math == "exact" else sf.MATH_FAST)
+                          math=sf.MATH_EXACT if math == "exact" else sf.MATH_FAST, flags=sf.FLAG_STATS)
     with sf.Sim(n, p) as s:
         s.set_state(d["pos"], d["vel"], d["mas"], d["rad"])
         s.solve(0)
         v = slab_views(s.download(), n, 16)
         nb = s.sph_neighbours()
+        hs = s.sph_neighbour_hashes()
         _, _, _, onb = oracle32.sph_reference(d["pos"], d["mas"], d["rad"])
         np.testing.assert_array_equal(nb, onb)
+        cnt, hsh = neighbour_sets_fp32(d["pos"], np.arange(n), "ref")
+        np.testing.assert_array_equal(nb, cnt)
+        np.testing.assert_array_equal(hs, hsh)
         assert rel_l2(v["rho"], d["solv_rho"]) < 1e-5
         assert rel_l2(v["prs"], d["solv_prs"]) < 1e-5
         assert rel_l2(v["acc"], d["solv_acc"]) < 1e-5
+        assert np.quantile(per_body_rel(v["rho"], d["solv_rho"]), 0.99) < 1e-5
         for k in range(int(d["steps"])):
             s.step(k)
         out = slab_views(s.download(), n, 16)
@@ -48,14 +60,17 @@ def test_sph_reference_golden(sf, oracle32, math):
         assert rel_l2(out["rho"], ref["rho"]) < 1e-5
 
 
-def test_sph_reference_standalone_pp(sf, oracle32):
-    """solve_sph alone on top of PP gravity, ragged N."""
+@pytest.mark.parametrize("hbig", [False, True])
+def test_sph_reference_standalone_pp(sf, oracle32, hbig):
+    """solve_sph alone on top of PP gravity, ragged N, per-body smoothing
+    lengths.  With h up to 0.2 the density's exp cutoff (9.4 h) reaches past
+    the grid's 4 cells, so the FAST density takes the all-pairs tiles."""
     from starflood_gb300.ics import plummer
     n = 3001
     pos, vel, mas = plummer(n, seed=41)
     rad = np.full(n, 0.05, np.float32)
-    rad[::7] = 0.08  # per-body smoothing lengths
-    p = sf.default_params(solver=sf.SOLVER_PP, sph=sf.SPH_REFERENCE, eps=0.01)
+    rad[::7] = 0.2 if hbig else 0.08
+    p = sf.default_params(solver=sf.SOLVER_PP, sph=sf.SPH_REFERENCE, eps=0.01, flags=sf.FLAG_STATS)
     with sf.Sim(n, p) as s:
         s.set_state(pos, vel, mas, rad)
         s.gravity_part()
@@ -64,10 +79,97 @@ def test_sph_reference_standalone_pp(sf, oracle32):
         s.solve_sph()
         v = slab_views(s.download(), n, 16)
         nb = s.sph_neighbours()
+        hs = s.sph_neighbour_hashes()
     rho, prs, acc, onb = oracle32.sph_reference(pos, mas, rad, acc_in=grav)
     np.testing.assert_array_equal(nb, onb)
+    cnt, hsh = neighbour_sets_fp32(pos, np.arange(n), "ref")
+    np.testing.assert_array_equal(hs, hsh)
     assert rel_l2(v["rho"], rho) < 1e-5
     assert rel_l2(v["acc"] - grav, acc - grav) < 1e-5
+
+
+def _ref_rho64(pos, mas, rad, ii):
+    x = pos.astype(np.float64)
+    h = rad.astype(np.float64)
+    m = mas.astype(np.float64)
+    out = np.zeros(len(ii))
+    for a in range(0, len(ii), 16):
+        sel = ii[a:a + 16]
+        d = x[sel][:, None, :] - x[None, :, :]
+        r2 = (d * d).sum(-1)
+        wi = (1.0 / (np.sqrt(np.pi) * h[sel]))[:, None] ** 3 * np.exp(-r2 / (h[sel] ** 2)[:, None])
+        wj = (1.0 / (np.sqrt(np.pi) * h))[None, :] ** 3 * np.exp(-r2 / (h ** 2)[None, :])
+        out[a:a + 16] = (0.5 * (wi + wj) * m[None, :]).sum(1)
+    return out
+
+
+def _ref_acc64(pos, mas, rad, rho, prs, ii, sets):
+    """sph.c:172-277 in FP64 for bodies ii over their neighbour sets (given
+    as boolean rows), with rho / P of every body taken as inputs; also the
+    sum of |term| per body, the scale of its rounding error."""
+    x = pos.astype(np.float64)
+    h = rad.astype(np.float64)
+    r64, p64 = rho.astype(np.float64), prs.astype(np.float64)
+    con = np.where(r64 * r64 > 0, p64 / np.where(r64 > 0, r64 * r64, 1.0), 0.0)
+    out = np.zeros((len(ii), 3))
+    mag = np.zeros(len(ii))
+    for a, i in enumerate(ii):
+        j = np.nonzero(sets[a])[0]
+        d = x[i][None, :] - x[j]
+        r2 = (d * d).sum(-1)
+        ni = -2.0 * np.exp(-r2 / h[i] ** 2) / (PI15 * h[i] ** 5)
+        nj = -2.0 * np.exp(-r2 / h[j] ** 2) / (PI15 * h[j] ** 5)
+        t = ((con[i] + con[j]) * 0.5 * (ni + nj))[:, None] * d
+        out[a] = -float(mas[i]) * t.sum(0)
+        mag[a] = float(mas[i]) * np.abs(t).sum()
+    return out, mag
+
+
+def _ref_sets(pos, ii):
+    pos = np.asarray(pos, np.float32)
+    out = np.zeros((len(ii), len(pos)), bool)
+    for a in range(0, len(ii), 32):
+        d = pos[ii[a:a + 32]][:, None, :] - pos[None, :, :]
+        r2 = (d[..., 0] * d[..., 0] + d[..., 1] * d[..., 1]) + d[..., 2] * d[..., 2]
+        out[a:a + 32] = r2 <= np.float32(1.0)
+    return out
+
+
+def test_sph_reference_plummer262144_subsample(sf):
+    """Mode A at N = 262,144 (Plummer a = 1, h = 0.05), FAST (the cell-grid
+    search): the neighbour sets of a seeded 256-body subsample equal the
+    brute-force FP32 enumeration over all bodies (counts and hashes); their
+    densities are within 1e-5 per body of the FP64 all-pairs sum, and their
+    accelerations within 1e-5 per body of the FP64 momentum sum over the
+    same sets (scaled by the body's sum of |terms|)."""
+    from starflood_gb300.ics import plummer
+    n = 1 << 18
+    pos, vel, mas = plummer(n, seed=7)
+    rad = np.full(n, 0.05, np.float32)
+    p = sf.default_params(solver=sf.SOLVER_PP, sph=sf.SPH_REFERENCE, eps=0.01, flags=sf.FLAG_STATS)
+    with sf.Sim(n, p) as s:
+        s.set_state(pos, vel, mas, rad)
+        s.solve_sph()
+        v = slab_views(s.download(), n, 16)
+        nb = s.sph_neighbours()
+        hs = s.sph_neighbour_hashes()
+        assert s.status() == 0
+    ii = np.sort(np.random.default_rng(262144).choice(n, 256, replace=False))
+    cnt, hsh = neighbour_sets_fp32(pos, ii, "ref")
+    np.testing.assert_array_equal(nb[ii], cnt)
+    np.testing.assert_array_equal(hs[ii], hsh)
+    rho64 = _ref_rho64(pos, mas, rad, ii)
+    e_rho = per_body_rel(v["rho"][ii], rho64)
+    print("mode A rho per-body rel err", err_summary(e_rho))
+    assert e_rho.max() < 1e-5
+    np.testing.assert_array_equal(v["prs"][ii], (np.float32(0.1) * v["rho"][ii]) ** 2)
+    acc64, mag = _ref_acc64(pos, mas, rad, v["rho"], v["prs"], ii, _ref_sets(pos, ii))
+    # bodies whose neighbours all lie beyond 9.4 h have only subnormal terms
+    # (the GPU leaves them out): the 1e-30 floor keeps them from dividing 0 by 0
+    e_acc = np.linalg.norm(v["acc"][ii] - acc64, axis=1) / (mag + 1e-30)
+    print("mode A acc per-body err / sum|terms|", err_summary(e_acc),
+          "plain per-body rel", err_summary(per_body_rel(v["acc"][ii], acc64)))
+    assert e_acc.max() < 1e-5
 
 
 def _cubic_sim(sf, n, pos, vel, mas, rad, u, **kw):
@@ -82,8 +184,10 @@ def _cubic_sim(sf, n, pos, vel, mas, rad, u, **kw):
 @pytest.mark.parametrize("path", [0, 1])
 @pytest.mark.parametrize("n,hvar", [(4096, False), (3000, True)])
 def test_sph_cubic_vs_fp64_oracle(sf, oracle64, n, hvar, path):
-    """Cubic-spline SPH: neighbour sets bit-identical to the brute-force FP32
-    enumeration; rho, dv/dt, du/dt within 1e-5 / 1e-4 of the FP64 oracle."""
+    """Cubic-spline SPH: neighbour sets (counts and hashes) bit-identical to
+    the brute-force FP32 enumeration; rho, dv/dt, du/dt within 1e-5 / 1e-4
+    of the FP64 oracle.  path 0: side-h cells with row culling; 1: the 27
+    side-2h cells."""
     from starflood_gb300.ics import plummer
     pos, vel, mas = plummer(n, seed=51)
     pos = pos * np.float32(0.3)  # denser: ~30 neighbours per body at h = 0.05
@@ -92,21 +196,134 @@ def test_sph_cubic_vs_fp64_oracle(sf, oracle64, n, hvar, path):
         rad[::5] = 0.07
     u = np.full(n, 0.05, np.float32)
     u[::3] = 0.08
-    with _cubic_sim(sf, n, pos, vel, mas, rad, u, sph_path=path) as s:
+    with _cubic_sim(sf, n, pos, vel, mas, rad, u, sph_path=path, flags=sf.FLAG_STATS) as s:
         s.gravity_part()
         s.sync()
         grav = slab_views(s.download(), n, 16)["acc"].copy()
         s.solve_sph()
         v = slab_views(s.download(), n, 16)
         nb = s.sph_neighbours()
+        hs = s.sph_neighbour_hashes()
         _, dudt = s.sph_get_u()
     rho, prs, acc, odu, onb = oracle64.sph_cubic(pos, vel, mas, rad, u)
     np.testing.assert_array_equal(nb, onb)
+    cnt, hsh = neighbour_sets_fp32(pos, np.arange(n), "cubic", rad)
+    np.testing.assert_array_equal(nb, cnt)
+    np.testing.assert_array_equal(hs, hsh)
     assert nb.mean() > 5
     assert rel_l2(v["rho"], rho) < 1e-5
+    assert per_body_rel(v["rho"], rho).max() < 1e-5
     assert rel_l2(v["prs"], prs) < 1e-5
     assert rel_l2(v["acc"] - grav, acc) < 1e-4
     assert rel_l2(dudt, odu) < 1e-4
+
+
+def _w(r, h):
+    q = r / h
+    s = 1.0 / (np.pi * h ** 3)
+    return np.where(q < 1, s * (1 - 1.5 * q * q + 0.75 * q ** 3), np.where(q < 2, s * 0.25 * (2 - q) ** 3, 0.0))
+
+
+def _dw(r, h):
+    q = r / h
+    s = 1.0 / (np.pi * h ** 4)
+    return np.where(q < 1, s * (-3 * q + 2.25 * q * q), np.where(q < 2, s * (-0.75 * (2 - q) ** 2), 0.0))
+
+
+def test_sph_cubic_plummer262144_subsample(sf):
+    """Mode B at its benchmark configuration (N = 262,144 Plummer gas, h =
+    0.05, u0 = 0.05, gamma 5/3, alpha 1, beta 2): the neighbour sets of a
+    seeded 256-body subsample equal the brute-force FP32 enumeration over
+    all bodies (counts and hashes); density within 1e-5 per body of the FP64
+    sum over the same sets; dv/dt and du/dt within 1e-4 per body of the FP64
+    sums (given every body's rho and P), scaled by the body's sum of
+    |terms|."""
+    from starflood_gb300.ics import plummer
+    n = 1 << 18
+    pos, vel, mas = plummer(n, seed=7)
+    rad = np.full(n, 0.05, np.float32)
+    u = np.full(n, 0.05, np.float32)
+    g, al, be = 5.0 / 3.0, 1.0, 2.0
+    with _cubic_sim(sf, n, pos, vel, mas, rad, u, flags=sf.FLAG_STATS) as s:
+        s.solve_sph()
+        v = slab_views(s.download(), n, 16)
+        nb = s.sph_neighbours()
+        hs = s.sph_neighbour_hashes()
+        _, dudt = s.sph_get_u()
+        assert s.status() == 0
+    ii = np.sort(np.random.default_rng(7).choice(n, 256, replace=False))
+    cnt, hsh = neighbour_sets_fp32(pos, ii, "cubic", rad)
+    np.testing.assert_array_equal(nb[ii], cnt)
+    np.testing.assert_array_equal(hs[ii], hsh)
+    x = pos.astype(np.float64)
+    vv = vel.astype(np.float64)
+    rho = v["rho"].astype(np.float64)
+    P = v["prs"].astype(np.float64)
+    c = np.sqrt(g * (g - 1) * u.astype(np.float64))
+    h = rad.astype(np.float64)
+    m = mas.astype(np.float64)
+    p32 = np.asarray(pos, np.float32)
+    rho64 = np.zeros(len(ii))
+    acc64, du64 = np.zeros((len(ii), 3)), np.zeros(len(ii))
+    amag, dmag = np.zeros(len(ii)), np.zeros(len(ii))
+    for a, i in enumerate(ii):
+        d32 = p32[i][None, :] - p32
+        r2f = (d32[:, 0] * d32[:, 0] + d32[:, 1] * d32[:, 1]) + d32[:, 2] * d32[:, 2]
+        s2 = np.float32(2.0) * np.maximum(rad[i], rad)
+        j = np.nonzero(r2f < s2 * s2)[0]
+        d = x[i][None, :] - x[j]
+        r = np.sqrt((d * d).sum(-1))
+        rho64[a] = (m[j] * 0.5 * (_w(r, h[i]) + _w(r, h[j]))).sum()
+        k = j != i
+        j, d, r = j[k], d[k], r[k]
+        gg = 0.5 * (_dw(r, h[i]) + _dw(r, h[j])) / r
+        vr = ((vv[i][None, :] - vv[j]) * d).sum(-1)
+        hb = 0.5 * (h[i] + h[j])
+        mu = hb * vr / (r * r + 0.01 * hb * hb)
+        pi_ij = np.where(vr < 0, (-al * 0.5 * (c[i] + c[j]) * mu + be * mu * mu) / (0.5 * (rho[i] + rho[j])), 0.0)
+        f = m[j] * (P[i] / rho[i] ** 2 + P[j] / rho[j] ** 2 + pi_ij) * gg
+        acc64[a] = -(f[:, None] * d).sum(0)
+        amag[a] = np.abs(f[:, None] * d).sum()
+        t = m[j] * (P[i] / rho[i] ** 2 + 0.5 * pi_ij) * gg * vr
+        du64[a] = t.sum()
+        dmag[a] = np.abs(t).sum()
+    e_rho = per_body_rel(v["rho"][ii], rho64)
+    # bodies with no neighbour but themselves have no terms: the 1e-30 floor
+    e_acc = np.linalg.norm(v["acc"][ii] - acc64, axis=1) / (amag + 1e-30)
+    e_du = np.abs(dudt[ii] - du64) / (dmag + 1e-30)
+    print("mode B rho", err_summary(e_rho), "acc / sum|terms|", err_summary(e_acc), "du/dt", err_summary(e_du))
+    assert e_rho.max() < 1e-5
+    assert e_acc.max() < 1e-4
+    assert e_du.max() < 1e-4
+
+
+@pytest.mark.parametrize("mode", ["reference", "cubic"])
+def test_sph_far_body_sets_cell_status(sf, mode):
+    """A body beyond the cell grid's 2^20 cells per axis is reported through
+    SFGPU_STATUS_SPH_CELLS; every neighbour set, the far body's own (itself
+    only) included, is still exact."""
+    from starflood_gb300.ics import plummer
+    n = 2000
+    pos, vel, mas = plummer(n, seed=3)
+    pos = pos * np.float32(0.3)
+    pos[17] = (3.0e6, -1.0, 0.5)
+    rad = np.full(n, 0.05, np.float32)
+    u = np.full(n, 0.05, np.float32)
+    if mode == "reference":
+        p = sf.default_params(solver=sf.SOLVER_PP, sph=sf.SPH_REFERENCE, eps=0.01, flags=sf.FLAG_STATS)
+        s = sf.Sim(n, p)
+        s.set_state(pos, vel, mas, rad)
+    else:
+        s = _cubic_sim(sf, n, pos, vel, mas, rad, u, flags=sf.FLAG_STATS)
+    with s:
+        s.solve_sph()
+        nb = s.sph_neighbours()
+        hs = s.sph_neighbour_hashes()
+        assert s.status() & sf.STATUS_SPH_CELLS
+    cnt, hsh = neighbour_sets_fp32(pos, np.arange(n), "ref" if mode == "reference" else "cubic", rad)
+    np.testing.assert_array_equal(nb, cnt)
+    np.testing.assert_array_equal(hs, hsh)
+    assert nb[17] == 1
 
 
 def test_sph_cubic_with_tree_steps(sf):

@@ -8,7 +8,7 @@ the reference."""
 import numpy as np
 import pytest
 
-from conftest import golden
+from conftest import err_summary, golden, per_body_rel
 from oracle.pyoracle import make_params, slab_views
 
 pytestmark = pytest.mark.gpu
@@ -150,9 +150,9 @@ def test_tree_node_overflow_flag(sf):
         assert s.status() & sf.STATUS_TREE_NODES
 
 
-def test_tree_outside_and_nan_bodies(sf, oracle32):
-    """Bodies outside the root cube (and NaN) are left out of the tree but
-    still receive forces (tree.c:186-190)."""
+def test_tree_outside_bodies(sf, oracle32):
+    """Bodies outside the root cube are left out of the tree but still
+    receive forces (tree.c:141-146)."""
     from starflood_gb300.ics import uniform_ball
     n = 3000
     pos, vel, mas = uniform_ball(n, seed=6)
@@ -172,11 +172,62 @@ def test_tree_outside_and_nan_bodies(sf, oracle32):
     np.testing.assert_array_equal(v["pot"], pt)
 
 
+@pytest.mark.parametrize("math", ["exact", "fast"])
+def test_tree_nan_body(sf, oracle32, math):
+    """A NaN coordinate is not skipped by the reference's root-cube test
+    (every comparison with NaN is false, tree.c:141-146): the body is
+    inserted, takes octant 0 at every level (tree.c:244-247, 282-285) and
+    makes the centre of mass of every node on its path NaN.  Built in an
+    explicit root cube (a NaN would also poison the mean radius), the GPU
+    tree has the reference's node count and membership; EXACT forces and
+    potentials are bit-identical (NaN where the reference has NaN); FAST
+    has NaN exactly where the reference has NaN and the per-body
+    interaction counts of every finite body.  The NaN reaches every body
+    here: a leaf is never opened, so every walk meets the NaN body's leaf or
+    one of its ancestors."""
+    from starflood_gb300.ics import uniform_ball
+    n = 3000
+    pos, vel, mas = uniform_ball(n, seed=9)
+    pos[11, 1] = np.nan
+    bounds = np.array([-1.5, -1.5, -1.5, 1.5, 1.5, 1.5], np.float32)
+    p = sf.default_params(solver=sf.SOLVER_TREE, eps=0.01, theta=0.5, flags=sf.FLAG_STATS,
+                          math=sf.MATH_EXACT if math == "exact" else sf.MATH_FAST)
+    op = make_params(eps=0.01, theta=0.5, use_tree=1)
+    st, nodes = oracle32.tree_build(pos, mas, bounds, op)
+    assert st == 0 and nodes[0]["bodies"] == n
+    a, pt, stats = oracle32.walk(pos, mas, nodes, op)
+    # every body meets the NaN leaf (a leaf is never opened) or one of its
+    # ancestors, so the reference's forces are all NaN
+    assert np.isnan(a).all(axis=1).all()
+    with sf.Sim(n, p) as s:
+        s.set_state(pos, vel, mas)
+        s.tree_build(bounds)
+        assert s.num_nodes() == len(nodes)
+        check_membership(s, nodes, n)
+        s.gravity_tree()
+        v = slab_views(s.download(), n, 13)
+        ni, no = s.walk_stats()
+    if math == "exact":
+        np.testing.assert_array_equal(v["acc"], a)
+        np.testing.assert_array_equal(v["pot"], pt)
+        np.testing.assert_array_equal(ni, stats[:, 0])
+    else:
+        np.testing.assert_array_equal(np.isnan(v["acc"]), np.isnan(a))
+        np.testing.assert_array_equal(np.isnan(v["pot"]), np.isnan(pt))
+        fin = np.isfinite(pos).all(1)
+        np.testing.assert_array_equal(ni[fin], stats[fin, 0])
+
+
 @pytest.mark.parametrize("split,group", [(0, 0), (0, 8), (0, 16), (0, 32), (1, 0), (8, 0), (64, 0)])
 @pytest.mark.parametrize("n,seed", [(65536, 2), (20000, 8)])
-def test_tree_fast_large(sf, oracle32, n, seed, split, group):
+def test_tree_fast_large(sf, oracle32, oracle64, n, seed, split, group):
     """FAST walks (group walk of 8, 16, 32 bodies; one thread per body; per
-    body and root octant; 32-body groups split over 8 warps)."""
+    body and root octant; 32-body groups split over 8 warps).  Per body:
+    |a_i - a_ref,i| within 1e-5 of sum_k |F_k| (the magnitudes of its
+    terms; |a_i| itself unless they cancel), or within twice the reference's
+    own FP32 error (its insertion-order centre-of-mass sums, against the
+    FP64 oracle on the same root cube) where that is larger; median and p99
+    of |a_i - a_ref,i| / |a_i| below 1e-6 and 1e-5."""
     from starflood_gb300.ics import uniform_ball, plummer
     gen = uniform_ball if n == 65536 else plummer
     pos, vel, mas = gen(n, seed=seed)
@@ -190,10 +241,29 @@ def test_tree_fast_large(sf, oracle32, n, seed, split, group):
         ni, no = s.walk_stats()
     op = make_params(eps=0.01, theta=0.5, use_tree=1)
     st, nodes = oracle32.tree_build(pos, mas, oracle32.root_bounds(pos, 5), op)
-    a, pt, stats = oracle32.walk(pos, mas, nodes, op)
+    a, pt, stats, mag = oracle32.walk(pos, mas, nodes, op, with_mag=True)
     np.testing.assert_array_equal(ni, stats[:, 0])
     assert rel_l2(v["acc"], a) < 1e-5
     assert rel_l2(v["pot"], pt) < 1e-5
+    # per-particle bounds: on every body, not on the ensemble
+    e = per_body_rel(v["acc"], a)
+    ep = per_body_rel(v["pot"], pt)
+    b = oracle32.root_bounds(pos, 5).astype(np.float64)
+    op64 = make_params(eps=0.01, theta=0.5, use_tree=1)
+    st64, nodes64 = oracle64.tree_build(pos.astype(np.float64), mas.astype(np.float64), b, op64)
+    a64, _, _ = oracle64.walk(pos.astype(np.float64), mas.astype(np.float64), nodes64, op64)
+    d_gpu = np.linalg.norm(v["acc"].astype(np.float64) - a, axis=1)
+    d_ref = np.linalg.norm(a.astype(np.float64) - a64, axis=1)  # the reference's own FP32 error
+    e_mag = d_gpu / mag
+    print("BH FAST per-body acc err (split %d, group %d, n %d): |da|/|a|" % (split, group, n), err_summary(e),
+          "|da|/sum|terms|", err_summary(e_mag), "ref vs FP64 /|a|", err_summary(d_ref / np.linalg.norm(a64, axis=1)),
+          "pot:", err_summary(ep))
+    # every body within 1e-5 of the sum of its terms' magnitudes (= |a_i|
+    # where they do not cancel), or within twice the reference's own FP32
+    # error where that is larger
+    bad = d_gpu > np.maximum(1e-5 * mag, 2.0 * d_ref)
+    assert not bad.any(), (np.nonzero(bad)[0], e[bad], e_mag[bad])
+    assert np.median(e) < 1e-6 and np.quantile(e, 0.99) < 1e-5 and ep.max() < 1e-5
 
 
 @pytest.mark.parametrize("leaf", [16, 4])
@@ -330,3 +400,91 @@ def test_tree_step_energies(sf, oracle32, math):
             Tg, Vg = s.energies()
             tol = 1e-13 if math == "exact" else 1e-5
             assert abs(Tg - T) <= tol * abs(T) and abs(Vg - V) <= tol * abs(V), (k, Tg, T, Vg, V)
+
+
+def test_tree_fast_trajectory_uniform65536(sf, oracle32):
+    """20 FAST KDK steps of the 65,536-body benchmark workload (uniform
+    sphere, theta = 0.5, leaf 8, dt = 1e-3) against 20 reference steps of
+    the FP32 restatement: positions, velocities and accelerations per body."""
+    from starflood_gb300.ics import uniform_ball
+    n, steps = 65536, 20
+    pos, vel, mas = uniform_ball(n, seed=2024)
+    p = sf.default_params(solver=sf.SOLVER_TREE, eps=0.01, dt=1e-3, theta=0.5)
+    op = make_params(dt=1e-3, eps=0.01, theta=0.5, use_tree=1)
+    osim, oslab, _ = oracle32.new_sim(n, op)
+    ov = slab_views(oslab, n, 13)
+    ov["pos"][:] = pos
+    ov["vel"][:] = vel
+    ov["mas"][:] = mas
+    oracle32.sim_solv(op, osim, 0)
+    for k in range(steps):
+        oracle32.sim_step(op, osim, k)
+    with sf.Sim(n, p) as s:
+        s.set_state(pos, vel, mas)
+        s.solve(0)
+        s.run(0, steps)
+        v = slab_views(s.download(), n, 13)
+        assert s.status() == 0
+    ex = per_body_rel(v["pos"], ov["pos"])
+    ev = per_body_rel(v["vel"], ov["vel"])
+    ea = per_body_rel(v["acc"], ov["acc"])
+    print("BH FAST 20-step trajectory per-body rel err: pos", err_summary(ex), "vel", err_summary(ev),
+          "acc", err_summary(ea))
+    assert ex.max() < 1e-5 and np.quantile(ex, 0.99) < 1e-6
+    assert np.quantile(ev, 0.99) < 1e-5
+    assert np.median(ea) < 1e-6 and np.quantile(ea, 0.99) < 1e-5
+
+
+def test_status_ties_overflow(sf):
+    """More bodies exactly on cell midplanes than the tie pass holds (1024):
+    the build says so through SFGPU_STATUS_TIES instead of failing silently."""
+    g = (np.arange(16, dtype=np.float32) - 8.0) / 8.0  # multiples of 1/8 in [-1, 0.875]
+    pos = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3).astype(np.float32)
+    n = len(pos)
+    mas = np.full(n, 1.0 / n, np.float32)
+    p = sf.default_params(solver=sf.SOLVER_TREE, eps=0.01, theta=0.5)
+    with sf.Sim(n, p) as s:
+        s.set_state(pos, np.zeros_like(pos), mas)
+        s.tree_build(np.array([-1, -1, -1, 1, 1, 1], np.float32))
+        assert s.status() & sf.STATUS_TIES
+
+
+@pytest.mark.parametrize("split,group", [(0, 16), (0, 32), (1, 0), (0, 0)])
+def test_status_walk_limit(sf, split, group):
+    """A walk stopped by its loop bound (walk_limit rounds per warp) returns
+    and sets SFGPU_STATUS_WALK; the same simulation then walks normally."""
+    from starflood_gb300.ics import uniform_ball
+    n = 8192
+    pos, vel, mas = uniform_ball(n, seed=14)
+    for math in (sf.MATH_FAST, sf.MATH_EXACT):
+        p = sf.default_params(solver=sf.SOLVER_TREE, eps=0.01, theta=0.5, walk_limit=3, walk_split=split,
+                              walk_group=group, math=math)
+        with sf.Sim(n, p) as s:
+            s.set_state(pos, vel, mas)
+            s.solve(0)
+            assert s.status() & sf.STATUS_WALK
+            assert np.all(np.isfinite(slab_views(s.download(), n, 13)["acc"]))
+    p = sf.default_params(solver=sf.SOLVER_TREE, eps=0.01, theta=0.5, walk_split=split, walk_group=group)
+    with sf.Sim(n, p) as s:
+        s.set_state(pos, vel, mas)
+        s.solve(0)
+        assert s.status() == 0
+
+
+def test_status_spin_withheld_lookback(sf):
+    """The sort's decoupled look-back waits a bounded number of rounds: with
+    one tile told not to publish, the tiles after it give up, set
+    SFGPU_STATUS_SPIN and the call returns; the same entry point sorts
+    correctly when no tile is withheld, before and after."""
+    rng = np.random.default_rng(5)
+    n = 300000
+    keys = rng.integers(0, 1 << 40, n, dtype=np.uint64)
+    want = np.argsort(keys & np.uint64(127), kind="stable")
+    out, idx, st = sf.sort_withheld_check(keys)
+    assert st == 0
+    np.testing.assert_array_equal(idx, want)
+    out, idx, st = sf.sort_withheld_check(keys, withheld_tile=3, spin_limit=4096)
+    assert st & sf.STATUS_SPIN
+    out, idx, st = sf.sort_withheld_check(keys)
+    assert st == 0
+    np.testing.assert_array_equal(idx, want)
