@@ -585,7 +585,7 @@ def gpu_sph(sf, steps, warmup, sph_path=0, mode="cubic"):
                     "alpha=1, beta=2), N=262144 Plummer a=1 M=1 with isotropic velocities, dt=5e-4",
         "neighbour_pairs_per_pass": pairs,
         "pairs_per_s": {"density": pairs / (d_ms * 1e-3), "force": pairs / (f_ms * 1e-3)},
-        "roofline": {"kernel": "k_cubic_body<2, %s>" % ("true" if dom[0] == "sph_force" else "false"),
+        "roofline": {"kernel": "k_cubic_body<1, %s>" % ("true" if dom[0] == "sph_force" else "false"),
                      "bound": "hbm", "achieved": dom[1], "peak": peak[0], "unit": "GB/s", "frac": dom[1] / peak[0],
                      "traffic": profiled_traffic("sph_cubic_body_plummer262144.md"),
                      "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum per launch of the force pass, "

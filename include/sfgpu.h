@@ -78,8 +78,9 @@ typedef struct {
     double   sph_beta;    /* CUBIC: Monaghan viscosity beta                 */
     uint32_t flags;       /* SFGPU_FLAG_*                                   */
     uint32_t walk_split;  /* walk variant: 0 group walk (default), 1 thread per body, 8 thread per body and root octant, 64 32-body group walk over 8 warps */
-    uint32_t sph_path;    /* CUBIC SPH neighbour search: 0 cells of side h, rows culled to the 2h sphere
-                             (default); 1 the 27 cells of side 2h around the body */
+    uint32_t sph_path;    /* CUBIC SPH neighbour search: 0 the 3 x 3 rows of cells of side 2h around
+                             the body, each cut to the cells the 2h sphere reaches (default); 1 cells
+                             of side h, rows culled the same way */
     uint32_t walk_group;  /* bodies per warp of the group walk: 0 the default (16), 8, 16 or 32 */
     uint32_t spin_limit;  /* rounds a bounded device wait (the look-backs of the sort and of the
                              node scan) spins on an unpublished word before it gives up and sets

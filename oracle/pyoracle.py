@@ -267,6 +267,9 @@ class Oracle:
         s.N = n
         s.mem = slab.ctypes.data
         s.nodes = nodes.ctypes.data
+        # the struct holds raw pointers: keep the arrays alive as long as it
+        # lives, even when a caller drops the returned arrays
+        s._arrays = (slab, nodes)
         return s, slab, nodes
 
     def sim_solv(self, params, sim, step):

@@ -164,8 +164,8 @@ __device__ __forceinline__ void two_sum2(float2& h, float2 a, float2& l) {
 // bodies, whose FP32 partial sum is far inside the 1e-6 bound.
 constexpr int COMP_TILES = 4;
 
-template <int BS, int PAIRS, bool COMP, int RSQ = 0>
-__global__ void __launch_bounds__(BS) k_pp_tile2(const float* __restrict__ pos, const float* __restrict__ mas,
+template <int BS, int PAIRS, bool COMP, int RSQ = 0, int MINB = 1>
+__global__ void __launch_bounds__(BS, MINB) k_pp_tile2(const float* __restrict__ pos, const float* __restrict__ mas,
                                                  uint32_t n, float eps2, uint32_t jchunk,
                                                  float4* __restrict__ part) {
     __shared__ float4 sj[2][BS];
@@ -203,7 +203,7 @@ __global__ void __launch_bounds__(BS) k_pp_tile2(const float* __restrict__ pos, 
         sj[0][threadIdx.x] = make_float4(x, x, y, y);
         sj[1][threadIdx.x] = make_float4(z, z, w, w);
         __syncthreads();
-#pragma unroll 4
+#pragma unroll 8
         for (int jj = 0; jj < BS; jj++) {
             const float4 A = sj[0][jj];
             const float4 B = sj[1][jj];
@@ -284,21 +284,30 @@ __global__ void k_pp_reduce(const float4* __restrict__ part, uint32_t n, uint32_
     }
 }
 
-// The production tile: 128 threads, 4 pairs (8 bodies) per thread, rsqrt
-// and 1/r^2 both from the MUFU (one FP32 multiply fewer per interaction: the
-// FMA pipe is the bound).  Measured at N = 1,048,576 on GB300:
-// 2.25e12 interactions/s, against 1.92e12 for the scalar k_pp_tile<128,4>.
+// The production tile: 128 threads, 2 pairs (4 bodies) per thread at 64
+// registers, 8 blocks (32 warps) per SM, rsqrt and 1/r^2 both from the MUFU
+// (one FP32 multiply fewer per interaction: the FMA pipe is the bound),
+// the j range split for about 16 waves.  Measured at N = 1,048,576 on GB300
+// (CUDA events, one launch): 2.366e12 interactions/s plain and 2.33e12
+// with the compensation every 4 tiles, against 2.253e12 for 4 pairs per
+// thread at 128 registers (16 warps per SM, 8 waves), 2.36e12 for 1 pair
+// at 32 registers, 2.28e12 for 3 pairs, and 1.92e12 for the scalar
+// k_pp_tile<128,4>.
 constexpr int FAST_BS = 128;
-constexpr int FAST_PAIRS = 4;
+constexpr int FAST_PAIRS = 2;
 constexpr int FAST_IPT = 2 * FAST_PAIRS;
 constexpr int FAST_RSQ = 2;
+constexpr int FAST_MINB = 8;
+constexpr uint32_t FAST_WAVES = 16;
 
 void launch_pp_tiles(bool comp, dim3 grid, const float* pos, const float* mas, uint32_t n, float eps2,
                      uint32_t jchunk, float4* part, cudaStream_t st) {
     if (comp)
-        k_pp_tile2<FAST_BS, FAST_PAIRS, true, FAST_RSQ><<<grid, FAST_BS, 0, st>>>(pos, mas, n, eps2, jchunk, part);
+        k_pp_tile2<FAST_BS, FAST_PAIRS, true, FAST_RSQ, FAST_MINB><<<grid, FAST_BS, 0, st>>>(pos, mas, n, eps2,
+                                                                                           jchunk, part);
     else
-        k_pp_tile2<FAST_BS, FAST_PAIRS, false, FAST_RSQ><<<grid, FAST_BS, 0, st>>>(pos, mas, n, eps2, jchunk, part);
+        k_pp_tile2<FAST_BS, FAST_PAIRS, false, FAST_RSQ, FAST_MINB><<<grid, FAST_BS, 0, st>>>(pos, mas, n, eps2,
+                                                                                            jchunk, part);
 }
 
 }  // namespace
@@ -321,8 +330,8 @@ struct PPShape {
 PPShape pp_shape(uint32_t n) {
     PPShape sh;
     sh.iblocks = sf_ceil_div(n, FAST_BS * FAST_IPT);
-    // enough blocks for ~8 waves at 4 resident blocks per SM
-    const uint32_t target = (uint32_t)sf_num_sms() * 4u * 8u;
+    // enough blocks for ~FAST_WAVES waves at FAST_MINB resident blocks per SM
+    const uint32_t target = (uint32_t)sf_num_sms() * (uint32_t)FAST_MINB * FAST_WAVES;
     uint32_t nsplit = std::max<uint32_t>(1u, sf_ceil_div(target, sh.iblocks));
     uint32_t jchunk = sf_ceil_div(n, nsplit);
     jchunk = sf_ceil_div(jchunk, FAST_BS) * FAST_BS;

@@ -17,10 +17,13 @@
 // One thread per body (bodies in sorted order, so a warp's bodies are close
 // together) scans the rows of cells (dy, dz) in [-REACH, REACH]^2 whose
 // distance from the body is below R, and in each row only the x-range of
-// cells the sphere of radius R reaches.  The default, REACH = 2
-// (sfgpu_params.sph_path 0), visits about 84 cells of side h per body
-// holding 2.5x the candidates of the sphere; REACH = 1 (sph_path 1) is the
-// 27-cell stencil of side-2h cells, 6.4x.  Each candidate is tested with the
+// cells the sphere of radius R reaches.  The default, REACH = 1
+// (sfgpu_params.sph_path 0), is the 3 x 3 rows of side-2h cells around the
+// body with at most 2 cells per row; REACH = 2 (sph_path 1) visits about 84
+// cells of side h holding 2.5x the candidates of the sphere, but its extra
+// cell look-ups cost more than the candidates it saves (measured on the
+// 262,144-body Plummer gas: force pass 1.17 against 1.10 ms).  Each
+// candidate is tested with the
 // FP32 expression above; bodies of another cell that shares the bucket are
 // skipped by cell key, so none is counted twice.  With SFGPU_FLAG_STATS the
 // density pass also sums an order-independent hash of every body's
@@ -46,7 +49,7 @@ struct CubicWork {
     float4* px = nullptr;      // sorted x, y, z, m
     float4* pv = nullptr;      // sorted vx, vy, vz, u
     float4* pd = nullptr;      // sorted rho, P/rho^2, c, h
-    float4* ph = nullptr;      // sorted h, u, c
+    float4* ph = nullptr;      // sorted h, u, c, 1/h
     uint32_t* bmix = nullptr;  // per bucket: holds more than one cell
     uint64_t* cell = nullptr;  // sorted packed cell coordinates
     uint64_t* mixv = nullptr;  // sorted: hash of each body's index (SFGPU_FLAG_STATS)
@@ -54,9 +57,11 @@ struct CubicWork {
     uint32_t* done = nullptr;
 };
 
-__device__ __forceinline__ float w_cubic(float r, float h) {
-    const float q = r / h;
-    const float s = 1.0f / (PI_F * h * h * h);
+// The kernel and its derivative from q = r / h and 1 / h (the passes keep
+// 1 / h of every body, so no division runs per pair).
+__device__ __forceinline__ float w_cubic(float r, float ih) {
+    const float q = r * ih;
+    const float s = ih * ih * ih * (1.0f / PI_F);
     if (q < 1.0f) return s * (1.0f - 1.5f * q * q + 0.75f * q * q * q);
     if (q < 2.0f) {
         const float t = 2.0f - q;
@@ -64,9 +69,10 @@ __device__ __forceinline__ float w_cubic(float r, float h) {
     }
     return 0.0f;
 }
-__device__ __forceinline__ float dw_cubic(float r, float h) {
-    const float q = r / h;
-    const float s = 1.0f / (PI_F * h * h * h * h);
+__device__ __forceinline__ float dw_cubic(float r, float ih) {
+    const float q = r * ih;
+    const float ih2 = ih * ih;
+    const float s = ih2 * ih2 * (1.0f / PI_F);
     if (q < 1.0f) return s * (-3.0f * q + 2.25f * q * q);
     if (q < 2.0f) {
         const float t = 2.0f - q;
@@ -140,7 +146,8 @@ __global__ void k_cell_gather(const uint64_t* __restrict__ keys, const uint32_t*
     pv[k] = make_float4(vel[3u * p], vel[3u * p + 1u], vel[3u * p + 2u], u[p]);
     cell[k] = pack_cell(cell_of(x, y, z, grid[1]));
     const float uu = u[p];
-    ph[k] = make_float4(slab[(size_t)13 * n + p], uu, sqrtf(gamma * (gamma - 1.0f) * uu), 0.0f);
+    const float hh = slab[(size_t)13 * n + p];
+    ph[k] = make_float4(hh, uu, sqrtf(gamma * (gamma - 1.0f) * uu), 1.0f / hh);
     if (mixv) mixv[k] = sf_mix64(p);
 }
 
@@ -154,17 +161,18 @@ __global__ void k_bucket_mix(const uint64_t* __restrict__ keys, uint32_t n, cons
     if (k != s && cell[k] != cell[s]) bmix[b] = 1u;
 }
 
-__device__ __forceinline__ bool density_pair(const float4& a, float hi, const float4& q, float hj, float& rho,
-                                             uint32_t& count) {
+__device__ __forceinline__ bool density_pair(const float4& a, float hi, float ihi, const float4& q, float hj,
+                                             float ihj, float& rho, uint32_t& count) {
     const float rx = fsub(a.x, q.x), ry = fsub(a.y, q.y), rz = fsub(a.z, q.z);
     float r2;
     if (!is_neighbour(rx, ry, rz, hi, hj, r2)) return false;
-    const float r = sqrtf(r2);
+    const float r = r2 > 0.0f ? r2 * rsqrtf(r2) : 0.0f;
     count++;
-    rho += q.w * 0.5f * (w_cubic(r, hi) + w_cubic(r, hj));
+    rho += q.w * 0.5f * (w_cubic(r, ihi) + w_cubic(r, ihj));
     return true;
 }
 
+// di: (rho, P/rho^2, c, 1/h) of body i; dj: (rho, P/rho^2, c, h) of body j
 __device__ __forceinline__ void force_pair(const float4& a, float hi, const float4& di, const float4& vi,
                                            const float4& q, const float4& vj, const float4& dj, float alpha,
                                            float beta, float& ax, float& ay, float& az, float& du) {
@@ -172,16 +180,17 @@ __device__ __forceinline__ void force_pair(const float4& a, float hi, const floa
     const float hj = dj.w;
     float r2;
     if (!is_neighbour(rx, ry, rz, hi, hj, r2)) return;
-    const float r = sqrtf(r2);
-    if (!(r > 0.0f)) return;
-    const float g = 0.5f * (dw_cubic(r, hi) + dw_cubic(r, hj)) / r;
+    if (!(r2 > 0.0f)) return;
+    const float rinv = rsqrtf(r2);
+    const float r = r2 * rinv;
+    const float g = 0.5f * (dw_cubic(r, di.w) + dw_cubic(r, __fdividef(1.0f, hj))) * rinv;
     const float vx = vi.x - vj.x, vy = vi.y - vj.y, vz = vi.z - vj.z;
     const float vr = vx * rx + vy * ry + vz * rz;
     float visc = 0.0f;
     if (vr < 0.0f) {
         const float h = 0.5f * (hi + hj);
-        const float mu = h * vr / (r2 + 0.01f * h * h);
-        visc = (-alpha * 0.5f * (di.z + dj.z) * mu + beta * mu * mu) / (0.5f * (di.x + dj.x));
+        const float mu = __fdividef(h * vr, r2 + 0.01f * h * h);
+        visc = __fdividef(-alpha * 0.5f * (di.z + dj.z) * mu + beta * mu * mu, 0.5f * (di.x + dj.x));
     }
     const float f = q.w * (di.y + dj.y + visc) * g;
     ax -= f * rx;
@@ -209,9 +218,11 @@ __global__ void __launch_bounds__(128) k_cubic_body(uint32_t n, const float* __r
     const float R2 = R * R * MARGIN_HI;
     const float4 a = px[k];
     const float hi = ph[k].x;
+    const float ihi = 1.0f / hi;
     float4 di = make_float4(0.f, 0.f, 0.f, 0.f), vi = di;
     if (FORCE) {
         di = pd[k];
+        di.w = ihi;  // the pair terms take body i's 1 / h
         vi = pv[k];
     }
     const int3 c0 = cell_of(a.x, a.y, a.z, inv);
@@ -244,7 +255,8 @@ __global__ void __launch_bounds__(128) k_cubic_body(uint32_t n, const float* __r
                     if (chk && cell[j] != want) continue;
                     const float4 q = px[j];
                     if (!FORCE) {
-                        const bool hit = density_pair(a, hi, q, ph[j].x, o0, count);
+                        const float4 hj = ph[j];
+                        const bool hit = density_pair(a, hi, ihi, q, hj.x, hj.w, o0, count);
                         if (HASH && hit) hs += mixv[j];
                     } else if (j != k) {
                         force_pair(a, hi, di, vi, q, pv[j], pd[j], alpha, beta, o0, o1, o2, o3);
@@ -307,7 +319,7 @@ int sf_sph_cubic_alloc(sfgpu_sim* s) {
     CubicWork* w = new CubicWork();
     s->sph_cubic = w;
     const uint32_t n = std::max<uint32_t>(s->n, 1);
-    w->reach = s->p.sph_path == 1 ? 1 : 2;
+    w->reach = s->p.sph_path == 1 ? 2 : 1;
     w->tbits = 1;
     while ((1u << w->tbits) < 2u * n) w->tbits++;
     w->tsize = 1u << w->tbits;

@@ -936,45 +936,123 @@ __global__ void k_ref_leaf_sums(const uint32_t* __restrict__ nsplit_p, uint32_t 
     nd.com[NODE_REC * v] = cnt ? ref_com(sx, sy, sz, sm) : make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
-__global__ void k_ref_merge(int level, const uint32_t* __restrict__ nsplit_p, uint32_t split_cap,
-                            const uint8_t* __restrict__ split_level, const uint32_t* __restrict__ split_node,
-                            NodeArrays nd, uint32_t* __restrict__ X, uint32_t* __restrict__ Y,
-                            const float* __restrict__ pos, const float* __restrict__ mas) {
-    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= min(*nsplit_p, split_cap) || split_level[s] != level) return;
-    const uint32_t v = split_node[s];
-    const uint32_t fc = 1u + 8u * s;
-    uint32_t cur[8], end[8];
-    for (int o = 0; o < 8; o++) {
-        cur[o] = nd.start[fc + o];
-        end[o] = cur[o] + __float_as_uint(nd.hi[NODE_REC * (fc + o)].z);
+// A CTA per split node of a level: the node's members in index order are
+// the merge of its eight children's index-ordered lists, each member's place
+// being its rank in its own list plus, for every other child, the number of
+// members with a smaller index (a binary search), so all members move at
+// once; then warp 0 adds them up in that order: lanes load and multiply 32
+// members side by side and the sums take them one by one through shuffles,
+// the FP32 chain the reference's insertion order makes.
+constexpr int REF_THREADS = 256;
+
+__device__ __forceinline__ uint32_t count_below(const uint32_t* __restrict__ L, uint32_t len, uint32_t x) {
+    uint32_t lo = 0, hi = len;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (L[mid] < x) lo = mid + 1; else hi = mid;
     }
-    const uint32_t s0 = nd.start[v];
-    const uint32_t cnt = __float_as_uint(nd.hi[NODE_REC * v].z);
+    return lo;
+}
+
+// the FP32 running sums of m x, m y, m z and m over `cnt` members (warp 0),
+// the member of step a being idx(a) when use(it); lane 0 returns the totals
+template <typename IdxF, typename UseF>
+__device__ __forceinline__ float4 ref_sum_in_order(uint32_t cnt, IdxF idx, UseF use, const float* __restrict__ pos,
+                                                   const float* __restrict__ mas) {
+    const int lane = threadIdx.x & 31;
     float sx = 0.f, sy = 0.f, sz = 0.f, sm = 0.f;
-    for (uint32_t a = 0; a < cnt; a++) {
-        int best = -1;
-        uint32_t bv = 0xFFFFFFFFu;
-        for (int o = 0; o < 8; o++) {
-            if (cur[o] < end[o]) {
-                const uint32_t x = X[cur[o]];
-                if (x < bv) {
-                    bv = x;
-                    best = o;
-                }
+    for (uint32_t a0 = 0; a0 < cnt; a0 += 32) {
+        const uint32_t a = a0 + (uint32_t)lane;
+        float mx = 0.f, my = 0.f, mz = 0.f, m = 0.f;
+        bool u = false;
+        if (a < cnt) {
+            const uint32_t p = idx(a);
+            u = use(p);
+            if (u) {
+                m = mas[p];
+                mx = fmul(m, pos[3u * p]);  // tree.c:166-169: m x, then +=
+                my = fmul(m, pos[3u * p + 1u]);
+                mz = fmul(m, pos[3u * p + 2u]);
             }
         }
-        if (best < 0) break;
-        cur[best]++;
-        Y[s0 + a] = bv;
-        const float m = mas[bv];
-        sx = fadd(sx, fmul(m, pos[3u * bv]));
-        sy = fadd(sy, fmul(m, pos[3u * bv + 1u]));
-        sz = fadd(sz, fmul(m, pos[3u * bv + 2u]));
-        sm = fadd(sm, m);
+        const uint32_t ub = __ballot_sync(0xffffffffu, u);
+        const int lim = (int)min(32u, cnt - a0);
+        for (int l = 0; l < lim; l++) {
+            const float tx = __shfl_sync(0xffffffffu, mx, l), ty = __shfl_sync(0xffffffffu, my, l);
+            const float tz = __shfl_sync(0xffffffffu, mz, l), tm = __shfl_sync(0xffffffffu, m, l);
+            if ((ub >> l) & 1u) {
+                sx = fadd(sx, tx);
+                sy = fadd(sy, ty);
+                sz = fadd(sz, tz);
+                sm = fadd(sm, tm);
+            }
+        }
     }
-    for (uint32_t a = 0; a < cnt; a++) X[s0 + a] = Y[s0 + a];
-    nd.com[NODE_REC * v] = ref_com(sx, sy, sz, sm);
+    return make_float4(sx, sy, sz, sm);
+}
+
+__device__ __forceinline__ void ref_level_node(uint32_t s, NodeArrays nd, const uint32_t* __restrict__ split_node,
+                                               uint32_t* __restrict__ X, uint32_t* __restrict__ Y,
+                                               const float* __restrict__ pos, const float* __restrict__ mas,
+                                               uint32_t* cst, uint32_t* cen) {
+    const uint32_t v = split_node[s];
+    const uint32_t fc = 1u + 8u * s;
+    const uint32_t s0 = nd.start[v];
+    const uint32_t cnt = __float_as_uint(nd.hi[NODE_REC * v].z);
+    if (threadIdx.x < 8) {
+        cst[threadIdx.x] = nd.start[fc + threadIdx.x];
+        cen[threadIdx.x] = cst[threadIdx.x] + __float_as_uint(nd.hi[NODE_REC * (fc + threadIdx.x)].z);
+    }
+    __syncthreads();
+    for (uint32_t k = threadIdx.x; k < cnt; k += REF_THREADS) {
+        const uint32_t q = s0 + k;
+        int o = 0;
+        while (o < 7 && q >= cen[o]) o++;
+        const uint32_t x = X[q];
+        uint32_t rank = q - cst[o];
+        for (int c = 0; c < 8; c++)
+            if (c != o) rank += count_below(X + cst[c], cen[c] - cst[c], x);
+        Y[s0 + rank] = x;
+    }
+    __syncthreads();
+    for (uint32_t k = threadIdx.x; k < cnt; k += REF_THREADS) X[s0 + k] = Y[s0 + k];
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const float4 t = ref_sum_in_order(
+            cnt, [&](uint32_t a) { return X[s0 + a]; }, [](uint32_t) { return true; }, pos, mas);
+        if (threadIdx.x == 0) nd.com[NODE_REC * v] = ref_com(t.x, t.y, t.z, t.w);
+    }
+    __syncthreads();  // cst / cen are reused by the CTA's next node
+}
+
+__global__ void __launch_bounds__(REF_THREADS) k_ref_level(int level, const uint32_t* __restrict__ nsplit_p,
+                                                           uint32_t split_cap, const uint8_t* __restrict__ split_level,
+                                                           const uint32_t* __restrict__ split_node, NodeArrays nd,
+                                                           uint32_t* __restrict__ X, uint32_t* __restrict__ Y,
+                                                           const float* __restrict__ pos,
+                                                           const float* __restrict__ mas) {
+    const uint32_t ns = min(*nsplit_p, split_cap);
+    __shared__ uint32_t cst[8], cen[8];
+    for (uint32_t s = blockIdx.x; s < ns; s += gridDim.x) {  // the same s on every thread of the CTA
+        if (split_level[s] != level) continue;
+        ref_level_node(s, nd, split_node, X, Y, pos, mas, cst, cen);
+    }
+}
+
+// The root's members in index order are simply the bodies inside the root
+// cube, by index (tree.c:141-146, the closed test that lets NaN in).
+__global__ void k_ref_root(uint32_t n, const float* __restrict__ bounds, NodeArrays nd, const float* __restrict__ pos,
+                           const float* __restrict__ mas) {
+    if (__float_as_uint(nd.hi[0].w) == NODE_NONE) return;  // a leaf root: k_ref_leaf_sums has it
+    const float b[6] = {bounds[0], bounds[1], bounds[2], bounds[3], bounds[4], bounds[5]};
+    const float4 t = ref_sum_in_order(
+        n, [](uint32_t a) { return a; },
+        [&](uint32_t p) {
+            const float x = pos[3u * p], y = pos[3u * p + 1u], z = pos[3u * p + 2u];
+            return !(b[0] > x || x > b[3] || b[1] > y || y > b[4] || b[2] > z || z > b[5]);
+        },
+        pos, mas);
+    if (threadIdx.x == 0) nd.com[0] = ref_com(t.x, t.y, t.z, t.w);
 }
 
 }  // namespace
@@ -1131,12 +1209,16 @@ int sf_tree_build(sfgpu_sim* s) {
         const uint32_t mb = sf_ceil_div(1u + 8u * t->split_cap, 256);
         k_ref_leaf_sums<<<mb, 256, 0, st>>>(nsplit, t->split_cap, t->nd, t->vals, t->ordA, pos, mas);
         SF_CHECK_LAUNCH();
-        const uint32_t sm = sf_ceil_div(std::max<uint32_t>(t->split_cap, 1), 128);
-        for (int L = (int)s->p.depth_max - 1; L >= 0; L--) {
-            k_ref_merge<<<sm, 128, 0, st>>>(L, nsplit, t->split_cap, t->split_level, t->split_node, t->nd, t->ordA,
-                                            t->ordB, pos, mas);
+        // CTAs stride over the split nodes, working those of the level;
+        // level 0, the root, by its own single-warp scan
+        const uint32_t sm = std::max<uint32_t>(1u, std::min<uint32_t>(t->split_cap, (uint32_t)sf_num_sms() * 8u));
+        for (int L = (int)s->p.depth_max - 1; L >= 1; L--) {
+            k_ref_level<<<sm, REF_THREADS, 0, st>>>(L, nsplit, t->split_cap, t->split_level, t->split_node, t->nd,
+                                                     t->ordA, t->ordB, pos, mas);
             SF_CHECK_LAUNCH();
         }
+        k_ref_root<<<1, 32, 0, st>>>(n, s->d_bounds, t->nd, pos, mas);
+        SF_CHECK_LAUNCH();
         s->timer.end(st, tk);
     }
     return SFGPU_OK;
