@@ -312,19 +312,23 @@ void sfgpu_vis_model_matrix(double time, float out[16]);
 /* solve_gravity_part_part (src/gravity.c:666-819) */
 int sfgpu_gravity_pp(const sfgpu_params* p, uint32_t n, const float* pos, const float* mas,
                      float* acc, float* pot, void* stream);
-/* No counterpart in the reference.  The same PP force as sfgpu_gravity_pp,
- * for callers that must not allocate device memory: code that issues its
- * kernels inside CUDA stream capture, hosts whose own allocator owns the
- * device memory, or loops that cannot afford cudaMalloc's implicit device
- * synchronisation.  It calls no cudaMalloc / cudaFree: the work array for
- * the j-split partial sums is a 16 MiB array built into the library, held by
- * every GPU that loads it until the process exits.  N is limited to
- * 1,048,576 bodies (524,288 in the compensated form); larger N fails with a
- * message in sfgpu_last_error().  The first call on a device looks up the
- * array's device address (cudaGetSymbolAddress), so make that first call
- * before any stream capture.  All calls share the one array: calls that
- * overlap on the GPU (other streams, other threads) race and must be
- * serialised by the caller.  No state carries over between calls. */
+/* No counterpart in the reference.  The same PP force as sfgpu_gravity_pp
+ * for callers that cannot allocate device memory: a host application whose
+ * own memory pool has already reserved the GPU's memory (a cudaMalloc there
+ * fails or fragments the pool), or a time-critical loop that cannot take the
+ * implicit device-wide synchronisation of cudaMalloc / cudaFree.  It calls
+ * neither: the work array for the j-split partial sums is a 16 MiB array
+ * built into the library, which every GPU that loads the library holds until
+ * the process exits.  With FAST math N is limited to 1,048,576 bodies
+ * (524,288 in the compensated form); larger N fails with a message in
+ * sfgpu_last_error().  EXACT math needs no work array and has no such limit.
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) and keeps it, so make that first call before any
+ * stream capture, and do not call it again on a device after
+ * cudaDeviceReset.  All calls share the one array and it keeps the last
+ * call's partial sums: calls that overlap on the GPU (other streams, other
+ * threads) race and must be serialised by the caller.  Each call writes
+ * every partial it reads, so no state carries over between calls. */
 int sfgpu_gravity_pp_noalloc(const sfgpu_params* p, uint32_t n, const float* pos, const float* mas,
                              float* acc, float* pot, void* stream);
 

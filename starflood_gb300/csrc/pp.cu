@@ -443,6 +443,14 @@ extern "C" int sfgpu_gravity_pp_noalloc(const sfgpu_params* p, uint32_t n, const
         sf_set_error("sfgpu_gravity_pp_noalloc: EXACT math applies to the PLAIN form only");
         return SFGPU_FAILURE;
     }
+    if (n == 0) return SFGPU_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    const ForceConsts fc = sf_force_consts(*p);
+    if (p->math == SFGPU_MATH_EXACT) {  // needs no work array at all, so no size limit
+        k_pp_exact<<<sf_ceil_div(n, EXACT_BS), EXACT_BS, 0, st>>>(pos, mas, n, fc, acc, pot);
+        SF_CHECK_LAUNCH();
+        return SFGPU_OK;
+    }
     const bool comp = p->form == SFGPU_FORM_COMPENSATED;
     const size_t per_split = (size_t)n * (comp ? 2 : 1);
     if (per_split > NOALLOC_PARTS) {
@@ -451,14 +459,6 @@ extern "C" int sfgpu_gravity_pp_noalloc(const sfgpu_params* p, uint32_t n, const
                      n, comp ? NOALLOC_PARTS / 2 : NOALLOC_PARTS, comp ? "compensated" : "plain",
                      (NOALLOC_PARTS * sizeof(float4)) >> 20);
         return SFGPU_FAILURE;
-    }
-    if (n == 0) return SFGPU_OK;
-    cudaStream_t st = (cudaStream_t)stream;
-    const ForceConsts fc = sf_force_consts(*p);
-    if (p->math == SFGPU_MATH_EXACT) {  // needs no work array at all
-        k_pp_exact<<<sf_ceil_div(n, EXACT_BS), EXACT_BS, 0, st>>>(pos, mas, n, fc, acc, pot);
-        SF_CHECK_LAUNCH();
-        return SFGPU_OK;
     }
     float4* parts = nullptr;
     if (noalloc_parts(&parts) != SFGPU_OK) return SFGPU_FAILURE;
