@@ -227,7 +227,10 @@ def test_tree_fast_large(sf, oracle32, oracle64, n, seed, split, group):
     terms; |a_i| itself unless they cancel), or within twice the reference's
     own FP32 error (its insertion-order centre-of-mass sums, against the
     FP64 oracle on the same root cube) where that is larger; median and p99
-    of |a_i - a_ref,i| / |a_i| below 1e-6 and 1e-5."""
+    of |a_i - a_ref,i| / |a_i| below 1e-6 and 1e-5, or below twice the
+    median and p99 of the reference's own FP32 error where those are larger
+    (a Plummer sphere's dense core, where insertion-order FP32 centre-of-mass
+    sums err by ~5e-6).  Potentials the same way, per body."""
     from starflood_gb300.ics import uniform_ball, plummer
     gen = uniform_ball if n == 65536 else plummer
     pos, vel, mas = gen(n, seed=seed)
@@ -251,7 +254,7 @@ def test_tree_fast_large(sf, oracle32, oracle64, n, seed, split, group):
     b = oracle32.root_bounds(pos, 5).astype(np.float64)
     op64 = make_params(eps=0.01, theta=0.5, use_tree=1)
     st64, nodes64 = oracle64.tree_build(pos.astype(np.float64), mas.astype(np.float64), b, op64)
-    a64, _, _ = oracle64.walk(pos.astype(np.float64), mas.astype(np.float64), nodes64, op64)
+    a64, pt64, _ = oracle64.walk(pos.astype(np.float64), mas.astype(np.float64), nodes64, op64)
     d_gpu = np.linalg.norm(v["acc"].astype(np.float64) - a, axis=1)
     d_ref = np.linalg.norm(a.astype(np.float64) - a64, axis=1)  # the reference's own FP32 error
     e_mag = d_gpu / mag
@@ -263,7 +266,16 @@ def test_tree_fast_large(sf, oracle32, oracle64, n, seed, split, group):
     # error where that is larger
     bad = d_gpu > np.maximum(1e-5 * mag, 2.0 * d_ref)
     assert not bad.any(), (np.nonzero(bad)[0], e[bad], e_mag[bad])
-    assert np.median(e) < 1e-6 and np.quantile(e, 0.99) < 1e-5 and ep.max() < 1e-5
+    e_ref = d_ref / np.linalg.norm(a64, axis=1)
+    e_gpu64 = np.linalg.norm(v["acc"].astype(np.float64) - a64, axis=1) / np.linalg.norm(a64, axis=1)
+    print("  GPU vs FP64 /|a|", err_summary(e_gpu64))
+    assert np.median(e) < max(1e-6, 2.0 * np.median(e_ref))
+    assert np.quantile(e, 0.99) < max(1e-5, 2.0 * np.quantile(e_ref, 0.99))
+    # no further from the FP64 sums than the reference itself, in the bulk
+    assert np.median(e_gpu64) < max(1e-6, 1.5 * np.median(e_ref))
+    dp_gpu = np.abs(v["pot"].astype(np.float64) - pt)
+    dp_ref = np.abs(pt.astype(np.float64) - pt64)
+    assert not (dp_gpu > np.maximum(1e-5 * np.abs(pt), 2.0 * dp_ref)).any()
 
 
 @pytest.mark.parametrize("leaf", [16, 4])
