@@ -517,7 +517,7 @@ def gpu_sph(sf, steps, warmup, sph_path=0, mode="cubic"):
                                   flags=flags, sph_path=sph_path)
         else:
             p = sf.default_params(solver=sf.SOLVER_TREE, sph=sf.SPH_REFERENCE, eps=0.01, dt=5e-4, theta=0.5,
-                                  flags=flags)
+                                  flags=flags, sph_path=sph_path)
         s = sf.Sim(n, p)
         s.set_state(pos, vel, mas, rad)
         if cubic:
@@ -568,7 +568,8 @@ def gpu_sph(sf, steps, warmup, sph_path=0, mode="cubic"):
     }
     if not cubic:
         out["workload"] = ("Barnes-Hut (theta=0.5, leaf 8, eps=0.01) + the reference's SPH (sph.c: Gaussian kernel, "
-                           "P=(0.1 rho)^2, momentum over r<=1; FAST arithmetic, cell-grid neighbour search), "
+                           "P=(0.1 rho)^2, momentum over r<=1; FAST arithmetic, cell-grid neighbour search by "
+                           "warps of 32 sorted bodies), "
                            "h=0.05, N=262144 Plummer a=1 M=1, dt=5e-4")
         out["momentum_set_pairs_per_pass"] = pairs
         out["set_pairs_per_s"] = pairs / (f_ms * 1e-3)
@@ -585,11 +586,12 @@ def gpu_sph(sf, steps, warmup, sph_path=0, mode="cubic"):
                     "alpha=1, beta=2), N=262144 Plummer a=1 M=1 with isotropic velocities, dt=5e-4",
         "neighbour_pairs_per_pass": pairs,
         "pairs_per_s": {"density": pairs / (d_ms * 1e-3), "force": pairs / (f_ms * 1e-3)},
-        "roofline": {"kernel": "k_cubic_body<1, %s>" % ("true" if dom[0] == "sph_force" else "false"),
+        "roofline": {"kernel": "k_cubic_warp<%s> (one warp per 32 sorted bodies)" % (
+                         "true" if dom[0] == "sph_force" else "false"),
                      "bound": "hbm", "achieved": dom[1], "peak": peak[0], "unit": "GB/s", "frac": dom[1] / peak[0],
-                     "traffic": profiled_traffic("sph_cubic_body_plummer262144.md"),
+                     "traffic": profiled_traffic("sph_cubic_warp_plummer262144.md"),
                      "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum per launch of the force pass, "
-                                       "profiles/sph_cubic_body_plummer262144.md (ncu)",
+                                       "profiles/sph_cubic_warp_plummer262144.md (ncu)",
                      "peak_source": peak[1],
                      "algorithmic_bytes_per_launch": dom[2], "avg_launch_ms": dom[3],
                      "density_pass_gbs": dens_gbs, "force_pass_gbs": force_gbs,
@@ -1064,13 +1066,13 @@ def main():
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded uniform unit sphere, pcg4d)",
             "config": bh_config(world),
             "clocks": r["clocks"], "e2e": r["e2e"], "gpu_launches": r["per_step"] * args.steps,
-            "roofline": {"kernel": "k_walk_group (Barnes-Hut group walk; its epilogue also applies the second "
-                                   "kick and the energy sums, included in its duration)",
+            "roofline": {"kernel": "k_walk_sib (Barnes-Hut group walk over sibling groups; its epilogue also "
+                                   "applies the second kick and the energy sums, included in its duration)",
                          "bound": "fp32", "achieved": achieved,
                          "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
-                         "traffic": profiled_traffic("walk_group_uniform65536.md"),
+                         "traffic": profiled_traffic("walk_sib_uniform65536.md"),
                          "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum per launch, "
-                                           "profiles/walk_group_uniform65536.md (ncu)",
+                                           "profiles/walk_sib_uniform65536.md (ncu)",
                          "peak_source": peak_src,
                          "flops_per_launch": flops_per_launch, "avg_launch_ms": walk_avg_ms,
                          "interactions_per_step": r["n_int"] / max(1, walk_launches),

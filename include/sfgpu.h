@@ -78,9 +78,13 @@ typedef struct {
     double   sph_beta;    /* CUBIC: Monaghan viscosity beta                 */
     uint32_t flags;       /* SFGPU_FLAG_*                                   */
     uint32_t walk_split;  /* walk variant: 0 group walk (default), 1 thread per body, 8 thread per body and root octant, 64 32-body group walk over 8 warps */
-    uint32_t sph_path;    /* CUBIC SPH neighbour search: 0 the 3 x 3 rows of cells of side 2h around
-                             the body, each cut to the cells the 2h sphere reaches (default); 1 cells
-                             of side h, rows culled the same way */
+    uint32_t sph_path;    /* SPH neighbour passes on the cell grid.  CUBIC: the 3 x 3 rows of cells
+                             of side 2h around each body, each row cut to the cells the 2h sphere
+                             reaches: 0 one warp per 32 sorted bodies over the union of their rows,
+                             candidates staged in shared memory (default); 2 one thread per body; 1
+                             one thread per body over cells of side h.  REFERENCE (FAST): 0 by warps
+                             (default), 2 one thread per body.  Every path adds the same terms in the
+                             same order. */
     uint32_t walk_group;  /* bodies per warp of the group walk: 0 the default (16), 8, 16 or 32 */
     uint32_t spin_limit;  /* rounds a bounded device wait (the look-backs of the sort and of the
                              node scan) spins on an unpublished word before it gives up and sets
@@ -234,6 +238,16 @@ int sfgpu_tree_export(sfgpu_sim* s, uint32_t* parent, uint32_t* bodies, uint32_t
  * no tile was withheld. */
 int sfgpu_sort_withheld_check(const uint64_t* keys, uint32_t n, uint32_t withheld_tile, uint32_t spin_limit,
                               uint64_t* sorted, uint32_t* index, uint32_t* status);
+
+/* The library's stable radix sort of (key, original index) pairs on the n
+ * host keys of `bits` significant bits (1..64), through the dispatch the
+ * tree build and the SPH cell grids use (up to 2^17 keys: one tile pass on
+ * the top 7-bit digit, then one CTA per bucket; above: one tile pass per
+ * digit).  A check of that sort on chosen key distributions (no reference
+ * counterpart: the reference sorts nothing).  Writes the sorted keys, the
+ * original index of each sorted slot and the device status word. */
+int sfgpu_sort_keys(const uint64_t* keys, uint32_t n, int bits, uint64_t* sorted, uint32_t* index,
+                    uint32_t* status);
 
 /* ---- process utilities ------------------------------------------------- */
 /* Kernel launches the host has issued through this library in this process.

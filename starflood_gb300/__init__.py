@@ -84,6 +84,7 @@ def lib():
             "sfgpu_sph_neighbours": (i32, [vp, u32p]),
             "sfgpu_sph_neighbour_hashes": (i32, [vp, C.POINTER(C.c_uint64)]),
             "sfgpu_sort_withheld_check": (i32, [vp, u32, u32, u32, vp, vp, u32p]),
+            "sfgpu_sort_keys": (i32, [vp, u32, i32, vp, vp, u32p]),
             "sfgpu_sph_set_u": (i32, [vp, f32p]),
             "sfgpu_sph_get_u": (i32, [vp, f32p, f32p]),
             "sfgpu_tree_keys": (i32, [vp, C.POINTER(C.c_uint64), u32p, u32p, f32p]),
@@ -158,6 +159,17 @@ def sort_withheld_check(keys, withheld_tile=0xFFFFFFFF, spin_limit=0):
     st = C.c_uint32()
     check(lib().sfgpu_sort_withheld_check(_ptr(keys), n, withheld_tile, spin_limit, _ptr(out), _ptr(idx),
                                           C.byref(st)), "sfgpu_sort_withheld_check")
+    return out, idx, st.value
+
+
+def sort_keys(keys, bits):
+    """sfgpu_sort_keys: (sorted keys, original index per slot, status word)."""
+    keys = np.ascontiguousarray(keys, np.uint64)
+    n = len(keys)
+    out = np.zeros(n, np.uint64)
+    idx = np.zeros(n, np.uint32)
+    st = C.c_uint32()
+    check(lib().sfgpu_sort_keys(_ptr(keys), n, bits, _ptr(out), _ptr(idx), C.byref(st)), "sfgpu_sort_keys")
     return out, idx, st.value
 
 

@@ -159,21 +159,32 @@ __device__ __forceinline__ void two_sum2(float2& h, float2 a, float2& l) {
     h = s;
     l = __fadd2_rn(l, e);
 }
+// The same on a (hi, lo) total kept in shared memory.
+__device__ __forceinline__ void two_sum2_at(float2* hs, float2* ls, float2 a) {
+    float2 h = *hs, l = *ls;
+    two_sum2(h, a, l);
+    *hs = h;
+    *ls = l;
+}
 
-// j-tiles the compensated form sums plainly before each two-sum: 512
-// bodies, whose FP32 partial sum is far inside the 1e-6 bound.
-constexpr int COMP_TILES = 4;
+// j-tiles the compensated form sums plainly before each two-sum: 1024
+// bodies, whose FP32 partial sum is far inside the 1e-6 bound (its error is
+// a few ulps of a partial ~1/1000 of the total at N = 1,048,576).
+constexpr int COMP_TILES = 8;
 
 template <int BS, int PAIRS, bool COMP, int RSQ = 0, int MINB = 1>
 __global__ void __launch_bounds__(BS, MINB) k_pp_tile2(const float* __restrict__ pos, const float* __restrict__ mas,
                                                  uint32_t n, float eps2, uint32_t jchunk,
                                                  float4* __restrict__ part) {
     __shared__ float4 sj[2][BS];
+    // compensated totals, (hi, lo) of x, y, z, potential per pair of bodies,
+    // in shared memory: touched once every COMP_TILES tiles, they would
+    // otherwise take 8 registers per pair from the tile loop (and spill at
+    // the 64-register budget of 8 blocks per SM)
+    __shared__ float2 s_tot[COMP ? 8 * PAIRS : 1][COMP ? BS : 1];
     const uint32_t ibase = blockIdx.x * (BS * 2 * PAIRS);
     float2 nx[PAIRS], ny[PAIRS], nz[PAIRS];
     float2 ax[PAIRS], ay[PAIRS], az[PAIRS], ph[PAIRS];
-    float2 hx[PAIRS], hy[PAIRS], hz[PAIRS], hp[PAIRS];  // compensated totals
-    float2 lx[PAIRS], ly[PAIRS], lz[PAIRS], lp[PAIRS];
     const float2 zero2 = make_float2(0.f, 0.f);
 #pragma unroll
     for (int q = 0; q < PAIRS; q++) {
@@ -183,46 +194,51 @@ __global__ void __launch_bounds__(BS, MINB) k_pp_tile2(const float* __restrict__
         ny[q] = make_float2(i0 < n ? -pos[3u * i0 + 1u] : 0.f, i1 < n ? -pos[3u * i1 + 1u] : 0.f);
         nz[q] = make_float2(i0 < n ? -pos[3u * i0 + 2u] : 0.f, i1 < n ? -pos[3u * i1 + 2u] : 0.f);
         ax[q] = ay[q] = az[q] = ph[q] = zero2;
-        hx[q] = hy[q] = hz[q] = hp[q] = zero2;
-        lx[q] = ly[q] = lz[q] = lp[q] = zero2;
+        if (COMP)
+#pragma unroll
+            for (int c = 0; c < 8; c++) s_tot[8 * q + c][threadIdx.x] = zero2;
     }
     const float2 e2 = make_float2(eps2, eps2);
     const uint32_t j0 = blockIdx.y * jchunk;
     const uint32_t j1 = min(n, j0 + jchunk);
-    int tiles = 0;
-    for (uint32_t jt = j0; jt < j1; jt += BS) {
-        const uint32_t j = jt + threadIdx.x;
-        float x = 0.f, y = 0.f, z = 0.f, w = 0.f;  // padding: zero mass
-        if (j < j1) {
-            x = pos[3u * j];
-            y = pos[3u * j + 1u];
-            z = pos[3u * j + 2u];
-            w = mas[j];
-        }
-        __syncthreads();
-        sj[0][threadIdx.x] = make_float4(x, x, y, y);
-        sj[1][threadIdx.x] = make_float4(z, z, w, w);
-        __syncthreads();
+    // the compensated form runs the plain tile loop over spans of
+    // COMP_TILES tiles and adds each span's partial sums into the (hi, lo)
+    // totals with a paired two-sum (the plain form: one span)
+    const uint32_t span = COMP ? (uint32_t)(BS * COMP_TILES) : j1 - j0;
+    for (uint32_t js = j0; js < j1; js += span) {
+        const uint32_t je = min(j1, js + span);
+        for (uint32_t jt = js; jt < je; jt += BS) {
+            const uint32_t j = jt + threadIdx.x;
+            float x = 0.f, y = 0.f, z = 0.f, w = 0.f;  // padding: zero mass
+            if (j < j1) {
+                x = pos[3u * j];
+                y = pos[3u * j + 1u];
+                z = pos[3u * j + 2u];
+                w = mas[j];
+            }
+            __syncthreads();
+            sj[0][threadIdx.x] = make_float4(x, x, y, y);
+            sj[1][threadIdx.x] = make_float4(z, z, w, w);
+            __syncthreads();
 #pragma unroll 8
-        for (int jj = 0; jj < BS; jj++) {
-            const float4 A = sj[0][jj];
-            const float4 B = sj[1][jj];
-            const float2 sx = make_float2(A.x, A.y), sy = make_float2(A.z, A.w);
-            const float2 sz = make_float2(B.x, B.y), sw = make_float2(B.z, B.w);
+            for (int jj = 0; jj < BS; jj++) {
+                const float4 A = sj[0][jj];
+                const float4 B = sj[1][jj];
+                const float2 sx = make_float2(A.x, A.y), sy = make_float2(A.z, A.w);
+                const float2 sz = make_float2(B.x, B.y), sw = make_float2(B.z, B.w);
 #pragma unroll
-            for (int q = 0; q < PAIRS; q++)
-                pp_pair_step<RSQ>(sx, sy, sz, sw, nx[q], ny[q], nz[q], e2, ax[q], ay[q], az[q], ph[q]);
+                for (int q = 0; q < PAIRS; q++)
+                    pp_pair_step<RSQ>(sx, sy, sz, sw, nx[q], ny[q], nz[q], e2, ax[q], ay[q], az[q], ph[q]);
+            }
         }
-        // every COMP_TILES tiles (and after the last) the running partial
-        // sums join the (hi, lo) totals through a paired two-sum
-        if (COMP && (++tiles == COMP_TILES || jt + BS >= j1)) {
-            tiles = 0;
+        if (COMP) {
 #pragma unroll
             for (int q = 0; q < PAIRS; q++) {
-                two_sum2(hx[q], ax[q], lx[q]);
-                two_sum2(hy[q], ay[q], ly[q]);
-                two_sum2(hz[q], az[q], lz[q]);
-                two_sum2(hp[q], ph[q], lp[q]);
+                float2* t = &s_tot[8 * q][threadIdx.x];  // rows 8q + (0..3 hi x y z p, 4..7 lo)
+                two_sum2_at(t, t + 4 * BS, ax[q]);
+                two_sum2_at(t + BS, t + 5 * BS, ay[q]);
+                two_sum2_at(t + 2 * BS, t + 6 * BS, az[q]);
+                two_sum2_at(t + 3 * BS, t + 7 * BS, ph[q]);
                 ax[q] = ay[q] = az[q] = ph[q] = zero2;
             }
         }
@@ -235,10 +251,12 @@ __global__ void __launch_bounds__(BS, MINB) k_pp_tile2(const float* __restrict__
             const uint32_t i = ibase + (2 * q + h) * BS + threadIdx.x;
             if (i >= n) continue;
             if (COMP) {
-                out[i] = h ? make_float4(hx[q].y, hy[q].y, hz[q].y, hp[q].y)
-                           : make_float4(hx[q].x, hy[q].x, hz[q].x, hp[q].x);
-                out[(size_t)n + i] = h ? make_float4(lx[q].y, ly[q].y, lz[q].y, lp[q].y)
-                                       : make_float4(lx[q].x, ly[q].x, lz[q].x, lp[q].x);
+                float2 v[8];
+#pragma unroll
+                for (int c = 0; c < 8; c++) v[c] = s_tot[8 * q + c][threadIdx.x];
+                out[i] = h ? make_float4(v[0].y, v[1].y, v[2].y, v[3].y) : make_float4(v[0].x, v[1].x, v[2].x, v[3].x);
+                out[(size_t)n + i] = h ? make_float4(v[4].y, v[5].y, v[6].y, v[7].y)
+                                       : make_float4(v[4].x, v[5].x, v[6].x, v[7].x);
             } else {
                 out[i] = h ? make_float4(ax[q].y, ay[q].y, az[q].y, ph[q].y)
                            : make_float4(ax[q].x, ay[q].x, az[q].x, ph[q].x);
@@ -302,9 +320,18 @@ constexpr uint32_t FAST_WAVES = 16;
 
 void launch_pp_tiles(bool comp, dim3 grid, const float* pos, const float* mas, uint32_t n, float eps2,
                      uint32_t jchunk, float4* part, cudaStream_t st) {
-    if (comp)
+    if (comp) {
+        // 8 blocks of 20 KB (tiles + totals) per SM: ask for the largest
+        // shared-memory carve-out
+        static bool carve = false;
+        if (!carve) {
+            cudaFuncSetAttribute(k_pp_tile2<FAST_BS, FAST_PAIRS, true, FAST_RSQ, FAST_MINB>,
+                                 cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
+            carve = true;
+        }
         k_pp_tile2<FAST_BS, FAST_PAIRS, true, FAST_RSQ, FAST_MINB><<<grid, FAST_BS, 0, st>>>(pos, mas, n, eps2,
                                                                                            jchunk, part);
+    }
     else
         k_pp_tile2<FAST_BS, FAST_PAIRS, false, FAST_RSQ, FAST_MINB><<<grid, FAST_BS, 0, st>>>(pos, mas, n, eps2,
                                                                                             jchunk, part);

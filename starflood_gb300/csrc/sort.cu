@@ -267,14 +267,13 @@ __global__ void __launch_bounds__(SORT_THREADS) k_onesweep_all(uint64_t* k0, uin
 #endif
 constexpr int BK_THREADS = SF_BK_THREADS;
 constexpr int BK_WARPS = BK_THREADS / 32;
-constexpr int BK_GROUPS = BK_WARPS / 4;  // warp groups of the per-digit prefix
 constexpr uint32_t BK_CAP = 8192;        // pairs per bucket, 12 B each, two buffers
 constexpr int BK_ITEMS = BK_CAP / BK_THREADS;
 static_assert(BK_THREADS >= RADIX && BK_WARPS % 4 == 0 && BK_CAP % BK_THREADS == 0, "bucket sort shape");
 
 struct BucketScratch {
     uint32_t* wcnt;   // [BK_WARPS][RADIX] per-warp counts, then their exclusive prefix
-    uint32_t* gsum;   // [BK_GROUPS][RADIX] warp-group totals
+    uint32_t* gsum;   // [BK_THREADS / RADIX][RADIX] warp-group totals
     uint32_t* run;    // [RADIX] start of each digit in the destination
     uint32_t* wtot;   // [4] digit-scan warp totals
 };
@@ -312,7 +311,7 @@ __device__ __forceinline__ void bucket_pass(const uint64_t* src_k, const uint32_
         }
     }
     __syncthreads();
-    // per digit: exclusive prefix over the warps (BK_GROUPS groups of 4;
+    // per digit: exclusive prefix over the warps (BK_THREADS / RADIX groups;
     // thread (d, q) owns digit d of group q)
     const int d = threadIdx.x & (RADIX - 1), q = threadIdx.x >> 7;
     constexpr int WPQ = BK_WARPS / (BK_THREADS / RADIX);  // warps per (d, q) thread
@@ -366,9 +365,89 @@ __device__ __forceinline__ void bucket_pass(const uint64_t* src_k, const uint32_
     __syncthreads();
 }
 
+// Sort of m <= RANK_MAX pairs by one warp: a bitonic network over 32 E
+// slots (E = 1, 2 or 4 per lane, the unused ones +inf) on composite keys
+// (the key bits below the digits the pairs share, shifted left 7, plus the
+// pair's position): the composites are unique, so equal keys keep their
+// order and the network's instability does not matter.  The pair at rank r
+// lands at gk[r], gv[r].  O(m log^2 m) work in registers and shuffles.
+constexpr uint32_t RANK_MAX = 128;
+template <int E>
+__device__ __forceinline__ void warp_bitonic_sort(const uint64_t* sk, const uint32_t* sv, uint32_t m,
+                                                  uint64_t lowmask, uint64_t* gk, uint32_t* gv) {
+    const uint32_t lane = threadIdx.x & 31;
+    uint64_t v[E];
+#pragma unroll
+    for (int q = 0; q < E; q++) {
+        const uint32_t e = (uint32_t)q * 32u + lane;
+        v[q] = e < m ? (((sk[e] & lowmask) << 7) | e) : ~0ull;
+    }
+#pragma unroll
+    for (int k = 2; k <= 32 * E; k <<= 1) {
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            if (j >= 32) {  // partner in another slot of the same lane
+                const int qj = j >> 5;
+#pragma unroll
+                for (int q = 0; q < E; q++) {
+                    if (q & qj) continue;
+                    const uint32_t e = (uint32_t)q * 32u + lane;
+                    const bool asc = (e & (uint32_t)k) == 0u;
+                    const uint64_t x = v[q], y = v[q | qj];
+                    const uint64_t lo = x < y ? x : y, hi = x < y ? y : x;
+                    v[q] = asc ? lo : hi;
+                    v[q | qj] = asc ? hi : lo;
+                }
+            } else {  // partner in lane ^ j, same slot
+#pragma unroll
+                for (int q = 0; q < E; q++) {
+                    const uint64_t o = __shfl_xor_sync(0xffffffffu, v[q], j);
+                    const uint32_t e = (uint32_t)q * 32u + lane;
+                    const bool asc = (e & (uint32_t)k) == 0u;
+                    const bool lower = (lane & (uint32_t)j) == 0u;
+                    const uint64_t lo = v[q] < o ? v[q] : o, hi = v[q] < o ? o : v[q];
+                    v[q] = (lower == asc) ? lo : hi;
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < E; q++) {
+        const uint32_t e = (uint32_t)q * 32u + lane;
+        if (e < m) {
+            const uint32_t i = (uint32_t)(v[q] & 127u);
+            gk[e] = sk[i];
+            gv[e] = sv[i];
+        }
+    }
+}
+__device__ __forceinline__ void warp_small_sort(const uint64_t* sk, const uint32_t* sv, uint32_t m, uint64_t lowmask,
+                                                uint64_t* gk, uint32_t* gv) {
+    if (m <= 1u) {
+        if (m == 1u && (threadIdx.x & 31) == 0) {
+            gk[0] = sk[0];
+            gv[0] = sv[0];
+        }
+    } else if (m <= 32u) {
+        warp_bitonic_sort<1>(sk, sv, m, lowmask, gk, gv);
+    } else if (m <= 64u) {
+        warp_bitonic_sort<2>(sk, sv, m, lowmask, gk, gv);
+    } else {
+        warp_bitonic_sort<4>(sk, sv, m, lowmask, gk, gv);
+    }
+}
+
+// Bucket blockIdx.x of (Kb, Vb), sorted on its low digits, into (K, V).
+// Up to RANK_MAX pairs, warp 0 sorts the bucket.  A larger bucket takes one
+// stable pass on its next digit (most significant first), which cuts it
+// into 128 sub-buckets that are already in order among themselves; the
+// warps sort the sub-buckets of up to RANK_MAX pairs side by side, and the
+// CTA finishes any larger sub-bucket with LSD passes on the digits below.
+// A large bucket thus costs one pass and ~m log^2 m network steps per
+// sub-bucket instead of one pass per digit, and the biggest bucket (the
+// long pole of the launch) no longer runs six passes.
 // A bucket larger than BK_CAP is left alone and raises *big, which enables
 // the full tile passes queued after this kernel.
-// Bucket blockIdx.x of (Kb, Vb), sorted on its low digits, into (K, V).
 __global__ void __launch_bounds__(BK_THREADS, 1) k_bucket_sort(const uint64_t* __restrict__ Kb,
                                                                const uint32_t* __restrict__ Vb,
                                                                uint64_t* __restrict__ K, uint32_t* __restrict__ V,
@@ -410,20 +489,44 @@ __global__ void __launch_bounds__(BK_THREADS, 1) k_bucket_sort(const uint64_t* _
         v0[e] = Vb[start + e];
     }
     __syncthreads();
-    uint64_t *ka = k0, *kb = k1;
-    uint32_t *va = v0, *vb = v1;
-    for (int p = 0; p < low_passes; p++) {
-        bucket_pass(ka, va, kb, vb, size, p * RADIX_BITS, sc);
-        uint64_t* tk = ka;
-        ka = kb;
-        kb = tk;
-        uint32_t* tv = va;
-        va = vb;
-        vb = tv;
+    const int warp = threadIdx.x >> 5;
+    if (size <= RANK_MAX) {  // the pairs share the top digit only
+        if (warp == 0) warp_small_sort(k0, v0, size, (1ull << (low_passes * RADIX_BITS)) - 1ull, K + start, V + start);
+        return;
     }
-    for (uint32_t e = threadIdx.x; e < size; e += BK_THREADS) {
-        K[start + e] = ka[e];
-        V[start + e] = va[e];
+    // the next digit, most significant first: sub-bucket d is k1[run[d], run[d + 1])
+    const int msd = low_passes - 1;
+    bucket_pass(k0, v0, k1, v1, size, msd * RADIX_BITS, sc);
+    __shared__ uint32_t s_sub[RADIX + 1];  // bucket_pass below rewrites run[]
+    if (threadIdx.x < RADIX) s_sub[threadIdx.x] = sc.run[threadIdx.x];
+    if (threadIdx.x == 0) s_sub[RADIX] = size;
+    __syncthreads();
+    for (int d = warp; d < RADIX; d += BK_WARPS) {
+        const uint32_t lo = s_sub[d], hi = s_sub[d + 1];
+        if (hi - lo <= RANK_MAX)  // the pairs share every digit from msd up
+            warp_small_sort(k1 + lo, v1 + lo, hi - lo, (1ull << (msd * RADIX_BITS)) - 1ull, K + start + lo,
+                            V + start + lo);
+    }
+    // larger sub-buckets: LSD passes over the digits below, by the whole CTA
+    // (uniform loop: every thread reads the same s_sub[])
+    for (int d = 0; d < RADIX; d++) {
+        const uint32_t lo = s_sub[d], hi = s_sub[d + 1];
+        if (hi - lo <= RANK_MAX) continue;
+        uint64_t *ka = k1 + lo, *kb = k0 + lo;
+        uint32_t *va = v1 + lo, *vb = v0 + lo;
+        for (int p = 0; p < msd; p++) {
+            bucket_pass(ka, va, kb, vb, hi - lo, p * RADIX_BITS, sc);
+            uint64_t* tk = ka;
+            ka = kb;
+            kb = tk;
+            uint32_t* tv = va;
+            va = vb;
+            vb = tv;
+        }
+        for (uint32_t e = threadIdx.x; e < hi - lo; e += BK_THREADS) {
+            K[start + lo + e] = ka[e];
+            V[start + lo + e] = va[e];
+        }
     }
 }
 
@@ -623,12 +726,17 @@ int sf_sort_pairs(uint64_t* keys, uint32_t* vals, uint32_t n, int bits, SortWork
 // fall short), so the call completes and the context stays usable; the
 // order is then wrong for the keys after the withheld tile.
 // ---------------------------------------------------------------------------
-extern "C" int sfgpu_sort_withheld_check(const uint64_t* keys, uint32_t n, uint32_t withheld_tile,
-                                         uint32_t spin_limit, uint64_t* sorted, uint32_t* index,
-                                         uint32_t* status) {
+namespace {
+int sort_host_keys(const char* who, const uint64_t* keys, uint32_t n, int bits, bool no_buckets,
+                   uint32_t withheld_tile, uint32_t spin_limit, uint64_t* sorted, uint32_t* index,
+                   uint32_t* status) {
     sf_clear_error();
     if (!keys || !sorted || !index || !status || n == 0) {
-        sf_set_error("sfgpu_sort_withheld_check: NULL argument or n = 0");
+        sf_set_error("%s: NULL argument or n = 0", who);
+        return SFGPU_FAILURE;
+    }
+    if (bits < 1 || bits > 64) {
+        sf_set_error("%s: %d key bits (1..64)", who, bits);
         return SFGPU_FAILURE;
     }
     uint64_t* dk = nullptr;
@@ -648,22 +756,39 @@ extern "C" int sfgpu_sort_withheld_check(const uint64_t* keys, uint32_t n, uint3
         if (cudaMemcpy(dv, iota.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice) != cudaSuccess) break;
         if (cudaMemset(ds, 0, sizeof(uint32_t)) != cudaSuccess) break;
         if (sf_sort_alloc(w, n) != SFGPU_OK) break;
-        w.flags |= SORT_NO_BUCKETS;
+        if (no_buckets) w.flags |= SORT_NO_BUCKETS;
         if (spin_limit) w.spin_limit = spin_limit;
         w.withheld = withheld_tile;
-        if (sf_sort_pairs(dk, dv, n, RADIX_BITS, w, st, ds) != SFGPU_OK) break;
+        if (sf_sort_pairs(dk, dv, n, bits, w, st, ds) != SFGPU_OK) break;
         if (cudaStreamSynchronize(st) != cudaSuccess) break;
         if (cudaMemcpy(sorted, dk, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost) != cudaSuccess) break;
         if (cudaMemcpy(index, dv, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost) != cudaSuccess) break;
         if (cudaMemcpy(status, ds, sizeof(uint32_t), cudaMemcpyDeviceToHost) != cudaSuccess) break;
         rc = SFGPU_OK;
     } while (0);
-    if (rc != SFGPU_OK && !*sfgpu_last_error())
-        sf_set_error("sfgpu_sort_withheld_check: %s", cudaGetErrorString(cudaGetLastError()));
+    if (rc != SFGPU_OK && !*sfgpu_last_error()) sf_set_error("%s: %s", who, cudaGetErrorString(cudaGetLastError()));
     sf_sort_free(w);
     cudaFree(dk);
     cudaFree(dv);
     cudaFree(ds);
     if (st) cudaStreamDestroy(st);
     return rc;
+}
+}  // namespace
+
+extern "C" int sfgpu_sort_withheld_check(const uint64_t* keys, uint32_t n, uint32_t withheld_tile,
+                                         uint32_t spin_limit, uint64_t* sorted, uint32_t* index,
+                                         uint32_t* status) {
+    return sort_host_keys("sfgpu_sort_withheld_check", keys, n, RADIX_BITS, true, withheld_tile, spin_limit, sorted,
+                          index, status);
+}
+
+// The library's stable sort of (key, index) pairs on host keys, through the
+// same dispatch the tree build and the SPH cell grids use: up to 2^17 pairs
+// one tile pass on the top digit and the per-bucket CTAs (with the
+// cooperative tile passes behind them for a bucket over 8192 pairs), above
+// that one tile pass per 7-bit digit.
+extern "C" int sfgpu_sort_keys(const uint64_t* keys, uint32_t n, int bits, uint64_t* sorted, uint32_t* index,
+                               uint32_t* status) {
+    return sort_host_keys("sfgpu_sort_keys", keys, n, bits, false, 0xFFFFFFFFu, 0u, sorted, index, status);
 }

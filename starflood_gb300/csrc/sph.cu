@@ -28,6 +28,7 @@
 // cutoff as its radius when it reaches at most 4 cells (h_max <= 0.107),
 // else the all-pairs tiles.
 #include "internal.cuh"
+#include "chunks.cuh"
 #include "sph_grid.cuh"
 
 namespace {
@@ -60,6 +61,7 @@ struct SphWork {
     float2* pq = nullptr;       // sorted h, c = P / rho^2
     float* hw = nullptr;        // [0] h_max, [1] 88 h_max^2, [2] density on the grid (1) or all pairs (0)
     uint32_t* done = nullptr;   // [0] ticket, [1..] block partials
+    sfchunk::ChunkQueue q;      // the warp passes' chunks, heaviest first
 };
 
 __global__ void __launch_bounds__(SPH_BS) k_sph_density(const float* __restrict__ pos, const float* __restrict__ mas,
@@ -245,15 +247,22 @@ __global__ void k_ref_gather(const uint64_t* __restrict__ keys, const uint32_t* 
     cell[k] = pack_cell(cell_of(x, y, z, GRID_INV));
 }
 
+// with q.level set, also each 32-body chunk's cost estimate (the
+// populations of its bodies' buckets)
 __global__ void k_ref_mix(const uint64_t* __restrict__ keys, const uint32_t* __restrict__ V, uint32_t n,
-                          const uint32_t* __restrict__ bstart, const uint64_t* __restrict__ cell,
-                          uint32_t* __restrict__ bmix, uint64_t* __restrict__ bhash) {
+                          const uint32_t* __restrict__ bstart, const uint32_t* __restrict__ bend,
+                          const uint64_t* __restrict__ cell, uint32_t* __restrict__ bmix,
+                          uint64_t* __restrict__ bhash, sfchunk::ChunkQueue q) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    const uint32_t b = (uint32_t)keys[k];
-    const uint32_t s = bstart[b];
-    if (k != s && cell[k] != cell[s]) bmix[b] = 1u;
-    if (bhash) atomicAdd((unsigned long long*)&bhash[b], (unsigned long long)sf_mix64(V[k]));
+    uint32_t pop = 0;
+    if (k < n) {
+        const uint32_t b = (uint32_t)keys[k];
+        const uint32_t s = bstart[b];
+        if (k != s && cell[k] != cell[s]) bmix[b] = 1u;
+        if (bhash) atomicAdd((unsigned long long*)&bhash[b], (unsigned long long)sf_mix64(V[k]));
+        pop = bend[b] - s;
+    }
+    if (q.level && (k & ~31u) < n) sfchunk::note_cost(q, k >> 5, pop);
 }
 
 // One body against the cells of its reach: a callback per candidate pair,
@@ -277,21 +286,25 @@ __device__ __forceinline__ bool cell_lookup(int3 c, uint32_t mask, const uint32_
 }
 
 // FAST density on the grid: pairs with r^2 < 88 h_max^2 (the rest have
-// exp(-r^2/h^2) below FLT_MIN for both kernels)
-__global__ void __launch_bounds__(128) k_ref_density_grid(uint32_t n, uint32_t mask, const uint32_t* __restrict__ bstart,
-                                                          const uint32_t* __restrict__ bend,
-                                                          const uint32_t* __restrict__ bmix,
-                                                          const uint64_t* __restrict__ cell,
-                                                          const float4* __restrict__ px, const float2* __restrict__ pq,
-                                                          const uint32_t* __restrict__ V, const float* __restrict__ hw,
-                                                          float* __restrict__ rho) {
-    if (hw[2] == 0.0f) return;  // the all-pairs tiles have it
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    const float rd2 = hw[1];
-    const int reach = min(SET_REACH, (int)ceilf(sqrtf(rd2 * MARGIN_HI) * GRID_INV));
-    const float4 a = px[k];
-    const float hi = pq[k].x;
+// exp(-r^2/h^2) below FLT_MIN for both kernels).  The per-pair term:
+__device__ __forceinline__ float ref_density_term(float r2, float ai3, float ihi2, float hj, float mj,
+                                                  float inv_sqrt_pi) {
+    const float aj = __fdividef(inv_sqrt_pi, hj);
+    const float wi = ai3 * expf(-r2 * ihi2);
+    const float wj = aj * aj * aj * expf(-r2 / (hj * hj));
+    return 0.5f * (wi + wj) * mj;
+}
+__device__ __forceinline__ int ref_density_reach(float rd2) {
+    return min(SET_REACH, (int)ceilf(sqrtf(rd2 * MARGIN_HI) * GRID_INV));
+}
+// One body's scan: every cell within `reach` whose box comes within the
+// radius, every pair tested.
+__device__ __forceinline__ float ref_density_body(const float4& a, float hi, float rd2, int reach, uint32_t mask,
+                                                  const uint32_t* __restrict__ bstart,
+                                                  const uint32_t* __restrict__ bend,
+                                                  const uint32_t* __restrict__ bmix,
+                                                  const uint64_t* __restrict__ cell, const float4* __restrict__ px,
+                                                  const float2* __restrict__ pq) {
     const float inv_sqrt_pi = (float)K_INV_SQRT_PI;
     const float ai = __fdividef(inv_sqrt_pi, hi);
     const float ai3 = ai * ai * ai;
@@ -314,14 +327,139 @@ __global__ void __launch_bounds__(128) k_ref_density_grid(uint32_t n, uint32_t m
                     const float ex = fsub(a.x, q.x), ey = fsub(a.y, q.y), ez = fsub(a.z, q.z);
                     const float r2 = fadd(fadd(fmul(ex, ex), fmul(ey, ey)), fmul(ez, ez));
                     if (!(r2 < rd2)) continue;
-                    const float hj = pq[j].x;
-                    const float aj = __fdividef(inv_sqrt_pi, hj);
-                    const float wi = ai3 * expf(-r2 * ihi2);
-                    const float wj = aj * aj * aj * expf(-r2 / (hj * hj));
-                    sum += 0.5f * (wi + wj) * q.w;
+                    sum += ref_density_term(r2, ai3, ihi2, pq[j].x, q.w, inv_sqrt_pi);
                 }
             }
-    rho[V[k]] = sum;
+    return sum;
+}
+
+// One thread per sorted body (sph_path 2).
+__global__ void __launch_bounds__(128) k_ref_density_grid(uint32_t n, uint32_t mask, const uint32_t* __restrict__ bstart,
+                                                          const uint32_t* __restrict__ bend,
+                                                          const uint32_t* __restrict__ bmix,
+                                                          const uint64_t* __restrict__ cell,
+                                                          const float4* __restrict__ px, const float2* __restrict__ pq,
+                                                          const uint32_t* __restrict__ V, const float* __restrict__ hw,
+                                                          float* __restrict__ rho) {
+    if (hw[2] == 0.0f) return;  // the all-pairs tiles have it
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const float rd2 = hw[1];
+    rho[V[k]] = ref_density_body(px[k], pq[k].x, rd2, ref_density_reach(rd2), mask, bstart, bend, bmix, cell, px, pq);
+}
+
+// The grid passes by warps (the default): one warp per 32 consecutive
+// sorted bodies, which nearly always share a cell of side 1/4.  The warp
+// visits the union of its bodies' cells; each lane classifies every cell
+// exactly as its per-body scan would (reach, box distance), the cell's
+// bodies are staged in shared memory 32 at a time, each lane first takes
+// its neighbour decisions over the staged bodies into a bit mask and then
+// evaluates its own terms in candidate order.  So every body adds the same
+// terms in the same order as the per-body scan, while the warp's loads are
+// coalesced and its loops no longer diverge body by body.  A warp whose
+// bodies span more than 3 cells on an axis, or reach beyond the packed
+// key's range, runs the per-body scans.  The warps are persistent and take
+// their chunks heaviest first (chunks.cuh).
+constexpr int RW_WARPS = 4;
+
+__device__ __forceinline__ void ref_density_chunk(uint32_t k0, uint32_t n, uint32_t mask,
+                                                  const uint32_t* __restrict__ bstart,
+                                                  const uint32_t* __restrict__ bend,
+                                                  const uint32_t* __restrict__ bmix,
+                                                  const uint64_t* __restrict__ cell, const float4* __restrict__ px,
+                                                  const float2* __restrict__ pq, const uint32_t* __restrict__ V,
+                                                  const float* __restrict__ hw, float* __restrict__ rho, float4* sq,
+                                                  float* sh) {
+    const int lane = threadIdx.x & 31;
+    if (k0 >= n) return;
+    const uint32_t k = k0 + (uint32_t)lane;
+    const bool live = k < n;
+    const uint32_t kk = live ? k : n - 1u;
+    const float rd2 = hw[1];
+    const int reach = ref_density_reach(rd2);
+    const float4 a = px[kk];
+    const float hi = pq[kk].x;
+    const int3 c0 = cell_of(a.x, a.y, a.z, GRID_INV);
+    const int zlo = __reduce_min_sync(0xffffffffu, c0.z), zhi = __reduce_max_sync(0xffffffffu, c0.z);
+    const int ylo = __reduce_min_sync(0xffffffffu, c0.y), yhi = __reduce_max_sync(0xffffffffu, c0.y);
+    const int xlo = __reduce_min_sync(0xffffffffu, c0.x), xhi = __reduce_max_sync(0xffffffffu, c0.x);
+    const bool compact = (uint32_t)zhi - (uint32_t)zlo <= 2u && (uint32_t)yhi - (uint32_t)ylo <= 2u &&
+                         (uint32_t)xhi - (uint32_t)xlo <= 2u && !__any_sync(0xffffffffu, cell_clamped(c0));
+    if (!compact) {
+        if (live) rho[V[k]] = ref_density_body(a, hi, rd2, reach, mask, bstart, bend, bmix, cell, px, pq);
+        return;
+    }
+    const float inv_sqrt_pi = (float)K_INV_SQRT_PI;
+    const float ai = __fdividef(inv_sqrt_pi, hi);
+    const float ai3 = ai * ai * ai;
+    const float ihi2 = 1.0f / (hi * hi);
+    float sum = 0.0f;
+    for (int cz = zlo - reach; cz <= zhi + reach; cz++)
+        for (int cy = ylo - reach; cy <= yhi + reach; cy++)
+            for (int cx = xlo - reach; cx <= xhi + reach; cx++) {
+                const int3 c = make_int3(cx, cy, cz);
+                bool need = false;
+                if (live && abs(cx - c0.x) <= reach && abs(cy - c0.y) <= reach && abs(cz - c0.z) <= reach) {
+                    float dmin2, dmax2;
+                    box_dist2(a.x, a.y, a.z, c.x * GRID_SIDE, c.y * GRID_SIDE, c.z * GRID_SIDE, GRID_SIDE, dmin2,
+                              dmax2);
+                    need = !(dmin2 * MARGIN_LO > rd2);
+                }
+                if (!__any_sync(0xffffffffu, need)) continue;
+                CellRange r;
+                uint32_t b;
+                if (!cell_lookup(c, mask, bstart, bend, bmix, cell, r, b)) continue;
+                for (uint32_t jb = r.j0; jb < r.j1; jb += 32u) {
+                    const uint32_t j = jb + (uint32_t)lane;
+                    const bool ok = j < r.j1 && (!r.chk || cell[j] == r.want);
+                    __syncwarp();
+                    if (ok) {
+                        sq[lane] = px[j];
+                        sh[lane] = pq[j].x;
+                    }
+                    const uint32_t vm = __ballot_sync(0xffffffffu, ok);
+                    __syncwarp();
+                    uint32_t hits = 0u;
+                    if (need) {
+                        for (uint32_t mm = vm; mm; mm &= mm - 1u) {
+                            const int t = __ffs(mm) - 1;
+                            const float4 q = sq[t];
+                            const float ex = fsub(a.x, q.x), ey = fsub(a.y, q.y), ez = fsub(a.z, q.z);
+                            const float r2 = fadd(fadd(fmul(ex, ex), fmul(ey, ey)), fmul(ez, ez));
+                            if (r2 < rd2) hits |= 1u << t;
+                        }
+                    }
+                    while (__any_sync(0xffffffffu, hits != 0u)) {
+                        if (hits) {
+                            const int t = __ffs(hits) - 1;
+                            hits &= hits - 1u;
+                            const float4 q = sq[t];
+                            const float ex = fsub(a.x, q.x), ey = fsub(a.y, q.y), ez = fsub(a.z, q.z);
+                            const float r2 = fadd(fadd(fmul(ex, ex), fmul(ey, ey)), fmul(ez, ez));
+                            sum += ref_density_term(r2, ai3, ihi2, sh[t], q.w, inv_sqrt_pi);
+                        }
+                    }
+                }
+            }
+    if (live) rho[V[k]] = sum;
+}
+
+__global__ void __launch_bounds__(RW_WARPS * 32) k_ref_density_warp(
+    uint32_t n, uint32_t mask, const uint32_t* __restrict__ bstart, const uint32_t* __restrict__ bend,
+    const uint32_t* __restrict__ bmix, const uint64_t* __restrict__ cell, const float4* __restrict__ px,
+    const float2* __restrict__ pq, const uint32_t* __restrict__ V, const float* __restrict__ hw,
+    float* __restrict__ rho, sfchunk::ChunkQueue q) {
+    __shared__ float4 s_q[RW_WARPS][32];
+    __shared__ float s_h[RW_WARPS][32];
+    if (hw[2] == 0.0f) return;  // the all-pairs tiles have it (no warp takes a chunk)
+    const int w = threadIdx.x >> 5;
+    sfchunk::Taker t = sfchunk::taker(q);
+    for (;;) {
+        const uint32_t c = sfchunk::next(q, t, 0u);
+        if (c == 0xFFFFFFFFu) break;
+        ref_density_chunk(c * 32u, n, mask, bstart, bend, bmix, cell, px, pq, V, hw, rho, s_q[w], s_h[w]);
+    }
+    sfchunk::warp_exit(q, gridDim.x * RW_WARPS);
 }
 
 // pressure (sph.c:148-159) into the slab, c = P/rho^2 into the sorted records
@@ -339,27 +477,33 @@ __global__ void k_ref_eos(const uint32_t* __restrict__ V, uint32_t n, float* __r
 }
 
 // FAST momentum on the grid: the set {j : fl(r^2) <= 1} (cells inside the
-// radius taken whole), force terms where r^2 < 88 h_max^2
+// radius taken whole), force terms where r^2 < 88 h_max^2.  The per-pair
+// term (sph.c:254-268, FAST arithmetic):
+__device__ __forceinline__ void ref_momentum_term(float ex, float ey, float ez, float r2, float ihi2, float m2_den_i,
+                                                  float ci, float hj, float cj, float pi15, float& sx, float& sy,
+                                                  float& sz) {
+    const float ni = m2_den_i * expf(-r2 * ihi2);
+    const float nj = -2.0f * expf(-r2 / (hj * hj)) / (pi15 * hj * hj * hj * hj * hj);
+    const float g = 0.5f * (ni + nj) * (ci + cj);
+    sx += g * ex;
+    sy += g * ey;
+    sz += g * ez;
+}
+
+// One body's scan: every cell within 4 whose box comes within the radius.
 template <bool HASH>
-__global__ void __launch_bounds__(128) k_ref_momentum_grid(
-    uint32_t n, uint32_t mask, const uint32_t* __restrict__ bstart, const uint32_t* __restrict__ bend,
-    const uint32_t* __restrict__ bmix, const uint64_t* __restrict__ bhash, const uint64_t* __restrict__ cell,
-    const float4* __restrict__ px, const float2* __restrict__ pq, const uint32_t* __restrict__ V,
-    const float* __restrict__ hw, float* __restrict__ acc, uint32_t* __restrict__ nbr,
-    uint64_t* __restrict__ hash) {
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    const float rf2 = hw[1];
-    const float4 a = px[k];
-    const float2 qi = pq[k];
-    const float hi = qi.x, ci = qi.y;
+__device__ __forceinline__ void ref_momentum_body(const float4& a, float hi, float ci, float rf2, uint32_t mask,
+                                                  const uint32_t* __restrict__ bstart,
+                                                  const uint32_t* __restrict__ bend,
+                                                  const uint32_t* __restrict__ bmix,
+                                                  const uint64_t* __restrict__ bhash,
+                                                  const uint64_t* __restrict__ cell, const float4* __restrict__ px,
+                                                  const float2* __restrict__ pq, const uint32_t* __restrict__ V,
+                                                  float& sx, float& sy, float& sz, uint32_t& count, uint64_t& hs) {
     const float pi15 = (float)K_PI_1_5;
     const float ihi2 = 1.0f / (hi * hi);
     const float m2_den_i = -2.0f / (pi15 * hi * hi * hi * hi * hi);
     const int3 c0 = cell_of(a.x, a.y, a.z, GRID_INV);
-    float sx = 0.f, sy = 0.f, sz = 0.f;
-    uint32_t count = 0;
-    uint64_t hs = 0;
     for (int dz = -SET_REACH; dz <= SET_REACH; dz++)
         for (int dy = -SET_REACH; dy <= SET_REACH; dy++)
             for (int dx = -SET_REACH; dx <= SET_REACH; dx++) {
@@ -388,22 +532,166 @@ __global__ void __launch_bounds__(128) k_ref_momentum_grid(
                     }
                     if (!(r2 < rf2)) continue;
                     const float2 qj = pq[j];
-                    const float hj = qj.x;
-                    const float ni = m2_den_i * expf(-r2 * ihi2);
-                    const float nj = -2.0f * expf(-r2 / (hj * hj)) / (pi15 * hj * hj * hj * hj * hj);
-                    const float g = 0.5f * (ni + nj) * (ci + qj.y);
-                    sx += g * ex;
-                    sy += g * ey;
-                    sz += g * ez;
+                    ref_momentum_term(ex, ey, ez, r2, ihi2, m2_den_i, ci, qj.x, qj.y, pi15, sx, sy, sz);
                 }
             }
-    const uint32_t p = V[k];
-    const float mi = a.w;
+}
+
+// sph.c:274-276: acc += -m_i * sum
+__device__ __forceinline__ void ref_momentum_store(uint32_t p, float mi, float sx, float sy, float sz, uint32_t count,
+                                                   uint64_t hs, bool with_hash, float* __restrict__ acc,
+                                                   uint32_t* __restrict__ nbr, uint64_t* __restrict__ hash) {
     acc[3u * p + 0u] = fadd(acc[3u * p + 0u], fmul(-mi, sx));
     acc[3u * p + 1u] = fadd(acc[3u * p + 1u], fmul(-mi, sy));
     acc[3u * p + 2u] = fadd(acc[3u * p + 2u], fmul(-mi, sz));
     nbr[p] = count;
-    if (HASH) hash[p] = hs;
+    if (with_hash) hash[p] = hs;
+}
+
+// One thread per sorted body (sph_path 2).
+template <bool HASH>
+__global__ void __launch_bounds__(128) k_ref_momentum_grid(
+    uint32_t n, uint32_t mask, const uint32_t* __restrict__ bstart, const uint32_t* __restrict__ bend,
+    const uint32_t* __restrict__ bmix, const uint64_t* __restrict__ bhash, const uint64_t* __restrict__ cell,
+    const float4* __restrict__ px, const float2* __restrict__ pq, const uint32_t* __restrict__ V,
+    const float* __restrict__ hw, float* __restrict__ acc, uint32_t* __restrict__ nbr,
+    uint64_t* __restrict__ hash) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const float4 a = px[k];
+    const float2 qi = pq[k];
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+    uint32_t count = 0;
+    uint64_t hs = 0;
+    ref_momentum_body<HASH>(a, qi.x, qi.y, hw[1], mask, bstart, bend, bmix, bhash, cell, px, pq, V, sx, sy, sz, count,
+                            hs);
+    ref_momentum_store(V[k], a.w, sx, sy, sz, count, hs, HASH, acc, nbr, hash);
+}
+
+// The default momentum pass, by warps (see k_ref_density_warp).  A lane
+// whose box test puts a cell wholly inside the radius counts it whole (as
+// its per-body scan does) and tests its bodies only for force terms.
+template <bool HASH>
+__device__ __forceinline__ void ref_momentum_chunk(
+    uint32_t k0, uint32_t n, uint32_t mask, const uint32_t* __restrict__ bstart, const uint32_t* __restrict__ bend,
+    const uint32_t* __restrict__ bmix, const uint64_t* __restrict__ bhash, const uint64_t* __restrict__ cell,
+    const float4* __restrict__ px, const float2* __restrict__ pq, const uint32_t* __restrict__ V,
+    const float* __restrict__ hw, float* __restrict__ acc, uint32_t* __restrict__ nbr, uint64_t* __restrict__ hash,
+    float4* sq, float2* sp, uint64_t* sm) {
+    const int lane = threadIdx.x & 31;
+    if (k0 >= n) return;
+    const uint32_t k = k0 + (uint32_t)lane;
+    const bool live = k < n;
+    const uint32_t kk = live ? k : n - 1u;
+    const float rf2 = hw[1];
+    const float4 a = px[kk];
+    const float2 qi = pq[kk];
+    const float hi = qi.x, ci = qi.y;
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+    uint32_t count = 0;
+    uint64_t hs = 0;
+    const int3 c0 = cell_of(a.x, a.y, a.z, GRID_INV);
+    const int zlo = __reduce_min_sync(0xffffffffu, c0.z), zhi = __reduce_max_sync(0xffffffffu, c0.z);
+    const int ylo = __reduce_min_sync(0xffffffffu, c0.y), yhi = __reduce_max_sync(0xffffffffu, c0.y);
+    const int xlo = __reduce_min_sync(0xffffffffu, c0.x), xhi = __reduce_max_sync(0xffffffffu, c0.x);
+    const bool compact = (uint32_t)zhi - (uint32_t)zlo <= 2u && (uint32_t)yhi - (uint32_t)ylo <= 2u &&
+                         (uint32_t)xhi - (uint32_t)xlo <= 2u && !__any_sync(0xffffffffu, cell_clamped(c0));
+    if (!compact) {
+        if (live) {
+            ref_momentum_body<HASH>(a, hi, ci, rf2, mask, bstart, bend, bmix, bhash, cell, px, pq, V, sx, sy, sz,
+                                    count, hs);
+            ref_momentum_store(V[k], a.w, sx, sy, sz, count, hs, HASH, acc, nbr, hash);
+        }
+        return;
+    }
+    const float pi15 = (float)K_PI_1_5;
+    const float ihi2 = 1.0f / (hi * hi);
+    const float m2_den_i = -2.0f / (pi15 * hi * hi * hi * hi * hi);
+    for (int cz = zlo - SET_REACH; cz <= zhi + SET_REACH; cz++)
+        for (int cy = ylo - SET_REACH; cy <= yhi + SET_REACH; cy++)
+            for (int cx = xlo - SET_REACH; cx <= xhi + SET_REACH; cx++) {
+                const int3 c = make_int3(cx, cy, cz);
+                bool need = false;
+                float dmin2 = 0.f, dmax2 = 0.f;
+                if (live && abs(cx - c0.x) <= SET_REACH && abs(cy - c0.y) <= SET_REACH &&
+                    abs(cz - c0.z) <= SET_REACH) {
+                    box_dist2(a.x, a.y, a.z, c.x * GRID_SIDE, c.y * GRID_SIDE, c.z * GRID_SIDE, GRID_SIDE, dmin2,
+                              dmax2);
+                    need = !(dmin2 * MARGIN_LO > 1.0f);
+                }
+                if (!__any_sync(0xffffffffu, need)) continue;
+                CellRange r;
+                uint32_t b;
+                if (!cell_lookup(c, mask, bstart, bend, bmix, cell, r, b)) continue;
+                const bool whole = need && !r.chk && !cell_clamped(c) && dmax2 * MARGIN_HI < 1.0f;
+                if (whole) {
+                    count += r.j1 - r.j0;
+                    if (HASH) hs += bhash[b];
+                }
+                const bool pairs = need && !(whole && dmin2 * MARGIN_LO >= rf2);
+                if (!__any_sync(0xffffffffu, pairs)) continue;
+                for (uint32_t jb = r.j0; jb < r.j1; jb += 32u) {
+                    const uint32_t j = jb + (uint32_t)lane;
+                    const bool ok = j < r.j1 && (!r.chk || cell[j] == r.want);
+                    __syncwarp();
+                    if (ok) {
+                        sq[lane] = px[j];
+                        sp[lane] = pq[j];
+                        if (HASH) sm[lane] = sf_mix64(V[j]);
+                    }
+                    const uint32_t vm = __ballot_sync(0xffffffffu, ok);
+                    __syncwarp();
+                    uint32_t hits = 0u;
+                    if (pairs) {
+                        for (uint32_t mm = vm; mm; mm &= mm - 1u) {
+                            const int t = __ffs(mm) - 1;
+                            const float4 q = sq[t];
+                            const float ex = fsub(a.x, q.x), ey = fsub(a.y, q.y), ez = fsub(a.z, q.z);
+                            const float r2 = fadd(fadd(fmul(ex, ex), fmul(ey, ey)), fmul(ez, ez));
+                            if (!whole) {
+                                if (r2 > 1.0f) continue;  // sph.c:231
+                                count++;
+                                if (HASH) hs += sm[t];
+                            }
+                            if (r2 < rf2) hits |= 1u << t;
+                        }
+                    }
+                    while (__any_sync(0xffffffffu, hits != 0u)) {
+                        if (hits) {
+                            const int t = __ffs(hits) - 1;
+                            hits &= hits - 1u;
+                            const float4 q = sq[t];
+                            const float ex = fsub(a.x, q.x), ey = fsub(a.y, q.y), ez = fsub(a.z, q.z);
+                            const float r2 = fadd(fadd(fmul(ex, ex), fmul(ey, ey)), fmul(ez, ez));
+                            const float2 qj = sp[t];
+                            ref_momentum_term(ex, ey, ez, r2, ihi2, m2_den_i, ci, qj.x, qj.y, pi15, sx, sy, sz);
+                        }
+                    }
+                }
+            }
+    if (live) ref_momentum_store(V[k], a.w, sx, sy, sz, count, hs, HASH, acc, nbr, hash);
+}
+
+template <bool HASH>
+__global__ void __launch_bounds__(RW_WARPS * 32) k_ref_momentum_warp(
+    uint32_t n, uint32_t mask, const uint32_t* __restrict__ bstart, const uint32_t* __restrict__ bend,
+    const uint32_t* __restrict__ bmix, const uint64_t* __restrict__ bhash, const uint64_t* __restrict__ cell,
+    const float4* __restrict__ px, const float2* __restrict__ pq, const uint32_t* __restrict__ V,
+    const float* __restrict__ hw, float* __restrict__ acc, uint32_t* __restrict__ nbr,
+    uint64_t* __restrict__ hash, sfchunk::ChunkQueue q) {
+    __shared__ float4 s_q[RW_WARPS][32];
+    __shared__ float2 s_p[RW_WARPS][32];
+    __shared__ uint64_t s_m[RW_WARPS][HASH ? 32 : 1];
+    const int w = threadIdx.x >> 5;
+    sfchunk::Taker t = sfchunk::taker(q);
+    const uint32_t pass = hw[2] != 0.0f ? 1u : 0u;  // after the grid density pass, or first
+    for (;;) {
+        const uint32_t c = sfchunk::next(q, t, pass);
+        if (c == 0xFFFFFFFFu) break;
+        ref_momentum_chunk<HASH>(c * 32u, n, mask, bstart, bend, bmix, bhash, cell, px, pq, V, hw, acc, nbr, hash,
+                                 s_q[w], s_p[w], s_m[w]);
+    }
+    sfchunk::warp_exit(q, gridDim.x * RW_WARPS);
 }
 
 }  // namespace
@@ -441,6 +729,7 @@ int sf_sph_alloc(sfgpu_sim* s) {
     SF_CUDA(cudaMalloc(&w->hw, sizeof(float) * 4));
     SF_CUDA(cudaMalloc(&w->done, sizeof(uint32_t) * (1 + 1024)));
     SF_CUDA(cudaMemset(w->done, 0, sizeof(uint32_t) * (1 + 1024)));
+    if (sfchunk::alloc(w->q, n) != SFGPU_OK) return SFGPU_FAILURE;
     return SFGPU_OK;
 }
 
@@ -462,6 +751,7 @@ void sf_sph_free(sfgpu_sim* s) {
     cudaFree(w->pq);
     cudaFree(w->hw);
     cudaFree(w->done);
+    sfchunk::release(w->q);
     delete w;
     s->sph = nullptr;
 }
@@ -515,12 +805,30 @@ int sf_stage_sph(sfgpu_sim* s) {
     if (w->bhash) SF_CUDA(cudaMemsetAsync(w->bhash, 0, sizeof(uint64_t) * w->tsize, st));
     k_ref_gather<<<nb, 256, 0, st>>>(w->keys, w->vals, n, slab, w->bstart, w->bend, w->px, w->pq, w->cell);
     SF_CHECK_LAUNCH();
-    k_ref_mix<<<nb, 256, 0, st>>>(w->keys, w->vals, n, w->bstart, w->cell, w->bmix, w->bhash);
+    const bool by_warp = s->p.sph_path != 2;
+    sfchunk::ChunkQueue q = w->q;
+    if (!by_warp) q.level = nullptr;  // the per-body passes take no chunks
+    k_ref_mix<<<nb, 256, 0, st>>>(w->keys, w->vals, n, w->bstart, w->bend, w->cell, w->bmix, w->bhash, q);
     SF_CHECK_LAUNCH();
+    if (by_warp) {
+        sfchunk::k_chunk_order<<<1, 1024, 0, st>>>(w->q);
+        SF_CHECK_LAUNCH();
+    }
     s->timer.end(st, tk);
     tk = s->timer.begin(st, "sph_density");
-    k_ref_density_grid<<<sf_ceil_div(n, 128), 128, 0, st>>>(n, mask, w->bstart, w->bend, w->bmix, w->cell, w->px,
-                                                           w->pq, w->vals, w->hw, rho);
+    static uint32_t wave[3] = {0, 0, 0};  // density, momentum with hashes, momentum
+    if (!wave[0]) {
+        wave[0] = sfchunk::wave_blocks(k_ref_density_warp, RW_WARPS * 32, 0xFFFFFFFFu);
+        wave[1] = sfchunk::wave_blocks(k_ref_momentum_warp<true>, RW_WARPS * 32, 0xFFFFFFFFu);
+        wave[2] = sfchunk::wave_blocks(k_ref_momentum_warp<false>, RW_WARPS * 32, 0xFFFFFFFFu);
+    }
+    const uint32_t most = sf_ceil_div(w->q.nchunks, RW_WARPS);
+    if (by_warp)
+        k_ref_density_warp<<<std::min(wave[0], most), RW_WARPS * 32, 0, st>>>(
+            n, mask, w->bstart, w->bend, w->bmix, w->cell, w->px, w->pq, w->vals, w->hw, rho, w->q);
+    else
+        k_ref_density_grid<<<sf_ceil_div(n, 128), 128, 0, st>>>(n, mask, w->bstart, w->bend, w->bmix, w->cell,
+                                                               w->px, w->pq, w->vals, w->hw, rho);
     SF_CHECK_LAUNCH();
     k_sph_density<<<grid, SPH_BS, 0, st>>>(pos, mas, rad, n, 0, w->hw, rho);
     SF_CHECK_LAUNCH();
@@ -528,7 +836,15 @@ int sf_stage_sph(sfgpu_sim* s) {
     SF_CHECK_LAUNCH();
     s->timer.end(st, tk);
     tk = s->timer.begin(st, "sph_force");
-    if (w->hash)
+    if (by_warp && w->hash)
+        k_ref_momentum_warp<true><<<std::min(wave[1], most), RW_WARPS * 32, 0, st>>>(
+            n, mask, w->bstart, w->bend, w->bmix, w->bhash, w->cell, w->px, w->pq, w->vals, w->hw, acc, w->nbr,
+            w->hash, w->q);
+    else if (by_warp)
+        k_ref_momentum_warp<false><<<std::min(wave[2], most), RW_WARPS * 32, 0, st>>>(
+            n, mask, w->bstart, w->bend, w->bmix, nullptr, w->cell, w->px, w->pq, w->vals, w->hw, acc, w->nbr,
+            nullptr, w->q);
+    else if (w->hash)
         k_ref_momentum_grid<true><<<sf_ceil_div(n, 128), 128, 0, st>>>(n, mask, w->bstart, w->bend, w->bmix,
                                                                        w->bhash, w->cell, w->px, w->pq, w->vals,
                                                                        w->hw, acc, w->nbr, w->hash);

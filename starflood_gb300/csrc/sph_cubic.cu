@@ -28,7 +28,10 @@
 // skipped by cell key, so none is counted twice.  With SFGPU_FLAG_STATS the
 // density pass also sums an order-independent hash of every body's
 // neighbour set (j = i included).
+#include <climits>
+
 #include "internal.cuh"
+#include "chunks.cuh"
 #include "sph_grid.cuh"
 
 namespace {
@@ -40,7 +43,8 @@ constexpr float MARGIN_HI = 1.0f + 1.0f / 1024.0f;
 
 struct CubicWork {
     uint32_t tbits = 0, tsize = 0;
-    int reach = 2;
+    int reach = 1;
+    uint32_t path = 0;  // sfgpu_params.sph_path
     uint64_t* keys = nullptr;
     uint32_t* vals = nullptr;
     SortWork sort;
@@ -55,6 +59,7 @@ struct CubicWork {
     uint64_t* mixv = nullptr;  // sorted: hash of each body's index (SFGPU_FLAG_STATS)
     float* grid = nullptr;     // [0] cell side, [1] 1/side, [2] search radius R = 2 h_max
     uint32_t* done = nullptr;
+    sfchunk::ChunkQueue q;     // the warp passes' chunks, heaviest first
 };
 
 // The kernel and its derivative from q = r / h and 1 / h (the passes keep
@@ -151,14 +156,20 @@ __global__ void k_cell_gather(const uint64_t* __restrict__ keys, const uint32_t*
     if (mixv) mixv[k] = sf_mix64(p);
 }
 
-// buckets that hold more than one cell
+// buckets that hold more than one cell; with q.level set, each 32-body
+// chunk's cost estimate (the populations of its bodies' buckets)
 __global__ void k_bucket_mix(const uint64_t* __restrict__ keys, uint32_t n, const uint32_t* __restrict__ bstart,
-                             const uint64_t* __restrict__ cell, uint32_t* __restrict__ bmix) {
+                             const uint32_t* __restrict__ bend, const uint64_t* __restrict__ cell,
+                             uint32_t* __restrict__ bmix, sfchunk::ChunkQueue q) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    const uint32_t b = (uint32_t)keys[k];
-    const uint32_t s = bstart[b];
-    if (k != s && cell[k] != cell[s]) bmix[b] = 1u;
+    uint32_t pop = 0;
+    if (k < n) {
+        const uint32_t b = (uint32_t)keys[k];
+        const uint32_t s = bstart[b];
+        if (k != s && cell[k] != cell[s]) bmix[b] = 1u;
+        pop = bend[b] - s;
+    }
+    if (q.level && (k & ~31u) < n) sfchunk::note_cost(q, k >> 5, pop);
 }
 
 __device__ __forceinline__ bool density_pair(const float4& a, float hi, float ihi, const float4& q, float hj,
@@ -199,36 +210,19 @@ __device__ __forceinline__ void force_pair(const float4& a, float hi, const floa
     du += q.w * (di.y + 0.5f * visc) * g * vr;
 }
 
-// One thread per sorted body: the rows of cells within R, each row's
-// x-range of cells within R, every candidate tested.
+// The per-body scan: the rows of cells within R of body k, each row's
+// x-range of cells within R, every candidate tested; results in o0..o3,
+// count, hs.
 template <int REACH, bool FORCE, bool HASH>
-__global__ void __launch_bounds__(128) k_cubic_body(uint32_t n, const float* __restrict__ grid, uint32_t mask,
-                                                    const uint32_t* __restrict__ bstart,
-                                                    const uint32_t* __restrict__ bend,
-                                                    const uint32_t* __restrict__ bmix, const float4* __restrict__ px,
-                                                    const float4* __restrict__ ph, const float4* __restrict__ pv,
-                                                    const uint64_t* __restrict__ cell, float4* __restrict__ pd,
-                                                    const uint32_t* __restrict__ V, float gamma, float alpha,
-                                                    float beta, float* __restrict__ slab, float* __restrict__ dudt,
-                                                    uint32_t* __restrict__ nbr, const uint64_t* __restrict__ mixv,
-                                                    uint64_t* __restrict__ hash) {
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    const float side = grid[0], inv = grid[1], R = grid[2];
-    const float R2 = R * R * MARGIN_HI;
-    const float4 a = px[k];
-    const float hi = ph[k].x;
-    const float ihi = 1.0f / hi;
-    float4 di = make_float4(0.f, 0.f, 0.f, 0.f), vi = di;
-    if (FORCE) {
-        di = pd[k];
-        di.w = ihi;  // the pair terms take body i's 1 / h
-        vi = pv[k];
-    }
+__device__ __forceinline__ void body_scan(uint32_t k, const float4& a, float hi, float ihi, const float4& di,
+                                          const float4& vi, float side, float inv, float R2, uint32_t mask,
+                                          const uint32_t* __restrict__ bstart, const uint32_t* __restrict__ bend,
+                                          const uint32_t* __restrict__ bmix, const float4* __restrict__ px,
+                                          const float4* __restrict__ ph, const float4* __restrict__ pv,
+                                          const uint64_t* __restrict__ cell, const float4* __restrict__ pd,
+                                          float alpha, float beta, const uint64_t* __restrict__ mixv, float& o0,
+                                          float& o1, float& o2, float& o3, uint32_t& count, uint64_t& hs) {
     const int3 c0 = cell_of(a.x, a.y, a.z, inv);
-    float o0 = 0.f, o1 = 0.f, o2 = 0.f, o3 = 0.f;
-    uint32_t count = 0;
-    uint64_t hs = 0;
     for (int dz = -REACH; dz <= REACH; dz++) {
         const float lz = (float)(c0.z + dz) * side;
         const float gz = fmaxf(0.f, fmaxf(lz - a.z, a.z - (lz + side)));
@@ -265,6 +259,17 @@ __global__ void __launch_bounds__(128) k_cubic_body(uint32_t n, const float* __r
             }
         }
     }
+}
+
+// Results of body k (sorted slot) to the slab: density pass rho, P, the
+// (rho, P/rho^2, c, h) record, neighbour count and hash; force pass the
+// added acceleration and du/dt.
+template <bool FORCE, bool HASH>
+__device__ __forceinline__ void body_store(uint32_t k, uint32_t n, const float4* __restrict__ ph,
+                                           float4* __restrict__ pd, const uint32_t* __restrict__ V, float gamma,
+                                           float* __restrict__ slab, float* __restrict__ dudt,
+                                           uint32_t* __restrict__ nbr, uint64_t* __restrict__ hash, float o0,
+                                           float o1, float o2, float o3, uint32_t count, uint64_t hs) {
     const uint32_t p = V[k];
     if (!FORCE) {
         const float4 hh = ph[k];
@@ -284,14 +289,232 @@ __global__ void __launch_bounds__(128) k_cubic_body(uint32_t n, const float* __r
     }
 }
 
+// One thread per sorted body (sfgpu_params.sph_path 1 and 2).
+template <int REACH, bool FORCE, bool HASH>
+__global__ void __launch_bounds__(128) k_cubic_body(uint32_t n, const float* __restrict__ grid, uint32_t mask,
+                                                    const uint32_t* __restrict__ bstart,
+                                                    const uint32_t* __restrict__ bend,
+                                                    const uint32_t* __restrict__ bmix, const float4* __restrict__ px,
+                                                    const float4* __restrict__ ph, const float4* __restrict__ pv,
+                                                    const uint64_t* __restrict__ cell, float4* __restrict__ pd,
+                                                    const uint32_t* __restrict__ V, float gamma, float alpha,
+                                                    float beta, float* __restrict__ slab, float* __restrict__ dudt,
+                                                    uint32_t* __restrict__ nbr, const uint64_t* __restrict__ mixv,
+                                                    uint64_t* __restrict__ hash) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const float side = grid[0], inv = grid[1], R = grid[2];
+    const float R2 = R * R * MARGIN_HI;
+    const float4 a = px[k];
+    const float hi = ph[k].x;
+    const float ihi = 1.0f / hi;
+    float4 di = make_float4(0.f, 0.f, 0.f, 0.f), vi = di;
+    if (FORCE) {
+        di = pd[k];
+        di.w = ihi;  // the pair terms take body i's 1 / h
+        vi = pv[k];
+    }
+    float o0 = 0.f, o1 = 0.f, o2 = 0.f, o3 = 0.f;
+    uint32_t count = 0;
+    uint64_t hs = 0;
+    body_scan<REACH, FORCE, HASH>(k, a, hi, ihi, di, vi, side, inv, R2, mask, bstart, bend, bmix, px, ph, pv, cell,
+                                  pd, alpha, beta, mixv, o0, o1, o2, o3, count, hs);
+    body_store<FORCE, HASH>(k, n, ph, pd, V, gamma, slab, dudt, nbr, hash, o0, o1, o2, o3, count, hs);
+}
+
+// The default pass (sph_path 0): one warp per 32 consecutive sorted bodies,
+// which sit close together.  The warp visits the union of its bodies'
+// rows and row x-ranges (the per-body scan above with REACH = 1); each cell's
+// bodies are staged in shared memory 32 at a time with coalesced loads.  A
+// lane first tests every staged candidate against its body (the FP32
+// neighbour decision, on cells its own scan visits) into a bit mask, then
+// evaluates its hits in ascending order: the warp iterates as many times as
+// its busiest lane has hits, not once per candidate, and every body adds
+// the same terms in the same order as the per-body scan, so both give the
+// same bits.  A warp whose bodies span more than 3 cells on an axis (sparse
+// regions) runs the per-body scan instead.
+constexpr int CW_WARPS = 4;
+template <bool FORCE, bool HASH>
+__device__ __forceinline__ void cubic_chunk(uint32_t k0, uint32_t n, const float* __restrict__ grid, uint32_t mask,
+                                            const uint32_t* __restrict__ bstart, const uint32_t* __restrict__ bend,
+                                            const uint32_t* __restrict__ bmix, const float4* __restrict__ px,
+                                            const float4* __restrict__ ph, const float4* __restrict__ pv,
+                                            const uint64_t* __restrict__ cell, float4* __restrict__ pd,
+                                            const uint32_t* __restrict__ V, float gamma, float alpha, float beta,
+                                            float* __restrict__ slab, float* __restrict__ dudt,
+                                            uint32_t* __restrict__ nbr, const uint64_t* __restrict__ mixv,
+                                            uint64_t* __restrict__ hash, float4* sq, float4* sh, float4* sv,
+                                            uint64_t* sm) {
+    const int lane = threadIdx.x & 31;
+    if (k0 >= n) return;
+    const uint32_t k = k0 + (uint32_t)lane;
+    const bool live = k < n;
+    const uint32_t kk = live ? k : n - 1u;  // a lane past the end shadows the warp's last body
+    const float side = grid[0], inv = grid[1], R = grid[2];
+    const float R2 = R * R * MARGIN_HI;
+    const float4 a = px[kk];
+    const float hi = ph[kk].x;
+    const float ihi = 1.0f / hi;
+    float4 di = make_float4(0.f, 0.f, 0.f, 0.f), vi = di;
+    if (FORCE) {
+        di = pd[kk];
+        di.w = ihi;
+        vi = pv[kk];
+    }
+    float o0 = 0.f, o1 = 0.f, o2 = 0.f, o3 = 0.f;
+    uint32_t count = 0;
+    uint64_t hs = 0;
+    const int3 c0 = cell_of(a.x, a.y, a.z, inv);
+    const int zlo = __reduce_min_sync(0xffffffffu, c0.z), zhi = __reduce_max_sync(0xffffffffu, c0.z);
+    const int ylo = __reduce_min_sync(0xffffffffu, c0.y), yhi = __reduce_max_sync(0xffffffffu, c0.y);
+    const int xlo = __reduce_min_sync(0xffffffffu, c0.x), xhi = __reduce_max_sync(0xffffffffu, c0.x);
+    // cell spans as unsigned differences (no overflow for far-apart cells);
+    // a body beyond the packed key's range takes the per-body scan
+    const bool compact = (uint32_t)zhi - (uint32_t)zlo <= 2u && (uint32_t)yhi - (uint32_t)ylo <= 2u &&
+                         (uint32_t)xhi - (uint32_t)xlo <= 2u && !__any_sync(0xffffffffu, cell_clamped(c0));
+    if (!compact) {
+        if (live) {
+            body_scan<1, FORCE, HASH>(k, a, hi, ihi, di, vi, side, inv, R2, mask, bstart, bend, bmix, px, ph, pv,
+                                      cell, pd, alpha, beta, mixv, o0, o1, o2, o3, count, hs);
+            body_store<FORCE, HASH>(k, n, ph, pd, V, gamma, slab, dudt, nbr, hash, o0, o1, o2, o3, count, hs);
+        }
+        return;
+    }
+    for (int cz = zlo - 1; cz <= zhi + 1; cz++) {
+        const float lz = (float)cz * side;
+        const float gz = fmaxf(0.f, fmaxf(lz - a.z, a.z - (lz + side)));
+        for (int cy = ylo - 1; cy <= yhi + 1; cy++) {
+            // this lane's part of the row, exactly as its per-body scan
+            // would take it (x0 > x1: none)
+            const float ly = (float)cy * side;
+            const float gy = fmaxf(0.f, fmaxf(ly - a.y, a.y - (ly + side)));
+            const float rem = R2 - (gy * gy + gz * gz);
+            int x0 = 1, x1 = 0;
+            if (live && rem > 0.0f && cz >= c0.z - 1 && cz <= c0.z + 1 && cy >= c0.y - 1 && cy <= c0.y + 1) {
+                const float ext = sqrtf(rem) * MARGIN_HI;
+                x0 = max(c0.x - 1, (int)floorf((a.x - ext) * inv));
+                x1 = min(c0.x + 1, (int)floorf((a.x + ext) * inv));
+            }
+            const bool any = x0 <= x1;
+            if (!__any_sync(0xffffffffu, any)) continue;
+            const int wx0 = __reduce_min_sync(0xffffffffu, any ? x0 : INT_MAX);
+            const int wx1 = __reduce_max_sync(0xffffffffu, any ? x1 : INT_MIN);
+            for (int cx = wx0; cx <= wx1; cx++) {
+                const int3 c = make_int3(cx, cy, cz);
+                const uint32_t b = bucket_of(c, mask);
+                const uint32_t j0 = bstart[b], j1 = bend[b];
+                if (j1 <= j0) continue;
+                const uint64_t want = pack_cell(c);
+                const uint32_t chk = bmix[b];
+                if (!chk && cell[j0] != want) continue;
+                const bool mine = cx >= x0 && cx <= x1;  // the cell is on this lane's own scan
+                for (uint32_t jb = j0; jb < j1; jb += 32u) {
+                    const uint32_t j = jb + (uint32_t)lane;
+                    const bool ok = j < j1 && (!chk || cell[j] == want);
+                    __syncwarp();
+                    if (ok) {
+                        sq[lane] = px[j];
+                        if (FORCE) {
+                            sh[lane] = pd[j];
+                            sv[lane] = pv[j];
+                        } else {
+                            sh[lane] = ph[j];
+                            if (HASH) sm[lane] = mixv[j];
+                        }
+                    }
+                    const uint32_t vm = __ballot_sync(0xffffffffu, ok);
+                    __syncwarp();
+                    // pass 1: the neighbour decisions of this lane's body
+                    uint32_t hits = 0u;
+                    if (mine) {
+                        for (uint32_t mm = vm; mm; mm &= mm - 1u) {
+                            const int t = __ffs(mm) - 1;
+                            const float4 q = sq[t];
+                            const float hj = FORCE ? sh[t].w : sh[t].x;
+                            float r2;
+                            const bool nb = is_neighbour(fsub(a.x, q.x), fsub(a.y, q.y), fsub(a.z, q.z), hi, hj, r2);
+                            if (nb && (!FORCE || jb + (uint32_t)t != k)) hits |= 1u << t;
+                        }
+                    }
+                    // pass 2: the terms, in candidate order
+                    while (__any_sync(0xffffffffu, hits != 0u)) {
+                        if (hits) {
+                            const int t = __ffs(hits) - 1;
+                            hits &= hits - 1u;
+                            const float4 q = sq[t];
+                            if (!FORCE) {
+                                const float4 hj = sh[t];
+                                density_pair(a, hi, ihi, q, hj.x, hj.w, o0, count);
+                                if (HASH) hs += sm[t];
+                            } else {
+                                force_pair(a, hi, di, vi, q, sv[t], sh[t], alpha, beta, o0, o1, o2, o3);
+                            }
+                        }
+                    }
+                }
+            }
+        }
+    }
+    if (live) body_store<FORCE, HASH>(k, n, ph, pd, V, gamma, slab, dudt, nbr, hash, o0, o1, o2, o3, count, hs);
+}
+
+// The pass: one resident wave of persistent warps taking chunks of 32
+// sorted bodies heaviest first (chunks.cuh).
+template <bool FORCE, bool HASH>
+__global__ void __launch_bounds__(CW_WARPS * 32) k_cubic_warp(uint32_t n, const float* __restrict__ grid,
+                                                             uint32_t mask, const uint32_t* __restrict__ bstart,
+                                                             const uint32_t* __restrict__ bend,
+                                                             const uint32_t* __restrict__ bmix,
+                                                             const float4* __restrict__ px,
+                                                             const float4* __restrict__ ph,
+                                                             const float4* __restrict__ pv,
+                                                             const uint64_t* __restrict__ cell,
+                                                             float4* __restrict__ pd, const uint32_t* __restrict__ V,
+                                                             float gamma, float alpha, float beta,
+                                                             float* __restrict__ slab, float* __restrict__ dudt,
+                                                             uint32_t* __restrict__ nbr,
+                                                             const uint64_t* __restrict__ mixv,
+                                                             uint64_t* __restrict__ hash, sfchunk::ChunkQueue q) {
+    __shared__ float4 s_q[CW_WARPS][32];  // candidate x, y, z, m
+    __shared__ float4 s_h[CW_WARPS][32];  // density: (h, u, c, 1/h); force: (rho, P/rho^2, c, h)
+    __shared__ float4 s_v[CW_WARPS][32];  // force: vx, vy, vz, u
+    __shared__ uint64_t s_m[CW_WARPS][HASH ? 32 : 1];
+    const int w = threadIdx.x >> 5;
+    sfchunk::Taker t = sfchunk::taker(q);
+    for (;;) {
+        const uint32_t c = sfchunk::next(q, t, FORCE ? 1u : 0u);  // density is pass 0, force pass 1
+        if (c == 0xFFFFFFFFu) break;
+        cubic_chunk<FORCE, HASH>(c * 32u, n, grid, mask, bstart, bend, bmix, px, ph, pv, cell, pd, V, gamma, alpha,
+                                 beta, slab, dudt, nbr, mixv, hash, s_q[w], s_h[w], s_v[w], s_m[w]);
+    }
+    sfchunk::warp_exit(q, gridDim.x * CW_WARPS);
+}
+
 template <int REACH>
 int launch_passes(sfgpu_sim* s, CubicWork* w, uint32_t mask, uint32_t* nbr, uint64_t* hash) {
     cudaStream_t st = s->stream;
     const uint32_t n = s->n;
     const float gamma = (float)s->p.sph_gamma, alpha = (float)s->p.sph_alpha, beta = (float)s->p.sph_beta;
+    const bool warp = w->path == 0;
     const uint32_t bb = sf_ceil_div(n, 128);
+    // one resident wave of each warp pass (chunks.cuh)
+    static uint32_t wave[3] = {0, 0, 0};  // density, density with hashes, force
+    const uint32_t most = sf_ceil_div(w->q.nchunks, CW_WARPS);
+    if (!wave[0]) {
+        wave[0] = sfchunk::wave_blocks(k_cubic_warp<false, false>, CW_WARPS * 32, 0xFFFFFFFFu);
+        wave[1] = sfchunk::wave_blocks(k_cubic_warp<false, true>, CW_WARPS * 32, 0xFFFFFFFFu);
+        wave[2] = sfchunk::wave_blocks(k_cubic_warp<true, false>, CW_WARPS * 32, 0xFFFFFFFFu);
+    }
     int tk = s->timer.begin(st, "sph_density");
-    if (hash)
+    if (warp && hash)
+        k_cubic_warp<false, true><<<std::min(wave[1], most), CW_WARPS * 32, 0, st>>>(
+            n, w->grid, mask, w->bstart, w->bend, w->bmix, w->px, w->ph, w->pv, w->cell, w->pd, w->vals, gamma, alpha,
+            beta, s->slab, s->dudt, nbr, w->mixv, hash, w->q);
+    else if (warp)
+        k_cubic_warp<false, false><<<std::min(wave[0], most), CW_WARPS * 32, 0, st>>>(
+            n, w->grid, mask, w->bstart, w->bend, w->bmix, w->px, w->ph, w->pv, w->cell, w->pd, w->vals, gamma, alpha,
+            beta, s->slab, s->dudt, nbr, nullptr, nullptr, w->q);
+    else if (hash)
         k_cubic_body<REACH, false, true><<<bb, 128, 0, st>>>(n, w->grid, mask, w->bstart, w->bend, w->bmix, w->px,
                                                              w->ph, w->pv, w->cell, w->pd, w->vals, gamma, alpha,
                                                              beta, s->slab, s->dudt, nbr, w->mixv, hash);
@@ -302,9 +525,14 @@ int launch_passes(sfgpu_sim* s, CubicWork* w, uint32_t mask, uint32_t* nbr, uint
     SF_CHECK_LAUNCH();
     s->timer.end(st, tk);
     tk = s->timer.begin(st, "sph_force");
-    k_cubic_body<REACH, true, false><<<bb, 128, 0, st>>>(n, w->grid, mask, w->bstart, w->bend, w->bmix, w->px, w->ph,
-                                                         w->pv, w->cell, w->pd, w->vals, gamma, alpha, beta, s->slab,
-                                                         s->dudt, nbr, nullptr, nullptr);
+    if (warp)
+        k_cubic_warp<true, false><<<std::min(wave[2], most), CW_WARPS * 32, 0, st>>>(
+            n, w->grid, mask, w->bstart, w->bend, w->bmix, w->px, w->ph, w->pv, w->cell, w->pd, w->vals, gamma, alpha,
+            beta, s->slab, s->dudt, nbr, nullptr, nullptr, w->q);
+    else
+        k_cubic_body<REACH, true, false><<<bb, 128, 0, st>>>(n, w->grid, mask, w->bstart, w->bend, w->bmix, w->px,
+                                                             w->ph, w->pv, w->cell, w->pd, w->vals, gamma, alpha,
+                                                             beta, s->slab, s->dudt, nbr, nullptr, nullptr);
     SF_CHECK_LAUNCH();
     s->timer.end(st, tk);
     return SFGPU_OK;
@@ -319,6 +547,7 @@ int sf_sph_cubic_alloc(sfgpu_sim* s) {
     CubicWork* w = new CubicWork();
     s->sph_cubic = w;
     const uint32_t n = std::max<uint32_t>(s->n, 1);
+    w->path = s->p.sph_path;
     w->reach = s->p.sph_path == 1 ? 2 : 1;
     w->tbits = 1;
     while ((1u << w->tbits) < 2u * n) w->tbits++;
@@ -339,6 +568,7 @@ int sf_sph_cubic_alloc(sfgpu_sim* s) {
     SF_CUDA(cudaMalloc(&w->grid, sizeof(float) * 4));
     SF_CUDA(cudaMalloc(&w->done, sizeof(uint32_t) * (1024 + 1)));
     SF_CUDA(cudaMemset(w->done, 0, sizeof(uint32_t) * (1024 + 1)));
+    if (sfchunk::alloc(w->q, n) != SFGPU_OK) return SFGPU_FAILURE;
     SF_CUDA(cudaMalloc(&s->u, sizeof(float) * n));
     SF_CUDA(cudaMalloc(&s->dudt, sizeof(float) * n));
     SF_CUDA(cudaMemset(s->u, 0, sizeof(float) * n));
@@ -363,6 +593,7 @@ void sf_sph_cubic_free(sfgpu_sim* s) {
     cudaFree(w->mixv);
     cudaFree(w->grid);
     cudaFree(w->done);
+    sfchunk::release(w->q);
     delete w;
     s->sph_cubic = nullptr;
 }
@@ -388,8 +619,14 @@ int sf_sph_cubic(sfgpu_sim* s) {
     k_cell_gather<<<nb, 256, 0, st>>>(w->keys, w->vals, n, s->slab, s->u, w->grid, w->bstart, w->bend, w->px, w->pv,
                                       w->cell, w->ph, gamma, w->mixv);
     SF_CHECK_LAUNCH();
-    k_bucket_mix<<<nb, 256, 0, st>>>(w->keys, n, w->bstart, w->cell, w->bmix);
+    sfchunk::ChunkQueue q = w->q;
+    if (w->path != 0) q.level = nullptr;  // the per-body passes take no chunks
+    k_bucket_mix<<<nb, 256, 0, st>>>(w->keys, n, w->bstart, w->bend, w->cell, w->bmix, q);
     SF_CHECK_LAUNCH();
+    if (w->path == 0) {
+        sfchunk::k_chunk_order<<<1, 1024, 0, st>>>(w->q);
+        SF_CHECK_LAUNCH();
+    }
     s->timer.end(st, tk);
     uint32_t* nbr = sf_sph_neighbour_counts(s);
     uint64_t* hash = w->mixv ? sf_sph_neighbour_hashes(s) : nullptr;

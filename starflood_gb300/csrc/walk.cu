@@ -480,6 +480,7 @@ constexpr int GW_GSTACK = 128;  // sibling-group entries per warp of k_walk_sib
 constexpr int GW_LIST = 112;  // accepted cells whose bounds miss the group box
 constexpr int GW_MIN_BLOCKS = 7;  // resident blocks per SM the register budget is cut for
 constexpr int GW_SLOW = 48;   // accepted cells that may contain a body (self-exclusion test)
+constexpr int PART_LEVELS = 3;  // k_walk_sib walks a group in parts that share their top 3 octants
 
 // Per-warp lists in shared memory.  The fast list holds the monopole itself
 // (centre of mass and mass) and the mask of the bodies taking it, entries
@@ -1076,7 +1077,7 @@ __global__ void __launch_bounds__(GW_THREADS, GW_MIN_BLOCKS) k_walk_sib(const fl
                                                            uint32_t* __restrict__ st_int,
                                                            uint32_t* __restrict__ st_open,
                                                            unsigned long long* __restrict__ tot, uint32_t* d_status,
-                                                           WalkKick wk) {
+                                                           WalkKick wk, const uint64_t* __restrict__ skeys) {
     __shared__ uint2 s_stk[GW_WARPS][GW_GSTACK];  // sibling groups: (first child, mask)
     __shared__ __align__(16) float l_xy[GW_WARPS][2 * GW_LIST];
     __shared__ __align__(16) float l_zm[GW_WARPS][2 * GW_LIST];
@@ -1103,20 +1104,37 @@ __global__ void __launch_bounds__(GW_THREADS, GW_MIN_BLOCKS) k_walk_sib(const fl
     // with the fused kick every warp reaches the block reduction; a warp
     // past the last body walks nothing
     if (!live_mask && !KICK) return;
-    const float4 b = sp[live ? k : min(group * (uint32_t)GB, n - 1u)];
+    const uint32_t kq = live ? k : min(group * (uint32_t)GB, n - 1u);
+    const float4 b = sp[kq];
     const float rx = b.x, ry = b.y, rz = b.z, mi = b.w;
     if (half == 0) sbd[bl] = b;
+    // The group is walked in parts: runs of its bodies that share the
+    // octants of the top PART_LEVELS levels.  A group cut by such a cell
+    // boundary (3 % of the 16-body groups of the uniform sphere, and those
+    // of the sparse outskirts) would otherwise walk with a box spanning
+    // both sides, find most cells mixed, and run several times as long as
+    // the others (the longest warp sets the launch's duration).
+    const uint32_t pfx = (uint32_t)(skeys[kq] >> (3 * (16 - PART_LEVELS)));
+    const uint32_t pprev = __shfl_up_sync(0xffffffffu, pfx, 1);
+    const uint32_t starts = __ballot_sync(0xffffffffu, live && (bl == 0 || pfx != pprev)) & body_bits;
     __syncwarp();
-    // bounding box of the group (dead lanes repeat the first body)
     float bx0 = rx, by0 = ry, bz0 = rz, bx1 = rx, by1 = ry, bz1 = rz;
-    for (int o = 16; o > 0; o >>= 1) {
-        bx0 = fminf(bx0, __shfl_xor_sync(0xffffffffu, bx0, o));
-        by0 = fminf(by0, __shfl_xor_sync(0xffffffffu, by0, o));
-        bz0 = fminf(bz0, __shfl_xor_sync(0xffffffffu, bz0, o));
-        bx1 = fmaxf(bx1, __shfl_xor_sync(0xffffffffu, bx1, o));
-        by1 = fmaxf(by1, __shfl_xor_sync(0xffffffffu, by1, o));
-        bz1 = fmaxf(bz1, __shfl_xor_sync(0xffffffffu, bz1, o));
-    }
+    // bounding box of the part (lanes outside it repeat its first body)
+    auto part_box = [&](uint32_t part, int s0) {
+        const bool inp = (part >> bl) & 1u;
+        const float4 r0 = sbd[s0];
+        bx0 = bx1 = inp ? rx : r0.x;
+        by0 = by1 = inp ? ry : r0.y;
+        bz0 = bz1 = inp ? rz : r0.z;
+        for (int o = 16; o > 0; o >>= 1) {
+            bx0 = fminf(bx0, __shfl_xor_sync(0xffffffffu, bx0, o));
+            by0 = fminf(by0, __shfl_xor_sync(0xffffffffu, by0, o));
+            bz0 = fminf(bz0, __shfl_xor_sync(0xffffffffu, bz0, o));
+            bx1 = fmaxf(bx1, __shfl_xor_sync(0xffffffffu, bx1, o));
+            by1 = fmaxf(by1, __shfl_xor_sync(0xffffffffu, by1, o));
+            bz1 = fmaxf(bz1, __shfl_xor_sync(0xffffffffu, bz1, o));
+        }
+    };
     KSum ax{0.f, 0.f}, ay{0.f, 0.f}, az{0.f, 0.f}, ph{0.f, 0.f};
     float2 a2x = make_float2(0.f, 0.f), a2y = a2x, a2z = a2x, p2 = a2x;
     uint32_t n_int = 0, n_open = 0;
@@ -1152,9 +1170,16 @@ __global__ void __launch_bounds__(GW_THREADS, GW_MIN_BLOCKS) k_walk_sib(const fl
     // per opened cell replaces eight.  The root is the first round's only
     // cell.  A round may push one group per lane: popping ng groups leaves
     // room when top + 7 ng <= GW_GSTACK.
-    bool root_round = live_mask != 0u;
-    __syncwarp();
     uint32_t guard = 0;
+    uint32_t rest = live_mask;
+    while (rest) {  // the group's parts, one walk each
+    const int s0 = __ffs(rest) - 1;
+    const uint32_t later = starts & ~((2u << s0) - 1u);  // part starts after s0
+    const uint32_t part = rest & (later ? (1u << (__ffs(later) - 1)) - 1u : 0xffffffffu);
+    rest &= ~part;
+    part_box(part, s0);
+    bool root_round = true;
+    __syncwarp();
     while (root_round || top > 0) {
         if (++guard > fc.walk_limit) {
             if (lane == 0) atomicOr(d_status, SFGPU_STATUS_WALK);
@@ -1164,7 +1189,7 @@ __global__ void __launch_bounds__(GW_THREADS, GW_MIN_BLOCKS) k_walk_sib(const fl
         bool valid = false;
         if (root_round) {
             valid = lane == 0;
-            M = live_mask;
+            M = part;
             root_round = false;
         } else {
             const int ng = min(4, min(top, (GW_GSTACK - top) / 7));
@@ -1284,6 +1309,7 @@ __global__ void __launch_bounds__(GW_THREADS, GW_MIN_BLOCKS) k_walk_sib(const fl
         flush(false);
     }
     flush(true);
+    }  // next part
     float sx = ax.s, sy = ay.s, sz = az.s, sw = ph.s;
     if (KIND == WALK_COMP) {
         sx -= ax.c;
@@ -1400,7 +1426,7 @@ int launch_sib(sfgpu_sim* s, bool stats) {
     if (stats) {
         k_walk_sib<KIND, GB, true><<<grid, GW_THREADS, 0, s->stream>>>(
             t->sp, t->vals, s->n, t->nd, fc, th_lo, th_hi, th_acc, th_open, s->p.leaf_cap, t->walk_part, acc, pot,
-            s->stat_int, s->stat_open, s->walk_tot, s->d_status, WalkKick{});
+            s->stat_int, s->stat_open, s->walk_tot, s->d_status, WalkKick{}, t->keys);
     } else if (s->fuse_kick && s->red_cap * 2u >= grid * 4u) {
         WalkKick wk;
         wk.vel = s->slab + (size_t)3 * s->n;
@@ -1417,12 +1443,12 @@ int launch_sib(sfgpu_sim* s, bool stats) {
         wk.d_step = s->d_step;
         k_walk_sib<KIND, GB, false, true><<<grid, GW_THREADS, 0, s->stream>>>(
             t->sp, t->vals, s->n, t->nd, fc, th_lo, th_hi, th_acc, th_open, s->p.leaf_cap, t->walk_part, acc, pot,
-            nullptr, nullptr, s->walk_tot, s->d_status, wk);
+            nullptr, nullptr, s->walk_tot, s->d_status, wk, t->keys);
         s->kicked = true;
     } else {
         k_walk_sib<KIND, GB, false><<<grid, GW_THREADS, 0, s->stream>>>(
             t->sp, t->vals, s->n, t->nd, fc, th_lo, th_hi, th_acc, th_open, s->p.leaf_cap, t->walk_part, acc, pot,
-            nullptr, nullptr, s->walk_tot, s->d_status, WalkKick{});
+            nullptr, nullptr, s->walk_tot, s->d_status, WalkKick{}, t->keys);
     }
     SF_CHECK_LAUNCH();
     return SFGPU_OK;

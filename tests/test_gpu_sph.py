@@ -135,6 +135,34 @@ def _ref_sets(pos, ii):
     return out
 
 
+@pytest.mark.parametrize("n,hvar", [(65536, False), (32768, True)])
+def test_sph_reference_paths_bit_identical(sf, n, hvar):
+    """Mode A, FAST: the passes by warps (sph_path 0, the default) and one
+    thread per body (sph_path 2) add the same terms in the same order: rho,
+    P, accelerations, momentum-set counts and hashes equal to the bit on a
+    Plummer sphere (and with varied h)."""
+    from starflood_gb300.ics import plummer
+    pos, vel, mas = plummer(n, seed=9)
+    rad = np.full(n, 0.05, np.float32)
+    if hvar:
+        rad[::4] = 0.09
+        rad[2::9] = 0.02
+    out = []
+    for path in (0, 2):
+        p = sf.default_params(solver=sf.SOLVER_PP, sph=sf.SPH_REFERENCE, eps=0.01, flags=sf.FLAG_STATS,
+                              sph_path=path)
+        with sf.Sim(n, p) as s:
+            s.set_state(pos, vel, mas, rad)
+            s.solve_sph()
+            v = slab_views(s.download(), n, 16)
+            out.append((v["rho"].copy(), v["prs"].copy(), v["acc"].copy(), s.sph_neighbours().copy(),
+                        s.sph_neighbour_hashes().copy()))
+            assert s.status() == 0
+    for a, b in zip(*out):
+        np.testing.assert_array_equal(a, b)
+    assert out[0][3].mean() > 100
+
+
 def test_sph_reference_plummer262144_subsample(sf):
     """Mode A at N = 262,144 (Plummer a = 1, h = 0.05), FAST (the cell-grid
     search): the neighbour sets of a seeded 256-body subsample equal the
@@ -181,13 +209,14 @@ def _cubic_sim(sf, n, pos, vel, mas, rad, u, **kw):
     return s
 
 
-@pytest.mark.parametrize("path", [0, 1])
+@pytest.mark.parametrize("path", [0, 1, 2])
 @pytest.mark.parametrize("n,hvar", [(4096, False), (3000, True)])
 def test_sph_cubic_vs_fp64_oracle(sf, oracle64, n, hvar, path):
     """Cubic-spline SPH: neighbour sets (counts and hashes) bit-identical to
     the brute-force FP32 enumeration; rho, dv/dt, du/dt within 1e-5 / 1e-4
-    of the FP64 oracle.  path 0: side-h cells with row culling; 1: the 27
-    side-2h cells."""
+    of the FP64 oracle.  path 0: one warp per 32 sorted bodies over side-2h
+    cells; 1: one thread per body over side-h cells; 2: one thread per body
+    over side-2h cells."""
     from starflood_gb300.ics import plummer
     pos, vel, mas = plummer(n, seed=51)
     pos = pos * np.float32(0.3)  # denser: ~30 neighbours per body at h = 0.05
@@ -295,6 +324,33 @@ def test_sph_cubic_plummer262144_subsample(sf):
     assert e_rho.max() < 1e-5
     assert e_acc.max() < 1e-4
     assert e_du.max() < 1e-4
+
+
+@pytest.mark.parametrize("n,hvar", [(1 << 18, False), (65536, True)])
+def test_sph_cubic_paths_bit_identical(sf, n, hvar):
+    """The warp-per-32-bodies pass (sph_path 0) and the thread-per-body pass
+    over the same side-2h cells (sph_path 2) add the same terms in the same
+    order: rho, P, dv/dt, du/dt, neighbour counts and hashes equal to the
+    bit on the Plummer gas of the benchmark (and with varied h)."""
+    from starflood_gb300.ics import plummer
+    pos, vel, mas = plummer(n, seed=7)
+    rad = np.full(n, 0.05, np.float32)
+    if hvar:
+        rad[::3] = 0.08
+        rad[1::7] = 0.03
+    u = np.full(n, 0.05, np.float32)
+    out = []
+    for path in (0, 2):
+        with _cubic_sim(sf, n, pos, vel, mas, rad, u, sph_path=path, flags=sf.FLAG_STATS) as s:
+            s.solve_sph()
+            v = slab_views(s.download(), n, 16)
+            _, dudt = s.sph_get_u()
+            out.append((v["rho"].copy(), v["prs"].copy(), v["acc"].copy(), dudt.copy(), s.sph_neighbours().copy(),
+                        s.sph_neighbour_hashes().copy()))
+            assert s.status() == 0
+    for a, b in zip(*out):
+        np.testing.assert_array_equal(a, b)
+    assert out[0][4].mean() > 10
 
 
 @pytest.mark.parametrize("mode", ["reference", "cubic"])
