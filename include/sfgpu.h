@@ -82,9 +82,9 @@ typedef struct {
                              of side 2h around each body, each row cut to the cells the 2h sphere
                              reaches: 0 one warp per 32 sorted bodies over the union of their rows,
                              candidates staged in shared memory (default); 2 one thread per body; 1
-                             one thread per body over cells of side h.  REFERENCE (FAST): 0 by warps
-                             (default), 2 one thread per body.  Every path adds the same terms in the
-                             same order. */
+                             one thread per body over cells of side h; 3 by warps over cells of side
+                             h.  REFERENCE (FAST): 0 by warps (default), 2 one thread per body.
+                             Every path adds the same terms in the same order. */
     uint32_t walk_group;  /* bodies per warp of the group walk: 0 the default (16), 8, 16 or 32 */
     uint32_t spin_limit;  /* rounds a bounded device wait (the look-backs of the sort and of the
                              node scan) spins on an unpublished word before it gives up and sets

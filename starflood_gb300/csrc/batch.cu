@@ -72,12 +72,14 @@ struct TileConfig {
     int bs, ipt;
     uint32_t jchunk;
 };
-// candidate shapes for the autotuner (threads per CTA, bodies per thread, j-chunk)
-const TileConfig kConfigs[] = {{128, 4, 2048}, {128, 8, 2048}, {128, 8, 4096}, {256, 4, 4096}, {128, 8, 8192}};
+// candidate shapes for the autotuner (threads per CTA, bodies per thread, j-chunk); the last two are held
+// to 64 registers so that 8 CTAs of 128 threads fit on an SM (the persistent grid's CTAs per SM)
+const TileConfig kConfigs[] = {{128, 4, 2048}, {128, 8, 2048}, {128, 8, 4096}, {256, 4, 4096}, {128, 8, 8192},
+                               {128, 4, 2048}, {128, 4, 4096}};
 constexpr int kNumConfigs = sizeof(kConfigs) / sizeof(kConfigs[0]);
 
-template <int BS, int IPT>
-__global__ void __launch_bounds__(BS) k_batch_pp(const BatchItem* __restrict__ items, uint32_t nitems,
+template <int BS, int IPT, int MINB = 1>
+__global__ void __launch_bounds__(BS, MINB) k_batch_pp(const BatchItem* __restrict__ items, uint32_t nitems,
                                                  uint32_t* ticket, const uint32_t* __restrict__ off,
                                                  const uint32_t* __restrict__ part_off, uint32_t jchunk,
                                                  const float* __restrict__ pos, const float* __restrict__ mas,
@@ -393,9 +395,9 @@ int batch_configure(sfgpu_batch* b, int cfg) {
     return SFGPU_OK;
 }
 
-template <int BS, int IPT>
+template <int BS, int IPT, int MINB = 1>
 void launch_pp(sfgpu_batch* b, cudaStream_t st, const float* pos, const float* mas, float eps2, int grid) {
-    k_batch_pp<BS, IPT><<<grid, BS, 0, st>>>(b->items, b->nitems, b->ticket, b->off, b->part_off, b->jchunk, pos,
+    k_batch_pp<BS, IPT, MINB><<<grid, BS, 0, st>>>(b->items, b->nitems, b->ticket, b->off, b->part_off, b->jchunk, pos,
                                               mas, eps2, b->part);
 }
 
@@ -410,6 +412,8 @@ int batch_forces(sfgpu_batch* b, const float* pos) {
         case 1: launch_pp<128, 8>(b, s->stream, pos, mas, fc.eps2, grid); break;
         case 2: launch_pp<128, 8>(b, s->stream, pos, mas, fc.eps2, grid); break;
         case 3: launch_pp<256, 4>(b, s->stream, pos, mas, fc.eps2, grid); break;
+        case 5:
+        case 6: launch_pp<128, 4, 8>(b, s->stream, pos, mas, fc.eps2, grid); break;
         default: launch_pp<128, 8>(b, s->stream, pos, mas, fc.eps2, grid); break;
     }
     SF_CHECK_LAUNCH();

@@ -8,17 +8,20 @@
 // busy); persistent warps taking the heaviest chunks first from one counter
 // do not fix it either, because each SM's ~40 resident warps take their
 // first ~40 chunks at once and those totals differ by a third from SM to
-// SM.  So each chunk gets a cost level (log2 of an estimate) where the cell
-// grid is built, one block orders the chunks by level, heaviest first (a
-// counting sort), and position p of that order belongs to SM bin
-// p mod B in snake order (rounds of B alternately forward and backward), so
-// the bins' estimated totals are nearly equal.  A warp takes the chunks of
-// its own SM's bin in order, heaviest first; when the bin is empty (or its
-// SM has no bin) it takes whatever is left through a global counter over
-// all positions, from the light end.  A chunk is claimed by a compare-and-swap on its position's
-// pass word, so each is done exactly once whichever way it is reached, and
-// its arithmetic is unchanged: the results are the same bits whichever warp
-// takes it.
+// SM.  So before each pass one block orders the chunks by cost level,
+// heaviest first (a counting sort over half-octave levels), and position p
+// of that order belongs to SM bin p mod B in snake order (rounds of B
+// alternately forward and backward), so the bins' totals are nearly equal.
+// The cost is the chunk's measured duration in the same pass of the
+// previous step (clock cycles, recorded by the warp that ran it: the sorted
+// order, and so each chunk's bodies, changes little from step to step), or
+// before the first, an estimate written where the cell grid is built.  A
+// warp takes the chunks of its own SM's bin in order, heaviest first; when
+// the bin is empty (or its SM has no bin) it takes whatever is left through
+// a global counter over all positions, from the light end.  A chunk is
+// claimed by a compare-and-swap on its position's word, so each is done
+// exactly once whichever way it is reached, and its arithmetic is
+// unchanged: the results are the same bits whichever warp takes it.
 #pragma once
 
 #include "internal.cuh"
@@ -26,13 +29,15 @@
 namespace sfchunk {
 namespace {  // a copy per translation unit (the kernel included)
 
-constexpr int LEVELS = 32;
+constexpr int LEVELS = 64;  // half-octave cost levels
+constexpr int KINDS = 2;    // passes with their own measured costs: 0 density, 1 force / momentum
 
 struct ChunkQueue {
-    uint32_t* level = nullptr;  // [nchunks] cost level of each chunk
-    uint32_t* hist = nullptr;   // [LEVELS] chunks per level (cleared by the ordering)
+    uint32_t* est = nullptr;    // [nchunks] cost estimate written where the grid is built
+    uint32_t* cost = nullptr;   // [KINDS][nchunks] measured cost of the last run of each pass kind
+    uint32_t* have = nullptr;   // [KINDS] the pass kind has run (its costs are valid)
     uint32_t* order = nullptr;  // [nchunks] chunk ids, heaviest first
-    uint32_t* claim = nullptr;  // [nchunks] per position: passes that have claimed it (cleared by the ordering)
+    uint32_t* claim = nullptr;  // [nchunks] per position: claimed in this pass (cleared by the ordering)
     uint32_t* ctr = nullptr;    // [0, B) next round of each SM bin, [B] global position, [B + 1] warps done
     uint32_t nchunks = 0;
     uint32_t bins = 0;          // B: the SM count
@@ -41,24 +46,33 @@ struct ChunkQueue {
 inline int alloc(ChunkQueue& q, uint32_t n) {
     q.nchunks = sf_ceil_div(std::max<uint32_t>(n, 1u), 32u);
     q.bins = (uint32_t)sf_num_sms();
-    SF_CUDA(cudaMalloc(&q.level, sizeof(uint32_t) * q.nchunks));
+    SF_CUDA(cudaMalloc(&q.est, sizeof(uint32_t) * q.nchunks));
+    SF_CUDA(cudaMalloc(&q.cost, sizeof(uint32_t) * KINDS * q.nchunks));
+    SF_CUDA(cudaMalloc(&q.have, sizeof(uint32_t) * KINDS));
     SF_CUDA(cudaMalloc(&q.order, sizeof(uint32_t) * q.nchunks));
     SF_CUDA(cudaMalloc(&q.claim, sizeof(uint32_t) * q.nchunks));
-    SF_CUDA(cudaMalloc(&q.hist, sizeof(uint32_t) * LEVELS));
     SF_CUDA(cudaMalloc(&q.ctr, sizeof(uint32_t) * (q.bins + 2)));
+    SF_CUDA(cudaMemset(q.est, 0, sizeof(uint32_t) * q.nchunks));
+    SF_CUDA(cudaMemset(q.have, 0, sizeof(uint32_t) * KINDS));
     SF_CUDA(cudaMemset(q.claim, 0, sizeof(uint32_t) * q.nchunks));
-    SF_CUDA(cudaMemset(q.hist, 0, sizeof(uint32_t) * LEVELS));
     SF_CUDA(cudaMemset(q.ctr, 0, sizeof(uint32_t) * (q.bins + 2)));
     return SFGPU_OK;
 }
 
 inline void release(ChunkQueue& q) {
-    cudaFree(q.level);
+    cudaFree(q.est);
+    cudaFree(q.cost);
+    cudaFree(q.have);
     cudaFree(q.order);
     cudaFree(q.claim);
-    cudaFree(q.hist);
     cudaFree(q.ctr);
     q = ChunkQueue{};
+}
+
+__device__ __forceinline__ uint32_t cost_level(uint32_t v) {
+    if (v < 2u) return v;
+    const uint32_t top = 31u - (uint32_t)__clz(v);
+    return min((uint32_t)LEVELS - 1u, 2u * top + ((v >> (top - 1u)) & 1u));
 }
 
 // Called by every lane of a warp whose lanes hold the bodies of one chunk
@@ -66,37 +80,50 @@ inline void release(ChunkQueue& q) {
 __device__ __forceinline__ void note_cost(const ChunkQueue& q, uint32_t chunk, uint32_t cost) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) cost += __shfl_xor_sync(0xffffffffu, cost, o);
+    if ((threadIdx.x & 31) == 0) q.est[chunk] = cost;
+}
+
+// The cost of a chunk a warp has just run (lane 0), for the next ordering
+// of the same pass kind.
+__device__ __forceinline__ void record(const ChunkQueue& q, int kind, uint32_t chunk, long long cycles) {
     if ((threadIdx.x & 31) == 0) {
-        const uint32_t lv = cost ? 31u - (uint32_t)__clz(cost) : 0u;
-        q.level[chunk] = lv;
-        atomicAdd(&q.hist[lv], 1u);
+        q.cost[(size_t)kind * q.nchunks + chunk] = (uint32_t)min(cycles, 0xFFFFFFFFll);
+        if (q.have[kind] == 0u) q.have[kind] = 1u;
     }
 }
 
-// One block: chunk ids into q.order by descending level; clears q.hist.
-__global__ void __launch_bounds__(1024) k_chunk_order(ChunkQueue q) {
+// One block: chunk ids into q.order by descending cost level (measured if
+// the pass kind has run, else estimated); clears the claims.
+__global__ void __launch_bounds__(1024) k_chunk_order(ChunkQueue q, int kind) {
     __shared__ uint32_t s_pos[LEVELS];
-    if (threadIdx.x < 32) {
-        const uint32_t h = q.hist[threadIdx.x];
-        uint32_t x = h;  // sum over levels >= this one
+    __shared__ uint32_t s_hist[LEVELS];
+    const bool measured = q.have[kind] != 0u;
+    const uint32_t* src = measured ? q.cost + (size_t)kind * q.nchunks : q.est;
+    if (threadIdx.x < LEVELS) s_hist[threadIdx.x] = 0u;
+    __syncthreads();
+    for (uint32_t c = threadIdx.x; c < q.nchunks; c += blockDim.x) atomicAdd(&s_hist[cost_level(src[c])], 1u);
+    __syncthreads();
+    if (threadIdx.x < 32) {  // positions by descending level: lane l holds levels 2l, 2l + 1
+        const uint32_t h0 = s_hist[2 * threadIdx.x], h1 = s_hist[2 * threadIdx.x + 1];
+        uint32_t x = h0 + h1;  // sum over levels >= 2l
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const uint32_t y = __shfl_down_sync(0xffffffffu, x, o);
             if (threadIdx.x + o < 32) x += y;
         }
-        s_pos[threadIdx.x] = x - h;
-        q.hist[threadIdx.x] = 0u;
+        s_pos[2 * threadIdx.x + 1] = x - h0 - h1;  // level 2l + 1 comes first
+        s_pos[2 * threadIdx.x] = x - h0;
     }
     __syncthreads();
     for (uint32_t c = threadIdx.x; c < q.nchunks; c += blockDim.x) {
-        const uint32_t pos = atomicAdd(&s_pos[q.level[c]], 1u);
+        const uint32_t pos = atomicAdd(&s_pos[cost_level(src[c])], 1u);
         q.order[pos] = c;
         q.claim[c] = 0u;
     }
 }
 
-// A warp's walk through the queue during pass `pass` (0, 1, ... since the
-// last ordering): its own SM's bin first, then the global counter.
+// A warp's walk through the queue: its own SM's bin first, then the global
+// counter.
 struct Taker {
     uint32_t bin;   // this SM's bin, or bins (none)
     bool global;    // the bin is empty: take from the global counter
@@ -108,7 +135,7 @@ __device__ __forceinline__ Taker taker(const ChunkQueue& q) {
 }
 
 // The warp's next chunk, or 0xFFFFFFFF when none is left.
-__device__ __forceinline__ uint32_t next(const ChunkQueue& q, Taker& t, uint32_t pass) {
+__device__ __forceinline__ uint32_t next(const ChunkQueue& q, Taker& t) {
     const int lane = threadIdx.x & 31;
     for (;;) {
         uint32_t pos = 0xFFFFFFFFu;
@@ -129,7 +156,7 @@ __device__ __forceinline__ uint32_t next(const ChunkQueue& q, Taker& t, uint32_t
             return 0xFFFFFFFFu;
         }
         bool won = false;
-        if (lane == 0) won = atomicCAS(&q.claim[pos], pass, pass + 1u) == pass;
+        if (lane == 0) won = atomicCAS(&q.claim[pos], 0u, 1u) == 0u;
         if (__shfl_sync(0xffffffffu, won, 0)) return q.order[pos];
         // taken already (through its bin or the global counter): go on
     }

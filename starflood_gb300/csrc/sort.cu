@@ -421,6 +421,59 @@ __device__ __forceinline__ void warp_bitonic_sort(const uint64_t* sk, const uint
         }
     }
 }
+// The same network on composites the caller built (unique, the position in
+// their low 13 bits): the pair at rank r is (ok[i], ov[i]), i the low 13
+// bits of the r-th composite, written to gk[r], gv[r].
+template <int E>
+__device__ __forceinline__ void warp_bitonic_comp(const uint64_t* comp, uint32_t m, const uint64_t* ok,
+                                                  const uint32_t* ov, uint64_t* gk, uint32_t* gv) {
+    const uint32_t lane = threadIdx.x & 31;
+    uint64_t v[E];
+#pragma unroll
+    for (int q = 0; q < E; q++) {
+        const uint32_t e = (uint32_t)q * 32u + lane;
+        v[q] = e < m ? comp[e] : ~0ull;
+    }
+#pragma unroll
+    for (int k = 2; k <= 32 * E; k <<= 1) {
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            if (j >= 32) {
+                const int qj = j >> 5;
+#pragma unroll
+                for (int q = 0; q < E; q++) {
+                    if (q & qj) continue;
+                    const uint32_t e = (uint32_t)q * 32u + lane;
+                    const bool asc = (e & (uint32_t)k) == 0u;
+                    const uint64_t x = v[q], y = v[q | qj];
+                    const uint64_t lo = x < y ? x : y, hi = x < y ? y : x;
+                    v[q] = asc ? lo : hi;
+                    v[q | qj] = asc ? hi : lo;
+                }
+            } else {
+#pragma unroll
+                for (int q = 0; q < E; q++) {
+                    const uint64_t o = __shfl_xor_sync(0xffffffffu, v[q], j);
+                    const uint32_t e = (uint32_t)q * 32u + lane;
+                    const bool asc = (e & (uint32_t)k) == 0u;
+                    const bool lower = (lane & (uint32_t)j) == 0u;
+                    const uint64_t lo = v[q] < o ? v[q] : o, hi = v[q] < o ? o : v[q];
+                    v[q] = (lower == asc) ? lo : hi;
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < E; q++) {
+        const uint32_t e = (uint32_t)q * 32u + lane;
+        if (e < m) {
+            const uint32_t i = (uint32_t)(v[q] & 8191u);
+            gk[e] = ok[i];
+            gv[e] = ov[i];
+        }
+    }
+}
+
 __device__ __forceinline__ void warp_small_sort(const uint64_t* sk, const uint32_t* sv, uint32_t m, uint64_t lowmask,
                                                 uint64_t* gk, uint32_t* gv) {
     if (m <= 1u) {
@@ -438,16 +491,12 @@ __device__ __forceinline__ void warp_small_sort(const uint64_t* sk, const uint32
 }
 
 // Bucket blockIdx.x of (Kb, Vb), sorted on its low digits, into (K, V).
-// Up to RANK_MAX pairs, warp 0 sorts the bucket.  A larger bucket takes one
-// stable pass on its next digit (most significant first), which cuts it
-// into 128 sub-buckets that are already in order among themselves; the
-// warps sort the sub-buckets of up to RANK_MAX pairs side by side, and the
-// CTA finishes any larger sub-bucket with LSD passes on the digits below.
-// A large bucket thus costs one pass and ~m log^2 m network steps per
-// sub-bucket instead of one pass per digit, and the biggest bucket (the
-// long pole of the launch) no longer runs six passes.
-// A bucket larger than BK_CAP is left alone and raises *big, which enables
-// the full tile passes queued after this kernel.
+// Up to RANK_MAX pairs, warp 0 sorts the bucket with one network.  A larger
+// bucket is split wide on its next bits (below), so that the biggest bucket
+// (the long pole of the launch: several thousand keys on a uniform sphere)
+// costs a count, a scatter and many tiny sorts side by side instead of six
+// passes.  A bucket larger than BK_CAP is left alone and raises *big, which
+// enables the full tile passes queued after this kernel.
 __global__ void __launch_bounds__(BK_THREADS, 1) k_bucket_sort(const uint64_t* __restrict__ Kb,
                                                                const uint32_t* __restrict__ Vb,
                                                                uint64_t* __restrict__ K, uint32_t* __restrict__ V,
@@ -484,9 +533,28 @@ __global__ void __launch_bounds__(BK_THREADS, 1) k_bucket_sort(const uint64_t* _
         if (threadIdx.x == 0) atomicOr(big, 1u);
         return;
     }
-    for (uint32_t e = threadIdx.x; e < size; e += BK_THREADS) {
-        k0[e] = Kb[start + e];
-        v0[e] = Vb[start + e];
+    // four loads in flight per thread before their stores (the bucket's
+    // pairs come from L2; one at a time the biggest bucket waits ~13 round
+    // trips)
+    for (uint32_t e0 = threadIdx.x; e0 < size; e0 += 4u * BK_THREADS) {
+        uint64_t kk[4];
+        uint32_t vv[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const uint32_t e = e0 + (uint32_t)u * BK_THREADS;
+            if (e < size) {
+                kk[u] = Kb[start + e];
+                vv[u] = Vb[start + e];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const uint32_t e = e0 + (uint32_t)u * BK_THREADS;
+            if (e < size) {
+                k0[e] = kk[u];
+                v0[e] = vv[u];
+            }
+        }
     }
     __syncthreads();
     const int warp = threadIdx.x >> 5;
@@ -494,39 +562,103 @@ __global__ void __launch_bounds__(BK_THREADS, 1) k_bucket_sort(const uint64_t* _
         if (warp == 0) warp_small_sort(k0, v0, size, (1ull << (low_passes * RADIX_BITS)) - 1ull, K + start, V + start);
         return;
     }
-    // the next digit, most significant first: sub-bucket d is k1[run[d], run[d + 1])
-    const int msd = low_passes - 1;
-    bucket_pass(k0, v0, k1, v1, size, msd * RADIX_BITS, sc);
-    __shared__ uint32_t s_sub[RADIX + 1];  // bucket_pass below rewrites run[]
-    if (threadIdx.x < RADIX) s_sub[threadIdx.x] = sc.run[threadIdx.x];
-    if (threadIdx.x == 0) s_sub[RADIX] = size;
+    // A wide split on the D bits below the top digit (D <= 10, sized for
+    // ~4 pairs per sub-bucket): counts by shared atomics, offsets by a block
+    // scan, and an unstable scatter of composites (the key bits below the
+    // top digit, shifted left 13, plus the pair's position in the bucket),
+    // which keep the pairs' order recoverable.  Sub-buckets of up to 16
+    // pairs are then sorted by one thread each (a rank count over the
+    // composites), up to RANK_MAX by one warp's network; a sub-bucket
+    // above RANK_MAX (dense clusters), or keys too wide for the composite,
+    // send the whole bucket through stable LSD passes instead.
+    const int lowbits = low_passes * RADIX_BITS;
+    int D = 1;
+    while (D < 10 && (4u << D) < size) D++;
+    D = min(D, lowbits);
+    const uint32_t nsub = 1u << D;
+    uint32_t* s_cnt = sc.wcnt;          // [1024]
+    uint32_t* s_off = sc.wcnt + 1024;   // [1024]
+    for (uint32_t d = threadIdx.x; d < nsub; d += BK_THREADS) s_cnt[d] = 0u;
     __syncthreads();
-    for (int d = warp; d < RADIX; d += BK_WARPS) {
-        const uint32_t lo = s_sub[d], hi = s_sub[d + 1];
-        if (hi - lo <= RANK_MAX)  // the pairs share every digit from msd up
-            warp_small_sort(k1 + lo, v1 + lo, hi - lo, (1ull << (msd * RADIX_BITS)) - 1ull, K + start + lo,
-                            V + start + lo);
+    const int dshift = lowbits - D;
+    for (uint32_t e = threadIdx.x; e < size; e += BK_THREADS)
+        atomicAdd(&s_cnt[(uint32_t)(k0[e] >> dshift) & (nsub - 1u)], 1u);
+    __syncthreads();
+    // exclusive scan of the counts (two per thread) and their maximum
+    __shared__ uint32_t s_wsum[BK_WARPS], s_wmax[BK_WARPS];
+    {
+        const int lane = threadIdx.x & 31;
+        const uint32_t i0 = 2u * threadIdx.x;
+        const uint32_t c0 = i0 < nsub ? s_cnt[i0] : 0u, c1 = i0 + 1u < nsub ? s_cnt[i0 + 1u] : 0u;
+        uint32_t x = c0 + c1, mx = max(c0, c1);
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        mx = __reduce_max_sync(0xffffffffu, mx);
+        if (lane == 31) s_wsum[warp] = x;
+        if (lane == 0) s_wmax[warp] = mx;
+        __syncthreads();
+        uint32_t add = 0, m_all = 0;
+        for (int u = 0; u < BK_WARPS; u++) {
+            if (u < warp) add += s_wsum[u];
+            m_all = max(m_all, s_wmax[u]);
+        }
+        const uint32_t ex = add + x - (c0 + c1);
+        if (i0 < nsub) s_off[i0] = ex;
+        if (i0 + 1u < nsub) s_off[i0 + 1u] = ex + c0;
+        if (threadIdx.x == 0) s_range[0] = m_all;  // the start is in a register already
     }
-    // larger sub-buckets: LSD passes over the digits below, by the whole CTA
-    // (uniform loop: every thread reads the same s_sub[])
-    for (int d = 0; d < RADIX; d++) {
-        const uint32_t lo = s_sub[d], hi = s_sub[d + 1];
-        if (hi - lo <= RANK_MAX) continue;
-        uint64_t *ka = k1 + lo, *kb = k0 + lo;
-        uint32_t *va = v1 + lo, *vb = v0 + lo;
-        for (int p = 0; p < msd; p++) {
-            bucket_pass(ka, va, kb, vb, hi - lo, p * RADIX_BITS, sc);
-            uint64_t* tk = ka;
-            ka = kb;
-            kb = tk;
-            uint32_t* tv = va;
-            va = vb;
-            vb = tv;
+    __syncthreads();
+    const uint32_t m_max = s_range[0];
+    if (m_max <= RANK_MAX && lowbits + 13 <= 64) {
+        const uint64_t lowmask = (lowbits >= 64) ? ~0ull : ((1ull << lowbits) - 1ull);
+        for (uint32_t e = threadIdx.x; e < size; e += BK_THREADS) {
+            const uint64_t key = k0[e];
+            const uint32_t pos = atomicAdd(&s_off[(uint32_t)(key >> dshift) & (nsub - 1u)], 1u);
+            k1[pos] = ((key & lowmask) << 13) | e;
         }
-        for (uint32_t e = threadIdx.x; e < hi - lo; e += BK_THREADS) {
-            K[start + lo + e] = ka[e];
-            V[start + lo + e] = va[e];
+        __syncthreads();
+        // s_off[d] is now the end of sub-bucket d
+        for (uint32_t d = threadIdx.x; d < nsub; d += BK_THREADS) {
+            const uint32_t m = s_cnt[d];
+            if (m == 0u || m > 16u) continue;
+            const uint32_t lo = s_off[d] - m;
+            for (uint32_t i = 0; i < m; i++) {
+                const uint64_t ci = k1[lo + i];
+                uint32_t r = 0;
+                for (uint32_t j = 0; j < m; j++) r += k1[lo + j] < ci ? 1u : 0u;
+                const uint32_t src = (uint32_t)(ci & 8191u);
+                K[start + lo + r] = k0[src];
+                V[start + lo + r] = v0[src];
+            }
         }
+        for (uint32_t d = warp; d < nsub; d += BK_WARPS) {
+            const uint32_t m = s_cnt[d];
+            if (m <= 16u) continue;
+            const uint32_t lo = s_off[d] - m;
+            if (m <= 32u) warp_bitonic_comp<1>(k1 + lo, m, k0, v0, K + start + lo, V + start + lo);
+            else if (m <= 64u) warp_bitonic_comp<2>(k1 + lo, m, k0, v0, K + start + lo, V + start + lo);
+            else warp_bitonic_comp<4>(k1 + lo, m, k0, v0, K + start + lo, V + start + lo);
+        }
+        return;
+    }
+    // stable LSD passes over every digit below the top one
+    uint64_t *ka = k0, *kb = k1;
+    uint32_t *va = v0, *vb = v1;
+    for (int p = 0; p < low_passes; p++) {
+        bucket_pass(ka, va, kb, vb, size, p * RADIX_BITS, sc);
+        uint64_t* tk = ka;
+        ka = kb;
+        kb = tk;
+        uint32_t* tv = va;
+        va = vb;
+        vb = tv;
+    }
+    for (uint32_t e = threadIdx.x; e < size; e += BK_THREADS) {
+        K[start + e] = ka[e];
+        V[start + e] = va[e];
     }
 }
 

@@ -247,7 +247,7 @@ __global__ void k_ref_gather(const uint64_t* __restrict__ keys, const uint32_t* 
     cell[k] = pack_cell(cell_of(x, y, z, GRID_INV));
 }
 
-// with q.level set, also each 32-body chunk's cost estimate (the
+// with q.est set, also each 32-body chunk's cost estimate (the
 // populations of its bodies' buckets)
 __global__ void k_ref_mix(const uint64_t* __restrict__ keys, const uint32_t* __restrict__ V, uint32_t n,
                           const uint32_t* __restrict__ bstart, const uint32_t* __restrict__ bend,
@@ -262,7 +262,7 @@ __global__ void k_ref_mix(const uint64_t* __restrict__ keys, const uint32_t* __r
         if (bhash) atomicAdd((unsigned long long*)&bhash[b], (unsigned long long)sf_mix64(V[k]));
         pop = bend[b] - s;
     }
-    if (q.level && (k & ~31u) < n) sfchunk::note_cost(q, k >> 5, pop);
+    if (q.est && (k & ~31u) < n) sfchunk::note_cost(q, k >> 5, pop);
 }
 
 // One body against the cells of its reach: a callback per candidate pair,
@@ -455,9 +455,11 @@ __global__ void __launch_bounds__(RW_WARPS * 32) k_ref_density_warp(
     const int w = threadIdx.x >> 5;
     sfchunk::Taker t = sfchunk::taker(q);
     for (;;) {
-        const uint32_t c = sfchunk::next(q, t, 0u);
+        const uint32_t c = sfchunk::next(q, t);
         if (c == 0xFFFFFFFFu) break;
+        const long long t0 = clock64();
         ref_density_chunk(c * 32u, n, mask, bstart, bend, bmix, cell, px, pq, V, hw, rho, s_q[w], s_h[w]);
+        sfchunk::record(q, 0, c, clock64() - t0);
     }
     sfchunk::warp_exit(q, gridDim.x * RW_WARPS);
 }
@@ -684,12 +686,13 @@ __global__ void __launch_bounds__(RW_WARPS * 32) k_ref_momentum_warp(
     __shared__ uint64_t s_m[RW_WARPS][HASH ? 32 : 1];
     const int w = threadIdx.x >> 5;
     sfchunk::Taker t = sfchunk::taker(q);
-    const uint32_t pass = hw[2] != 0.0f ? 1u : 0u;  // after the grid density pass, or first
     for (;;) {
-        const uint32_t c = sfchunk::next(q, t, pass);
+        const uint32_t c = sfchunk::next(q, t);
         if (c == 0xFFFFFFFFu) break;
+        const long long t0 = clock64();
         ref_momentum_chunk<HASH>(c * 32u, n, mask, bstart, bend, bmix, bhash, cell, px, pq, V, hw, acc, nbr, hash,
                                  s_q[w], s_p[w], s_m[w]);
+        sfchunk::record(q, 1, c, clock64() - t0);
     }
     sfchunk::warp_exit(q, gridDim.x * RW_WARPS);
 }
@@ -807,13 +810,10 @@ int sf_stage_sph(sfgpu_sim* s) {
     SF_CHECK_LAUNCH();
     const bool by_warp = s->p.sph_path != 2;
     sfchunk::ChunkQueue q = w->q;
-    if (!by_warp) q.level = nullptr;  // the per-body passes take no chunks
+    if (!by_warp) q.est = nullptr;  // the per-body passes take no chunks
     k_ref_mix<<<nb, 256, 0, st>>>(w->keys, w->vals, n, w->bstart, w->bend, w->cell, w->bmix, w->bhash, q);
     SF_CHECK_LAUNCH();
-    if (by_warp) {
-        sfchunk::k_chunk_order<<<1, 1024, 0, st>>>(w->q);
-        SF_CHECK_LAUNCH();
-    }
+
     s->timer.end(st, tk);
     tk = s->timer.begin(st, "sph_density");
     static uint32_t wave[3] = {0, 0, 0};  // density, momentum with hashes, momentum
@@ -823,6 +823,10 @@ int sf_stage_sph(sfgpu_sim* s) {
         wave[2] = sfchunk::wave_blocks(k_ref_momentum_warp<false>, RW_WARPS * 32, 0xFFFFFFFFu);
     }
     const uint32_t most = sf_ceil_div(w->q.nchunks, RW_WARPS);
+    if (by_warp) {
+        sfchunk::k_chunk_order<<<1, 1024, 0, st>>>(w->q, 0);
+        SF_CHECK_LAUNCH();
+    }
     if (by_warp)
         k_ref_density_warp<<<std::min(wave[0], most), RW_WARPS * 32, 0, st>>>(
             n, mask, w->bstart, w->bend, w->bmix, w->cell, w->px, w->pq, w->vals, w->hw, rho, w->q);
@@ -836,6 +840,10 @@ int sf_stage_sph(sfgpu_sim* s) {
     SF_CHECK_LAUNCH();
     s->timer.end(st, tk);
     tk = s->timer.begin(st, "sph_force");
+    if (by_warp) {
+        sfchunk::k_chunk_order<<<1, 1024, 0, st>>>(w->q, 1);
+        SF_CHECK_LAUNCH();
+    }
     if (by_warp && w->hash)
         k_ref_momentum_warp<true><<<std::min(wave[1], most), RW_WARPS * 32, 0, st>>>(
             n, mask, w->bstart, w->bend, w->bmix, w->bhash, w->cell, w->px, w->pq, w->vals, w->hw, acc, w->nbr,

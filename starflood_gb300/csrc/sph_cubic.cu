@@ -156,7 +156,7 @@ __global__ void k_cell_gather(const uint64_t* __restrict__ keys, const uint32_t*
     if (mixv) mixv[k] = sf_mix64(p);
 }
 
-// buckets that hold more than one cell; with q.level set, each 32-body
+// buckets that hold more than one cell; with q.est set, each 32-body
 // chunk's cost estimate (the populations of its bodies' buckets)
 __global__ void k_bucket_mix(const uint64_t* __restrict__ keys, uint32_t n, const uint32_t* __restrict__ bstart,
                              const uint32_t* __restrict__ bend, const uint64_t* __restrict__ cell,
@@ -169,7 +169,7 @@ __global__ void k_bucket_mix(const uint64_t* __restrict__ keys, uint32_t n, cons
         if (k != s && cell[k] != cell[s]) bmix[b] = 1u;
         pop = bend[b] - s;
     }
-    if (q.level && (k & ~31u) < n) sfchunk::note_cost(q, k >> 5, pop);
+    if (q.est && (k & ~31u) < n) sfchunk::note_cost(q, k >> 5, pop);
 }
 
 __device__ __forceinline__ bool density_pair(const float4& a, float hi, float ihi, const float4& q, float hj,
@@ -334,7 +334,7 @@ __global__ void __launch_bounds__(128) k_cubic_body(uint32_t n, const float* __r
 // same bits.  A warp whose bodies span more than 3 cells on an axis (sparse
 // regions) runs the per-body scan instead.
 constexpr int CW_WARPS = 4;
-template <bool FORCE, bool HASH>
+template <int REACH, bool FORCE, bool HASH>
 __device__ __forceinline__ void cubic_chunk(uint32_t k0, uint32_t n, const float* __restrict__ grid, uint32_t mask,
                                             const uint32_t* __restrict__ bstart, const uint32_t* __restrict__ bend,
                                             const uint32_t* __restrict__ bmix, const float4* __restrict__ px,
@@ -374,26 +374,27 @@ __device__ __forceinline__ void cubic_chunk(uint32_t k0, uint32_t n, const float
                          (uint32_t)xhi - (uint32_t)xlo <= 2u && !__any_sync(0xffffffffu, cell_clamped(c0));
     if (!compact) {
         if (live) {
-            body_scan<1, FORCE, HASH>(k, a, hi, ihi, di, vi, side, inv, R2, mask, bstart, bend, bmix, px, ph, pv,
+            body_scan<REACH, FORCE, HASH>(k, a, hi, ihi, di, vi, side, inv, R2, mask, bstart, bend, bmix, px, ph, pv,
                                       cell, pd, alpha, beta, mixv, o0, o1, o2, o3, count, hs);
             body_store<FORCE, HASH>(k, n, ph, pd, V, gamma, slab, dudt, nbr, hash, o0, o1, o2, o3, count, hs);
         }
         return;
     }
-    for (int cz = zlo - 1; cz <= zhi + 1; cz++) {
+    for (int cz = zlo - REACH; cz <= zhi + REACH; cz++) {
         const float lz = (float)cz * side;
         const float gz = fmaxf(0.f, fmaxf(lz - a.z, a.z - (lz + side)));
-        for (int cy = ylo - 1; cy <= yhi + 1; cy++) {
+        for (int cy = ylo - REACH; cy <= yhi + REACH; cy++) {
             // this lane's part of the row, exactly as its per-body scan
             // would take it (x0 > x1: none)
             const float ly = (float)cy * side;
             const float gy = fmaxf(0.f, fmaxf(ly - a.y, a.y - (ly + side)));
             const float rem = R2 - (gy * gy + gz * gz);
             int x0 = 1, x1 = 0;
-            if (live && rem > 0.0f && cz >= c0.z - 1 && cz <= c0.z + 1 && cy >= c0.y - 1 && cy <= c0.y + 1) {
+            if (live && rem > 0.0f && cz >= c0.z - REACH && cz <= c0.z + REACH && cy >= c0.y - REACH &&
+                cy <= c0.y + REACH) {
                 const float ext = sqrtf(rem) * MARGIN_HI;
-                x0 = max(c0.x - 1, (int)floorf((a.x - ext) * inv));
-                x1 = min(c0.x + 1, (int)floorf((a.x + ext) * inv));
+                x0 = max(c0.x - REACH, (int)floorf((a.x - ext) * inv));
+                x1 = min(c0.x + REACH, (int)floorf((a.x + ext) * inv));
             }
             const bool any = x0 <= x1;
             if (!__any_sync(0xffffffffu, any)) continue;
@@ -460,7 +461,7 @@ __device__ __forceinline__ void cubic_chunk(uint32_t k0, uint32_t n, const float
 
 // The pass: one resident wave of persistent warps taking chunks of 32
 // sorted bodies heaviest first (chunks.cuh).
-template <bool FORCE, bool HASH>
+template <int REACH, bool FORCE, bool HASH>
 __global__ void __launch_bounds__(CW_WARPS * 32) k_cubic_warp(uint32_t n, const float* __restrict__ grid,
                                                              uint32_t mask, const uint32_t* __restrict__ bstart,
                                                              const uint32_t* __restrict__ bend,
@@ -482,10 +483,12 @@ __global__ void __launch_bounds__(CW_WARPS * 32) k_cubic_warp(uint32_t n, const 
     const int w = threadIdx.x >> 5;
     sfchunk::Taker t = sfchunk::taker(q);
     for (;;) {
-        const uint32_t c = sfchunk::next(q, t, FORCE ? 1u : 0u);  // density is pass 0, force pass 1
+        const uint32_t c = sfchunk::next(q, t);
         if (c == 0xFFFFFFFFu) break;
-        cubic_chunk<FORCE, HASH>(c * 32u, n, grid, mask, bstart, bend, bmix, px, ph, pv, cell, pd, V, gamma, alpha,
+        const long long t0 = clock64();
+        cubic_chunk<REACH, FORCE, HASH>(c * 32u, n, grid, mask, bstart, bend, bmix, px, ph, pv, cell, pd, V, gamma, alpha,
                                  beta, slab, dudt, nbr, mixv, hash, s_q[w], s_h[w], s_v[w], s_m[w]);
+        sfchunk::record(q, FORCE ? 1 : 0, c, clock64() - t0);
     }
     sfchunk::warp_exit(q, gridDim.x * CW_WARPS);
 }
@@ -495,23 +498,27 @@ int launch_passes(sfgpu_sim* s, CubicWork* w, uint32_t mask, uint32_t* nbr, uint
     cudaStream_t st = s->stream;
     const uint32_t n = s->n;
     const float gamma = (float)s->p.sph_gamma, alpha = (float)s->p.sph_alpha, beta = (float)s->p.sph_beta;
-    const bool warp = w->path == 0;
+    const bool warp = w->path == 0 || w->path == 3;
     const uint32_t bb = sf_ceil_div(n, 128);
     // one resident wave of each warp pass (chunks.cuh)
     static uint32_t wave[3] = {0, 0, 0};  // density, density with hashes, force
     const uint32_t most = sf_ceil_div(w->q.nchunks, CW_WARPS);
     if (!wave[0]) {
-        wave[0] = sfchunk::wave_blocks(k_cubic_warp<false, false>, CW_WARPS * 32, 0xFFFFFFFFu);
-        wave[1] = sfchunk::wave_blocks(k_cubic_warp<false, true>, CW_WARPS * 32, 0xFFFFFFFFu);
-        wave[2] = sfchunk::wave_blocks(k_cubic_warp<true, false>, CW_WARPS * 32, 0xFFFFFFFFu);
+        wave[0] = sfchunk::wave_blocks(k_cubic_warp<REACH, false, false>, CW_WARPS * 32, 0xFFFFFFFFu);
+        wave[1] = sfchunk::wave_blocks(k_cubic_warp<REACH, false, true>, CW_WARPS * 32, 0xFFFFFFFFu);
+        wave[2] = sfchunk::wave_blocks(k_cubic_warp<REACH, true, false>, CW_WARPS * 32, 0xFFFFFFFFu);
     }
     int tk = s->timer.begin(st, "sph_density");
+    if (warp) {
+        sfchunk::k_chunk_order<<<1, 1024, 0, st>>>(w->q, 0);
+        SF_CHECK_LAUNCH();
+    }
     if (warp && hash)
-        k_cubic_warp<false, true><<<std::min(wave[1], most), CW_WARPS * 32, 0, st>>>(
+        k_cubic_warp<REACH, false, true><<<std::min(wave[1], most), CW_WARPS * 32, 0, st>>>(
             n, w->grid, mask, w->bstart, w->bend, w->bmix, w->px, w->ph, w->pv, w->cell, w->pd, w->vals, gamma, alpha,
             beta, s->slab, s->dudt, nbr, w->mixv, hash, w->q);
     else if (warp)
-        k_cubic_warp<false, false><<<std::min(wave[0], most), CW_WARPS * 32, 0, st>>>(
+        k_cubic_warp<REACH, false, false><<<std::min(wave[0], most), CW_WARPS * 32, 0, st>>>(
             n, w->grid, mask, w->bstart, w->bend, w->bmix, w->px, w->ph, w->pv, w->cell, w->pd, w->vals, gamma, alpha,
             beta, s->slab, s->dudt, nbr, nullptr, nullptr, w->q);
     else if (hash)
@@ -525,8 +532,12 @@ int launch_passes(sfgpu_sim* s, CubicWork* w, uint32_t mask, uint32_t* nbr, uint
     SF_CHECK_LAUNCH();
     s->timer.end(st, tk);
     tk = s->timer.begin(st, "sph_force");
+    if (warp) {
+        sfchunk::k_chunk_order<<<1, 1024, 0, st>>>(w->q, 1);
+        SF_CHECK_LAUNCH();
+    }
     if (warp)
-        k_cubic_warp<true, false><<<std::min(wave[2], most), CW_WARPS * 32, 0, st>>>(
+        k_cubic_warp<REACH, true, false><<<std::min(wave[2], most), CW_WARPS * 32, 0, st>>>(
             n, w->grid, mask, w->bstart, w->bend, w->bmix, w->px, w->ph, w->pv, w->cell, w->pd, w->vals, gamma, alpha,
             beta, s->slab, s->dudt, nbr, nullptr, nullptr, w->q);
     else
@@ -548,7 +559,7 @@ int sf_sph_cubic_alloc(sfgpu_sim* s) {
     s->sph_cubic = w;
     const uint32_t n = std::max<uint32_t>(s->n, 1);
     w->path = s->p.sph_path;
-    w->reach = s->p.sph_path == 1 ? 2 : 1;
+    w->reach = (s->p.sph_path == 1 || s->p.sph_path == 3) ? 2 : 1;
     w->tbits = 1;
     while ((1u << w->tbits) < 2u * n) w->tbits++;
     w->tsize = 1u << w->tbits;
@@ -620,13 +631,10 @@ int sf_sph_cubic(sfgpu_sim* s) {
                                       w->cell, w->ph, gamma, w->mixv);
     SF_CHECK_LAUNCH();
     sfchunk::ChunkQueue q = w->q;
-    if (w->path != 0) q.level = nullptr;  // the per-body passes take no chunks
+    if (w->path != 0 && w->path != 3) q.est = nullptr;  // the per-body passes take no chunks
     k_bucket_mix<<<nb, 256, 0, st>>>(w->keys, n, w->bstart, w->bend, w->cell, w->bmix, q);
     SF_CHECK_LAUNCH();
-    if (w->path == 0) {
-        sfchunk::k_chunk_order<<<1, 1024, 0, st>>>(w->q);
-        SF_CHECK_LAUNCH();
-    }
+
     s->timer.end(st, tk);
     uint32_t* nbr = sf_sph_neighbour_counts(s);
     uint64_t* hash = w->mixv ? sf_sph_neighbour_hashes(s) : nullptr;

@@ -209,14 +209,14 @@ def _cubic_sim(sf, n, pos, vel, mas, rad, u, **kw):
     return s
 
 
-@pytest.mark.parametrize("path", [0, 1, 2])
+@pytest.mark.parametrize("path", [0, 1, 2, 3])
 @pytest.mark.parametrize("n,hvar", [(4096, False), (3000, True)])
 def test_sph_cubic_vs_fp64_oracle(sf, oracle64, n, hvar, path):
     """Cubic-spline SPH: neighbour sets (counts and hashes) bit-identical to
     the brute-force FP32 enumeration; rho, dv/dt, du/dt within 1e-5 / 1e-4
     of the FP64 oracle.  path 0: one warp per 32 sorted bodies over side-2h
     cells; 1: one thread per body over side-h cells; 2: one thread per body
-    over side-2h cells."""
+    over side-2h cells; 3: by warps over side-h cells."""
     from starflood_gb300.ics import plummer
     pos, vel, mas = plummer(n, seed=51)
     pos = pos * np.float32(0.3)  # denser: ~30 neighbours per body at h = 0.05
@@ -326,12 +326,14 @@ def test_sph_cubic_plummer262144_subsample(sf):
     assert e_du.max() < 1e-4
 
 
+@pytest.mark.parametrize("paths", [(0, 2), (3, 1)])
 @pytest.mark.parametrize("n,hvar", [(1 << 18, False), (65536, True)])
-def test_sph_cubic_paths_bit_identical(sf, n, hvar):
-    """The warp-per-32-bodies pass (sph_path 0) and the thread-per-body pass
-    over the same side-2h cells (sph_path 2) add the same terms in the same
-    order: rho, P, dv/dt, du/dt, neighbour counts and hashes equal to the
-    bit on the Plummer gas of the benchmark (and with varied h)."""
+def test_sph_cubic_paths_bit_identical(sf, n, hvar, paths):
+    """The warp-per-32-bodies passes and the thread-per-body passes over the
+    same cells (sph_path 0 and 2: side 2h; 3 and 1: side h) add the same
+    terms in the same order: rho, P, dv/dt, du/dt, neighbour counts and
+    hashes equal to the bit on the Plummer gas of the benchmark (and with
+    varied h)."""
     from starflood_gb300.ics import plummer
     pos, vel, mas = plummer(n, seed=7)
     rad = np.full(n, 0.05, np.float32)
@@ -340,7 +342,7 @@ def test_sph_cubic_paths_bit_identical(sf, n, hvar):
         rad[1::7] = 0.03
     u = np.full(n, 0.05, np.float32)
     out = []
-    for path in (0, 2):
+    for path in paths:
         with _cubic_sim(sf, n, pos, vel, mas, rad, u, sph_path=path, flags=sf.FLAG_STATS) as s:
             s.solve_sph()
             v = slab_views(s.download(), n, 16)
