@@ -429,14 +429,22 @@ __device__ __forceinline__ void ref_density_chunk(uint32_t k0, uint32_t n, uint3
                             if (r2 < rd2) hits |= 1u << t;
                         }
                     }
+                    // two terms per round: the second's arithmetic overlaps the
+                    // first's, the sum takes them in order
+                    auto dterm = [&](int t) {
+                        const float4 q = sq[t];
+                        const float ex = fsub(a.x, q.x), ey = fsub(a.y, q.y), ez = fsub(a.z, q.z);
+                        const float r2 = fadd(fadd(fmul(ex, ex), fmul(ey, ey)), fmul(ez, ez));
+                        sum += ref_density_term(r2, ai3, ihi2, sh[t], q.w, inv_sqrt_pi);
+                    };
                     while (__any_sync(0xffffffffu, hits != 0u)) {
                         if (hits) {
-                            const int t = __ffs(hits) - 1;
+                            const int t1 = __ffs(hits) - 1;
                             hits &= hits - 1u;
-                            const float4 q = sq[t];
-                            const float ex = fsub(a.x, q.x), ey = fsub(a.y, q.y), ez = fsub(a.z, q.z);
-                            const float r2 = fadd(fadd(fmul(ex, ex), fmul(ey, ey)), fmul(ez, ez));
-                            sum += ref_density_term(r2, ai3, ihi2, sh[t], q.w, inv_sqrt_pi);
+                            const int t2 = hits ? __ffs(hits) - 1 : -1;
+                            if (t2 >= 0) hits &= hits - 1u;
+                            dterm(t1);
+                            if (t2 >= 0) dterm(t2);
                         }
                     }
                 }
@@ -658,15 +666,22 @@ __device__ __forceinline__ void ref_momentum_chunk(
                             if (r2 < rf2) hits |= 1u << t;
                         }
                     }
+                    // two terms per round (the sums take them in order)
+                    auto mterm = [&](int t) {
+                        const float4 q = sq[t];
+                        const float ex = fsub(a.x, q.x), ey = fsub(a.y, q.y), ez = fsub(a.z, q.z);
+                        const float r2 = fadd(fadd(fmul(ex, ex), fmul(ey, ey)), fmul(ez, ez));
+                        const float2 qj = sp[t];
+                        ref_momentum_term(ex, ey, ez, r2, ihi2, m2_den_i, ci, qj.x, qj.y, pi15, sx, sy, sz);
+                    };
                     while (__any_sync(0xffffffffu, hits != 0u)) {
                         if (hits) {
-                            const int t = __ffs(hits) - 1;
+                            const int t1 = __ffs(hits) - 1;
                             hits &= hits - 1u;
-                            const float4 q = sq[t];
-                            const float ex = fsub(a.x, q.x), ey = fsub(a.y, q.y), ez = fsub(a.z, q.z);
-                            const float r2 = fadd(fadd(fmul(ex, ex), fmul(ey, ey)), fmul(ez, ez));
-                            const float2 qj = sp[t];
-                            ref_momentum_term(ex, ey, ez, r2, ihi2, m2_den_i, ci, qj.x, qj.y, pi15, sx, sy, sz);
+                            const int t2 = hits ? __ffs(hits) - 1 : -1;
+                            if (t2 >= 0) hits &= hits - 1u;
+                            mterm(t1);
+                            if (t2 >= 0) mterm(t2);
                         }
                     }
                 }

@@ -63,27 +63,25 @@ struct CubicWork {
 };
 
 // The kernel and its derivative from q = r / h and 1 / h (the passes keep
-// 1 / h of every body, so no division runs per pair).
+// 1 / h of every body, so no division runs per pair).  Both pieces are
+// computed and one selected (no branch), so consecutive pairs' terms can
+// be computed side by side.
 __device__ __forceinline__ float w_cubic(float r, float ih) {
     const float q = r * ih;
     const float s = ih * ih * ih * (1.0f / PI_F);
-    if (q < 1.0f) return s * (1.0f - 1.5f * q * q + 0.75f * q * q * q);
-    if (q < 2.0f) {
-        const float t = 2.0f - q;
-        return s * 0.25f * t * t * t;
-    }
-    return 0.0f;
+    const float inner = s * (1.0f - 1.5f * q * q + 0.75f * q * q * q);
+    const float t = 2.0f - q;
+    const float outer = s * 0.25f * t * t * t;
+    return q < 1.0f ? inner : (q < 2.0f ? outer : 0.0f);
 }
 __device__ __forceinline__ float dw_cubic(float r, float ih) {
     const float q = r * ih;
     const float ih2 = ih * ih;
     const float s = ih2 * ih2 * (1.0f / PI_F);
-    if (q < 1.0f) return s * (-3.0f * q + 2.25f * q * q);
-    if (q < 2.0f) {
-        const float t = 2.0f - q;
-        return s * (-0.75f * t * t);
-    }
-    return 0.0f;
+    const float inner = s * (-3.0f * q + 2.25f * q * q);
+    const float t = 2.0f - q;
+    const float outer = s * (-0.75f * t * t);
+    return q < 1.0f ? inner : (q < 2.0f ? outer : 0.0f);
 }
 // the FP32 neighbour decision (same expression as the oracle)
 __device__ __forceinline__ bool is_neighbour(float dx, float dy, float dz, float hi, float hj, float& r2) {
@@ -197,12 +195,10 @@ __device__ __forceinline__ void force_pair(const float4& a, float hi, const floa
     const float g = 0.5f * (dw_cubic(r, di.w) + dw_cubic(r, __fdividef(1.0f, hj))) * rinv;
     const float vx = vi.x - vj.x, vy = vi.y - vj.y, vz = vi.z - vj.z;
     const float vr = vx * rx + vy * ry + vz * rz;
-    float visc = 0.0f;
-    if (vr < 0.0f) {
-        const float h = 0.5f * (hi + hj);
-        const float mu = __fdividef(h * vr, r2 + 0.01f * h * h);
-        visc = __fdividef(-alpha * 0.5f * (di.z + dj.z) * mu + beta * mu * mu, 0.5f * (di.x + dj.x));
-    }
+    const float h = 0.5f * (hi + hj);
+    const float mu = __fdividef(h * vr, r2 + 0.01f * h * h);
+    const float pi_ij = __fdividef(-alpha * 0.5f * (di.z + dj.z) * mu + beta * mu * mu, 0.5f * (di.x + dj.x));
+    const float visc = vr < 0.0f ? pi_ij : 0.0f;  // approaching pairs only (computed for all, no branch)
     const float f = q.w * (di.y + dj.y + visc) * g;
     ax -= f * rx;
     ay -= f * ry;
@@ -426,30 +422,44 @@ __device__ __forceinline__ void cubic_chunk(uint32_t k0, uint32_t n, const float
                     const uint32_t vm = __ballot_sync(0xffffffffu, ok);
                     __syncwarp();
                     // pass 1: the neighbour decisions of this lane's body
+                    // (a full batch unrolled: its tests are independent)
                     uint32_t hits = 0u;
+                    auto test = [&](int t) {
+                        const float4 q = sq[t];
+                        const float hj = FORCE ? sh[t].w : sh[t].x;
+                        float r2;
+                        const bool nb = is_neighbour(fsub(a.x, q.x), fsub(a.y, q.y), fsub(a.z, q.z), hi, hj, r2);
+                        if (nb && (!FORCE || jb + (uint32_t)t != k)) hits |= 1u << t;
+                    };
                     if (mine) {
-                        for (uint32_t mm = vm; mm; mm &= mm - 1u) {
-                            const int t = __ffs(mm) - 1;
-                            const float4 q = sq[t];
-                            const float hj = FORCE ? sh[t].w : sh[t].x;
-                            float r2;
-                            const bool nb = is_neighbour(fsub(a.x, q.x), fsub(a.y, q.y), fsub(a.z, q.z), hi, hj, r2);
-                            if (nb && (!FORCE || jb + (uint32_t)t != k)) hits |= 1u << t;
+                        if (vm == 0xffffffffu) {
+#pragma unroll 8
+                            for (int t = 0; t < 32; t++) test(t);
+                        } else {
+                            for (uint32_t mm = vm; mm; mm &= mm - 1u) test(__ffs(mm) - 1);
                         }
                     }
-                    // pass 2: the terms, in candidate order
+                    // pass 2: the terms, in candidate order, two per round
+                    // (the second's arithmetic overlaps the first's; the
+                    // sums take them in order)
+                    auto term = [&](int t) {
+                        const float4 q = sq[t];
+                        if (!FORCE) {
+                            const float4 hj = sh[t];
+                            density_pair(a, hi, ihi, q, hj.x, hj.w, o0, count);
+                            if (HASH) hs += sm[t];
+                        } else {
+                            force_pair(a, hi, di, vi, q, sv[t], sh[t], alpha, beta, o0, o1, o2, o3);
+                        }
+                    };
                     while (__any_sync(0xffffffffu, hits != 0u)) {
                         if (hits) {
-                            const int t = __ffs(hits) - 1;
+                            const int t1 = __ffs(hits) - 1;
                             hits &= hits - 1u;
-                            const float4 q = sq[t];
-                            if (!FORCE) {
-                                const float4 hj = sh[t];
-                                density_pair(a, hi, ihi, q, hj.x, hj.w, o0, count);
-                                if (HASH) hs += sm[t];
-                            } else {
-                                force_pair(a, hi, di, vi, q, sv[t], sh[t], alpha, beta, o0, o1, o2, o3);
-                            }
+                            const int t2 = hits ? __ffs(hits) - 1 : -1;
+                            if (t2 >= 0) hits &= hits - 1u;
+                            term(t1);
+                            if (t2 >= 0) term(t2);
                         }
                     }
                 }
