@@ -205,7 +205,7 @@ int launch_kind(sfgpu_sim* s, bool stats) {
 // p (warp 0 also takes the root itself as a monopole for lanes that do not
 // open it).  Partial sums go to scratch and k_walk_reduce adds them in octant
 // order.  All four node vectors are loaded at once per visit, and the
-// opening test divides approximately, falling back to the IEEE divide only
+// opening test compares by products, falling back to the IEEE divide only
 // within 2^-19 of theta, so every decision equals the reference's.
 constexpr int SPLIT = 8;
 
@@ -214,9 +214,11 @@ __device__ __forceinline__ bool opens(const float4& G, float rx, float ry, float
     const float ox = fsub(G.x, rx), oy = fsub(G.y, ry), oz = fsub(G.z, rz);
     const float d2 = fadd(fadd(fmul(ox, ox), fmul(oy, oy)), fmul(oz, oz));
     if (!(0.0f < d2)) return fc.theta <= 0.0f;
-    const float q = __fdividef(G.w, d2);
-    if (q > th_hi) return true;
-    if (q < th_lo) return false;
+    // G.w / d2 against theta by products (each within 2^-24 of exact, far
+    // inside the 2^-19 margins of th_lo, th_hi); the IEEE quotient only in
+    // between
+    if (G.w > fmul(th_hi, d2)) return true;
+    if (G.w < fmul(th_lo, d2)) return false;
     return fc.theta <= fdiv(G.w, d2);
 }
 
