@@ -490,13 +490,20 @@ __device__ __forceinline__ void warp_small_sort(const uint64_t* sk, const uint32
     }
 }
 
-// Bucket blockIdx.x of (Kb, Vb), sorted on its low digits, into (K, V).
-// Up to RANK_MAX pairs, warp 0 sorts the bucket with one network.  A larger
-// bucket is split wide on its next bits (below), so that the biggest bucket
-// (the long pole of the launch: several thousand keys on a uniform sphere)
-// costs a count, a scatter and many tiny sorts side by side instead of six
-// passes.  A bucket larger than BK_CAP is left alone and raises *big, which
-// enables the full tile passes queued after this kernel.
+// CTAs per bucket: a bucket of m pairs is shared by min(BK_SPLIT,
+// ceil(m / BK_SHARE)) CTAs, each sorting a range of its sub-buckets (the
+// biggest bucket of a uniform sphere, 6,606 of 65,536 keys, set the whole
+// launch when one CTA sorted it).
+constexpr uint32_t BK_SPLIT = 4;
+constexpr uint32_t BK_SHARE = 1024;
+
+// Bucket blockIdx.x % RADIX of (Kb, Vb), sorted on its low digits, into (K,
+// V), by share blockIdx.x / RADIX of its CTAs.  Up to RANK_MAX pairs, warp 0
+// of the first CTA sorts the bucket with one network.  A larger bucket is
+// split wide on its next bits (below), so that the biggest bucket costs a
+// count, a scatter and many tiny sorts side by side instead of six passes.
+// A bucket larger than BK_CAP is left alone and raises *big, which enables
+// the full tile passes queued after this kernel.
 __global__ void __launch_bounds__(BK_THREADS, 1) k_bucket_sort(const uint64_t* __restrict__ Kb,
                                                                const uint32_t* __restrict__ Vb,
                                                                uint64_t* __restrict__ K, uint32_t* __restrict__ V,
@@ -515,7 +522,7 @@ __global__ void __launch_bounds__(BK_THREADS, 1) k_bucket_sort(const uint64_t* _
     sc.run = s_run;
     sc.wtot = s_wtot;
     __shared__ uint32_t s_range[2];
-    const uint32_t b = blockIdx.x;
+    const uint32_t b = blockIdx.x % RADIX, share = blockIdx.x / RADIX;
     if (threadIdx.x < 32) {
         uint32_t start = 0;
         for (uint32_t j = threadIdx.x; j < b; j += 32) start += hist_top[j];
@@ -530,35 +537,41 @@ __global__ void __launch_bounds__(BK_THREADS, 1) k_bucket_sort(const uint64_t* _
     const uint32_t start = s_range[0], size = s_range[1];
     if (size == 0u) return;
     if (size > BK_CAP) {
-        if (threadIdx.x == 0) atomicOr(big, 1u);
+        if (share == 0u && threadIdx.x == 0) atomicOr(big, 1u);
         return;
     }
-    // four loads in flight per thread before their stores (the bucket's
-    // pairs come from L2; one at a time the biggest bucket waits ~13 round
+    const uint32_t shares = min(BK_SPLIT, (size + BK_SHARE - 1u) / BK_SHARE);
+    if (share >= shares) return;
+    // the bucket's pairs into shared memory (by the only CTA of a bucket
+    // sorted whole), four loads in flight per thread before their stores
+    // (they come from L2; one at a time the biggest bucket waits ~13 round
     // trips)
-    for (uint32_t e0 = threadIdx.x; e0 < size; e0 += 4u * BK_THREADS) {
-        uint64_t kk[4];
-        uint32_t vv[4];
+    auto load_bucket = [&]() {
+        for (uint32_t e0 = threadIdx.x; e0 < size; e0 += 4u * BK_THREADS) {
+            uint64_t kk[4];
+            uint32_t vv[4];
 #pragma unroll
-        for (int u = 0; u < 4; u++) {
-            const uint32_t e = e0 + (uint32_t)u * BK_THREADS;
-            if (e < size) {
-                kk[u] = Kb[start + e];
-                vv[u] = Vb[start + e];
+            for (int u = 0; u < 4; u++) {
+                const uint32_t e = e0 + (uint32_t)u * BK_THREADS;
+                if (e < size) {
+                    kk[u] = Kb[start + e];
+                    vv[u] = Vb[start + e];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const uint32_t e = e0 + (uint32_t)u * BK_THREADS;
+                if (e < size) {
+                    k0[e] = kk[u];
+                    v0[e] = vv[u];
+                }
             }
         }
-#pragma unroll
-        for (int u = 0; u < 4; u++) {
-            const uint32_t e = e0 + (uint32_t)u * BK_THREADS;
-            if (e < size) {
-                k0[e] = kk[u];
-                v0[e] = vv[u];
-            }
-        }
-    }
-    __syncthreads();
+        __syncthreads();
+    };
     const int warp = threadIdx.x >> 5;
     if (size <= RANK_MAX) {  // the pairs share the top digit only
+        load_bucket();
         if (warp == 0) warp_small_sort(k0, v0, size, (1ull << (low_passes * RADIX_BITS)) - 1ull, K + start, V + start);
         return;
     }
@@ -581,8 +594,23 @@ __global__ void __launch_bounds__(BK_THREADS, 1) k_bucket_sort(const uint64_t* _
     for (uint32_t d = threadIdx.x; d < nsub; d += BK_THREADS) s_cnt[d] = 0u;
     __syncthreads();
     const int dshift = lowbits - D;
-    for (uint32_t e = threadIdx.x; e < size; e += BK_THREADS)
-        atomicAdd(&s_cnt[(uint32_t)(k0[e] >> dshift) & (nsub - 1u)], 1u);
+    // the keys from L2, four loads in flight per thread: f(e, key) for each
+    auto each_key = [&](auto&& f) {
+        for (uint32_t e0 = threadIdx.x; e0 < size; e0 += 4u * BK_THREADS) {
+            uint64_t kk[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const uint32_t e = e0 + (uint32_t)u * BK_THREADS;
+                if (e < size) kk[u] = Kb[start + e];
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const uint32_t e = e0 + (uint32_t)u * BK_THREADS;
+                if (e < size) f(e, kk[u]);
+            }
+        }
+    };
+    each_key([&](uint32_t, uint64_t key) { atomicAdd(&s_cnt[(uint32_t)(key >> dshift) & (nsub - 1u)], 1u); });
     __syncthreads();
     // exclusive scan of the counts (two per thread) and their maximum
     __shared__ uint32_t s_wsum[BK_WARPS], s_wmax[BK_WARPS];
@@ -613,38 +641,50 @@ __global__ void __launch_bounds__(BK_THREADS, 1) k_bucket_sort(const uint64_t* _
     __syncthreads();
     const uint32_t m_max = s_range[0];
     if (m_max <= RANK_MAX && lowbits + 13 <= 64) {
-        const uint64_t lowmask = (lowbits >= 64) ? ~0ull : ((1ull << lowbits) - 1ull);
-        for (uint32_t e = threadIdx.x; e < size; e += BK_THREADS) {
-            const uint64_t key = k0[e];
-            const uint32_t pos = atomicAdd(&s_off[(uint32_t)(key >> dshift) & (nsub - 1u)], 1u);
-            k1[pos] = ((key & lowmask) << 13) | e;
-        }
+        // this CTA's sub-buckets [d0, d1), which start at `base` in the bucket
+        const uint32_t d0 = share * nsub / shares, d1 = (share + 1u) * nsub / shares;
+        const uint32_t base = s_off[d0];
         __syncthreads();
-        // s_off[d] is now the end of sub-bucket d
-        for (uint32_t d = threadIdx.x; d < nsub; d += BK_THREADS) {
+        const uint64_t lowmask = (lowbits >= 64) ? ~0ull : ((1ull << lowbits) - 1ull);
+        each_key([&](uint32_t e, uint64_t key) {
+            const uint32_t d = (uint32_t)(key >> dshift) & (nsub - 1u);
+            if (d < d0 || d >= d1) return;
+            const uint32_t pos = atomicAdd(&s_off[d], 1u);
+            k1[pos - base] = ((key & lowmask) << 13) | e;
+        });
+        __syncthreads();
+        // s_off[d] is now the end of sub-bucket d; the pairs themselves are
+        // read back from (Kb, Vb) by their position in the bucket
+        const uint64_t* kb = Kb + start;
+        const uint32_t* vb = Vb + start;
+        for (uint32_t d = d0 + threadIdx.x; d < d1; d += BK_THREADS) {
             const uint32_t m = s_cnt[d];
             if (m == 0u || m > 16u) continue;
             const uint32_t lo = s_off[d] - m;
+            const uint64_t* c = k1 + (lo - base);
             for (uint32_t i = 0; i < m; i++) {
-                const uint64_t ci = k1[lo + i];
+                const uint64_t ci = c[i];
                 uint32_t r = 0;
-                for (uint32_t j = 0; j < m; j++) r += k1[lo + j] < ci ? 1u : 0u;
+                for (uint32_t j = 0; j < m; j++) r += c[j] < ci ? 1u : 0u;
                 const uint32_t src = (uint32_t)(ci & 8191u);
-                K[start + lo + r] = k0[src];
-                V[start + lo + r] = v0[src];
+                K[start + lo + r] = kb[src];
+                V[start + lo + r] = vb[src];
             }
         }
-        for (uint32_t d = warp; d < nsub; d += BK_WARPS) {
+        for (uint32_t d = d0 + (uint32_t)warp; d < d1; d += BK_WARPS) {
             const uint32_t m = s_cnt[d];
             if (m <= 16u) continue;
             const uint32_t lo = s_off[d] - m;
-            if (m <= 32u) warp_bitonic_comp<1>(k1 + lo, m, k0, v0, K + start + lo, V + start + lo);
-            else if (m <= 64u) warp_bitonic_comp<2>(k1 + lo, m, k0, v0, K + start + lo, V + start + lo);
-            else warp_bitonic_comp<4>(k1 + lo, m, k0, v0, K + start + lo, V + start + lo);
+            const uint64_t* c = k1 + (lo - base);
+            if (m <= 32u) warp_bitonic_comp<1>(c, m, kb, vb, K + start + lo, V + start + lo);
+            else if (m <= 64u) warp_bitonic_comp<2>(c, m, kb, vb, K + start + lo, V + start + lo);
+            else warp_bitonic_comp<4>(c, m, kb, vb, K + start + lo, V + start + lo);
         }
         return;
     }
-    // stable LSD passes over every digit below the top one
+    // stable LSD passes over every digit below the top one, by the first CTA
+    if (share != 0u) return;
+    load_bucket();
     uint64_t *ka = k0, *kb = k1;
     uint32_t *va = v0, *vb = v1;
     for (int p = 0; p < low_passes; p++) {
@@ -771,7 +811,7 @@ int sf_sort_pairs_keep(uint64_t* keys, uint32_t* vals, uint32_t n, int bits, Sor
                                                       w.hist + top * RADIX, w.status, w.counters, d_status, enable,
                                                       w.spin_limit, w.withheld);
         SF_CHECK_LAUNCH();
-        k_bucket_sort<<<RADIX, BK_THREADS, bucket_sort_smem(), st>>>(w.keys_b, w.vals_b, keys, vals,
+        k_bucket_sort<<<RADIX * BK_SPLIT, BK_THREADS, bucket_sort_smem(), st>>>(w.keys_b, w.vals_b, keys, vals,
                                                                      w.hist + top * RADIX, top, big, enable);
         SF_CHECK_LAUNCH();
         // fallback (only if a bucket overflowed): every pass from the top
