@@ -330,6 +330,10 @@ __global__ void __launch_bounds__(128) k_cubic_body(uint32_t n, const float* __r
 // same bits.  A warp whose bodies span more than 3 cells on an axis (sparse
 // regions) runs the per-body scan instead.
 constexpr int CW_WARPS = 4;
+// the density passes' register budget: 64 (without the hint ptxas settles
+// at 56 with spills); the force pass takes no hint (0), its 64 registers
+// measured faster than with the hint (0.68 against 0.71 ms)
+constexpr int CW_MIN_BLOCKS = 8;
 template <int REACH, bool FORCE, bool HASH>
 __device__ __forceinline__ void cubic_chunk(uint32_t k0, uint32_t n, const float* __restrict__ grid, uint32_t mask,
                                             const uint32_t* __restrict__ bstart, const uint32_t* __restrict__ bend,
@@ -340,7 +344,7 @@ __device__ __forceinline__ void cubic_chunk(uint32_t k0, uint32_t n, const float
                                             float* __restrict__ slab, float* __restrict__ dudt,
                                             uint32_t* __restrict__ nbr, const uint64_t* __restrict__ mixv,
                                             uint64_t* __restrict__ hash, float4* sq, float4* sh, float4* sv,
-                                            uint64_t* sm) {
+                                            uint64_t* sm, float* st4) {
     const int lane = threadIdx.x & 31;
     if (k0 >= n) return;
     const uint32_t k = k0 + (uint32_t)lane;
@@ -351,6 +355,7 @@ __device__ __forceinline__ void cubic_chunk(uint32_t k0, uint32_t n, const float
     const float4 a = px[kk];
     const float hi = ph[kk].x;
     const float ihi = 1.0f / hi;
+    const float Si = fmul(fmul(2.0f, hi), fmul(2.0f, hi));  // (2 h_i)^2
     float4 di = make_float4(0.f, 0.f, 0.f, 0.f), vi = di;
     if (FORCE) {
         di = pd[kk];
@@ -410,13 +415,26 @@ __device__ __forceinline__ void cubic_chunk(uint32_t k0, uint32_t n, const float
                     const bool ok = j < j1 && (!chk || cell[j] == want);
                     __syncwarp();
                     if (ok) {
-                        sq[lane] = px[j];
+                        const float4 qj = px[j];
+                        float hj;
+                        sq[lane] = qj;
                         if (FORCE) {
-                            sh[lane] = pd[j];
+                            const float4 dj = pd[j];
+                            sh[lane] = dj;
                             sv[lane] = pv[j];
+                            hj = dj.w;
                         } else {
-                            sh[lane] = ph[j];
+                            const float4 pj = ph[j];
+                            sh[lane] = pj;
                             if (HASH) sm[lane] = mixv[j];
+                            hj = pj.x;
+                        }
+                        if (!FORCE) {  // the paired test's operands: -x, -y, -z and (2 h)^2
+                            const float sj = fmul(2.0f, hj);
+                            st4[lane] = -qj.x;
+                            st4[32 + lane] = -qj.y;
+                            st4[64 + lane] = -qj.z;
+                            st4[96 + lane] = fmul(sj, sj);
                         }
                     }
                     const uint32_t vm = __ballot_sync(0xffffffffu, ok);
@@ -432,7 +450,30 @@ __device__ __forceinline__ void cubic_chunk(uint32_t k0, uint32_t n, const float
                         if (nb && (!FORCE || jb + (uint32_t)t != k)) hits |= 1u << t;
                     };
                     if (mine) {
-                        if (vm == 0xffffffffu) {
+                        if (!FORCE && vm == 0xffffffffu) {
+                            // two candidates per paired FP32 instruction:
+                            // a - q as a + (-q), and r^2 < (2 max(h_i, h_j))^2
+                            // as r^2 < max((2 h_i)^2, (2 h_j)^2) (squaring
+                            // and rounding keep the order), the same
+                            // decision bits as is_neighbour
+                            const float2* tx = reinterpret_cast<const float2*>(st4);
+                            const float2* ty = reinterpret_cast<const float2*>(st4 + 32);
+                            const float2* tz = reinterpret_cast<const float2*>(st4 + 64);
+                            const float2* tS = reinterpret_cast<const float2*>(st4 + 96);
+                            const float2 ax2 = make_float2(a.x, a.x), ay2 = make_float2(a.y, a.y);
+                            const float2 az2 = make_float2(a.z, a.z);
+#pragma unroll 8
+                            for (int u = 0; u < 16; u++) {
+                                const float2 dx = __fadd2_rn(ax2, tx[u]);
+                                const float2 dy = __fadd2_rn(ay2, ty[u]);
+                                const float2 dz = __fadd2_rn(az2, tz[u]);
+                                const float2 r2 =
+                                    __fadd2_rn(__fadd2_rn(__fmul2_rn(dx, dx), __fmul2_rn(dy, dy)), __fmul2_rn(dz, dz));
+                                const float2 S = tS[u];
+                                hits |= (r2.x < fmaxf(Si, S.x) ? 1u : 0u) << (2 * u);
+                                hits |= (r2.y < fmaxf(Si, S.y) ? 2u : 0u) << (2 * u);
+                            }
+                        } else if (vm == 0xffffffffu) {
 #pragma unroll 8
                             for (int t = 0; t < 32; t++) test(t);
                         } else {
@@ -472,7 +513,7 @@ __device__ __forceinline__ void cubic_chunk(uint32_t k0, uint32_t n, const float
 // The pass: one resident wave of persistent warps taking chunks of 32
 // sorted bodies heaviest first (chunks.cuh).
 template <int REACH, bool FORCE, bool HASH>
-__global__ void __launch_bounds__(CW_WARPS * 32) k_cubic_warp(uint32_t n, const float* __restrict__ grid,
+__global__ void __launch_bounds__(CW_WARPS * 32, FORCE ? 0 : CW_MIN_BLOCKS) k_cubic_warp(uint32_t n, const float* __restrict__ grid,
                                                              uint32_t mask, const uint32_t* __restrict__ bstart,
                                                              const uint32_t* __restrict__ bend,
                                                              const uint32_t* __restrict__ bmix,
@@ -490,6 +531,7 @@ __global__ void __launch_bounds__(CW_WARPS * 32) k_cubic_warp(uint32_t n, const 
     __shared__ float4 s_h[CW_WARPS][32];  // density: (h, u, c, 1/h); force: (rho, P/rho^2, c, h)
     __shared__ float4 s_v[CW_WARPS][32];  // force: vx, vy, vz, u
     __shared__ uint64_t s_m[CW_WARPS][HASH ? 32 : 1];
+    __shared__ __align__(16) float s_t[CW_WARPS][4 * 32];  // -x, -y, -z, (2 h)^2 of each candidate
     const int w = threadIdx.x >> 5;
     sfchunk::Taker t = sfchunk::taker(q);
     for (;;) {
@@ -497,7 +539,7 @@ __global__ void __launch_bounds__(CW_WARPS * 32) k_cubic_warp(uint32_t n, const 
         if (c == 0xFFFFFFFFu) break;
         const long long t0 = clock64();
         cubic_chunk<REACH, FORCE, HASH>(c * 32u, n, grid, mask, bstart, bend, bmix, px, ph, pv, cell, pd, V, gamma, alpha,
-                                 beta, slab, dudt, nbr, mixv, hash, s_q[w], s_h[w], s_v[w], s_m[w]);
+                                 beta, slab, dudt, nbr, mixv, hash, s_q[w], s_h[w], s_v[w], s_m[w], s_t[w]);
         sfchunk::record(q, FORCE ? 1 : 0, c, clock64() - t0);
     }
     sfchunk::warp_exit(q, gridDim.x * CW_WARPS);
