@@ -14,18 +14,18 @@
 // Neighbour search on the hashed cell grid of sph_grid.cuh.  The search
 // radius is R = 2 h_max; cells have side R / REACH (slightly enlarged, so
 // that FP32 rounding never puts a neighbour more than REACH cells away).
-// One thread per body (bodies in sorted order, so a warp's bodies are close
-// together) scans the rows of cells (dy, dz) in [-REACH, REACH]^2 whose
+// A body's scan takes the rows of cells (dy, dz) in [-REACH, REACH]^2 whose
 // distance from the body is below R, and in each row only the x-range of
-// cells the sphere of radius R reaches.  The default, REACH = 1
-// (sfgpu_params.sph_path 0), is the 3 x 3 rows of side-2h cells around the
-// body with at most 2 cells per row; REACH = 2 (sph_path 1) visits about 84
-// cells of side h holding 2.5x the candidates of the sphere, but its extra
-// cell look-ups cost more than the candidates it saves (measured on the
-// 262,144-body Plummer gas: force pass 1.17 against 1.10 ms).  Each
-// candidate is tested with the
-// FP32 expression above; bodies of another cell that shares the bucket are
-// skipped by cell key, so none is counted twice.  With SFGPU_FLAG_STATS the
+// cells the sphere of radius R reaches: with REACH = 1 the 3 x 3 rows of
+// side-2h cells with at most 2 cells per row, with REACH = 2 about 84 cells
+// of side h holding 2.5x the candidates of the sphere, whose extra cell
+// look-ups cost more than the candidates they save.  The default pass
+// (sfgpu_params.sph_path 0, REACH = 1; 3 with REACH = 2) runs one warp per
+// 32 sorted bodies over the union of their scans (cubic_chunk below),
+// persistent warps taking the chunks heaviest first (chunks.cuh); paths 2
+// (REACH = 1) and 1 (REACH = 2) run one thread per body.  Each candidate is
+// tested with the FP32 expression above; bodies of another cell that
+// shares the bucket are skipped by cell key, so none is counted twice.  With SFGPU_FLAG_STATS the
 // density pass also sums an order-independent hash of every body's
 // neighbour set (j = i included).
 #include <climits>
@@ -330,10 +330,13 @@ __global__ void __launch_bounds__(128) k_cubic_body(uint32_t n, const float* __r
 // same bits.  A warp whose bodies span more than 3 cells on an axis (sparse
 // regions) runs the per-body scan instead.
 constexpr int CW_WARPS = 4;
-// the density passes' register budget: 64 (without the hint ptxas settles
-// at 56 with spills); the force pass takes no hint (0), its 64 registers
-// measured faster than with the hint (0.68 against 0.71 ms)
+// Register budgets by the resident blocks each pass asks for (without a
+// hint ptxas settles at 56 registers with spills for the density passes,
+// 64 with spills for the force pass).  Measured on the 262,144-body Plummer
+// gas: the force pass at 96 registers (one block asked for, no spills)
+// 0.58 ms against 0.67 at 64; the density passes at 64.
 constexpr int CW_MIN_BLOCKS = 8;
+constexpr int CW_MIN_BLOCKS_FORCE = 1;
 template <int REACH, bool FORCE, bool HASH>
 __device__ __forceinline__ void cubic_chunk(uint32_t k0, uint32_t n, const float* __restrict__ grid, uint32_t mask,
                                             const uint32_t* __restrict__ bstart, const uint32_t* __restrict__ bend,
@@ -513,7 +516,7 @@ __device__ __forceinline__ void cubic_chunk(uint32_t k0, uint32_t n, const float
 // The pass: one resident wave of persistent warps taking chunks of 32
 // sorted bodies heaviest first (chunks.cuh).
 template <int REACH, bool FORCE, bool HASH>
-__global__ void __launch_bounds__(CW_WARPS * 32, FORCE ? 0 : CW_MIN_BLOCKS) k_cubic_warp(uint32_t n, const float* __restrict__ grid,
+__global__ void __launch_bounds__(CW_WARPS * 32, FORCE ? CW_MIN_BLOCKS_FORCE : CW_MIN_BLOCKS) k_cubic_warp(uint32_t n, const float* __restrict__ grid,
                                                              uint32_t mask, const uint32_t* __restrict__ bstart,
                                                              const uint32_t* __restrict__ bend,
                                                              const uint32_t* __restrict__ bmix,
