@@ -646,17 +646,36 @@ __global__ void __launch_bounds__(BK_THREADS, 1) k_bucket_sort(const uint64_t* _
         const uint32_t base = s_off[d0];
         __syncthreads();
         const uint64_t lowmask = (lowbits >= 64) ? ~0ull : ((1ull << lowbits) - 1ull);
-        each_key([&](uint32_t e, uint64_t key) {
-            const uint32_t d = (uint32_t)(key >> dshift) & (nsub - 1u);
-            if (d < d0 || d >= d1) return;
-            const uint32_t pos = atomicAdd(&s_off[d], 1u);
-            k1[pos - base] = ((key & lowmask) << 13) | e;
-        });
+        // the pairs again from L2 (four in flight per thread): this CTA's
+        // composites, and its pairs themselves at their bucket positions
+        for (uint32_t e0 = threadIdx.x; e0 < size; e0 += 4u * BK_THREADS) {
+            uint64_t kk[4];
+            uint32_t vv[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const uint32_t e = e0 + (uint32_t)u * BK_THREADS;
+                if (e < size) {
+                    kk[u] = Kb[start + e];
+                    vv[u] = Vb[start + e];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const uint32_t e = e0 + (uint32_t)u * BK_THREADS;
+                if (e >= size) continue;
+                const uint32_t d = (uint32_t)(kk[u] >> dshift) & (nsub - 1u);
+                if (d < d0 || d >= d1) continue;
+                const uint32_t pos = atomicAdd(&s_off[d], 1u);
+                k1[pos - base] = ((kk[u] & lowmask) << 13) | e;
+                k0[e] = kk[u];
+                v0[e] = vv[u];
+            }
+        }
         __syncthreads();
-        // s_off[d] is now the end of sub-bucket d; the pairs themselves are
-        // read back from (Kb, Vb) by their position in the bucket
-        const uint64_t* kb = Kb + start;
-        const uint32_t* vb = Vb + start;
+        // s_off[d] is now the end of sub-bucket d; the pairs are at their
+        // bucket positions in (k0, v0)
+        const uint64_t* kb = k0;
+        const uint32_t* vb = v0;
         for (uint32_t d = d0 + threadIdx.x; d < d1; d += BK_THREADS) {
             const uint32_t m = s_cnt[d];
             if (m == 0u || m > 16u) continue;

@@ -2,13 +2,15 @@
 stable argsort: keys, the original index of every sorted slot (equal keys
 keep their input order), and a clear device status word.
 
-Up to 2^17 keys the sort takes one tile pass on the top 7-bit digit, then one
-CTA per top-digit bucket: a bucket of up to 128 pairs is rank-sorted by one
-warp; a larger one takes one pass on its next digit and its sub-buckets are
-rank-sorted by warps (up to 128 pairs) or finished by LSD passes of the CTA
-(above 128); a bucket over 8192 pairs sends the whole array through the
-cooperative tile passes.  The cases below put buckets and sub-buckets on
-each side of those limits."""
+Up to 2^17 keys the sort takes one tile pass on the top 7-bit digit, then
+sorts each top-digit bucket in shared memory: a bucket of up to 128 pairs is
+sorted by one warp's network; a larger one is split wide on its next bits
+and its sub-buckets are ranked by threads (up to 16 pairs) or warp networks
+(up to 128), a bucket of m pairs shared by min(4, ceil(m / 1024)) CTAs, or,
+with a sub-bucket above 128 pairs, finished by LSD passes of one CTA; a
+bucket over 8192 pairs sends the whole array through the cooperative tile
+passes.  The cases below put buckets and sub-buckets on each side of those
+limits."""
 import numpy as np
 import pytest
 
@@ -73,6 +75,23 @@ def test_sort_sub_bucket_limits(sf, sizes):
         parts.append(compose(9, 3 + 5 * d, low, 49))          # sub-buckets of bucket 9
         parts.append(compose(20 + d, d, low & np.uint64(7), 49))  # whole buckets, many ties
     keys = np.concatenate(parts)
+    keys = keys[rng.permutation(len(keys))]
+    check_sort(sf, keys, 49)
+
+
+@pytest.mark.parametrize("size", [1025, 2048, 3000, 6606, 8000])
+def test_sort_shared_buckets(sf, size):
+    """Top-digit buckets of over 1024 pairs with small sub-buckets, sorted by
+    up to four CTAs that each take a range of the sub-buckets; a quarter of
+    the keys repeat others (equal keys keep their order across the CTAs'
+    ranges)."""
+    rng = np.random.default_rng(size)
+    low = rng.integers(0, 1 << 42, size, dtype=np.uint64)
+    low[: size // 4] = low[size // 2: size // 2 + size // 4]
+    a = compose(33, 0, 0, 49) + low
+    b = compose(90, 0, 0, 49) + rng.integers(0, 1 << 42, size // 2 + 1, dtype=np.uint64)
+    c = rng.integers(0, 1 << 49, 3000, dtype=np.uint64)
+    keys = np.concatenate([a, b, c])
     keys = keys[rng.permutation(len(keys))]
     check_sort(sf, keys, 49)
 
