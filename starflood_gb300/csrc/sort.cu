@@ -592,25 +592,11 @@ __global__ void __launch_bounds__(BK_THREADS, 1) k_bucket_sort(const uint64_t* _
     uint32_t* s_cnt = sc.wcnt;          // [1024]
     uint32_t* s_off = sc.wcnt + 1024;   // [1024]
     for (uint32_t d = threadIdx.x; d < nsub; d += BK_THREADS) s_cnt[d] = 0u;
-    __syncthreads();
+    // every CTA of the bucket holds all of its pairs (read once from L2)
+    load_bucket();
     const int dshift = lowbits - D;
-    // the keys from L2, four loads in flight per thread: f(e, key) for each
-    auto each_key = [&](auto&& f) {
-        for (uint32_t e0 = threadIdx.x; e0 < size; e0 += 4u * BK_THREADS) {
-            uint64_t kk[4];
-#pragma unroll
-            for (int u = 0; u < 4; u++) {
-                const uint32_t e = e0 + (uint32_t)u * BK_THREADS;
-                if (e < size) kk[u] = Kb[start + e];
-            }
-#pragma unroll
-            for (int u = 0; u < 4; u++) {
-                const uint32_t e = e0 + (uint32_t)u * BK_THREADS;
-                if (e < size) f(e, kk[u]);
-            }
-        }
-    };
-    each_key([&](uint32_t, uint64_t key) { atomicAdd(&s_cnt[(uint32_t)(key >> dshift) & (nsub - 1u)], 1u); });
+    for (uint32_t e = threadIdx.x; e < size; e += BK_THREADS)
+        atomicAdd(&s_cnt[(uint32_t)(k0[e] >> dshift) & (nsub - 1u)], 1u);
     __syncthreads();
     // exclusive scan of the counts (two per thread) and their maximum
     __shared__ uint32_t s_wsum[BK_WARPS], s_wmax[BK_WARPS];
@@ -646,30 +632,12 @@ __global__ void __launch_bounds__(BK_THREADS, 1) k_bucket_sort(const uint64_t* _
         const uint32_t base = s_off[d0];
         __syncthreads();
         const uint64_t lowmask = (lowbits >= 64) ? ~0ull : ((1ull << lowbits) - 1ull);
-        // the pairs again from L2 (four in flight per thread): this CTA's
-        // composites, and its pairs themselves at their bucket positions
-        for (uint32_t e0 = threadIdx.x; e0 < size; e0 += 4u * BK_THREADS) {
-            uint64_t kk[4];
-            uint32_t vv[4];
-#pragma unroll
-            for (int u = 0; u < 4; u++) {
-                const uint32_t e = e0 + (uint32_t)u * BK_THREADS;
-                if (e < size) {
-                    kk[u] = Kb[start + e];
-                    vv[u] = Vb[start + e];
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < 4; u++) {
-                const uint32_t e = e0 + (uint32_t)u * BK_THREADS;
-                if (e >= size) continue;
-                const uint32_t d = (uint32_t)(kk[u] >> dshift) & (nsub - 1u);
-                if (d < d0 || d >= d1) continue;
-                const uint32_t pos = atomicAdd(&s_off[d], 1u);
-                k1[pos - base] = ((kk[u] & lowmask) << 13) | e;
-                k0[e] = kk[u];
-                v0[e] = vv[u];
-            }
+        for (uint32_t e = threadIdx.x; e < size; e += BK_THREADS) {  // this CTA's composites
+            const uint64_t key = k0[e];
+            const uint32_t d = (uint32_t)(key >> dshift) & (nsub - 1u);
+            if (d < d0 || d >= d1) continue;
+            const uint32_t pos = atomicAdd(&s_off[d], 1u);
+            k1[pos - base] = ((key & lowmask) << 13) | e;
         }
         __syncthreads();
         // s_off[d] is now the end of sub-bucket d; the pairs are at their
@@ -703,7 +671,6 @@ __global__ void __launch_bounds__(BK_THREADS, 1) k_bucket_sort(const uint64_t* _
     }
     // stable LSD passes over every digit below the top one, by the first CTA
     if (share != 0u) return;
-    load_bucket();
     uint64_t *ka = k0, *kb = k1;
     uint32_t *va = v0, *vb = v1;
     for (int p = 0; p < low_passes; p++) {
