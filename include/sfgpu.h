@@ -249,6 +249,14 @@ int sfgpu_sort_withheld_check(const uint64_t* keys, uint32_t n, uint32_t withhel
 int sfgpu_sort_keys(const uint64_t* keys, uint32_t n, int bits, uint64_t* sorted, uint32_t* index,
                     uint32_t* status);
 
+/* A check of the paired FP32 decisions (no reference counterpart): the
+ * walk's opening test for two cells at once and the SPH density pass's
+ * neighbour test for two candidates at once, against their scalar forms
+ * (the reference's FP32 expressions) on n random cases around the decision
+ * boundaries, seeded by `seed`.  mismatches[0] walk, [1] SPH; both 0 when
+ * the paired forms decide every case as the scalar ones. */
+int sfgpu_paired_check(uint32_t n, uint32_t seed, uint64_t mismatches[2]);
+
 /* ---- process utilities ------------------------------------------------- */
 /* Kernel launches the host has issued through this library in this process.
  * Replays of a captured CUDA graph issue no host launches and are not

@@ -85,6 +85,7 @@ def lib():
             "sfgpu_sph_neighbour_hashes": (i32, [vp, C.POINTER(C.c_uint64)]),
             "sfgpu_sort_withheld_check": (i32, [vp, u32, u32, u32, vp, vp, u32p]),
             "sfgpu_sort_keys": (i32, [vp, u32, i32, vp, vp, u32p]),
+            "sfgpu_paired_check": (i32, [u32, u32, vp]),
             "sfgpu_sph_set_u": (i32, [vp, f32p]),
             "sfgpu_sph_get_u": (i32, [vp, f32p, f32p]),
             "sfgpu_tree_keys": (i32, [vp, C.POINTER(C.c_uint64), u32p, u32p, f32p]),
@@ -171,6 +172,13 @@ def sort_keys(keys, bits):
     st = C.c_uint32()
     check(lib().sfgpu_sort_keys(_ptr(keys), n, bits, _ptr(out), _ptr(idx), C.byref(st)), "sfgpu_sort_keys")
     return out, idx, st.value
+
+
+def paired_check(n, seed=1):
+    """sfgpu_paired_check: (walk mismatches, SPH mismatches)."""
+    out = np.zeros(2, np.uint64)
+    check(lib().sfgpu_paired_check(n, seed, _ptr(out)), "sfgpu_paired_check")
+    return int(out[0]), int(out[1])
 
 
 def last_error() -> str:

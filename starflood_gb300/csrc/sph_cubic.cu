@@ -89,6 +89,20 @@ __device__ __forceinline__ bool is_neighbour(float dx, float dy, float dz, float
     const float s = fmul(2.0f, fmaxf(hi, hj));
     return r2 < fmul(s, s);
 }
+// The same decision for two candidates (negated coordinates nx, ny, nz and
+// S = (2 h_j)^2 each) against body (ax, ay, az) with Si = (2 h_i)^2, bit 0
+// and bit 1: a - q as a + (-q), the squares on paired instructions, their
+// sums scalar (ptxas fuses a paired product into a following paired add,
+// which would round r^2 differently), and r^2 < (2 max(h_i, h_j))^2 as
+// r^2 < max((2 h_i)^2, (2 h_j)^2) (squaring and rounding keep the order):
+// the same bits as is_neighbour.
+__device__ __forceinline__ uint32_t neighbours2(float2 ax, float2 ay, float2 az, float2 nx, float2 ny, float2 nz,
+                                                float2 S, float Si) {
+    const float2 dx = __fadd2_rn(ax, nx), dy = __fadd2_rn(ay, ny), dz = __fadd2_rn(az, nz);
+    const float2 px = __fmul2_rn(dx, dx), py = __fmul2_rn(dy, dy), pz = __fmul2_rn(dz, dz);
+    const float r0 = fadd(fadd(px.x, py.x), pz.x), r1 = fadd(fadd(px.y, py.y), pz.y);
+    return (r0 < fmaxf(Si, S.x) ? 1u : 0u) | (r1 < fmaxf(Si, S.y) ? 2u : 0u);
+}
 
 __global__ void __launch_bounds__(256) k_hmax(const float* __restrict__ rad, uint32_t n, int reach, uint32_t* done,
                                               float* __restrict__ grid, uint32_t* part) {
@@ -454,11 +468,9 @@ __device__ __forceinline__ void cubic_chunk(uint32_t k0, uint32_t n, const float
                     };
                     if (mine) {
                         if (!FORCE && vm == 0xffffffffu) {
-                            // two candidates per paired FP32 instruction:
-                            // a - q as a + (-q), and r^2 < (2 max(h_i, h_j))^2
-                            // as r^2 < max((2 h_i)^2, (2 h_j)^2) (squaring
-                            // and rounding keep the order), the same
-                            // decision bits as is_neighbour
+                            // two candidates per paired FP32 instruction
+                            // (neighbours2: the same decision bits as
+                            // is_neighbour)
                             const float2* tx = reinterpret_cast<const float2*>(st4);
                             const float2* ty = reinterpret_cast<const float2*>(st4 + 32);
                             const float2* tz = reinterpret_cast<const float2*>(st4 + 64);
@@ -466,16 +478,8 @@ __device__ __forceinline__ void cubic_chunk(uint32_t k0, uint32_t n, const float
                             const float2 ax2 = make_float2(a.x, a.x), ay2 = make_float2(a.y, a.y);
                             const float2 az2 = make_float2(a.z, a.z);
 #pragma unroll 8
-                            for (int u = 0; u < 16; u++) {
-                                const float2 dx = __fadd2_rn(ax2, tx[u]);
-                                const float2 dy = __fadd2_rn(ay2, ty[u]);
-                                const float2 dz = __fadd2_rn(az2, tz[u]);
-                                const float2 r2 =
-                                    __fadd2_rn(__fadd2_rn(__fmul2_rn(dx, dx), __fmul2_rn(dy, dy)), __fmul2_rn(dz, dz));
-                                const float2 S = tS[u];
-                                hits |= (r2.x < fmaxf(Si, S.x) ? 1u : 0u) << (2 * u);
-                                hits |= (r2.y < fmaxf(Si, S.y) ? 2u : 0u) << (2 * u);
-                            }
+                            for (int u = 0; u < 16; u++)
+                                hits |= neighbours2(ax2, ay2, az2, tx[u], ty[u], tz[u], tS[u], Si) << (2 * u);
                         } else if (vm == 0xffffffffu) {
 #pragma unroll 8
                             for (int t = 0; t < 32; t++) test(t);
@@ -695,4 +699,56 @@ int sf_sph_cubic(sfgpu_sim* s) {
     uint64_t* hash = w->mixv ? sf_sph_neighbour_hashes(s) : nullptr;
     if (w->reach == 1) return launch_passes<1>(s, w, mask, nbr, hash);
     return launch_passes<2>(s, w, mask, nbr, hash);
+}
+
+// ---- check of the paired neighbour test ---------------------------------------
+namespace {
+__device__ __forceinline__ uint32_t chk_mix(uint32_t x) {
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+// n random cases of a body and two candidates placed about 2 max(h_i, h_j)
+// away (r^2 within a few ulps of the bound in many of them): neighbours2
+// against is_neighbour, mismatches counted in *bad.
+__global__ void k_neighbours2_check(uint32_t n, uint32_t seed, unsigned long long* bad) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    auto u = [&](uint32_t k) {
+        return (float)(chk_mix(seed * 0x9E3779B9u ^ chk_mix(16u * i + k)) >> 8) * (1.0f / 16777216.0f);
+    };
+    const float ax = fsub(fmul(2.0f, u(0)), 1.0f), ay = fsub(fmul(2.0f, u(1)), 1.0f), az = fsub(fmul(2.0f, u(2)), 1.0f);
+    const float hi = fadd(0.01f, fmul(0.09f, u(3)));
+    float qx[2], qy[2], qz[2], hj[2];
+    uint32_t want = 0;
+#pragma unroll
+    for (int c = 0; c < 2; c++) {
+        hj[c] = fadd(0.01f, fmul(0.09f, u(4 + 5 * c)));
+        const float R = fmul(2.0f, fmaxf(hi, hj[c]));
+        const float dx = fsub(fmul(2.0f, u(5 + 5 * c)), 1.0f), dy = fsub(fmul(2.0f, u(6 + 5 * c)), 1.0f);
+        const float dz = fsub(fmul(2.0f, u(7 + 5 * c)), 1.0f);
+        const float len = fadd(__fsqrt_rn(fadd(fadd(fmul(dx, dx), fmul(dy, dy)), fmul(dz, dz))), 1e-6f);
+        const float sc = fdiv(R, len);
+        qx[c] = fadd(ax, fmul(dx, sc));
+        qy[c] = fadd(ay, fmul(dy, sc));
+        qz[c] = fadd(az, fmul(dz, sc));
+        float r2;
+        if (is_neighbour(fsub(ax, qx[c]), fsub(ay, qy[c]), fsub(az, qz[c]), hi, hj[c], r2)) want |= 1u << c;
+    }
+    const float si = fmul(2.0f, hi), s0 = fmul(2.0f, hj[0]), s1 = fmul(2.0f, hj[1]);
+    const uint32_t got = neighbours2(make_float2(ax, ax), make_float2(ay, ay), make_float2(az, az),
+                                     make_float2(-qx[0], -qx[1]), make_float2(-qy[0], -qy[1]),
+                                     make_float2(-qz[0], -qz[1]), make_float2(fmul(s0, s0), fmul(s1, s1)),
+                                     fmul(si, si));
+    if (got != want) atomicAdd(bad, 1ull);
+}
+}  // namespace
+
+int sf_sph_neighbours2_check(uint32_t n, uint32_t seed, unsigned long long* d_bad, cudaStream_t st) {
+    k_neighbours2_check<<<sf_ceil_div(n, 256), 256, 0, st>>>(n, seed, d_bad);
+    SF_CHECK_LAUNCH();
+    return SFGPU_OK;
 }

@@ -222,9 +222,13 @@ __device__ __forceinline__ bool opens(const float4& G, float rx, float ry, float
     return fc.theta <= fdiv(G.w, d2);
 }
 
-// The same test for two (cell, body) pairs at once: paired FP32 operations
-// round each element as the scalar ones do (a - b as a + (-b), which IEEE
-// defines to be the same), so both decisions equal opens().
+// The same test for two (cell, body) pairs at once, each element rounded as
+// the scalar test: differences and products on paired FP32 instructions
+// (a - b as a + (-b), which IEEE defines to be the same), the sums of the
+// squares scalar (measured on GB300: ptxas fuses a paired product into a
+// following paired add, even one written as add.rn.f32x2, which rounds d^2
+// differently in about a fifth of the cases), so both decisions equal
+// opens().
 __device__ __forceinline__ bool open_decide(float w, float d2, float hi, float lo, const ForceConsts& fc) {
     if (!(0.0f < d2)) return fc.theta <= 0.0f;
     if (w > hi) return true;
@@ -236,7 +240,8 @@ __device__ __forceinline__ void opens2(float2 gx, float2 gy, float2 gz, float2 g
     const float2 ox = __fadd2_rn(gx, make_float2(-rx.x, -rx.y));
     const float2 oy = __fadd2_rn(gy, make_float2(-ry.x, -ry.y));
     const float2 oz = __fadd2_rn(gz, make_float2(-rz.x, -rz.y));
-    const float2 d2 = __fadd2_rn(__fadd2_rn(__fmul2_rn(ox, ox), __fmul2_rn(oy, oy)), __fmul2_rn(oz, oz));
+    const float2 px = __fmul2_rn(ox, ox), py = __fmul2_rn(oy, oy), pz = __fmul2_rn(oz, oz);
+    const float2 d2 = make_float2(fadd(fadd(px.x, py.x), pz.x), fadd(fadd(px.y, py.y), pz.y));
     const float2 hi = __fmul2_rn(make_float2(th_hi, th_hi), d2);
     const float2 lo = __fmul2_rn(make_float2(th_lo, th_lo), d2);
     o0 = open_decide(gw.x, d2.x, hi.x, lo.x, fc);
@@ -522,8 +527,8 @@ __device__ __forceinline__ int lx_of(int e) { return 4 * (e >> 1) + (e & 1); }
 
 // Fast list: every lane runs every entry, its mask bit selecting the result,
 // so the inner loop has no per-lane branch.  FAST kind evaluates two entries
-// per instruction (paired FP32), each element rounded as the scalar code
-// would; COMP kind adds each interaction to Kahan sums in list order.
+// per instruction (paired FP32); COMP kind adds each interaction to Kahan
+// sums in list order.
 // With 16- or 8-body groups the 2 or 4 sub-warps hold the same bodies and
 // take entries in turn (FAST: entry pairs), `lane` being the body slot and
 // `half` the sub-warp.
@@ -1511,9 +1516,83 @@ int launch_fast(sfgpu_sim* s, bool stats) {
     return launch_sib<KIND, 32>(s, stats);
 }
 
+__device__ __forceinline__ uint32_t chk_mix(uint32_t x) {
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+// n random cases of a body and two cells whose w^2 lies within 3 ulps of
+// theta d^2 (so the IEEE-divide fallback decides many of them): opens2, as
+// the walk pairs cells, against opens, mismatches counted in *bad.
+__global__ void k_opens2_check(uint32_t n, uint32_t seed, float theta, float th_lo, float th_hi,
+                               unsigned long long* bad) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    auto u = [&](uint32_t k) {
+        return (float)(chk_mix(seed * 0x9E3779B9u ^ chk_mix(16u * i + k)) >> 8) * (1.0f / 16777216.0f);
+    };
+    ForceConsts fc{};
+    fc.theta = theta;
+    const float rx = fsub(fmul(2.0f, u(0)), 1.0f), ry = fsub(fmul(2.0f, u(1)), 1.0f), rz = fsub(fmul(2.0f, u(2)), 1.0f);
+    float4 G[2];
+    bool want[2];
+#pragma unroll
+    for (int c = 0; c < 2; c++) {
+        const float gx = fsub(fmul(2.0f, u(3 + 4 * c)), 1.0f), gy = fsub(fmul(2.0f, u(4 + 4 * c)), 1.0f);
+        const float gz = fsub(fmul(2.0f, u(5 + 4 * c)), 1.0f);
+        const float ox = fsub(gx, rx), oy = fsub(gy, ry), oz = fsub(gz, rz);
+        const float d2 = fadd(fadd(fmul(ox, ox), fmul(oy, oy)), fmul(oz, oz));
+        const int k = (int)(chk_mix(seed ^ (0x51ED27u * (2u * i + (uint32_t)c))) % 7u) - 3;
+        G[c] = make_float4(gx, gy, gz, __int_as_float(__float_as_int(fmul(theta, d2)) + k));
+        want[c] = opens(G[c], rx, ry, rz, fc, th_lo, th_hi);
+    }
+    bool g0, g1;
+    opens2(make_float2(G[0].x, G[1].x), make_float2(G[0].y, G[1].y), make_float2(G[0].z, G[1].z),
+           make_float2(G[0].w, G[1].w), make_float2(rx, rx), make_float2(ry, ry), make_float2(rz, rz), fc, th_lo,
+           th_hi, g0, g1);
+    if (g0 != want[0] || g1 != want[1]) atomicAdd(bad, 1ull);
+}
+
 }  // namespace
 
 size_t sf_walk_scratch_floats4(uint32_t n) { return (size_t)SPLIT * n; }
+
+int sf_sph_neighbours2_check(uint32_t n, uint32_t seed, unsigned long long* d_bad, cudaStream_t st);
+
+// Check of the paired FP32 decisions (no counterpart in the reference): the
+// walk's opening test for two cells and the SPH density pass's neighbour test
+// for two candidates, against their scalar forms on n random cases around
+// the decision boundaries.  mismatches[0] walk, [1] SPH.
+extern "C" int sfgpu_paired_check(uint32_t n, uint32_t seed, uint64_t* mismatches) {
+    sf_clear_error();
+    if (!mismatches || n == 0u) {
+        sf_set_error("sfgpu_paired_check needs n > 0 and an output array");
+        return SFGPU_FAILURE;
+    }
+    unsigned long long* d = nullptr;
+    SF_CUDA(cudaMalloc(&d, 2 * sizeof(unsigned long long)));
+    cudaError_t e = cudaMemset(d, 0, 2 * sizeof(unsigned long long));
+    const float theta = 0.5f;
+    const float th_lo = theta * (1.0f - 1.0f / 524288.0f), th_hi = theta * (1.0f + 1.0f / 524288.0f);
+    if (e == cudaSuccess) {
+        k_opens2_check<<<sf_ceil_div(n, 256), 256>>>(n, seed, theta, th_lo, th_hi, d);
+        e = cudaGetLastError();
+    }
+    int rc = e == cudaSuccess ? sf_sph_neighbours2_check(n, seed, d + 1, 0) : SFGPU_FAILURE;
+    unsigned long long h[2] = {0, 0};
+    if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) {
+        sf_set_error("sfgpu_paired_check: %s", cudaGetErrorString(e));
+        return SFGPU_FAILURE;
+    }
+    mismatches[0] = h[0];
+    mismatches[1] = h[1];
+    return rc;
+}
 
 int sf_walk_launch(sfgpu_sim* s) {
     const bool stats = (s->p.flags & SFGPU_FLAG_STATS) && s->stat_int;

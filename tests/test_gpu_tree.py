@@ -500,3 +500,14 @@ def test_status_spin_withheld_lookback(sf):
     out, idx, st = sf.sort_withheld_check(keys)
     assert st == 0
     np.testing.assert_array_equal(idx, want)
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_paired_decisions_match_scalar(sf, seed):
+    """The walk's opening test for two cells per paired FP32 instruction and
+    the SPH density pass's neighbour test for two candidates decide every
+    case as the scalar FP32 expressions, on 4M random cases each placed
+    within a few ulps of the decision boundary (where a fused product would
+    flip some)."""
+    walk_bad, sph_bad = sf.paired_check(1 << 22, seed)
+    assert (walk_bad, sph_bad) == (0, 0)
