@@ -299,7 +299,7 @@ def bh_per_particle_err(sf, oracle_threads_ok=True):
 
 def bh_variant_rates(sf, steps=20, warmup=3):
     """Particle-steps/s of the headline workload with leaf 16 (the leaf size
-    BASELINE's Barnes-Hut config names) and with EXACT arithmetic (the
+    of the published Barnes-Hut configuration) and with EXACT arithmetic (the
     reference's FP32 expressions, bit-identical results), each K graph
     replays with the L2 flushed between steps (CUDA events)."""
     import ctypes as C
