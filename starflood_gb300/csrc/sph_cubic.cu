@@ -348,8 +348,9 @@ constexpr int CW_WARPS = 4;
 // hint ptxas settles at 56 registers with spills for the density passes,
 // 64 with spills for the force pass).  Measured on the 262,144-body Plummer
 // gas: the force pass at 96 registers (one block asked for, no spills)
-// 0.58 ms against 0.67 at 64; the density passes at 64.
-constexpr int CW_MIN_BLOCKS = 8;
+// 0.58 ms against 0.67 at 64; the density passes at 80 registers (six
+// blocks) 0.435 ms against 0.449 at 64.
+constexpr int CW_MIN_BLOCKS = 6;
 constexpr int CW_MIN_BLOCKS_FORCE = 1;
 template <int REACH, bool FORCE, bool HASH>
 __device__ __forceinline__ void cubic_chunk(uint32_t k0, uint32_t n, const float* __restrict__ grid, uint32_t mask,
