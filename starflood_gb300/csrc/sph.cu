@@ -361,6 +361,10 @@ __global__ void __launch_bounds__(128) k_ref_density_grid(uint32_t n, uint32_t m
 // key's range, runs the per-body scans.  The warps are persistent and take
 // their chunks heaviest first (chunks.cuh).
 constexpr int RW_WARPS = 4;
+// The density warp pass takes a register-budget hint (one resident block
+// asked for: 68 registers, no spills, instead of 56 with spills; measured
+// 13.0-13.5 against 13.7-14.6 ms per pass on the 262,144-body gas); the
+// momentum pass measured slower with it and keeps ptxas's own choice.
 
 __device__ __forceinline__ void ref_density_chunk(uint32_t k0, uint32_t n, uint32_t mask,
                                                   const uint32_t* __restrict__ bstart,
@@ -452,7 +456,7 @@ __device__ __forceinline__ void ref_density_chunk(uint32_t k0, uint32_t n, uint3
     if (live) rho[V[k]] = sum;
 }
 
-__global__ void __launch_bounds__(RW_WARPS * 32) k_ref_density_warp(
+__global__ void __launch_bounds__(RW_WARPS * 32, 1) k_ref_density_warp(
     uint32_t n, uint32_t mask, const uint32_t* __restrict__ bstart, const uint32_t* __restrict__ bend,
     const uint32_t* __restrict__ bmix, const uint64_t* __restrict__ cell, const float4* __restrict__ px,
     const float2* __restrict__ pq, const uint32_t* __restrict__ V, const float* __restrict__ hw,
