@@ -77,7 +77,9 @@ typedef struct {
     double   sph_alpha;   /* CUBIC: Monaghan viscosity alpha                */
     double   sph_beta;    /* CUBIC: Monaghan viscosity beta                 */
     uint32_t flags;       /* SFGPU_FLAG_*                                   */
-    uint32_t walk_split;  /* walk variant: 0 group walk (default), 1 thread per body, 8 thread per body and root octant, 64 32-body group walk over 8 warps */
+    uint32_t walk_split;  /* walk variant: 0 group walk over a stack of sibling groups (default), 32 the same
+                             group walk over a stack of single cells, 1 thread per body, 8 thread per body
+                             and root octant, 64 32-body group walk over 8 warps */
     uint32_t sph_path;    /* SPH neighbour passes on the cell grid.  CUBIC: the 3 x 3 rows of cells
                              of side 2h around each body, each row cut to the cells the 2h sphere
                              reaches: 0 one warp per 32 sorted bodies over the union of their rows,
