@@ -42,22 +42,30 @@ __device__ __forceinline__ uint32_t digit_peers(uint32_t d, bool ok, int lane) {
 #endif
 }
 
-__global__ void __launch_bounds__(256) k_hist(const uint64_t* __restrict__ keys, uint32_t n, int passes,
-                                              uint32_t* __restrict__ hist, const uint32_t* enable) {
-    if (enable && *enable == 0u) return;
-    __shared__ uint32_t sh[MAX_PASSES * RADIX];
+// Digit histograms of passes [p0, passes) of the n keys, added into hist
+// (cleared by the caller).
+__device__ __forceinline__ void hist_digits(const uint64_t* __restrict__ keys, uint32_t n, int p0, int passes,
+                                            uint32_t* __restrict__ hist, uint32_t* sh, uint32_t first,
+                                            uint32_t stride) {
     for (int i = threadIdx.x; i < passes * RADIX; i += blockDim.x) sh[i] = 0u;
     __syncthreads();
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    for (uint32_t i = first; i < n; i += stride) {
         const uint64_t k = keys[i];
-        for (int p = 0; p < passes; p++) {
+        for (int p = p0; p < passes; p++) {
             const uint32_t d = (uint32_t)(k >> (p * RADIX_BITS)) & (RADIX - 1);
             atomicAdd(&sh[p * RADIX + d], 1u);
         }
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < passes * RADIX; i += blockDim.x)
+    for (int i = p0 * RADIX + threadIdx.x; i < passes * RADIX; i += blockDim.x)
         if (sh[i]) atomicAdd(&hist[i], sh[i]);
+}
+
+__global__ void __launch_bounds__(256) k_hist(const uint64_t* __restrict__ keys, uint32_t n, int p0, int passes,
+                                              uint32_t* __restrict__ hist, const uint32_t* enable) {
+    if (enable && *enable == 0u) return;
+    __shared__ uint32_t sh[MAX_PASSES * RADIX];
+    hist_digits(keys, n, p0, passes, hist, sh, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
 }
 
 // One tile of one pass: tile `tile` of (kin, vin) ranked and scattered into
@@ -218,7 +226,7 @@ __global__ void __launch_bounds__(SORT_THREADS) k_onesweep(
 template <int SORT_ITEMS>
 __global__ void __launch_bounds__(SORT_THREADS) k_onesweep_all(uint64_t* k0, uint32_t* v0, uint64_t* k1,
                                                                uint32_t* v1, uint32_t n, int passes,
-                                                               const uint32_t* __restrict__ hist, uint32_t* status,
+                                                               uint32_t* hist, uint32_t* status,
                                                                uint32_t* d_status, const uint32_t* enable,
                                                                uint32_t spin_limit) {
     if (*enable == 0u) return;
@@ -228,6 +236,12 @@ __global__ void __launch_bounds__(SORT_THREADS) k_onesweep_all(uint64_t* k0, uin
     for (size_t i = (size_t)blockIdx.x * SORT_THREADS + threadIdx.x; i < (size_t)passes * tiles * RADIX;
          i += (size_t)tiles * SORT_THREADS)
         status[i] = 0u;
+    // the digit histograms below the top one (the bucket path counted only
+    // the top digit; its caller cleared them all)
+    {
+        __shared__ uint32_t sh[MAX_PASSES * RADIX];
+        hist_digits(k0, n, 0, passes - 1, hist, sh, blockIdx.x * SORT_THREADS + threadIdx.x, tiles * SORT_THREADS);
+    }
     grid.sync();
     uint64_t *ka = k0, *kb = k1;
     uint32_t *va = v0, *vb = v1;
@@ -790,7 +804,8 @@ int sf_sort_pairs_keep(uint64_t* keys, uint32_t* vals, uint32_t n, int bits, Sor
         }
         w.flags &= ~SORT_PRECLEARED;
         const uint32_t hb = std::min<uint32_t>(sf_ceil_div(n, 256 * 8), (uint32_t)sf_num_sms() * 4);
-        k_hist<<<hb, 256, 0, st>>>(keys, n, passes, w.hist, enable);
+        // the top digit's histogram (the fallback counts the others itself)
+        k_hist<<<hb, 256, 0, st>>>(keys, n, passes - 1, passes, w.hist, enable);
         SF_CHECK_LAUNCH();
         const int top = passes - 1;
         k_onesweep<4><<<tiles, SORT_THREADS, 0, st>>>(keys, vals, w.keys_b, w.vals_b, n, top * RADIX_BITS,
@@ -810,7 +825,7 @@ int sf_sort_pairs_keep(uint64_t* keys, uint32_t* vals, uint32_t n, int bits, Sor
             uint32_t* v1 = vals;
             uint32_t nn = n;
             int np = passes;
-            const uint32_t* hh = w.hist;
+            uint32_t* hh = w.hist;
             uint32_t* ss = w.status + (size_t)tiles * RADIX;
             uint32_t* ds = d_status;
             const uint32_t* en = big;
@@ -832,7 +847,7 @@ int sf_sort_pairs_keep(uint64_t* keys, uint32_t* vals, uint32_t n, int bits, Sor
     SF_CUDA(cudaMemsetAsync(w.counters, 0, sizeof(uint32_t) * passes, st));
     SF_CUDA(cudaMemsetAsync(w.status, 0, sizeof(uint32_t) * (size_t)passes * tiles * RADIX, st));
     const uint32_t hb = std::min<uint32_t>(sf_ceil_div(n, 256 * 8), (uint32_t)sf_num_sms() * 4);
-    k_hist<<<hb, 256, 0, st>>>(keys, n, passes, w.hist, enable);
+    k_hist<<<hb, 256, 0, st>>>(keys, n, 0, passes, w.hist, enable);
     SF_CHECK_LAUNCH();
     uint64_t* ka = keys;
     uint32_t* va = vals;
